@@ -1,0 +1,208 @@
+"""Generate the golden vectors in tests/golden/ from RenderToy's OWN code.
+
+Run where the RenderToy sources are present (they are read, never copied):
+
+    python tests/golden/make_golden.py [--ref /path/to/RenderToy]
+
+It builds oracle/_ref/libref.so (reference sources with the recursion cap as a
+parameter, RNG wrapped) and oracle/_ref/libref_orig.so (unmodified sources) via
+``make -C oracle ref``, runs both on seeded synthetic inputs, checks that the
+patched build at the reference cap equals the unmodified one and that the
+restatement (oracle/_build/liboracle.so) equals the reference bit for bit, and
+writes the reference's outputs as .npz fixtures.  The tests compare the oracle
+with these fixtures on every machine, and the CUDA path with the oracle.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import bind  # noqa: E402
+from rendertoy_gb300 import scenes  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+SEED = 7
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def check_equal(name, a, b, mask=None):
+    a, b = bits(a), bits(b)
+    if mask is not None:
+        a, b = a[mask], b[mask]
+    ok = np.array_equal(a, b)
+    print(f"  {name}: {'bit-exact' if ok else 'MISMATCH'}")
+    if not ok:
+        raise SystemExit(f"oracle differs from the reference on {name}")
+
+
+def scene_case(ref, refo, orc, sc, W, H, tag):
+    rs, ro, os_ = ref.scene(sc), refo.scene(sc), orc.scene(sc)
+    near, far = float(sc.camera[19]), float(sc.camera[20])
+    out = dict(verts=sc.verts, norms=sc.norms, tri_mesh=sc.tri_mesh, mesh_mat=sc.mesh_mat,
+               mesh_smooth=sc.mesh_smooth, mats=sc.mats, sky=sc.sky, ground=sc.ground,
+               camera=sc.camera, W=W, H=H, seed=SEED)
+    em = rs.emitters()
+    assert np.array_equal(em, sc.emitters()), "emitter order"
+    assert np.array_equal(em, os_.emitters())
+    out["emitters"] = em
+    tri, tuv = rs.primary(W, H)
+    t2, u2 = os_.primary(W, H)
+    assert np.array_equal(tri, t2)
+    check_equal(f"{tag} primary t/u/v", tuv, u2)
+    out["primary_tri"], out["primary_tuv"] = tri, tuv
+    n, a, d = rs.aov(W, H, near, far)
+    n2, a2, d2 = os_.aov(W, H, near, far)
+    check_equal(f"{tag} normal", n, n2)
+    check_equal(f"{tag} albedo", a, a2)
+    check_equal(f"{tag} depth", d, d2)
+    out["aov_normal"], out["aov_albedo"], out["aov_depth"] = n, a, d
+    for depth, spp in ((5, 2), (8, 2)):
+        p = rs.trace_paths(W, H, 0, spp, depth, SEED)
+        if depth == 5:
+            p0 = ro.trace_paths(W, H, 0, spp, depth, SEED)
+            check_equal(f"{tag} patched cap == unmodified (depth 5)", p, p0)
+        p2 = os_.trace_paths(W, H, 0, spp, depth, SEED)
+        check_equal(f"{tag} paths depth {depth}", p, p2)
+        out[f"paths_d{depth}"] = p
+    np.savez_compressed(os.path.join(OUT, f"scene_{tag}.npz"), **out)
+
+
+def intersect_case(ref, orc, sc, n=4096):
+    rng = np.random.RandomState(11)
+    o = rng.uniform(5, 550, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    # a quarter of the rays start on a triangle (barycentric point) and
+    # exclude it, as bounce and shadow rays do
+    k = n // 4
+    tid = rng.randint(0, sc.n_tris, k)
+    uv = rng.uniform(0, 1, (k, 2))
+    swap = uv.sum(1) > 1
+    uv[swap] = 1 - uv[swap]
+    v = sc.verts[tid].reshape(k, 3, 3).astype(np.float64)
+    o[:k] = (v[:, 0] + uv[:, :1] * (v[:, 1] - v[:, 0]) + uv[:, 1:] * (v[:, 2] - v[:, 0])).astype(np.float32)
+    ex = np.full(n, -1, np.int32)
+    ex[:k] = tid
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    rs, os_ = ref.scene(sc), orc.scene(sc)
+    t1, u1 = rs.intersect(rays, ex)
+    t2, u2 = os_.intersect(rays, ex)
+    assert np.array_equal(t1, t2)
+    check_equal("intersect t/u/v", u1, u2)
+    np.savez_compressed(os.path.join(OUT, "intersect_mixed.npz"), rays=rays, exclude=ex, tri=t1, tuv=u1)
+
+
+def bsdf_case(ref, orc, n=3000):
+    rng = np.random.RandomState(5)
+    mats = np.stack([scenes.material(
+        base_color=tuple(rng.uniform(0, 1, 3)), roughness=rng.uniform(0.001, 1.0),
+        metallic=rng.choice([0.0, 1.0, rng.uniform()]), subsurface=rng.uniform(),
+        specular_tint=rng.uniform(), sheen=rng.uniform(), sheen_tint=rng.uniform(),
+        clearcoat=rng.choice([0.0, rng.uniform()]), clearcoat_roughness=rng.uniform(0.001, 1.0),
+        spec_trans=rng.choice([0.0, 1.0, rng.uniform()]), ior=rng.uniform(1.05, 2.0))
+        for _ in range(n)])
+    eta = np.where(rng.uniform(size=n) < 0.5, 1.0 / mats[:, 16], mats[:, 16]).astype(np.float32)
+
+    def unit(m):
+        v = rng.normal(size=(m, 3))
+        return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+
+    N, V, L = unit(n), unit(n), unit(n)
+    V = np.where((np.sum(V * N, 1) < 0)[:, None], -V, V).astype(np.float32)
+    ef, ep = np.zeros((n, 3), np.float32), np.zeros(n, np.float32)
+    ok, od, col, sp = (np.zeros(n, np.int32), np.zeros((n, 3), np.float32),
+                       np.zeros((n, 3), np.float32), np.zeros(n, np.float32))
+    for i in range(n):
+        f, p = ref.bsdf_eval(mats[i], eta[i], N[i], V[i], L[i])
+        f2, p2 = orc.bsdf_eval(mats[i], eta[i], N[i], V[i], L[i])
+        assert np.array_equal(bits(f), bits(f2)) and bits(p) == bits(p2), ("eval", i)
+        ef[i], ep[i] = f, p
+        r = ref.bsdf_sample(mats[i], eta[i], N[i], V[i], SEED, i, 3)
+        r2 = orc.bsdf_sample(mats[i], eta[i], N[i], V[i], SEED, i, 3)
+        assert r[0] == r2[0] and all(np.array_equal(bits(x), bits(y)) for x, y in zip(r[1:], r2[1:])), ("sample", i)
+        ok[i], od[i], col[i], sp[i] = r
+    print(f"  bsdf eval/sample ({n} cases): bit-exact; sample ok fraction {ok.mean():.3f}")
+    np.savez_compressed(os.path.join(OUT, "bsdf.npz"), mats=mats, eta=eta, N=N, V=V, L=L,
+                        eval_f=ef, eval_pdf=ep, sample_ok=ok, sample_dir=od, sample_color=col,
+                        sample_pdf=sp, seed=SEED)
+
+
+def valid_rows(H, radius):
+    """Rows whose taps stay inside the buffer in the reference (its reflect
+    index can read one row past the end: include/RenderToy/compositor.h:25-39)."""
+    m = np.zeros(H, bool)
+    m[: max(H - 1 - radius, 0)] = True
+    return m
+
+
+def compositor_case(ref, orc):
+    rng = np.random.RandomState(3)
+    out = {}
+    for tag, (W, H) in (("a", (37, 29)), ("b", (64, 64))):
+        img = (rng.exponential(0.6, (H, W, 3)) * (rng.uniform(size=(H, W, 1)) < 0.9)).astype(np.float32)
+        out[f"img_{tag}"] = img
+        cases = {
+            "blur7": (lambda c: c.gaussian_blur(img, 7, 1.5), 3),
+            "blur49": (lambda c: c.gaussian_blur(img, 49, 8.0), 24),
+            "edge": (lambda c: c.edge_detect(img), 1),
+            "bloom": (lambda c: c.bloom(img, 9, 2.0, 0.8), 4),
+        }
+        k5 = rng.normal(size=(5, 5)).astype(np.float32)
+        out[f"k5_{tag}"] = k5
+        for flags in ((0, 0, 0), (0, 0, 1), (0, 1, 0), (1, 0, 0), (0, 1, 1)):
+            cases[f"conv5_{''.join(map(str, flags))}"] = (
+                lambda c, f=flags: c.convolve(img, k5, normalize=f[0], length=f[1], absval=f[2]), 2)
+        for name, (fn, radius) in cases.items():
+            a, b = fn(ref), fn(orc)
+            rows = valid_rows(H, radius)
+            check_equal(f"compositor {tag}/{name}", a, b, mask=rows)
+            out[f"{name}_{tag}"] = np.where(rows[:, None, None], a, np.float32(0))
+            out[f"rows_{name}_{tag}"] = rows
+    for size, sigma in ((3, 0.8), (7, 1.5), (49, 8.0), (9, 2.0)):
+        w = ref.gaussian_weights(size, sigma)
+        check_equal(f"gaussian weights {size}/{sigma}", w, orc.gaussian_weights(size, sigma))
+        out[f"gw_{size}"] = w
+    np.savez_compressed(os.path.join(OUT, "compositor.npz"), **out)
+
+
+def rng_case(ref, orc):
+    out = {}
+    for (seed, pixel, sample) in ((0, 0, 0), (7, 12345, 3), (2**40 + 5, 2**31, 1023)):
+        a = ref.rng_floats(seed, pixel, sample, 64)
+        check_equal(f"rng {seed}/{pixel}/{sample}", a, orc.rng_floats(seed, pixel, sample, 64))
+        out[f"rng_{seed}_{pixel}_{sample}"] = a
+    np.savez_compressed(os.path.join(OUT, "rng.npz"), **out)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={args.ref}", "all", "ref"])
+    ref, refo, orc = bind.load("ref"), bind.load("ref_orig"), bind.load("oracle")
+    print("scenes:")
+    scene_case(ref, refo, orc, scenes.cornell_box(), 48, 40, "cornell")
+    scene_case(ref, refo, orc, scenes.cornell_mixed(), 40, 32, "mixed")
+    print("intersect:")
+    intersect_case(ref, orc, scenes.cornell_mixed())
+    print("bsdf:")
+    bsdf_case(ref, orc)
+    print("compositor:")
+    compositor_case(ref, orc)
+    print("rng:")
+    rng_case(ref, orc)
+    print("written to", OUT)
+
+
+if __name__ == "__main__":
+    main()
