@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""bench.py — path-tracing throughput of librtx on GB300.
+
+Workload (one step = one frame): the seeded displaced icosphere (20 * 4^8 =
+1,310,720 triangles, Perlin displacement 0.05 r) in the Cornell room,
+1024 x 1024 pixels, 64 samples per pixel, max depth 12, then the Compositor's
+Gaussian blur (sigma 8, size 49) and a 5 x 5 edge-detect convolution of the
+result.  Metric: Msamples/s (pixel samples per second), with Mrays/s beside it.
+
+  value : device time of the step with the scene and image resident in HBM
+          (CUDA events on the library's stream, L2 flushed between steps);
+  e2e   : the same step through the C ABI with host (pinned) buffers: the image
+          is copied back after the render and each filter copies its image in
+          and out, as RenderToy's Image does; host wall clock.
+  roofline : the closest-hit traversal kernel (k_extend), algorithmic bytes =
+          BVH nodes visited x 64 B + triangles tested x 48 B + 52 B of ray I/O
+          per ray, counted by an instrumented (untimed) run of the same step.
+  cpu_baseline : the oracle's restatement of RenderToy's renderer (octree +
+          priority-queue traversal) on the host cores, on a bounded sample.
+
+``--impl reference`` times RenderToy's CPU path on the same workload (its
+compiled sources where they run here, otherwise the oracle restatement).
+Multi-GPU: each rank renders its own frame (no collective on the data path);
+scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RES = 1024
+SPP = 64
+DEPTH = 12
+SUBDIV = 8
+BLUR_SIZE, BLUR_SIGMA = 49, 8.0
+EDGE5 = np.array([[0, 0, -1, 0, 0], [0, -1, -2, -1, 0], [-1, -2, 16, -2, -1],
+                  [0, -1, -2, -1, 0], [0, 0, -1, 0, 0]], np.float32)
+WORKLOAD = (f"displaced icosphere ({20 * 4 ** SUBDIV} tris, subdiv {SUBDIV}, Perlin 0.05r, seed 1) "
+            f"in the Cornell room; {RES}x{RES}, {SPP} spp, max depth {DEPTH}; "
+            f"Gaussian blur sigma {BLUR_SIGMA} size {BLUR_SIZE} + 5x5 edge convolution")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample_rate(sc, seconds=12.0, threads=0, kind="oracle"):
+    """Msamples/s of RenderToy's CPU path (restated) on a bounded sample of
+    the workload: random pixels of the 1024^2 film, 1 sample each, depth 12."""
+    from oracle import bind
+    if kind == "reference":
+        chk = bind.load("ref")
+    else:
+        bind.build()
+        chk = bind.load("oracle")
+    s = chk.scene(sc)
+    rng = np.random.RandomState(0)
+    n = 256
+    total_samples, total_t = 0, 0.0
+    while True:
+        pix = rng.choice(RES * RES, n, replace=False).astype(np.int32)
+        t0 = time.perf_counter()
+        s.trace_paths(RES, RES, 0, 1, DEPTH, 1, pixels=pix, threads=threads)
+        dt = time.perf_counter() - t0
+        total_samples += n
+        total_t += dt
+        if total_t >= seconds:
+            break
+        left = seconds - total_t
+        n = int(min(max(n * 2, n * left / max(dt, 1e-3)), 200000))
+    cores = threads or os.cpu_count()
+    return total_samples / total_t / 1e6, total_samples, total_t, cores
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--subdiv", type=int, default=SUBDIV)
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    from rendertoy_gb300 import scenes
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sc = scenes.displaced_icosphere(subdiv=args.subdiv)
+        kind = "oracle"
+        try:
+            from oracle import bind
+            bind.load("ref")
+            kind = "reference"
+        except OSError:
+            kind = "oracle"
+        except FileNotFoundError:
+            kind = "oracle"
+        per_step = max(args.cpu_seconds / max(args.steps, 1), 2.0)
+        vals = []
+        for _ in range(args.warmup and 1):
+            cpu_sample_rate(sc, seconds=1.0, kind=kind)
+        tot_s, tot_t = 0, 0.0
+        for _ in range(args.steps):
+            v, ns, t, cores = cpu_sample_rate(sc, seconds=per_step, kind=kind)
+            vals.append(v)
+            tot_s += ns
+            tot_t += t
+        value = tot_s / tot_t / 1e6
+        line = {"impl": "reference", "metric": "Msamples/s", "value": value, "unit": "Msamples/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": tot_t / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "sample": "random pixels of the film, 1 spp each"},
+                "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": cores,
+                                 "kind": "reference" if kind == "reference" else "port",
+                                 "sample": f"{tot_s} samples (random pixels x 1 spp) in {tot_t:.1f} s"},
+                "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    import rendertoy_gb300 as rt
+
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    t0 = time.perf_counter()
+    sc = scenes.displaced_icosphere(subdiv=args.subdiv)
+    gen_s = time.perf_counter() - t0
+    ctx = rt.Context(local)
+    ctx.upload(sc)
+    st0 = ctx.stats()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    dev = torch.device("cuda", local)
+    img = torch.empty((RES, RES, 3), dtype=torch.float32, device=dev)
+    blur = torch.empty_like(img)
+    edge = torch.empty_like(img)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    seed = 1 + rank
+
+    def step(i):
+        ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed + 1000 * i, out=img)
+        ctx.gaussian_blur(img, BLUR_SIZE, BLUR_SIGMA, out=blur)
+        ctx.convolve(blur, EDGE5, absval=True, out=edge)
+
+    ctx.set_option(rt.OPT_ASYNC, 1)
+    ctx.set_option(rt.OPT_KERNEL_TIMING, 1)
+    for i in range(args.warmup):
+        step(i)
+    ctx.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+    step_ms, ext_ms, ext_launch, rays_e, rays_s = [], 0.0, 0, 0, 0
+    with Clocks(local) as clk:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed + 1000 * i, out=img)
+            ctx.gaussian_blur(img, BLUR_SIZE, BLUR_SIGMA, out=blur)
+            ctx.convolve(blur, EDGE5, absval=True, out=edge)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            # the filters leave the render's timers and ray counters untouched
+            s = ctx.stats()
+            ext_ms += s["extend_ms"]
+            ext_launch += s["extend_launches"]
+            rays_e += s["extension_rays"]
+            rays_s += s["shadow_rays"]
+    total_ms = reduce_max(sum(step_ms), ws)
+    samples = RES * RES * SPP * args.steps
+    value = samples * ws / (total_ms / 1e3) / 1e6
+    mrays = (rays_e + rays_s) * ws / (total_ms / 1e3) / 1e6
+
+    # instrumented run (untimed): node visits and triangle tests per frame
+    ctx.set_option(rt.OPT_COUNT_VISITS, 1)
+    ctx.set_option(rt.OPT_KERNEL_TIMING, 0)
+    ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed, out=img)
+    cs = ctx.stats()
+    ctx.set_option(rt.OPT_COUNT_VISITS, 0)
+    # kernels per step: the render's launches + blur (2) + convolution (1)
+    launches = (cs["kernel_launches"] + 3) * args.steps
+    ext_bytes_frame = cs["ext_node_visits"] * 64 + cs["ext_tri_tests"] * 48 + cs["extension_rays"] * 52
+    frames = args.steps
+    ext_launch_per_frame = ext_launch / frames
+    avg_launch_ms = ext_ms / ext_launch
+    bytes_per_launch = ext_bytes_frame / ext_launch_per_frame
+    achieved = bytes_per_launch / (avg_launch_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "k_extend_traffic.txt")
+    if os.path.exists(tf):
+        for ln in open(tf):
+            if ln.startswith("dram_bytes_per_extension_ray"):
+                traffic = float(ln.split()[1]) * cs["extension_rays"] / ext_launch_per_frame
+
+    # end to end through the C ABI with pinned host buffers
+    ctx.set_option(rt.OPT_ASYNC, 0)
+    h_img = torch.empty((RES, RES, 3), dtype=torch.float32, pin_memory=True)
+    h_blur = torch.empty_like(h_img, pin_memory=True)
+    h_edge = torch.empty_like(h_img, pin_memory=True)
+    e2e_steps = max(1, min(args.steps, 3))
+    ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed, out=h_img)
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed + 1000 * i, out=h_img)
+        ctx.gaussian_blur(h_img, BLUR_SIZE, BLUR_SIGMA, out=h_blur)
+        ctx.convolve(h_blur, EDGE5, absval=True, out=h_edge)
+    e2e_s = reduce_max(time.perf_counter() - t0, ws)
+    img_bytes = RES * RES * 12
+    e2e = {"value": RES * RES * SPP * e2e_steps * ws / e2e_s / 1e6, "unit": "Msamples/s",
+           "h2d_bytes_per_step": 2 * img_bytes + 84 + BLUR_SIZE * 4 + 25 * 4,
+           "d2h_bytes_per_step": 3 * img_bytes, "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0:
+        v, ns, t, cores = cpu_sample_rate(sc, seconds=args.cpu_seconds)
+        cpu = {"value": v, "unit": "Msamples/s", "cores": cores, "kind": "port",
+               "sample": f"{ns} samples (random pixels of the 1024^2 film x 1 spp, depth {DEPTH}) "
+                         f"in {t:.1f} s; octree build excluded"}
+
+    if rank == 0:
+        line = {
+            "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scene; no dataset)",
+            "config": {"workload": WORKLOAD, "resolution": [RES, RES], "spp": SPP,
+                       "max_depth": DEPTH, "triangles": sc.n_tris,
+                       "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                       "bvh_build_ms": st0["bvh_build_ms"], "bvh_nodes": st0["bvh_nodes"],
+                       "scene_gen_s": round(gen_s, 2)},
+            "mrays_per_s": mrays,
+            "rays_per_step": {"extension": rays_e / args.steps, "shadow": rays_s / args.steps},
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic,
+                         "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
+                         "extend_share_of_step": ext_ms / sum(step_ms),
+                         "per_extension_ray": {
+                             "node_visits": cs["ext_node_visits"] / cs["extension_rays"],
+                             "tri_tests": cs["ext_tri_tests"] / cs["extension_rays"]}},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

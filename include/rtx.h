@@ -1,0 +1,187 @@
+/*
+ * rtx.h — C ABI of librtx, the GB300 (sm_103a) implementation of RenderToy's
+ * path-tracing hot path: camera rays, closest-hit traversal, Moller-Trumbore,
+ * the principled BSDF with MIS and direct-light sampling, accumulation, the
+ * normal / albedo / depth passes and the Compositor filters.
+ *
+ * Plain C: pointers, sizes and int status codes; no C++ or torch types.
+ * Every entry point returns RTX_OK (0) or an RTX_ERR_* code; the message of the
+ * last failure on a context is rtx_last_error().  Nothing throws.
+ *
+ * Buffers: image, ray and hit arrays may be HOST or DEVICE memory; each call
+ * detects which (cudaPointerGetAttributes) and copies host data through its
+ * own device buffers.  Images are packed float3, row-major, pixel (x, y) at
+ * index y*W + x, row 0 at the bottom of the film (RenderToy's
+ * RenderContext::buffer, include/RenderToy/renderer.h:44-62).
+ *
+ * Threading: a context is used by one host thread at a time.  Work runs on the
+ * context's CUDA stream (rtx_get_stream / rtx_set_stream).  By default every
+ * call returns after its work is complete; with RTX_OPT_ASYNC = 1, calls whose
+ * buffers are all device memory return once their work is enqueued.
+ *
+ * Records shared with the caller:
+ *   material (RTX_MATERIAL_FLOATS = 24 floats) — PrincipledBSDF,
+ *     include/RenderToy/material.h:14-30:
+ *       [0..2] base_color  [3..5] emission  [6] roughness  [7] metallic
+ *       [8] anisotropic (unused by the BSDF, as in the reference)
+ *       [9] subsurface  [10] specular_tint  [11] sheen  [12] sheen_tint
+ *       [13] clearcoat  [14] clearcoat_roughness  [15] spec_trans  [16] ior
+ *       [17] at_distance  [18..20] extinction  [21..23] padding
+ *   camera (RTX_CAMERA_FLOATS = 21 floats) — Camera,
+ *     include/RenderToy/object.h:69-95:
+ *       [0..15] object-to-world 4x4, row-major  [16] focal length (mm)
+ *       [17..18] gate dimension (inches)  [19] near  [20] far
+ *   ray (6 floats): source xyz, direction xyz (not necessarily unit).
+ *
+ * Random numbers: RenderToy's shared mt19937 (src/rtmath.cpp:355-373) is
+ * replaced by a counter-based stream.  Draw k of the path (pixel p, sample s)
+ * is word (k & 3) of Philox4x32-10 (Salmon et al., SC'11) with key
+ * (seed low, seed high) and counter (k >> 2, s, p, 0); Random::Float is
+ * (w >> 8) * 2^-24 and Random::Int(a, b) is a + ((w * (b - a + 1)) >> 32).
+ * Each shaded vertex draws, in order: emitter index, two for the point on the
+ * emitter, two for the BSDF sample (src/world.cpp:9, src/object.cpp:171-172,
+ * src/material.cpp:214-215).
+ */
+#ifndef RTX_H
+#define RTX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTX_VERSION 1
+#define RTX_MATERIAL_FLOATS 24
+#define RTX_CAMERA_FLOATS 21
+
+enum rtx_status {
+  RTX_OK = 0,
+  RTX_ERR_INVALID = 1,   /* bad argument */
+  RTX_ERR_CUDA = 2,      /* CUDA runtime error */
+  RTX_ERR_NOMEM = 3,     /* device or host allocation failed */
+  RTX_ERR_NO_SCENE = 4,  /* render or trace before rtx_scene_upload */
+  RTX_ERR_DEVICE = 5     /* a kernel reported an error (see rtx_last_error) */
+};
+
+enum rtx_option {
+  RTX_OPT_ASYNC = 1,          /* 0/1: return before device-only work ends */
+  RTX_OPT_WAVE_PATHS = 2,     /* max paths in flight per wavefront (0 = auto) */
+  RTX_OPT_BLOCK = 3,          /* threads per block of the wavefront kernels */
+  RTX_OPT_SORT_MATERIAL = 4,  /* 0/1: sort hits by material before shading */
+  RTX_OPT_COUNT_VISITS = 5,   /* 0/1: count node visits and triangle tests */
+  RTX_OPT_LEAF_SIZE = 6,      /* max triangles per BVH leaf (1..8), next upload */
+  RTX_OPT_PRIMARY_CACHE = 7,  /* 0/1: trace each pixel's primary ray once */
+  RTX_OPT_KERNEL_TIMING = 8   /* 0/1: CUDA events around each traversal and
+                                 shading launch (rtx_stats.*_ms) */
+};
+
+typedef struct rtx_context rtx_context;
+
+typedef struct rtx_stats {
+  uint64_t extension_rays;   /* closest-hit rays of the last render */
+  uint64_t shadow_rays;      /* occlusion rays of the last render */
+  uint64_t ext_node_visits;  /* with RTX_OPT_COUNT_VISITS: BVH nodes fetched */
+  uint64_t ext_tri_tests;    /*   and triangles tested by closest-hit rays */
+  uint64_t shadow_node_visits; /* ... and by occlusion rays */
+  uint64_t shadow_tri_tests;
+  uint64_t kernel_launches;  /* kernels launched by the last call */
+  uint64_t extend_launches;  /* closest-hit traversal launches (last call) */
+  double last_gpu_ms;        /* device time of the last call (CUDA events) */
+  double extend_ms;          /* with RTX_OPT_KERNEL_TIMING: summed device time */
+  double shade_ms;           /*   of the closest-hit, shading and occlusion */
+  double connect_ms;         /*   launches of the last call */
+  double bvh_build_ms;       /* host time of the last BVH build */
+  int32_t bvh_nodes;         /* inner nodes of the current BVH */
+  int32_t bvh_leaves;
+  int32_t bvh_depth;
+  int32_t node_bytes;        /* bytes per BVH node record */
+  int32_t tri_bytes;         /* bytes per triangle record */
+  int32_t reserved;
+} rtx_stats;
+
+/* ---- context ------------------------------------------------------------ */
+int rtx_create(rtx_context** out, int device);
+void rtx_destroy(rtx_context* ctx);
+const char* rtx_last_error(const rtx_context* ctx);
+int rtx_version(void);
+int rtx_set_option(rtx_context* ctx, int option, int64_t value);
+int rtx_get_option(rtx_context* ctx, int option, int64_t* value);
+/* the CUDA stream (a cudaStream_t) work is enqueued on */
+void* rtx_get_stream(rtx_context* ctx);
+int rtx_set_stream(rtx_context* ctx, void* stream);
+int rtx_synchronize(rtx_context* ctx);
+int rtx_get_stats(rtx_context* ctx, rtx_stats* out);
+
+/* ---- scene ---------------------------------------------------------------
+ * Replaces RenderContext::RenderContext's BVH build (src/renderer.cpp:77-85,
+ * BVH::BVH src/bvh.cpp:242-264) and World::PrepareDirectLightSampling
+ * (src/world.cpp:24-37).  verts: n_tris x 9 world-space floats (v0, v1, v2 of
+ * World::triangles in order, Triangle::vert_w, include/RenderToy/object.h:161);
+ * norms: n_tris x 9 per-vertex normals (Triangle::norm; may be NULL when no
+ * mesh is smooth); tri_mesh: the mesh (Triangle::parent) of each triangle;
+ * mesh_mat / mesh_smooth: Mesh::tex as an index into materials, Mesh::smooth;
+ * sky / ground: World::sky_emission / ground_reflection.  Emitters are the
+ * triangles of meshes whose emission is not zero, in mesh order then triangle
+ * order, as the reference collects them.  The arrays are copied; the
+ * caller's buffers may be released on return. */
+int rtx_scene_upload(rtx_context* ctx, int n_tris, const float* verts,
+                     const float* norms, const int32_t* tri_mesh, int n_meshes,
+                     const int32_t* mesh_mat, const uint8_t* mesh_smooth,
+                     int n_materials, const float* materials, const float* sky,
+                     const float* ground);
+/* emitter triangle ids in sampling order; returns the count in *n_out */
+int rtx_scene_emitters(rtx_context* ctx, int32_t* out, int cap, int* n_out);
+
+/* ---- renderers ------------------------------------------------------------
+ * PathTracingRenderer::Render (src/renderer.cpp:236-270): out_rgb[p] =
+ * sum over samples s = 0..spp-1 of L(p, s) / spp, summed in sample order;
+ * max_depth = shaded vertices per path (the reference's fixed value is 5,
+ * src/renderer.cpp:274). */
+int rtx_render_pt(rtx_context* ctx, const float* camera, int W, int H, int spp,
+                  int max_depth, uint64_t seed, float* out_rgb);
+/* Per-path radiance L(p, s) for samples first_sample .. first_sample+n-1:
+ * out[(s - first_sample) * W*H + p] (PathTracingRenderer::Radiance,
+ * src/renderer.cpp:272-333, one call per (pixel, sample)). */
+int rtx_trace_paths(rtx_context* ctx, const float* camera, int W, int H,
+                    int first_sample, int n_samples, int max_depth,
+                    uint64_t seed, float* out_rgb);
+/* NormalRenderer / AlbedoRenderer / DepthBufferRenderer::Render
+ * (src/renderer.cpp:138-229, 391-427) in one primary pass; any output may be
+ * NULL.  near/far as DepthBufferRenderer(ctx, near, far). */
+int rtx_render_aov(rtx_context* ctx, const float* camera, int W, int H,
+                   float near_, float far_, float* out_normal,
+                   float* out_albedo, float* out_depth);
+/* BVH::Intersect (src/bvh.cpp:266-341) of the W x H primary rays:
+ * out_tri[p] (-1 on a miss), out_tuv[3p..3p+2] = t, u, v (1e7, 0, 0 on miss) */
+int rtx_primary_hits(rtx_context* ctx, const float* camera, int W, int H,
+                     int32_t* out_tri, float* out_tuv);
+/* BVH::Intersect of n arbitrary rays; exclude[i] = triangle skipped (-1 none;
+ * exclude may be NULL). */
+int rtx_intersect(rtx_context* ctx, int n, const float* rays,
+                  const int32_t* exclude, int32_t* out_tri, float* out_tuv);
+
+/* ---- compositor ------------------------------------------------------------
+ * Image operations (include/RenderToy/compositor.h:107-178,
+ * src/compositor.cpp:42-77) on packed float3 W x H images, in != out.
+ * Edge taps use the reference's reflect mapping (compositor.h:25-39); a tap
+ * whose linear index falls outside the image reads zero. */
+/* Image::Convolute<normalize, length, abs>(k): k is kr x kc, row-major */
+int rtx_image_convolve(rtx_context* ctx, const float* in, float* out, int W,
+                       int H, const float* kernel, int kr, int kc,
+                       int normalize, int length, int absval);
+/* Image::GaussianBlur(size, sigma) */
+int rtx_image_gaussian_blur(rtx_context* ctx, const float* in, float* out,
+                            int W, int H, int size, float sigma);
+/* Image::EdgeDetection<Orientation::All>() */
+int rtx_image_edge_detect(rtx_context* ctx, const float* in, float* out, int W,
+                          int H);
+/* Image::Bloom(size, sigma, threshold) */
+int rtx_image_bloom(rtx_context* ctx, const float* in, float* out, int W,
+                    int H, int size, float sigma, float threshold);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RTX_H */

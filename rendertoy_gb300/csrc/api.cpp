@@ -1,0 +1,727 @@
+// api.cpp — implementation of the C ABI declared in include/rtx.h.
+//
+// Host code here is compiled with -ffp-contract=off: the per-triangle data it
+// derives (edges, flat normal, area: RenderToy Triangle::UpdateCache,
+// src/object.cpp:224-243), the camera's film extents
+// (Renderer::PrepareScreenSpace, src/renderer.cpp:103-124) and the Gaussian
+// weights (UnitizedGaussianKernel, include/RenderToy/rtmath.h:1019-1059) are
+// computed in the reference's operation order, so they equal the reference's.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "rtx_internal.h"
+
+using namespace rtx;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max(bytes, (size_t)256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct V3 {
+  float x, y, z;
+};
+inline V3 sub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline float dot(V3 a, V3 b) {
+  float r = 0.0f;
+  r += a.x * b.x;
+  r += a.y * b.y;
+  r += a.z * b.z;
+  return r;
+}
+inline V3 cross(V3 a, V3 b) {
+  return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 normalized(V3 a) {
+  float l = std::sqrt(dot(a, a));
+  return V3{a.x / l, a.y / l, a.z / l};
+}
+
+}  // namespace
+
+struct rtx_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  // options
+  bool async = false;
+  int64_t wave_paths = 0;
+  int block = 128;
+  bool sort_material = false;
+  bool count_visits = false;
+  int leaf_size = 4;
+  bool primary_cache = false;
+  KernelTimer timer;
+  // scene
+  bool has_scene = false;
+  DeviceScene ds{};
+  DevBuf nodes, tris, shade, geo, mats, emit;
+  std::vector<int32_t> emitters;
+  // device scratch
+  int* d_err = nullptr;
+  Counters* d_counters = nullptr;
+  PtWorkspace* pt = nullptr;
+  DevBuf stage[4];
+  DevBuf weights;
+  std::vector<float> host_weights;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  rtx_stats stats{};
+  bool pending_timing = false;
+};
+
+namespace {
+
+int fail(rtx_context* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(rtx_context* c, cudaError_t e, const char* where) {
+  return fail(c, e == cudaErrorMemoryAllocation ? RTX_ERR_NOMEM : RTX_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+#define RTX_CUDA(call, where)                         \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, where); \
+  } while (0)
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Begin a call: select the device, clear the error word, start the timer.
+int begin(rtx_context* c) {
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream), "cudaMemsetAsync(err)");
+  RTX_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
+  c->stats.kernel_launches = 0;
+  return RTX_OK;
+}
+
+// End a call: stop the timer; synchronise unless the call may stay async.
+int finish(rtx_context* c, bool may_async) {
+  RTX_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
+  if (may_async && c->async) {
+    c->pending_timing = true;
+    return RTX_OK;
+  }
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  float ms = 0.0f;
+  RTX_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "cudaEventElapsedTime");
+  c->stats.last_gpu_ms = ms;
+  c->pending_timing = false;
+  int herr = 0;
+  RTX_CUDA(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read error word");
+  if (herr) {
+    std::string m = "kernel error:";
+    if (herr & kErrStackOverflow) m += " traversal stack overflow";
+    if (herr & kErrQueueOverflow) m += " queue overflow";
+    if (herr & kErrBadIndex) m += " index out of range";
+    return fail(c, RTX_ERR_DEVICE, m);
+  }
+  return RTX_OK;
+}
+
+// A caller buffer of `bytes`: device pointers are used in place, host
+// pointers are staged through stage[slot].
+struct Arg {
+  void* dev = nullptr;
+  void* host = nullptr;
+  size_t bytes = 0;
+};
+
+int bind_in(rtx_context* c, const void* p, size_t bytes, int slot, Arg& a) {
+  a.bytes = bytes;
+  if (!p || bytes == 0) return RTX_OK;
+  if (is_device_ptr(p)) {
+    a.dev = const_cast<void*>(p);
+    return RTX_OK;
+  }
+  RTX_CUDA(c->stage[slot].ensure(bytes), "stage alloc");
+  a.dev = c->stage[slot].p;
+  RTX_CUDA(cudaMemcpyAsync(a.dev, p, bytes, cudaMemcpyHostToDevice, c->stream), "H2D");
+  return RTX_OK;
+}
+
+int bind_out(rtx_context* c, void* p, size_t bytes, int slot, Arg& a) {
+  a.bytes = bytes;
+  if (!p || bytes == 0) return RTX_OK;
+  if (is_device_ptr(p)) {
+    a.dev = p;
+    return RTX_OK;
+  }
+  RTX_CUDA(c->stage[slot].ensure(bytes), "stage alloc");
+  a.dev = c->stage[slot].p;
+  a.host = p;
+  return RTX_OK;
+}
+
+int copy_back(rtx_context* c, const Arg& a) {
+  if (a.host)
+    RTX_CUDA(cudaMemcpyAsync(a.host, a.dev, a.bytes, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  return RTX_OK;
+}
+
+bool all_device(std::initializer_list<const Arg*> args) {
+  for (const Arg* a : args)
+    if (a->host) return false;
+  return true;
+}
+
+int check_cam(rtx_context* c, const float* cam, int W, int H) {
+  if (!cam) return fail(c, RTX_ERR_INVALID, "camera is NULL");
+  if (W <= 0 || H <= 0) return fail(c, RTX_ERR_INVALID, "image size must be positive");
+  if ((long long)W * H > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "image too large");
+  if (!c->has_scene) return fail(c, RTX_ERR_NO_SCENE, "no scene uploaded");
+  return RTX_OK;
+}
+
+// UnitizedGaussianKernel<float, X> weights (rtmath.h:1019-1059)
+void gaussian_weights(int size, float sigma, float* w) {
+  float orig = float(size >> 1);
+  float sum = 0.0f;
+  for (int j = 0; j < size; ++j) {
+    float x2 = std::pow(float(j) - orig, 2.0f);
+    float g = std::exp(-(x2) / (2.0f * sigma * sigma));
+    sum += g;
+    w[j] = g;
+  }
+  for (int j = 0; j < size; ++j) w[j] /= sum;
+}
+
+int upload_weights(rtx_context* c, const float* w, size_t n) {
+  c->host_weights.assign(w, w + n);
+  RTX_CUDA(c->weights.ensure(n * sizeof(float)), "weights alloc");
+  RTX_CUDA(cudaMemcpyAsync(c->weights.p, c->host_weights.data(), n * sizeof(float),
+                           cudaMemcpyHostToDevice, c->stream),
+           "weights H2D");
+  return RTX_OK;
+}
+
+}  // namespace
+
+namespace rtx {
+// Renderer::PrepareScreenSpace (renderer.cpp:103-124); InchToMM multiplies by
+// float(25.4) (rtmath.h:1098-1103)
+CamParams make_cam_params(const float* cam, int W, int H) {
+  CamParams k;
+  for (int i = 0; i < 12; ++i) k.m[i] = cam[i];
+  float focal = cam[16], gx = cam[17], gy = cam[18];
+  k.top = ((gy * 25.4f) / 2.0f) / focal;
+  k.right = ((gx * 25.4f) / 2.0f) / focal;
+  float gate_aspr = gx / gy;
+  float film_aspr = float(W) / float(H);
+  float xscale = 1.0f, yscale = 1.0f;
+  if (gate_aspr >= film_aspr)
+    xscale = film_aspr / gate_aspr;
+  else
+    yscale = gate_aspr / film_aspr;
+  k.right *= xscale;
+  k.top *= yscale;
+  k.inv_w = 1.0f / float(W);
+  k.inv_h = 1.0f / float(H);
+  k.W = W;
+  k.H = H;
+  return k;
+}
+}  // namespace rtx
+
+extern "C" {
+
+int rtx_version(void) { return RTX_VERSION; }
+
+int rtx_create(rtx_context** out, int device) {
+  if (!out) return RTX_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return RTX_ERR_CUDA;
+  }
+  if (device < 0 || device >= n) return RTX_ERR_INVALID;
+  rtx_context* c = new (std::nothrow) rtx_context();
+  if (!c) return RTX_ERR_NOMEM;
+  c->device = device;
+  auto bail = [&](cudaError_t e) {
+    cuda_fail(c, e, "rtx_create");
+    rtx_destroy(c);
+    return e == cudaErrorMemoryAllocation ? RTX_ERR_NOMEM : RTX_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e);
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e);
+  c->own_stream = true;
+  if ((e = cudaEventCreate(&c->ev0)) != cudaSuccess) return bail(e);
+  if ((e = cudaEventCreate(&c->ev1)) != cudaSuccess) return bail(e);
+  if ((e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess) return bail(e);
+  if ((e = cudaMalloc(&c->d_counters, sizeof(Counters))) != cudaSuccess) return bail(e);
+  if ((e = cudaMemset(c->d_counters, 0, sizeof(Counters))) != cudaSuccess) return bail(e);
+  c->pt = pt_workspace_create();
+  *out = c;
+  return RTX_OK;
+}
+
+void rtx_destroy(rtx_context* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->nodes.release();
+  c->tris.release();
+  c->shade.release();
+  c->geo.release();
+  c->mats.release();
+  c->emit.release();
+  for (auto& s : c->stage) s.release();
+  c->weights.release();
+  if (c->pt) pt_workspace_destroy(c->pt);
+  if (c->d_err) cudaFree(c->d_err);
+  if (c->d_counters) cudaFree(c->d_counters);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* rtx_last_error(const rtx_context* c) { return c ? c->err.c_str() : "null context"; }
+
+int rtx_set_option(rtx_context* c, int option, int64_t v) {
+  if (!c) return RTX_ERR_INVALID;
+  switch (option) {
+    case RTX_OPT_ASYNC: c->async = v != 0; return RTX_OK;
+    case RTX_OPT_WAVE_PATHS:
+      if (v < 0 || v > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "wave paths out of range");
+      c->wave_paths = v;
+      return RTX_OK;
+    case RTX_OPT_BLOCK:
+      if (v < 32 || v > 1024 || v % 32) return fail(c, RTX_ERR_INVALID, "block must be a multiple of 32 in [32, 1024]");
+      c->block = (int)v;
+      return RTX_OK;
+    case RTX_OPT_SORT_MATERIAL: c->sort_material = v != 0; return RTX_OK;
+    case RTX_OPT_COUNT_VISITS: c->count_visits = v != 0; return RTX_OK;
+    case RTX_OPT_LEAF_SIZE:
+      if (v < 1 || v > kMaxLeaf) return fail(c, RTX_ERR_INVALID, "leaf size must be in [1, 8]");
+      c->leaf_size = (int)v;
+      return RTX_OK;
+    case RTX_OPT_PRIMARY_CACHE: c->primary_cache = v != 0; return RTX_OK;
+    case RTX_OPT_KERNEL_TIMING: c->timer.on = v != 0; return RTX_OK;
+  }
+  return fail(c, RTX_ERR_INVALID, "unknown option");
+}
+
+int rtx_get_option(rtx_context* c, int option, int64_t* v) {
+  if (!c || !v) return RTX_ERR_INVALID;
+  switch (option) {
+    case RTX_OPT_ASYNC: *v = c->async; return RTX_OK;
+    case RTX_OPT_WAVE_PATHS: *v = c->wave_paths; return RTX_OK;
+    case RTX_OPT_BLOCK: *v = c->block; return RTX_OK;
+    case RTX_OPT_SORT_MATERIAL: *v = c->sort_material; return RTX_OK;
+    case RTX_OPT_COUNT_VISITS: *v = c->count_visits; return RTX_OK;
+    case RTX_OPT_LEAF_SIZE: *v = c->leaf_size; return RTX_OK;
+    case RTX_OPT_PRIMARY_CACHE: *v = c->primary_cache; return RTX_OK;
+    case RTX_OPT_KERNEL_TIMING: *v = c->timer.on; return RTX_OK;
+  }
+  return fail(c, RTX_ERR_INVALID, "unknown option");
+}
+
+void* rtx_get_stream(rtx_context* c) { return c ? (void*)c->stream : nullptr; }
+
+int rtx_set_stream(rtx_context* c, void* stream) {
+  if (!c) return RTX_ERR_INVALID;
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  c->stream = (cudaStream_t)stream;
+  c->own_stream = false;
+  return RTX_OK;
+}
+
+int rtx_synchronize(rtx_context* c) {
+  if (!c) return RTX_ERR_INVALID;
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  if (c->pending_timing) {
+    float ms = 0.0f;
+    RTX_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "cudaEventElapsedTime");
+    c->stats.last_gpu_ms = ms;
+    c->pending_timing = false;
+  }
+  int herr = 0;
+  RTX_CUDA(cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost), "read error word");
+  if (herr) return fail(c, RTX_ERR_DEVICE, "kernel error reported by an asynchronous call");
+  return RTX_OK;
+}
+
+int rtx_get_stats(rtx_context* c, rtx_stats* out) {
+  if (!c || !out) return RTX_ERR_INVALID;
+  int r = rtx_synchronize(c);
+  if (r) return r;
+  Counters h;
+  RTX_CUDA(cudaMemcpy(&h, c->d_counters, sizeof(Counters), cudaMemcpyDeviceToHost), "read counters");
+  c->stats.extension_rays = h.ext_rays;
+  c->stats.shadow_rays = h.shadow_rays;
+  c->stats.ext_node_visits = h.ext_node_visits;
+  c->stats.ext_tri_tests = h.ext_tri_tests;
+  c->stats.shadow_node_visits = h.sh_node_visits;
+  c->stats.shadow_tri_tests = h.sh_tri_tests;
+  RTX_CUDA(c->timer.collect(), "kernel timing");
+  c->stats.extend_ms = c->timer.ms[0];
+  c->stats.shade_ms = c->timer.ms[1];
+  c->stats.connect_ms = c->timer.ms[2];
+  *out = c->stats;
+  return RTX_OK;
+}
+
+int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* norms,
+                     const int32_t* tri_mesh, int n_meshes, const int32_t* mesh_mat,
+                     const uint8_t* mesh_smooth, int n_mat, const float* mats, const float* sky,
+                     const float* ground) {
+  if (!c) return RTX_ERR_INVALID;
+  if (n < 0 || n_meshes < 0 || n_mat < 0) return fail(c, RTX_ERR_INVALID, "negative count");
+  if (n > (1 << 27)) return fail(c, RTX_ERR_INVALID, "more than 2^27 triangles");
+  if (n > 0 && (!verts || !tri_mesh)) return fail(c, RTX_ERR_INVALID, "verts / tri_mesh is NULL");
+  if (n_meshes > 0 && (!mesh_mat || !mesh_smooth)) return fail(c, RTX_ERR_INVALID, "mesh arrays are NULL");
+  if (n_mat > 0 && !mats) return fail(c, RTX_ERR_INVALID, "materials is NULL");
+  if (!sky || !ground) return fail(c, RTX_ERR_INVALID, "sky / ground is NULL");
+  for (int m = 0; m < n_meshes; ++m)
+    if (mesh_mat[m] < 0 || mesh_mat[m] >= n_mat) return fail(c, RTX_ERR_INVALID, "mesh material index out of range");
+  bool any_smooth = false;
+  for (int m = 0; m < n_meshes; ++m) any_smooth |= mesh_smooth[m] != 0;
+  if (any_smooth && !norms) return fail(c, RTX_ERR_INVALID, "a smooth mesh needs vertex normals");
+  for (int i = 0; i < n; ++i)
+    if (tri_mesh[i] < 0 || tri_mesh[i] >= n_meshes) return fail(c, RTX_ERR_INVALID, "triangle mesh index out of range");
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+
+  // Mesh's identity object-to-world turns -0.0 into +0.0 (object.cpp:42-48)
+  std::vector<float> v((size_t)n * 9);
+  for (size_t i = 0; i < v.size(); ++i) v[i] = verts[i] + 0.0f;
+
+  BvhBuildResult b = build_bvh(v.data(), n, c->leaf_size);
+
+  std::vector<float4> shade((size_t)n * 4), geo((size_t)n * 3);
+  for (int i = 0; i < n; ++i) {
+    const float* p = &v[9 * (size_t)i];
+    V3 v0{p[0], p[1], p[2]}, v1{p[3], p[4], p[5]}, v2{p[6], p[7], p[8]};
+    V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+    V3 cr = cross(e1, e2);
+    float area = std::sqrt(dot(cr, cr)) * 0.5f;        // Triangle::Area
+    V3 nrm = normalized(cross(normalized(e1), sub(v2, v1)));  // Triangle::Normal
+    int mesh = tri_mesh[i];
+    uint32_t info = (uint32_t)mesh_mat[mesh] | (mesh_smooth[mesh] ? 0x80000000u : 0u);
+    float infof;
+    std::memcpy(&infof, &info, 4);
+    const float* q = norms ? norms + 9 * (size_t)i : nullptr;
+    shade[4 * (size_t)i] = make_float4(nrm.x, nrm.y, nrm.z, area);
+    shade[4 * (size_t)i + 1] = make_float4(q ? q[0] : 0.f, q ? q[1] : 0.f, q ? q[2] : 0.f, infof);
+    shade[4 * (size_t)i + 2] = make_float4(q ? q[3] : 0.f, q ? q[4] : 0.f, q ? q[5] : 0.f, 0.f);
+    shade[4 * (size_t)i + 3] = make_float4(q ? q[6] : 0.f, q ? q[7] : 0.f, q ? q[8] : 0.f, 0.f);
+    geo[3 * (size_t)i] = make_float4(v0.x, v0.y, v0.z, 0.f);
+    geo[3 * (size_t)i + 1] = make_float4(e1.x, e1.y, e1.z, 0.f);
+    geo[3 * (size_t)i + 2] = make_float4(e2.x, e2.y, e2.z, 0.f);
+  }
+  // World::PrepareDirectLightSampling (world.cpp:24-37)
+  std::vector<std::vector<int>> per_mesh(n_meshes);
+  for (int i = 0; i < n; ++i) per_mesh[tri_mesh[i]].push_back(i);
+  c->emitters.clear();
+  for (int m = 0; m < n_meshes; ++m) {
+    const float* em = mats + RTX_MATERIAL_FLOATS * (size_t)mesh_mat[m] + 3;
+    bool emissive = std::fabs(em[0]) > 1e-7f || std::fabs(em[1]) > 1e-7f || std::fabs(em[2]) > 1e-7f;
+    if (emissive)
+      for (int t : per_mesh[m]) c->emitters.push_back(t);
+  }
+
+  auto up = [&](DevBuf& d, const void* src, size_t bytes, const char* what) -> int {
+    RTX_CUDA(d.ensure(bytes), what);
+    if (bytes) RTX_CUDA(cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice), what);
+    return RTX_OK;
+  };
+  int r;
+  if ((r = up(c->nodes, b.nodes.data(), b.nodes.size() * sizeof(float4), "upload nodes"))) return r;
+  if ((r = up(c->tris, b.tris.data(), b.tris.size() * sizeof(float4), "upload tris"))) return r;
+  if ((r = up(c->shade, shade.data(), shade.size() * sizeof(float4), "upload shade"))) return r;
+  if ((r = up(c->geo, geo.data(), geo.size() * sizeof(float4), "upload geo"))) return r;
+  if ((r = up(c->mats, mats, (size_t)n_mat * RTX_MATERIAL_FLOATS * sizeof(float), "upload mats"))) return r;
+  if ((r = up(c->emit, c->emitters.data(), c->emitters.size() * sizeof(int32_t), "upload emitters"))) return r;
+
+  DeviceScene& s = c->ds;
+  s.nodes = (const float4*)c->nodes.p;
+  s.tris = (const float4*)c->tris.p;
+  s.shade = (const float4*)c->shade.p;
+  s.geo = (const float4*)c->geo.p;
+  s.mats = (const float*)c->mats.p;
+  s.emitters = (const int*)c->emit.p;
+  s.root = b.root;
+  s.n_tris = n;
+  s.n_emitters = (int)c->emitters.size();
+  s.n_mats = n_mat;
+  for (int k = 0; k < 3; ++k) {
+    s.sky[k] = sky[k];
+    s.ground[k] = ground[k];
+  }
+  c->has_scene = true;
+  c->stats.bvh_build_ms = b.ms;
+  c->stats.bvh_nodes = b.n_nodes;
+  c->stats.bvh_leaves = b.n_leaves;
+  c->stats.bvh_depth = b.depth;
+  c->stats.node_bytes = 64;
+  c->stats.tri_bytes = 48;
+  return RTX_OK;
+}
+
+int rtx_scene_emitters(rtx_context* c, int32_t* out, int cap, int* n_out) {
+  if (!c || !n_out) return RTX_ERR_INVALID;
+  if (!c->has_scene) return fail(c, RTX_ERR_NO_SCENE, "no scene uploaded");
+  *n_out = (int)c->emitters.size();
+  if (out)
+    for (int i = 0; i < *n_out && i < cap; ++i) out[i] = c->emitters[i];
+  return RTX_OK;
+}
+
+static int render_paths(rtx_context* c, const float* cam, int W, int H, int first, int n_samples,
+                        int spp, int max_depth, uint64_t seed, float* out, bool per_path) {
+  if (!c) return RTX_ERR_INVALID;
+  int r;
+  if ((r = check_cam(c, cam, W, H))) return r;
+  if (!out) return fail(c, RTX_ERR_INVALID, "output is NULL");
+  if (n_samples < 0 || spp < 0 || first < 0) return fail(c, RTX_ERR_INVALID, "negative sample count");
+  if (max_depth < 1 || max_depth > 63) return fail(c, RTX_ERR_INVALID, "max_depth must be in [1, 63]");
+  size_t npix = (size_t)W * H;
+  size_t out_elems = per_path ? npix * (size_t)n_samples : npix;
+  if ((r = begin(c))) return r;
+  Arg o;
+  if ((r = bind_out(c, out, out_elems * 3 * sizeof(float), 0, o))) return r;
+  CamParams cp = make_cam_params(cam, W, H);
+  PtParams p;
+  p.W = W;
+  p.H = H;
+  p.spp = spp;
+  p.first_sample = first;
+  p.n_samples = n_samples;
+  p.max_depth = max_depth;
+  p.seed = seed;
+  p.wave_paths = (int)c->wave_paths;
+  p.block = c->block;
+  p.per_path = per_path;
+  p.count_visits = c->count_visits;
+  p.primary_cache = c->primary_cache;
+  RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
+  int launches = 0, ext_launches = 0;
+  std::string why;
+  RTX_CUDA(c->timer.collect(), "kernel timing");
+  c->timer.reset();
+  cudaError_t e = pt_render(c->pt, c->ds, cp, p, (float*)o.dev, c->d_err, c->d_counters,
+                            &c->timer, c->stream, &launches, &ext_launches, &why);
+  c->stats.kernel_launches = launches;
+  c->stats.extend_launches = ext_launches;
+  if (e != cudaSuccess) {
+    if (!why.empty()) return fail(c, RTX_ERR_INVALID, why);
+    return cuda_fail(c, e, "pt_render");
+  }
+  if ((r = copy_back(c, o))) return r;
+  return finish(c, all_device({&o}));
+}
+
+int rtx_render_pt(rtx_context* c, const float* cam, int W, int H, int spp, int max_depth,
+                  uint64_t seed, float* out) {
+  if (c && spp <= 0) return fail(c, RTX_ERR_INVALID, "spp must be positive");
+  return render_paths(c, cam, W, H, 0, spp, spp, max_depth, seed, out, false);
+}
+
+int rtx_trace_paths(rtx_context* c, const float* cam, int W, int H, int first_sample,
+                    int n_samples, int max_depth, uint64_t seed, float* out) {
+  return render_paths(c, cam, W, H, first_sample, n_samples, 1, max_depth, seed, out, true);
+}
+
+static int primary_pass(rtx_context* c, const float* cam, int W, int H, int mode, float near_,
+                        float far_, float* n_out, float* a_out, float* d_out, int32_t* tri_out,
+                        float* tuv_out) {
+  if (!c) return RTX_ERR_INVALID;
+  int r;
+  if ((r = check_cam(c, cam, W, H))) return r;
+  size_t npix = (size_t)W * H;
+  if ((r = begin(c))) return r;
+  Arg an, aa, ad, at, au;
+  if ((r = bind_out(c, n_out, npix * 12, 0, an))) return r;
+  if ((r = bind_out(c, a_out, npix * 12, 1, aa))) return r;
+  if ((r = bind_out(c, d_out, npix * 12, 2, ad))) return r;
+  if (mode & 2) {
+    if (!tri_out || !tuv_out) return fail(c, RTX_ERR_INVALID, "hit outputs are NULL");
+    if ((r = bind_out(c, tri_out, npix * 4, 0, at))) return r;
+    if ((r = bind_out(c, tuv_out, npix * 12, 1, au))) return r;
+  }
+  CamParams cp = make_cam_params(cam, W, H);
+  int launches = 0;
+  cudaError_t e = launch_primary(c->ds, cp, mode, near_, far_, (float*)an.dev, (float*)aa.dev,
+                                 (float*)ad.dev, (int*)at.dev, (float*)au.dev, c->d_err,
+                                 c->stream, &launches);
+  c->stats.kernel_launches = launches;
+  if (e != cudaSuccess) return cuda_fail(c, e, "primary kernel");
+  for (const Arg* a : {&an, &aa, &ad, &at, &au})
+    if ((r = copy_back(c, *a))) return r;
+  return finish(c, all_device({&an, &aa, &ad, &at, &au}));
+}
+
+int rtx_render_aov(rtx_context* c, const float* cam, int W, int H, float near_, float far_,
+                   float* n_out, float* a_out, float* d_out) {
+  return primary_pass(c, cam, W, H, 1, near_, far_, n_out, a_out, d_out, nullptr, nullptr);
+}
+
+int rtx_primary_hits(rtx_context* c, const float* cam, int W, int H, int32_t* tri, float* tuv) {
+  return primary_pass(c, cam, W, H, 2, 0.0f, 1.0f, nullptr, nullptr, nullptr, tri, tuv);
+}
+
+int rtx_intersect(rtx_context* c, int n, const float* rays, const int32_t* exclude,
+                  int32_t* tri_out, float* tuv_out) {
+  if (!c) return RTX_ERR_INVALID;
+  if (n < 0) return fail(c, RTX_ERR_INVALID, "negative ray count");
+  if (!c->has_scene) return fail(c, RTX_ERR_NO_SCENE, "no scene uploaded");
+  if (n == 0) return RTX_OK;
+  if (!rays || !tri_out || !tuv_out) return fail(c, RTX_ERR_INVALID, "NULL buffer");
+  int r;
+  if ((r = begin(c))) return r;
+  Arg ar, ae, at, au;
+  if ((r = bind_in(c, rays, (size_t)n * 24, 0, ar))) return r;
+  if ((r = bind_in(c, exclude, exclude ? (size_t)n * 4 : 0, 1, ae))) return r;
+  if ((r = bind_out(c, tri_out, (size_t)n * 4, 2, at))) return r;
+  if ((r = bind_out(c, tuv_out, (size_t)n * 12, 3, au))) return r;
+  int launches = 0;
+  cudaError_t e = launch_intersect(c->ds, n, (const float*)ar.dev, (const int*)ae.dev,
+                                   (int*)at.dev, (float*)au.dev, c->d_err, c->stream, &launches);
+  c->stats.kernel_launches = launches;
+  if (e != cudaSuccess) return cuda_fail(c, e, "intersect kernel");
+  if ((r = copy_back(c, at))) return r;
+  if ((r = copy_back(c, au))) return r;
+  return finish(c, all_device({&ar, &ae, &at, &au}));
+}
+
+// Bind an image input; when it aliases the output (the reference filters in
+// place) it is first copied so that no kernel reads what it writes.
+static int bind_image_in(rtx_context* c, const float* in, float* out, size_t bytes, int slot,
+                         Arg& a) {
+  int r;
+  if ((r = bind_in(c, in, bytes, slot, a))) return r;
+  if (a.dev == out) {
+    RTX_CUDA(c->stage[slot].ensure(bytes), "stage alloc");
+    RTX_CUDA(cudaMemcpyAsync(c->stage[slot].p, in, bytes, cudaMemcpyDeviceToDevice, c->stream), "copy");
+    a.dev = c->stage[slot].p;
+  }
+  return RTX_OK;
+}
+
+static int check_image(rtx_context* c, const float* in, float* out, int W, int H) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!in || !out) return fail(c, RTX_ERR_INVALID, "NULL image");
+  if (W <= 0 || H <= 0) return fail(c, RTX_ERR_INVALID, "image size must be positive");
+  if ((long long)W * H > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "image too large");
+  return RTX_OK;
+}
+
+int rtx_image_convolve(rtx_context* c, const float* in, float* out, int W, int H,
+                       const float* kernel, int kr, int kc, int normalize, int length,
+                       int absval) {
+  int r;
+  if ((r = check_image(c, in, out, W, H))) return r;
+  if (!kernel || kr <= 0 || kc <= 0 || (long long)kr * kc > (1 << 20))
+    return fail(c, RTX_ERR_INVALID, "bad kernel");
+  size_t bytes = (size_t)W * H * 12;
+  if ((r = begin(c))) return r;
+  Arg ai, ao;
+  if ((r = bind_out(c, out, bytes, 1, ao))) return r;
+  if ((r = bind_image_in(c, in, (float*)ao.dev, bytes, 0, ai))) return r;
+  if ((r = upload_weights(c, kernel, (size_t)kr * kc))) return r;
+  int flags = (absval ? 1 : 0) | (length ? 2 : 0) | (normalize ? 4 : 0);
+  int launches = 0;
+  cudaError_t e = launch_convolve((const float*)ai.dev, (float*)ao.dev, W, H,
+                                  (const float*)c->weights.p, kr, kc, flags, c->stream, &launches);
+  c->stats.kernel_launches = launches;
+  if (e != cudaSuccess) return cuda_fail(c, e, "convolve kernel");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&ai, &ao}));
+}
+
+static int gaussian_common(rtx_context* c, const float* in, float* out, int W, int H, int size,
+                           float sigma, bool bloom, float threshold) {
+  int r;
+  if ((r = check_image(c, in, out, W, H))) return r;
+  if (size <= 0 || size > (1 << 16)) return fail(c, RTX_ERR_INVALID, "bad kernel size");
+  size_t bytes = (size_t)W * H * 12;
+  if ((r = begin(c))) return r;
+  Arg ai, ao;
+  if ((r = bind_out(c, out, bytes, 1, ao))) return r;
+  if ((r = bind_image_in(c, in, (float*)ao.dev, bytes, 0, ai))) return r;
+  std::vector<float> w(size);
+  gaussian_weights(size, sigma, w.data());
+  if ((r = upload_weights(c, w.data(), w.size()))) return r;
+  RTX_CUDA(c->stage[2].ensure(bytes), "stage alloc");
+  if (bloom) RTX_CUDA(c->stage[3].ensure(bytes), "stage alloc");
+  int launches = 0;
+  cudaError_t e = launch_gaussian((const float*)ai.dev, (float*)c->stage[2].p,
+                                  bloom ? (float*)c->stage[3].p : nullptr, (float*)ao.dev, W, H,
+                                  (const float*)c->weights.p, size, bloom ? 1 : 0, threshold,
+                                  c->stream, &launches);
+  c->stats.kernel_launches = launches;
+  if (e != cudaSuccess) return cuda_fail(c, e, "gaussian kernels");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&ai, &ao}));
+}
+
+int rtx_image_gaussian_blur(rtx_context* c, const float* in, float* out, int W, int H, int size,
+                            float sigma) {
+  return gaussian_common(c, in, out, W, H, size, sigma, false, 0.0f);
+}
+
+int rtx_image_bloom(rtx_context* c, const float* in, float* out, int W, int H, int size,
+                    float sigma, float threshold) {
+  return gaussian_common(c, in, out, W, H, size, sigma, true, threshold);
+}
+
+int rtx_image_edge_detect(rtx_context* c, const float* in, float* out, int W, int H) {
+  int r;
+  if ((r = check_image(c, in, out, W, H))) return r;
+  size_t bytes = (size_t)W * H * 12;
+  if ((r = begin(c))) return r;
+  Arg ai, ao;
+  if ((r = bind_out(c, out, bytes, 1, ao))) return r;
+  if ((r = bind_image_in(c, in, (float*)ao.dev, bytes, 0, ai))) return r;
+  int launches = 0;
+  cudaError_t e = launch_edge((const float*)ai.dev, (float*)ao.dev, W, H, c->stream, &launches);
+  c->stats.kernel_launches = launches;
+  if (e != cudaSuccess) return cuda_fail(c, e, "edge kernel");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&ai, &ao}));
+}
+
+}  // extern "C"

@@ -1,0 +1,398 @@
+// device_math.cuh — float3 arithmetic, principled BSDF and RNG on the device,
+// in RenderToy's evaluation order.
+//
+// This header is compiled with --fmad=false: no multiply-add is fused unless
+// written as __fmaf_rn, so +, -, *, / and sqrtf round exactly as in the
+// reference's x86/Arm builds; only the transcendental functions (sinf, cosf,
+// powf, logf) may differ by an ulp from the host C library.
+//
+// Each function names the reference function it restates
+// (RenderToy src/rtmath.cpp, src/material.cpp, include/RenderToy/rtmath.h).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rtx {
+
+#define RTX_DEV __device__ __forceinline__
+
+struct F3 {
+  float x, y, z;
+};
+RTX_DEV F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+RTX_DEV F3 f3s(float s) { return F3{s, s, s}; }
+RTX_DEV F3 operator+(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+RTX_DEV F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+RTX_DEV F3 operator-(F3 a) { return F3{-a.x, -a.y, -a.z}; }
+RTX_DEV F3 operator*(F3 a, F3 b) { return F3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+RTX_DEV F3 operator*(F3 a, float s) { return F3{a.x * s, a.y * s, a.z * s}; }
+RTX_DEV F3 operator/(F3 a, float s) { return F3{a.x / s, a.y / s, a.z / s}; }
+// Vector::Dot (rtmath.h:328-338): accumulate from zero, x, y, z
+RTX_DEV float dot(F3 a, F3 b) {
+  float r = 0.0f;
+  r = r + a.x * b.x;
+  r = r + a.y * b.y;
+  r = r + a.z * b.z;
+  return r;
+}
+RTX_DEV float length(F3 a) { return sqrtf(dot(a, a)); }
+// Vector::Normalize (rtmath.h:144-150): divide by the length
+RTX_DEV F3 normalized(F3 a) {
+  float l = length(a);
+  return F3{a.x / l, a.y / l, a.z / l};
+}
+RTX_DEV F3 cross(F3 a, F3 b) {
+  return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// Vector::operator== (rtmath.h:296-308): epsilon test; NaN compares equal
+RTX_DEV bool eq_zero_eps(F3 a) {
+  if (fabsf(a.x) > 1e-7f) return false;
+  if (fabsf(a.y) > 1e-7f) return false;
+  if (fabsf(a.z) > 1e-7f) return false;
+  return true;
+}
+RTX_DEV float lerp(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+RTX_DEV F3 lerpv(F3 x, F3 y, F3 a) { return x * (f3s(1.0f) - a) + y * a; }
+RTX_DEV float luma(F3 v) { return 0.2126f * v.x + 0.7152f * v.y + 0.0722f * v.z; }
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInf = 1e7f;
+constexpr float kE = 2.718281828459045235360287471352662498f;
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 stream (see include/rtx.h)
+// ---------------------------------------------------------------------------
+RTX_DEV uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+struct Rng {
+  uint32_t k0, k1, pixel, sample, draw;
+  RTX_DEV uint32_t next_u32() {
+    uint4 r = philox4x32_10(make_uint4(draw >> 2, sample, pixel, 0u), k0, k1);
+    uint32_t s = draw & 3u;
+    ++draw;
+    return s == 0 ? r.x : (s == 1 ? r.y : (s == 2 ? r.z : r.w));
+  }
+  RTX_DEV float uniform() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+  RTX_DEV int uniform_int(int a, int b) {
+    uint32_t n = (uint32_t)(b - a + 1);
+    return a + (int)(((uint64_t)next_u32() * (uint64_t)n) >> 32);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Material record (24 floats, include/rtx.h)
+// ---------------------------------------------------------------------------
+struct Mat {
+  F3 base_color, emission;
+  float roughness, metallic, subsurface, specular_tint, sheen, sheen_tint,
+      clearcoat, clearcoat_roughness, spec_trans, ior, at_distance;
+  F3 extinction;
+};
+
+RTX_DEV Mat load_mat(const float* __restrict__ m) {
+  Mat r;
+  r.base_color = f3(__ldg(m + 0), __ldg(m + 1), __ldg(m + 2));
+  r.emission = f3(__ldg(m + 3), __ldg(m + 4), __ldg(m + 5));
+  r.roughness = __ldg(m + 6);
+  r.metallic = __ldg(m + 7);
+  r.subsurface = __ldg(m + 9);
+  r.specular_tint = __ldg(m + 10);
+  r.sheen = __ldg(m + 11);
+  r.sheen_tint = __ldg(m + 12);
+  r.clearcoat = __ldg(m + 13);
+  r.clearcoat_roughness = __ldg(m + 14);
+  r.spec_trans = __ldg(m + 15);
+  r.ior = __ldg(m + 16);
+  r.at_distance = __ldg(m + 17);
+  r.extinction = f3(__ldg(m + 18), __ldg(m + 19), __ldg(m + 20));
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// PBR helpers (src/rtmath.cpp:169-353)
+// ---------------------------------------------------------------------------
+// std::clamp(x, 0, 1): NaN passes through as in the reference
+RTX_DEV float clamp01(float x) { return x < 0.0f ? 0.0f : (1.0f < x ? 1.0f : x); }
+RTX_DEV float GTR1(float NdotH, float a) {
+  if (a >= 1.0f) return 1.0f / kPi;
+  float a2 = a * a;
+  float t = 1.0f + (a2 - 1.0f) * NdotH * NdotH;
+  return (a2 - 1.0f) / (kPi * logf(a2) * t);
+}
+RTX_DEV F3 SampleGTR1(float rgh, float r1) {
+  float a = fmaxf(0.001f, rgh);
+  float a2 = a * a;
+  float phi = r1 * 2.0f * kPi;
+  float cos_theta = sqrtf((1.0f - powf(a2, 1.0f - r1)) / (1.0f - a2));
+  float sin_theta = clamp01(sqrtf(1.0f - (cos_theta * cos_theta)));
+  float sin_phi = sinf(phi);
+  float cos_phi = cosf(phi);
+  return f3(sin_theta * cos_phi, sin_theta * sin_phi, cos_theta);
+}
+RTX_DEV float GTR2(float NdotH, float a) {
+  float a2 = a * a;
+  float t = 1.0f + (a2 - 1.0f) * NdotH * NdotH;
+  return a2 / (kPi * t * t);
+}
+RTX_DEV F3 SampleGGXVNDF(F3 V, float rgh, float r1, float r2) {
+  F3 Vh = normalized(f3(rgh * V.x, rgh * V.y, V.z));
+  float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+  F3 T1 = lensq > 0.0f ? f3(-Vh.y, Vh.x, 0.0f) * (1.0f / sqrtf(lensq)) : f3(1.0f, 0.0f, 0.0f);
+  F3 T2 = cross(Vh, T1);
+  float r = sqrtf(r1);
+  float phi = 2.0f * kPi * r2;
+  float t1 = r * cosf(phi);
+  float t2 = r * sinf(phi);
+  float s = 0.5f * (1.0f + Vh.z);
+  t2 = (1.0f - s) * sqrtf(1.0f - t1 * t1) + s * t2;
+  F3 Nh = (T1 * t1 + T2 * t2) + Vh * sqrtf(fmaxf(0.0f, 1.0f - t1 * t1 - t2 * t2));
+  return normalized(f3(rgh * Nh.x, rgh * Nh.y, fmaxf(0.0f, Nh.z)));
+}
+RTX_DEV float SmithG(float NdotV, float alpha_g) {
+  float a = alpha_g * alpha_g;
+  float b = NdotV * NdotV;
+  return (2.0f * NdotV) / (NdotV + sqrtf(a + b - a * b));
+}
+RTX_DEV float SchlickFresnel(float u) {
+  float m = clamp01(1.0f - u);
+  float m2 = m * m;
+  return m2 * m2 * m;
+}
+// std::max(a, b) returns a unless a < b
+RTX_DEV float smax(float a, float b) { return (a < b) ? b : a; }
+RTX_DEV float DielectricFresnel(float cos_theta_i, float eta) {
+  float sin_theta_t_sq = eta * eta * (1.0f - cos_theta_i * cos_theta_i);
+  if (sin_theta_t_sq > 1.0f) return 1.0f;
+  float cos_theta_t = sqrtf(smax(1.0f - sin_theta_t_sq, 0.0f));
+  float rs = (eta * cos_theta_t - cos_theta_i) / (eta * cos_theta_t + cos_theta_i);
+  float rp = (eta * cos_theta_i - cos_theta_t) / (eta * cos_theta_i + cos_theta_t);
+  return 0.5f * (rs * rs + rp * rp);
+}
+RTX_DEV F3 CosineSampleHemisphere(float r1, float r2) {
+  F3 d;
+  float r = sqrtf(r1);
+  float phi = 2.0f * kPi * r2;
+  d.x = r * cosf(phi);
+  d.y = r * sinf(phi);
+  d.z = sqrtf(smax(0.0f, 1.0f - d.x * d.x - d.y * d.y));
+  return d;
+}
+RTX_DEV float PowerHeuristic(float a, float b) {
+  float t = a * a;
+  return t / (b * b + t);
+}
+RTX_DEV void Onb(F3 N, F3& T, F3& B) {
+  F3 up = fabsf(N.z) < 0.999f ? f3(0.0f, 0.0f, 1.0f) : f3(1.0f, 0.0f, 0.0f);
+  T = normalized(cross(up, N));
+  B = cross(N, T);
+}
+RTX_DEV F3 ToWorld(F3 X, F3 Y, F3 Z, F3 V) { return (X * V.x + Y * V.y) + Z * V.z; }
+RTX_DEV F3 ToLocal(F3 X, F3 Y, F3 Z, F3 V) { return f3(dot(V, X), dot(V, Y), dot(V, Z)); }
+RTX_DEV F3 Reflect(F3 I, F3 N) { return I - N * (2.0f * dot(I, N)); }
+RTX_DEV F3 Refract(F3 I, F3 N, float eta) {
+  float NdotI = dot(N, I);
+  float k = 1.f - eta * eta * (1.f - NdotI * NdotI);
+  if (k < 0.f) return f3(0.f, 0.f, 0.f);
+  return I * eta - N * (eta * NdotI + sqrtf(k));
+}
+
+// ---------------------------------------------------------------------------
+// PrincipledBSDF (src/material.cpp:35-295)
+// ---------------------------------------------------------------------------
+RTX_DEV float FresnelMix(const Mat& m, float eta, float VdotH) {
+  float mf = SchlickFresnel(VdotH);
+  float df = DielectricFresnel(VdotH, eta);
+  return lerp(df, mf, m.metallic);
+}
+RTX_DEV F3 EvalDiffuse(const Mat& m, F3 Csheen, F3 V, F3 L, F3 H, float& pdf) {
+  pdf = 0.0f;
+  if (L.z <= 0.0f) return f3s(0.0f);
+  float FL = SchlickFresnel(L.z);
+  float FV = SchlickFresnel(V.z);
+  float FH = SchlickFresnel(dot(L, H));
+  float Fd90 = 0.5f + 2.0f * dot(L, H) * dot(L, H) * m.roughness;
+  float Fd = lerp(1.0f, Fd90, FL) * lerp(1.0f, Fd90, FV);
+  float Fss90 = dot(L, H) * dot(L, H) * m.roughness;
+  float Fss = lerp(1.0f, Fss90, FL) * lerp(1.0f, Fss90, FV);
+  float ss = 1.25f * (Fss * (1.0f / (L.z + V.z) - 0.5f) + 0.5f);
+  F3 Fsheen = Csheen * (FH * m.sheen);
+  pdf = L.z * (1.0f / kPi);
+  F3 r = m.base_color * ((1.0f / kPi) * lerp(Fd, ss, m.subsurface));
+  r = r + Fsheen;
+  r = r * (1.0f - m.metallic);
+  r = r * (1.0f - m.spec_trans);
+  return r;
+}
+RTX_DEV F3 EvalSpecReflection(const Mat& m, float eta, F3 specCol, F3 V, F3 L, F3 H,
+                              float& pdf) {
+  pdf = 0.0f;
+  if (L.z <= 0.0f) return f3s(0.0f);
+  float FM = FresnelMix(m, eta, dot(L, H));
+  F3 F = lerpv(specCol, f3s(1.0f), f3s(FM));
+  float D = GTR2(H.z, m.roughness);
+  float G1 = SmithG(fabsf(V.z), m.roughness);
+  float G2 = G1 * SmithG(fabsf(L.z), m.roughness);
+  float jacobian = 1.0f / (4.0f * dot(V, H));
+  pdf = G1 * smax(0.0f, dot(V, H)) * D * jacobian / V.z;
+  F3 r = F * D;
+  r = r * G2;
+  return r / (4.0f * L.z * V.z);
+}
+RTX_DEV F3 EvalSpecRefraction(const Mat& m, float eta, F3 V, F3 L, F3 H, float& pdf) {
+  pdf = 0.0f;
+  if (L.z >= 0.0f) return f3s(0.0f);
+  float F = DielectricFresnel(fabsf(dot(V, H)), eta);
+  float D = GTR2(H.z, m.roughness);
+  float denom = dot(L, H) + dot(V, H) * eta;
+  denom *= denom;
+  float G1 = SmithG(fabsf(V.z), m.roughness);
+  float G2 = G1 * SmithG(fabsf(L.z), m.roughness);
+  float jacobian = fabsf(dot(L, H)) / denom;
+  pdf = G1 * smax(0.0f, dot(V, H)) * D * jacobian / V.z;
+  F3 spec_color = f3(powf(m.base_color.x, 0.5f), powf(m.base_color.y, 0.5f),
+                     powf(m.base_color.z, 0.5f));
+  F3 r = spec_color * (1.0f - m.metallic);
+  r = r * m.spec_trans;
+  r = r * (1.0f - F);
+  r = r * D;
+  r = r * G2;
+  r = r * fabsf(dot(V, H));
+  r = r * fabsf(dot(L, H));
+  r = r * eta;
+  r = r * eta;
+  return r / (denom * fabsf(L.z) * fabsf(V.z));
+}
+RTX_DEV F3 EvalClearcoat(const Mat& m, F3 V, F3 L, F3 H, float& pdf) {
+  pdf = 0.0f;
+  if (L.z <= 0.0f) return f3s(0.0f);
+  float FH = DielectricFresnel(dot(V, H), 1.0f / 1.5f);
+  float F = lerp(0.04f, 1.0f, FH);
+  float D = GTR1(H.z, m.clearcoat_roughness);
+  float G = SmithG(L.z, 0.25f) * SmithG(V.z, 0.25f);
+  float jacobian = 1.0f / (4.0f * dot(V, H));
+  pdf = D * H.z * jacobian;
+  F3 r = f3s(0.25f) * m.clearcoat;
+  r = r * F;
+  r = r * D;
+  r = r * G;
+  return r / (4.0f * L.z * V.z);
+}
+RTX_DEV void GetSpecColor(const Mat& m, float eta, F3& spec_col, F3& sheen_col) {
+  float lum = luma(m.base_color);
+  F3 ctint = lum > 0.0f ? m.base_color / lum : f3s(1.0f);
+  float F0 = (1.0f - eta) / (1.0f + eta);
+  spec_col = lerpv(lerpv(f3s(1.0f), ctint, f3s(m.specular_tint)) * (F0 * F0), m.base_color,
+                   f3s(m.metallic));
+  sheen_col = lerpv(f3s(1.0f), ctint, f3s(m.sheen_tint));
+}
+RTX_DEV void GetLobeProbabilities(const Mat& m, F3 spec_col, float af, float& dw, float& srw,
+                                  float& strw, float& cw) {
+  dw = luma(m.base_color) * (1.0f - m.metallic) * (1.0f - m.spec_trans);
+  srw = luma(lerpv(spec_col, f3s(1.0f), f3s(af)));
+  strw = (1.0f - af) * (1.0f - m.metallic) * m.spec_trans * luma(m.base_color);
+  cw = m.clearcoat * (1.0f - m.metallic);
+  float total = dw + srw + strw + cw;
+  dw /= total;
+  srw /= total;
+  strw /= total;
+  cw /= total;
+}
+RTX_DEV F3 BsdfEval(const Mat& m, float eta, F3 V, F3 N, F3 L, float& bsdf_pdf) {
+  bsdf_pdf = 0.0f;
+  F3 f = f3s(0.0f);
+  F3 T, B;
+  Onb(N, T, B);
+  V = ToLocal(T, B, N, V);
+  L = ToLocal(T, B, N, L);
+  F3 H;
+  if (L.z > 0.0f)
+    H = normalized(L + V);
+  else
+    H = normalized(L + V * eta);
+  if (H.z < 0.0f) H = -H;
+  F3 spec_color, sheen_color;
+  GetSpecColor(m, eta, spec_color, sheen_color);
+  float dw, srw, strw, cw;
+  float fresnel = FresnelMix(m, eta, dot(V, H));
+  GetLobeProbabilities(m, spec_color, fresnel, dw, srw, strw, cw);
+  float pdf;
+  if (dw > 0.0f && L.z > 0.0f) {
+    f = f + EvalDiffuse(m, sheen_color, V, L, H, pdf);
+    bsdf_pdf = bsdf_pdf + pdf * dw;
+  }
+  if (srw > 0.0f && L.z > 0.0f && V.z > 0.0f) {
+    f = f + EvalSpecReflection(m, eta, spec_color, V, L, H, pdf);
+    bsdf_pdf = bsdf_pdf + pdf * srw;
+  }
+  if (strw > 0.0f && L.z < 0.0f) {
+    f = f + EvalSpecRefraction(m, eta, V, L, H, pdf);
+    bsdf_pdf = bsdf_pdf + pdf * strw;
+  }
+  if (cw > 0.0f && L.z > 0.0f && V.z > 0.0f) {
+    f = f + EvalClearcoat(m, V, L, H, pdf);
+    bsdf_pdf = bsdf_pdf + pdf * cw;
+  }
+  return f * fabsf(L.z);
+}
+RTX_DEV bool BsdfSample(const Mat& m, float eta, F3 N, F3 in_dir, float r1, float r2,
+                        F3& out_dir, F3& color_o, float& pdf) {
+  pdf = 0.0f;
+  F3 f = f3s(0.0f);
+  F3 V = in_dir;
+  F3 T, B;
+  Onb(N, T, B);
+  V = ToLocal(T, B, N, V);
+  F3 specCol, sheenCol;
+  GetSpecColor(m, eta, specCol, sheenCol);
+  float dw, srw, strw, cw;
+  float approxFresnel = FresnelMix(m, eta, V.z);
+  GetLobeProbabilities(m, specCol, approxFresnel, dw, srw, strw, cw);
+  float cdf0 = dw;
+  float cdf1 = cdf0 + srw;
+  float cdf2 = cdf1 + strw;
+  if (r1 < cdf0) {
+    r1 /= cdf0;
+    out_dir = CosineSampleHemisphere(r1, r2);
+    F3 H = normalized(out_dir + V);
+    f = EvalDiffuse(m, sheenCol, V, out_dir, H, pdf);
+    pdf *= dw;
+  } else if (r1 < cdf1) {
+    r1 = (r1 - cdf0) / (cdf1 - cdf0);
+    F3 H = SampleGGXVNDF(V, m.roughness, r1, r2);
+    if (H.z < 0.0f) H = -H;
+    out_dir = normalized(Reflect(-V, H));
+    f = EvalSpecReflection(m, eta, specCol, V, out_dir, H, pdf);
+    pdf *= srw;
+  } else if (r1 < cdf2) {
+    r1 = (r1 - cdf1) / (cdf2 - cdf1);
+    F3 H = SampleGGXVNDF(V, m.roughness, r1, r2);
+    if (H.z < 0.0f) H = -H;
+    out_dir = normalized(Refract(-V, H, eta));
+    f = EvalSpecRefraction(m, eta, V, out_dir, H, pdf);
+    pdf *= strw;
+  } else {
+    // material.cpp:279 divides in double and narrows to float
+    float num = r1 - cdf2;
+    r1 = (float)(__ddiv_rn((double)num, __dsub_rn(1.0, (double)cdf2)));
+    F3 H = SampleGTR1(m.clearcoat_roughness, r1);
+    if (H.z < 0.0f) H = -H;
+    out_dir = normalized(Reflect(-V, H));
+    f = EvalClearcoat(m, V, out_dir, H, pdf);
+    pdf *= cw;
+  }
+  out_dir = ToWorld(T, B, N, out_dir);
+  color_o = f * fabsf(dot(N, out_dir));
+  return !eq_zero_eps(out_dir);
+}
+
+}  // namespace rtx

@@ -1,0 +1,474 @@
+// pt_kernels.cu — wavefront path tracer restating RenderToy's
+// PathTracingRenderer (src/renderer.cpp:236-384) for the GPU.
+//
+// The reference evaluates one path per recursion (Radiance, renderer.cpp:272)
+// with the light sample of DirectLight (renderer.cpp:335) in the middle.  Here
+// a wave of paths advances one vertex per step through four kernels:
+//
+//   raygen   primary ray of each (pixel, sample)            renderer.cpp:252-259
+//   extend   closest hit of every live path                 renderer.cpp:282
+//   shade    emission + MIS, light sample + BSDF Eval,      renderer.cpp:284-325
+//            BSDF Sample -> next ray; emits a shadow record  renderer.cpp:341-371
+//   connect  occlusion of each shadow record; adds the light renderer.cpp:352-379
+//            contribution to its path
+//   accumulate  image += L / spp in sample order            renderer.cpp:261
+//
+// Radiance is accumulated forward (sum over vertices of throughput x
+// (emission + light)) instead of the reference's backward recursion; the two
+// agree to rounding.  Paths live in structure-of-arrays float4 buffers in HBM
+// (96 B per path); live paths and shadow records are compacted into queues with
+// warp-aggregated atomics, and queue lengths stay on the device, so the host
+// issues a fixed launch sequence per wave with no synchronisation.
+// Traversal kernels run persistent warps that fetch 32 rays at a time.
+#include <algorithm>
+
+#include "traverse.cuh"
+
+namespace rtx {
+
+constexpr int kMaxDepthSlots = 64;
+
+struct PtWorkspace {
+  size_t cap = 0;
+  float4 *ray_o = nullptr, *ray_d = nullptr, *thr = nullptr, *rad = nullptr, *absb = nullptr,
+         *hit = nullptr;
+  int* queue[2] = {nullptr, nullptr};
+  float4* shadow = nullptr;
+  int* counters = nullptr;  // counts[64] | shadow_counts[64] | work[2 * 64]
+  int num_sms = 0;
+  int occ_extend = 0, occ_connect = 0, occ_shade = 0, block_cached = 0;
+};
+
+PtWorkspace* pt_workspace_create() { return new PtWorkspace(); }
+
+static void ws_free(PtWorkspace* w) {
+  float4* f[] = {w->ray_o, w->ray_d, w->thr, w->rad, w->absb, w->hit, w->shadow};
+  for (float4* p : f)
+    if (p) cudaFree(p);
+  if (w->queue[0]) cudaFree(w->queue[0]);
+  if (w->queue[1]) cudaFree(w->queue[1]);
+  if (w->counters) cudaFree(w->counters);
+  w->ray_o = w->ray_d = w->thr = w->rad = w->absb = w->hit = w->shadow = nullptr;
+  w->queue[0] = w->queue[1] = nullptr;
+  w->counters = nullptr;
+  w->cap = 0;
+}
+
+void pt_workspace_destroy(PtWorkspace* ws) {
+  if (!ws) return;
+  ws_free(ws);
+  delete ws;
+}
+
+static cudaError_t ws_reserve(PtWorkspace* w, size_t cap) {
+  if (w->cap >= cap && w->counters) return cudaSuccess;
+  ws_free(w);
+  cudaError_t e;
+  float4** f[] = {&w->ray_o, &w->ray_d, &w->thr, &w->rad, &w->absb, &w->hit};
+  for (float4** p : f)
+    if ((e = cudaMalloc(p, cap * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->shadow, cap * 4 * sizeof(float4))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->queue[0], cap * sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->queue[1], cap * sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->counters, 4 * kMaxDepthSlots * sizeof(int))) != cudaSuccess) return e;
+  w->cap = cap;
+  return cudaSuccess;
+}
+
+struct PtArgs {
+  float4 *ray_o, *ray_d, *thr, *rad, *absb, *hit, *shadow;
+  int *queue_in, *queue_out;
+  int *counts, *shadow_counts, *work;
+  int* err;
+  Counters* ctr;
+  long long q0;
+  int n_wave, npix, W, first_sample, max_depth, depth;
+  uint32_t k0, k1;
+};
+
+// Append with one atomic per warp; returns this thread's slot.
+RTX_DEV int warp_append(int* counter) {
+  unsigned mask = __activemask();
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// Persistent-warp work fetch: returns the first item of this warp's batch.
+RTX_DEV int warp_fetch(int* work) {
+  int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(work, 32);
+  return __shfl_sync(0xffffffffu, base, 0);
+}
+
+__global__ void k_raygen(PtArgs a, CamParams cam) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) a.counts[0] = a.n_wave;
+  if (i >= a.n_wave) return;
+  long long q = a.q0 + i;
+  int pix = (int)(q % a.npix);
+  F3 o, d;
+  camera_ray(cam, pix % a.W, pix / a.W, o, d);
+  a.ray_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
+  a.ray_d[i] = make_float4(d.x, d.y, d.z, __int_as_float(-1));
+  a.thr[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+  a.rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  a.absb[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  a.queue_in[i] = i;
+}
+
+template <bool kCount>
+__global__ void k_extend(PtArgs a, DeviceScene s) {
+  int n = a.counts[a.depth];
+  VisitCount vc;
+  int lane = threadIdx.x & 31;
+  while (true) {
+    int base = warp_fetch(a.work + 2 * a.depth);
+    if (base >= n) break;
+    int i = base + lane;
+    if (i < n) {
+      int p = a.queue_in[i];
+      float4 ro = a.ray_o[p], rd = a.ray_d[p];
+      float t, u, v;
+      int h = closest_hit<kCount>(s, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z),
+                                  __float_as_int(rd.w), t, u, v, a.err, vc);
+      a.hit[p] = make_float4(__int_as_float(h), t, u, v);
+    }
+  }
+  if (kCount) {
+    atomicAdd(&a.ctr->ext_node_visits, (unsigned long long)vc.nodes);
+    atomicAdd(&a.ctr->ext_tri_tests, (unsigned long long)vc.tris);
+  }
+}
+
+__global__ void k_shade(PtArgs a, DeviceScene s) {
+  int n = a.counts[a.depth];
+  const int depth = a.depth;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int p = a.queue_in[i];
+    float4 ro = a.ray_o[p], rd = a.ray_d[p], h = a.hit[p], th = a.thr[p], rr = a.rad[p];
+    F3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z);
+    float last_pdf = ro.w;
+    int tri = __float_as_int(h.x);
+    F3 T = f3(th.x, th.y, th.z);
+    F3 acc = f3(rr.x, rr.y, rr.z);
+    if (tri < 0) {
+      // World::GetDefaultEmission (world.cpp:39-42) of -direction
+      F3 env = (-d.z < 0.0f) ? f3(s.sky[0], s.sky[1], s.sky[2])
+                             : f3(s.ground[0], s.ground[1], s.ground[2]);
+      acc = acc + T * env;
+      a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+      continue;
+    }
+    float4 ab = a.absb[p];
+    F3 absorption = f3(ab.x, ab.y, ab.z);
+    float t = h.y, u = h.z, v = h.w;
+    float4 s0 = __ldg(s.shade + 4 * (size_t)tri), s1 = __ldg(s.shade + 4 * (size_t)tri + 1);
+    int info = __float_as_int(s1.w);
+    Mat m = load_mat(s.mats + 24 * (size_t)(info & 0x7fffffff));
+    F3 pos = o + d * t;  // BVH::Intersect: src + t * direction
+    F3 N = shading_normal(s, tri, u, v, s0, s1, info < 0);
+    F3 ff = N;
+    float eta;
+    if (dot(d, ff) > 0.0f) {  // renderer.cpp:288-298
+      ff = -ff;
+      eta = m.ior;
+      absorption = f3s(0.0f);
+    } else {
+      eta = 1.0f / m.ior;
+    }
+    // SurfacePoint::GetEmission<true> (surfacepoint.h:21-45) toward the ray source
+    F3 re = o - pos;
+    float d2 = dot(re, re);
+    float cos_area = dot(-d, N) * s0.w;
+    float self_pdf = fabsf(d2 / cos_area);
+    F3 E = m.emission;
+    if (depth > 0) E = E * PowerHeuristic(last_pdf, self_pdf);
+    acc = acc + T * E;
+    float dist = length(pos - o);
+    F3 expo = (-absorption) * dist;
+    F3 br = f3(powf(kE, expo.x), powf(kE, expo.y), powf(kE, expo.z));
+
+    long long q = a.q0 + p;
+    Rng rng{a.k0, a.k1, (uint32_t)(q % a.npix), (uint32_t)(a.first_sample + q / a.npix),
+            __float_as_uint(th.w)};
+    if (s.n_emitters > 0) {
+      // World::SampleEmitter + Triangle::GetSamplePoint (world.cpp:5-17, object.cpp:169-178)
+      int e = __ldg(s.emitters + rng.uniform_int(0, s.n_emitters - 1));
+      float sqr1 = sqrtf(rng.uniform());
+      float r2 = rng.uniform();
+      float aa = 1.0f - sqr1;
+      float bb = (1.0f - r2) * sqr1;
+      const float4* g = s.geo + 3 * (size_t)e;
+      float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2);
+      F3 emit_pos = (f3(g1.x, g1.y, g1.z) * aa + f3(g2.x, g2.y, g2.z) * bb) + f3(g0.x, g0.y, g0.z);
+      F3 dl = normalized(emit_pos - pos);
+      float bpdf;
+      F3 f = BsdfEval(m, eta, -d, ff, dl, bpdf);
+      if (bpdf > 0.0f) {
+        int slot = warp_append(a.shadow_counts + depth);
+        F3 tb = T * br;
+        float4* r = a.shadow + 4 * (size_t)slot;
+        r[0] = make_float4(pos.x, pos.y, pos.z, __int_as_float(p));
+        r[1] = make_float4(emit_pos.x, emit_pos.y, emit_pos.z, __int_as_float(e));
+        r[2] = make_float4(f.x, f.y, f.z, bpdf);
+        r[3] = make_float4(tb.x, tb.y, tb.z, __int_as_float(tri));
+      }
+    }
+    float r1 = rng.uniform();
+    float r2 = rng.uniform();
+    F3 nd, color;
+    float pdf;
+    bool cont = false;
+    if (BsdfSample(m, eta, ff, -d, r1, r2, nd, color, pdf)) {
+      absorption = f3(-logf(m.extinction.x), -logf(m.extinction.y), -logf(m.extinction.z)) /
+                   m.at_distance;
+      if (pdf > 0.0f) {
+        F3 w = (br * color) / pdf;
+        if (depth + 1 < a.max_depth) {
+          T = T * w;
+          cont = true;
+        } else {
+          // the reference multiplies by the (zero) radiance beyond the cap,
+          // which keeps an infinite or NaN weight visible as NaN
+          acc = acc + T * (w * 0.0f);
+        }
+      }
+    }
+    a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+    if (cont) {
+      a.ray_o[p] = make_float4(pos.x, pos.y, pos.z, pdf);
+      a.ray_d[p] = make_float4(nd.x, nd.y, nd.z, __int_as_float(tri));
+      a.thr[p] = make_float4(T.x, T.y, T.z, __uint_as_float(rng.draw));
+      a.absb[p] = make_float4(absorption.x, absorption.y, absorption.z, 0.0f);
+      int slot = warp_append(a.counts + depth + 1);
+      a.queue_out[slot] = p;
+    }
+  }
+}
+
+template <bool kCount>
+__global__ void k_connect(PtArgs a, DeviceScene s) {
+  int n = a.shadow_counts[a.depth];
+  VisitCount vc;
+  int lane = threadIdx.x & 31;
+  while (true) {
+    int base = warp_fetch(a.work + 2 * a.depth + 1);
+    if (base >= n) break;
+    int i = base + lane;
+    if (i >= n) continue;
+    const float4* r = a.shadow + 4 * (size_t)i;
+    float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
+    F3 pos = f3(r0.x, r0.y, r0.z), emit_pos = f3(r1.x, r1.y, r1.z);
+    int p = __float_as_int(r0.w), e = __float_as_int(r1.w), ex = __float_as_int(r3.w);
+    F3 dir = normalized(emit_pos - pos);
+    // Closest-hit visibility of renderer.cpp:352-354 as an occlusion query:
+    // the light is seen when no other triangle lies nearer than the emitter
+    // (or, when the emitter itself is missed, when nothing is hit at all).
+    float te = kInf, ue = 0.0f, ve = 0.0f;
+    bool he = false;
+    if (e != ex) {
+      const float4* g = s.geo + 3 * (size_t)e;
+      float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2);
+      float tt, uu, vv;
+      if (tri_hit(pos, dir, f3(g0.x, g0.y, g0.z), f3(g1.x, g1.y, g1.z), f3(g2.x, g2.y, g2.z), tt,
+                  uu, vv) &&
+          tt < kInf) {
+        he = true;
+        te = tt;
+        ue = uu;
+        ve = vv;
+      }
+    }
+    bool occ = he ? occluded<kCount>(s, pos, dir, ex, e, te, a.err, vc)
+                  : occluded<kCount>(s, pos, dir, ex, -1, kInf, a.err, vc);
+    if (occ) continue;
+    float4 s0 = __ldg(s.shade + 4 * (size_t)e), s1 = __ldg(s.shade + 4 * (size_t)e + 1);
+    int info = __float_as_int(s1.w);
+    F3 Ne = shading_normal(s, e, ue, ve, s0, s1, info < 0);
+    F3 rv = pos - emit_pos;
+    float d2 = dot(rv, rv);
+    float cos_area = dot(-dir, Ne) * s0.w;
+    float lpdf = fabsf(d2 / cos_area);
+    const float* me = s.mats + 24 * (size_t)(info & 0x7fffffff);
+    F3 Le = f3(__ldg(me + 3), __ldg(me + 4), __ldg(me + 5));
+    float w = PowerHeuristic(lpdf, r2.w);
+    F3 c = f3(r2.x, r2.y, r2.z) * w;
+    c = c * Le;
+    c = c * (float)s.n_emitters;
+    c = c / lpdf;
+    float4 acc = a.rad[p];
+    F3 tb = f3(r3.x, r3.y, r3.z) * c;
+    a.rad[p] = make_float4(acc.x + tb.x, acc.y + tb.y, acc.z + tb.z, 0.0f);
+  }
+  if (kCount) {
+    atomicAdd(&a.ctr->sh_node_visits, (unsigned long long)vc.nodes);
+    atomicAdd(&a.ctr->sh_tri_tests, (unsigned long long)vc.tris);
+  }
+}
+
+__global__ void k_accumulate(const float4* rad, long long q0, int n_wave, int npix, float spp,
+                             float* out, int per_path) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (per_path) {
+    if (i >= n_wave) return;
+    float4 r = rad[i];
+    size_t q = (size_t)(q0 + i);
+    out[3 * q] = r.x;
+    out[3 * q + 1] = r.y;
+    out[3 * q + 2] = r.z;
+    return;
+  }
+  if (i >= npix) return;
+  long long off = ((long long)i - q0 % npix + npix) % npix;
+  long long qs = q0 + off;
+  if (qs >= q0 + n_wave) return;
+  float* o = out + 3 * (size_t)i;
+  F3 acc = f3(o[0], o[1], o[2]);
+  for (long long q = qs; q < q0 + n_wave; q += npix) {
+    float4 r = rad[q - q0];
+    acc = acc + f3(r.x, r.y, r.z) / spp;
+  }
+  o[0] = acc.x;
+  o[1] = acc.y;
+  o[2] = acc.z;
+}
+
+__global__ void k_tally(const int* counts, const int* shadow_counts, int max_depth, Counters* c) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long e = 0, sh = 0;
+  for (int d = 0; d < max_depth; ++d) {
+    e += (unsigned)counts[d];
+    sh += (unsigned)shadow_counts[d];
+  }
+  c->ext_rays += e;
+  c->shadow_rays += sh;
+}
+
+KernelTimer::~KernelTimer() {
+  for (cudaEvent_t e : pool) cudaEventDestroy(e);
+}
+
+cudaError_t KernelTimer::mark(int kind, cudaStream_t st, bool start) {
+  if (!on) return cudaSuccess;
+  if (used == pool.size()) {
+    cudaEvent_t e;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return r;
+    pool.push_back(e);
+  }
+  if (start) marks.emplace_back(kind, (int)used);
+  return cudaEventRecord(pool[used++], st);
+}
+
+cudaError_t KernelTimer::collect() {
+  for (auto& m : marks) {
+    float t = 0.0f;
+    cudaError_t r = cudaEventElapsedTime(&t, pool[m.second], pool[m.second + 1]);
+    if (r != cudaSuccess) return r;
+    ms[m.first] += t;
+  }
+  marks.clear();
+  used = 0;
+  return cudaSuccess;
+}
+
+cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& cam,
+                      const PtParams& p, float* d_out, int* err, Counters* d_counters,
+                      KernelTimer* timer, cudaStream_t st, int* launches, int* extend_launches,
+                      std::string* why) {
+  cudaError_t e;
+  if (p.max_depth < 1 || p.max_depth > kMaxDepthSlots - 1) {
+    *why = "max_depth must be in [1, 63]";
+    return cudaErrorInvalidValue;
+  }
+  long long npix = (long long)p.W * p.H;
+  long long total = npix * p.n_samples;
+  if (!p.per_path && (e = cudaMemsetAsync(d_out, 0, (size_t)npix * 3 * sizeof(float), st)))
+    return e;
+  if (total == 0) return cudaSuccess;
+  long long wave = p.wave_paths > 0 ? p.wave_paths : (1LL << 22);
+  wave = std::min(wave, total);
+  if ((e = ws_reserve(ws, (size_t)wave)) != cudaSuccess) return e;
+  int block = p.block > 0 ? p.block : 128;
+  if (ws->num_sms == 0 || ws->block_cached != block) {
+    int dev;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_extend, k_extend<false>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_connect, k_connect<false>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade, block, 0);
+    ws->block_cached = block;
+  }
+  int grid_ext = ws->num_sms * std::max(ws->occ_extend, 1);
+  int grid_con = ws->num_sms * std::max(ws->occ_connect, 1);
+  int grid_sh = ws->num_sms * std::max(ws->occ_shade, 1);
+
+  PtArgs a;
+  a.ray_o = ws->ray_o;
+  a.ray_d = ws->ray_d;
+  a.thr = ws->thr;
+  a.rad = ws->rad;
+  a.absb = ws->absb;
+  a.hit = ws->hit;
+  a.shadow = ws->shadow;
+  a.counts = ws->counters;
+  a.shadow_counts = ws->counters + kMaxDepthSlots;
+  a.work = ws->counters + 2 * kMaxDepthSlots;
+  a.err = err;
+  a.ctr = d_counters;
+  a.npix = (int)npix;
+  a.W = p.W;
+  a.first_sample = p.first_sample;
+  a.max_depth = p.max_depth;
+  a.k0 = (uint32_t)p.seed;
+  a.k1 = (uint32_t)(p.seed >> 32);
+  float spp = (float)p.spp;
+
+  for (long long q0 = 0; q0 < total; q0 += wave) {
+    int nw = (int)std::min(wave, total - q0);
+    a.q0 = q0;
+    a.n_wave = nw;
+    if ((e = cudaMemsetAsync(ws->counters, 0, 4 * kMaxDepthSlots * sizeof(int), st))) return e;
+    a.queue_in = ws->queue[0];
+    a.queue_out = ws->queue[1];
+    a.depth = 0;
+    k_raygen<<<(nw + 255) / 256, 256, 0, st>>>(a, cam);
+    ++*launches;
+    for (int depth = 0; depth < p.max_depth; ++depth) {
+      a.depth = depth;
+      a.queue_in = ws->queue[depth & 1];
+      a.queue_out = ws->queue[(depth + 1) & 1];
+      if ((e = timer->mark(0, st, true))) return e;
+      if (p.count_visits)
+        k_extend<true><<<grid_ext, block, 0, st>>>(a, s);
+      else
+        k_extend<false><<<grid_ext, block, 0, st>>>(a, s);
+      if ((e = timer->mark(0, st, false))) return e;
+      if ((e = timer->mark(1, st, true))) return e;
+      k_shade<<<grid_sh, block, 0, st>>>(a, s);
+      if ((e = timer->mark(1, st, false))) return e;
+      if ((e = timer->mark(2, st, true))) return e;
+      if (p.count_visits)
+        k_connect<true><<<grid_con, block, 0, st>>>(a, s);
+      else
+        k_connect<false><<<grid_con, block, 0, st>>>(a, s);
+      if ((e = timer->mark(2, st, false))) return e;
+      *launches += 3;
+      ++*extend_launches;
+    }
+    int acc_n = p.per_path ? nw : (int)npix;
+    k_accumulate<<<(acc_n + 255) / 256, 256, 0, st>>>(ws->rad, q0, nw, (int)npix, spp, d_out,
+                                                     p.per_path ? 1 : 0);
+    k_tally<<<1, 32, 0, st>>>(a.counts, a.shadow_counts, p.max_depth, d_counters);
+    *launches += 2;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace rtx

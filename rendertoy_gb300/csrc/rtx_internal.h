@@ -1,0 +1,139 @@
+// rtx_internal.h — librtx internals shared by the host API (api.cpp), the BVH
+// builder (bvh_build.cpp) and the CUDA kernels (*.cu).
+//
+// Scene layout in HBM (all arrays 16-byte aligned, read through the
+// non-coherent cache with 16-byte vector loads):
+//   nodes   : binary BVH, 4 x float4 = 64 B per inner node:
+//             [0] c0.lo.x c0.hi.x c0.lo.y c0.hi.y
+//             [1] c1.lo.x c1.hi.x c1.lo.y c1.hi.y
+//             [2] c0.lo.z c0.hi.z c1.lo.z c1.hi.z
+//             [3] child0 child1 (int bits; >= 0 inner node, < 0 leaf ref)
+//             leaf ref = ~((first_tri << 3) | (count - 1)), count 1..8
+//   tris    : leaf-ordered triangles, 3 x float4 = 48 B each:
+//             (v0.xyz, triangle id) (e1.xyz, 0) (e2.xyz, 0)
+//             e1 = v1 - v0, e2 = v2 - v0 (Triangle::v0v1_w / v0v2_w)
+//   shade   : per triangle id, 4 x float4 = 64 B:
+//             (flat normal.xyz, area) (n0.xyz, info) (n1.xyz, 0) (n2.xyz, 0)
+//             info = material index | 0x80000000 when the mesh is smooth
+//   geo     : per triangle id, 3 x float4 (v0, e1, e2): emitter sampling
+//   mats    : 24 floats per material; emitters: triangle ids.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/rtx.h"
+
+namespace rtx {
+
+constexpr int kMaxLeaf = 8;
+constexpr int kStackSize = 64;
+constexpr int kEmptyRoot = -2147483647 - 1;  // INT_MIN: scene without triangles
+
+// Device error word bits (set by kernels, read back by the host)
+enum DeviceError : int {
+  kErrStackOverflow = 1,
+  kErrQueueOverflow = 2,
+  kErrBadIndex = 4,
+};
+
+struct DeviceScene {
+  const float4* __restrict__ nodes;
+  const float4* __restrict__ tris;
+  const float4* __restrict__ shade;
+  const float4* __restrict__ geo;
+  const float* __restrict__ mats;
+  const int* __restrict__ emitters;
+  int root;  // node index (>= 0), leaf ref (< 0) or kEmptyRoot
+  int n_tris, n_emitters, n_mats;
+  float sky[3], ground[3];
+};
+
+// Camera reduced to what ray generation needs (src/renderer.cpp:103-124,
+// 252-259): the top three rows of the object-to-world matrix and the film
+// half extents.
+struct CamParams {
+  float m[12];
+  float top, right;
+  float inv_w, inv_h;
+  int W, H;
+};
+
+struct BvhBuildResult {
+  std::vector<float4> nodes;  // 4 per node
+  std::vector<float4> tris;   // 3 per triangle, leaf order
+  int root = kEmptyRoot;
+  int n_nodes = 0, n_leaves = 0, depth = 0;
+  double ms = 0.0;
+};
+
+// Host binned-SAH build over world-space triangles (verts: n x 9 floats)
+BvhBuildResult build_bvh(const float* verts, int n, int max_leaf);
+
+// Host-side camera preparation, restating Renderer::PrepareScreenSpace
+CamParams make_cam_params(const float* cam, int W, int H);
+
+// Visit counters (RTX_OPT_COUNT_VISITS)
+struct Counters {
+  unsigned long long ext_node_visits;
+  unsigned long long ext_tri_tests;
+  unsigned long long sh_node_visits;
+  unsigned long long sh_tri_tests;
+  unsigned long long ext_rays;
+  unsigned long long shadow_rays;
+};
+
+// Per-kernel CUDA-event timing of a render (RTX_OPT_KERNEL_TIMING)
+struct KernelTimer {
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<int, int>> marks;  // (kind, event index of the start)
+  size_t used = 0;
+  bool on = false;
+  double ms[3] = {0, 0, 0};  // extend, shade, connect
+  cudaError_t mark(int kind, cudaStream_t st, bool start);
+  cudaError_t collect();  // after the stream is synchronised
+  void reset() {
+    used = 0;
+    marks.clear();
+    ms[0] = ms[1] = ms[2] = 0;
+  }
+  ~KernelTimer();
+};
+
+// ---- kernel launchers (implemented in the .cu files) ----------------------
+cudaError_t launch_primary(const DeviceScene& s, const CamParams& cam, int mode,
+                           float near_, float far_, float* normal, float* albedo,
+                           float* depth, int* tri, float* tuv, int* err,
+                           cudaStream_t st, int* launches);
+cudaError_t launch_intersect(const DeviceScene& s, int n, const float* rays,
+                             const int* exclude, int* tri, float* tuv, int* err,
+                             cudaStream_t st, int* launches);
+
+struct PtWorkspace;  // defined in pt_kernels.cu
+struct PtParams {
+  int W, H, spp, first_sample, n_samples, max_depth;
+  uint64_t seed;
+  int wave_paths;  // paths per wave (<= capacity)
+  int block;
+  bool per_path;   // write L(p, s) instead of accumulating
+  bool count_visits;
+  bool primary_cache;
+};
+PtWorkspace* pt_workspace_create();
+void pt_workspace_destroy(PtWorkspace* ws);
+cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& cam,
+                      const PtParams& p, float* d_out, int* err, Counters* d_counters,
+                      KernelTimer* timer, cudaStream_t st, int* launches, int* extend_launches,
+                      std::string* why);
+
+cudaError_t launch_convolve(const float* in, float* out, int W, int H, const float* d_k,
+                            int kr, int kc, int flags, cudaStream_t st, int* launches);
+cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out, int W, int H,
+                            const float* d_w, int size, int extract_mode, float threshold,
+                            cudaStream_t st, int* launches);
+cudaError_t launch_edge(const float* in, float* out, int W, int H, cudaStream_t st,
+                        int* launches);
+
+}  // namespace rtx

@@ -1,0 +1,223 @@
+"""CUDA path (librtx, through the C ABI) against the reference's golden vectors
+and the oracle.
+
+Bars (from the reference's own outputs, tests/golden):
+  * primary-hit triangle ids equal on >= 99.99 % of pixels, hit t within 1e-5
+    relative where they are equal;
+  * normal / albedo / depth passes within 1e-5;
+  * per-path radiance within 1e-4 relative on >= 99 % of paths (paths whose
+    direction is decided by a transcendental rounded one ulp apart can take
+    another branch; both renderers run the same Philox stream);
+  * mean image at 1024 spp: relMSE against the oracle <= 1e-3;
+  * compositor bit-exact (the sums run in the reference's order, unfused).
+"""
+import numpy as np
+import pytest
+
+from helpers import bits, rel_close, relmse, scene_from_fixture
+from rendertoy_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+TAGS = ["cornell", "mixed"]
+
+
+@pytest.fixture(scope="module")
+def fixture_scene(ctx, golden):
+    cache = {}
+
+    def get(tag):
+        g = golden(f"scene_{tag}")
+        ctx.upload(scene_from_fixture(g))
+        return g
+    return get
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_emitter_order(ctx, fixture_scene, tag):
+    g = fixture_scene(tag)
+    assert np.array_equal(ctx.emitters(), g["emitters"])
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_primary_hits(ctx, fixture_scene, tag):
+    g = fixture_scene(tag)
+    W, H = int(g["W"]), int(g["H"])
+    tri, tuv = ctx.primary(W, H)
+    same = tri == g["primary_tri"]
+    assert same.mean() >= 0.9999, same.mean()
+    assert rel_close(tuv[..., 0][same], g["primary_tuv"][..., 0][same], 1e-5).all()
+    # the exact Moller-Trumbore restatement reproduces t, u, v bit for bit
+    assert (bits(tuv)[same] == bits(g["primary_tuv"])[same]).all(-1).mean() >= 0.9999
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_aov(ctx, fixture_scene, tag):
+    g = fixture_scene(tag)
+    W, H = int(g["W"]), int(g["H"])
+    near, far = float(g["camera"][19]), float(g["camera"][20])
+    n, a, d = ctx.aov(W, H, near, far)
+    same = ctx.primary(W, H)[0] == g["primary_tri"]
+    for got, key in ((n, "aov_normal"), (a, "aov_albedo"), (d, "aov_depth")):
+        diff = np.abs(got - g[key]).max(-1)
+        assert (diff[same] <= 1e-5).all(), (key, diff.max())
+
+
+@pytest.mark.parametrize("tag", TAGS)
+@pytest.mark.parametrize("depth", [5, 8])
+def test_per_path_radiance(ctx, fixture_scene, tag, depth):
+    g = fixture_scene(tag)
+    W, H = int(g["W"]), int(g["H"])
+    ref = g[f"paths_d{depth}"]
+    got = ctx.trace_paths(W, H, 0, ref.shape[0], depth, int(g["seed"]))
+    ok = rel_close(got, ref, 1e-4, atol=1e-6).all(-1)
+    print(f"{tag} depth {depth}: {ok.mean() * 100:.3f} % of {ok.size} paths within 1e-4")
+    assert ok.mean() >= 0.99, ok.mean()
+
+
+def test_intersect(ctx, golden):
+    g = golden("intersect_mixed")
+    ctx.upload(scenes.cornell_mixed())
+    tri, tuv = ctx.intersect(g["rays"], g["exclude"])
+    same = tri == g["tri"]
+    assert same.mean() >= 0.9999, same.mean()
+    assert (bits(tuv)[same] == bits(g["tuv"])[same]).all()
+
+
+def test_compositor_bit_exact(ctx, golden, oracle):
+    g = golden("compositor")
+    for tag in ("a", "b"):
+        img = g[f"img_{tag}"]
+        k5 = g[f"k5_{tag}"]
+        cases = {
+            "blur7": (lambda c: c.gaussian_blur(img, 7, 1.5)),
+            "blur49": (lambda c: c.gaussian_blur(img, 49, 8.0)),
+            "edge": (lambda c: c.edge_detect(img)),
+            "bloom": (lambda c: c.bloom(img, 9, 2.0, 0.8)),
+        }
+        for flags in ((0, 0, 0), (0, 0, 1), (0, 1, 0), (1, 0, 0), (0, 1, 1)):
+            cases["conv5_" + "".join(map(str, flags))] = (
+                lambda c, f=flags: c.convolve(img, k5, normalize=f[0], length=f[1], absval=f[2]))
+        for name, fn in cases.items():
+            gpu, orc = fn(ctx), fn(oracle)
+            assert np.array_equal(bits(gpu), bits(orc)), (tag, name)
+            rows = g[f"rows_{name}_{tag}"]
+            assert np.array_equal(bits(gpu[rows]), bits(g[f"{name}_{tag}"][rows])), (tag, name)
+
+
+def test_compositor_large_kernel(ctx, oracle):
+    """Bloom(500, 50, 1) as RenderToy's Cornell demo applies it: a kernel wider
+    than the image takes the direct path; still bit-exact."""
+    rng = np.random.RandomState(0)
+    img = rng.exponential(0.7, (40, 64, 3)).astype(np.float32)
+    assert np.array_equal(bits(ctx.bloom(img, 101, 20.0, 1.0)), bits(oracle.bloom(img, 101, 20.0, 1.0)))
+    assert np.array_equal(bits(ctx.gaussian_blur(img, 500, 50.0)),
+                          bits(oracle.gaussian_blur(img, 500, 50.0)))
+
+
+def test_mean_image_1024spp(ctx, oracle):
+    sc = scenes.cornell_box()
+    ctx.upload(sc)
+    W = H = 24
+    gpu = ctx.render_pt(W, H, 1024, 8, seed=3)
+    ref = oracle.scene(sc).render_pt(W, H, 1024, 8, 3)
+    e = relmse(gpu, ref)
+    print("relMSE(gpu, oracle) at 1024 spp:", e)
+    assert e <= 1e-3
+    assert np.isfinite(gpu).mean() > 0.99
+
+
+def test_accumulation_matches_paths(ctx):
+    """render_pt == sum_s trace_paths(s) / spp, in sample order."""
+    sc = scenes.cornell_box()
+    ctx.upload(sc)
+    W, H, spp = 16, 12, 5
+    img = ctx.render_pt(W, H, spp, 6, seed=9)
+    paths = ctx.trace_paths(W, H, 0, spp, 6, seed=9)
+    acc = np.zeros((H * W, 3), np.float32)
+    for s in range(spp):
+        acc = acc + paths[s] / np.float32(spp)
+    assert np.array_equal(bits(img.reshape(-1, 3)), bits(acc))
+
+
+def test_waves_do_not_change_results(ctx):
+    """The wavefront split (paths in flight) does not change any path."""
+    import rendertoy_gb300 as rt
+    sc = scenes.cornell_mixed()
+    ctx.upload(sc)
+    a = ctx.trace_paths(20, 16, 0, 3, 8, seed=1)
+    ctx.set_option(rt.OPT_WAVE_PATHS, 97)
+    try:
+        b = ctx.trace_paths(20, 16, 0, 3, 8, seed=1)
+        c = ctx.render_pt(20, 16, 3, 8, seed=1)
+    finally:
+        ctx.set_option(rt.OPT_WAVE_PATHS, 0)
+    d = ctx.render_pt(20, 16, 3, 8, seed=1)
+    assert np.array_equal(bits(a), bits(b))
+    assert np.array_equal(bits(c), bits(d))
+
+
+def test_edge_cases(ctx, oracle):
+    import rendertoy_gb300 as rt
+    # no emitters: no light samples are drawn; only the environment lights
+    sc = scenes.cornell_box()
+    sc.mats[:, 3:6] = 0
+    sc.sky[:] = (0.5, 0.6, 0.7)
+    sc.ground[:] = (0.2, 0.1, 0.0)
+    ctx.upload(sc)
+    assert len(ctx.emitters()) == 0
+    got = ctx.trace_paths(8, 8, 0, 2, 5, seed=4)
+    ref = oracle.scene(sc).trace_paths(8, 8, 0, 2, 5, 4)
+    assert rel_close(got, ref, 1e-4, 1e-6).all(-1).mean() >= 0.99
+    # 1 x 1 image, max depth 1
+    ctx.upload(scenes.cornell_box())
+    one = ctx.render_pt(1, 1, 3, 1, seed=0)
+    assert one.shape == (1, 1, 3)
+    # empty scene: every ray misses and sees the environment
+    sc0 = scenes.cornell_box()
+    sc0.verts = sc0.verts[:0]
+    sc0.norms = sc0.norms[:0]
+    sc0.tri_mesh = sc0.tri_mesh[:0]
+    sc0.sky[:] = (1.0, 2.0, 3.0)
+    ctx.upload(sc0)
+    tri, _ = ctx.primary(4, 4)
+    assert (tri == -1).all()
+    img = ctx.render_pt(4, 4, 2, 5)
+    assert np.isfinite(img).all()
+    # invalid arguments return errors, not crashes
+    ctx.upload(scenes.cornell_box())
+    with pytest.raises(rt.RtxError):
+        ctx.render_pt(0, 4, 1, 5)
+    with pytest.raises(rt.RtxError):
+        ctx.render_pt(4, 4, 1, 0)
+    bad = scenes.cornell_box()
+    bad.tri_mesh = bad.tri_mesh.copy()
+    bad.tri_mesh[3] = 99
+    with pytest.raises(rt.RtxError):
+        ctx.upload(bad)
+
+
+@pytest.fixture(scope="module")
+def icosphere_scene():
+    return scenes.displaced_icosphere(subdiv=8)
+
+
+def test_full_size_icosphere(ctx, oracle, icosphere_scene):
+    """The 1.3M-triangle displaced icosphere: primary hits of a 256 x 256 film
+    and per-path radiance of 256 pixels at max depth 12 against the oracle."""
+    sc = icosphere_scene
+    assert sc.n_tris == 20 * 4 ** 8 + 12
+    ctx.upload(sc)
+    osc = oracle.scene(sc)
+    tri, tuv = ctx.primary(256, 256)
+    rtri, rtuv = osc.primary(256, 256)
+    same = tri == rtri
+    assert same.mean() >= 0.9999, same.mean()
+    assert rel_close(tuv[..., 0][same], rtuv[..., 0][same], 1e-5).all()
+    W = H = 256
+    pix = np.random.RandomState(2).choice(W * H, 256, replace=False).astype(np.int32)
+    got = ctx.trace_paths(W, H, 0, 1, 12, seed=5).reshape(W * H, 3)[pix]
+    ref = osc.trace_paths(W, H, 0, 1, 12, 5, pixels=pix)[0]
+    ok = rel_close(got, ref, 1e-4, 1e-6).all(-1)
+    print(f"icosphere depth 12: {ok.mean() * 100:.2f} % of paths within 1e-4")
+    assert ok.mean() >= 0.97
