@@ -167,6 +167,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--subdiv", type=int, default=SUBDIV)
+    ap.add_argument("--profile", action="store_true",
+                    help="render one step of the workload and exit (for ncu)")
+    ap.add_argument("--res", type=int, default=RES, help="with --profile: film size")
+    ap.add_argument("--spp", type=int, default=SPP, help="with --profile: samples per pixel")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     from rendertoy_gb300 import scenes
@@ -224,6 +228,16 @@ def main():
     ctx = rt.Context(local)
     ctx.upload(sc)
     st0 = ctx.stats()
+    if args.profile:
+        import torch
+        out = torch.empty((args.res, args.res, 3), dtype=torch.float32, device="cuda")
+        ctx.render_pt(args.res, args.res, args.spp, DEPTH, seed=1, out=out)
+        tmp = torch.empty_like(out)
+        ctx.gaussian_blur(out, BLUR_SIZE, BLUR_SIGMA, out=tmp)
+        ctx.convolve(tmp, EDGE5, absval=True, out=out)
+        ctx.synchronize()
+        print(json.dumps({"profile": True, "res": args.res, "spp": args.spp, **ctx.stats()}))
+        return
     stream = torch.cuda.ExternalStream(ctx.stream)
     dev = torch.device("cuda", local)
     img = torch.empty((RES, RES, 3), dtype=torch.float32, device=dev)

@@ -540,8 +540,7 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
   int launches = 0, ext_launches = 0;
   std::string why;
-  RTX_CUDA(c->timer.collect(), "kernel timing");
-  c->timer.reset();
+  c->timer.reset();  // times are per render; rtx_get_stats collects them
   cudaError_t e = pt_render(c->pt, c->ds, cp, p, (float*)o.dev, c->d_err, c->d_counters,
                             &c->timer, c->stream, &launches, &ext_launches, &why);
   c->stats.kernel_launches = launches;

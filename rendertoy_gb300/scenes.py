@@ -111,7 +111,7 @@ class _Builder:
         return len(self.mats) - 1
 
     def add_mesh(self, tris, mat, smooth=False, norms=None):
-        tris = np.asarray(tris, np.float32).reshape(-1, 3, 3)
+        tris = np.asarray(tris, np.float64).reshape(-1, 3, 3)
         mid = len(self.mesh_mat)
         self.mesh_mat.append(mat)
         self.mesh_smooth.append(1 if smooth else 0)
@@ -131,7 +131,16 @@ class _Builder:
         return self.add_mesh([[a, b, c], [a, c, d]], mat)
 
     def finish(self, cam, name, sky=(0, 0, 0), ground=(0, 0, 0)) -> Scene:
-        verts = np.concatenate(self.tris).reshape(-1, 9)
+        # The room is modelled in the classic [0, 555]^3 coordinates and then
+        # centred on the world origin, where RenderToy's own demo scenes sit:
+        # its octree refits every node box starting from a box at the origin
+        # (src/bvh.cpp:9-12, 197-228), so a room in the positive octant would
+        # leave it nearly unable to cull.
+        verts = np.concatenate(self.tris).reshape(-1, 9).astype(np.float64) - ROOM_CENTER
+        cam = np.asarray(cam, np.float32).copy()
+        cam[3] -= ROOM_CENTER
+        cam[7] -= ROOM_CENTER
+        cam[11] -= ROOM_CENTER
         # -0.0 -> +0.0, as the identity object-to-world transform of a Mesh does
         verts = (verts + np.float32(0.0)).astype(np.float32)
         return Scene(
@@ -146,7 +155,10 @@ class _Builder:
 
 
 def _box_tris(center, size, rot_y_deg):
-    """12 triangles of an axis-aligned box rotated about +y."""
+    """12 triangles of an axis-aligned box rotated about +y.  Boxes standing on
+    the floor are sunk 1 unit into it so that no face is coplanar with (and
+    overlapping) another: overlapping coplanar faces make the closest hit a
+    tie that RenderToy resolves by its traversal order."""
     cx, cy, cz = center
     sx, sy, sz = (s / 2.0 for s in size)
     a = math.radians(rot_y_deg)
@@ -170,6 +182,7 @@ GREEN = (0.14, 0.45, 0.091)
 WHITE = (0.725, 0.725, 0.725)
 LIGHT_LE = (17.0, 12.0, 4.0)
 CORNELL_EYE = (278.0, 273.0, -800.0)
+ROOM_CENTER = 277.5  # subtracted from every coordinate (see _Builder.finish)
 
 
 def _cornell_room(b: _Builder, white, red, green, light):
@@ -196,8 +209,8 @@ def cornell_box() -> Scene:
     green = b.add_material(material(GREEN, roughness=1.0, metallic=0.0))
     light = b.add_material(material((0.78, 0.78, 0.78), emission=LIGHT_LE, roughness=1.0))
     _cornell_room(b, white, red, green, light)
-    b.add_mesh(_box_tris((185.5, 82.5, 169.0), (165.0, 165.0, 165.0), -18.0), white)
-    b.add_mesh(_box_tris((368.5, 165.0, 351.5), (165.0, 330.0, 165.0), 15.0), white)
+    b.add_mesh(_box_tris((185.5, 81.5, 169.0), (165.0, 165.0, 165.0), -18.0), white)
+    b.add_mesh(_box_tris((368.5, 164.0, 351.5), (165.0, 330.0, 165.0), 15.0), white)
     _cornell_light(b, light)
     cam = fov_camera(CORNELL_EYE, vfov_deg=40.0, near=700.0, far=1500.0)
     return b.finish(cam, "cornell_box")
@@ -340,8 +353,8 @@ def cornell_mixed() -> Scene:
     sss = b.add_material(material((0.8, 0.6, 0.5), roughness=0.6, subsurface=1.0,
                                   clearcoat=0.3, clearcoat_roughness=1.0))
     _cornell_room(b, white, red, green, light)
-    b.add_mesh(_box_tris((185.5, 82.5, 169.0), (165.0, 165.0, 165.0), -18.0), metal)
-    b.add_mesh(_box_tris((368.5, 165.0, 351.5), (165.0, 330.0, 165.0), 15.0), coat)
+    b.add_mesh(_box_tris((185.5, 81.5, 169.0), (165.0, 165.0, 165.0), -18.0), metal)
+    b.add_mesh(_box_tris((368.5, 164.0, 351.5), (165.0, 330.0, 165.0), 15.0), coat)
     v, f = icosphere(2)
     vn = v.copy()
     tris = (v * 70.0 + np.array([200.0, 240.0, 160.0]))[f].astype(np.float32)
@@ -349,7 +362,7 @@ def cornell_mixed() -> Scene:
     v2, f2 = icosphere(1)
     tris2 = (v2 * 60.0 + np.array([420.0, 390.0, 250.0]))[f2].astype(np.float32)
     b.add_mesh(tris2, sss, smooth=True, norms=v2[f2].astype(np.float32))
-    b.add_mesh(_box_tris((120.0, 40.0, 420.0), (80.0, 80.0, 80.0), 30.0), rough_glass)
+    b.add_mesh(_box_tris((120.0, 39.0, 420.0), (80.0, 80.0, 80.0), 30.0), rough_glass)
     _cornell_light(b, light)
     cam = fov_camera(CORNELL_EYE, vfov_deg=40.0, near=700.0, far=1500.0)
     return b.finish(cam, "cornell_mixed")
