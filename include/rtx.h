@@ -73,8 +73,11 @@ enum rtx_option {
   RTX_OPT_COUNT_VISITS = 5,   /* 0/1: count node visits and triangle tests */
   RTX_OPT_LEAF_SIZE = 6,      /* max triangles per BVH leaf (1..8), next upload */
   RTX_OPT_PRIMARY_CACHE = 7,  /* 0/1: trace each pixel's primary ray once */
-  RTX_OPT_KERNEL_TIMING = 8   /* 0/1: CUDA events around each traversal and
+  RTX_OPT_KERNEL_TIMING = 8,  /* 0/1: CUDA events around each traversal and
                                  shading launch (rtx_stats.*_ms) */
+  RTX_OPT_ACCUMULATE = 9      /* 0/1: rtx_render_pt adds its mean to out_rgb
+                                 (RenderToy's buffer +=, renderer.cpp:261)
+                                 instead of overwriting it */
 };
 
 typedef struct rtx_context rtx_context;
@@ -99,6 +102,7 @@ typedef struct rtx_stats {
   int32_t node_bytes;        /* bytes per BVH node record */
   int32_t tri_bytes;         /* bytes per triangle record */
   int32_t reserved;
+  uint64_t ext_rays_by_depth[16]; /* closest-hit rays per path vertex 0..15 */
 } rtx_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -133,6 +137,10 @@ int rtx_scene_upload(rtx_context* ctx, int n_tris, const float* verts,
                      const float* ground);
 /* emitter triangle ids in sampling order; returns the count in *n_out */
 int rtx_scene_emitters(rtx_context* ctx, int32_t* out, int cap, int* n_out);
+/* Replace the emitter list by an explicit one (ids in sampling order), as
+ * World::PrepareDirectLightSampling left it (src/world.cpp:24-37); n = 0
+ * disables light sampling, as in a World where it was never called. */
+int rtx_scene_set_emitters(rtx_context* ctx, const int32_t* ids, int n);
 
 /* ---- renderers ------------------------------------------------------------
  * PathTracingRenderer::Render (src/renderer.cpp:236-270): out_rgb[p] =

@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "librtx.so")
 
 OPT_ASYNC, OPT_WAVE_PATHS, OPT_BLOCK, OPT_SORT_MATERIAL, OPT_COUNT_VISITS, OPT_LEAF_SIZE, \
-    OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING = 1, 2, 3, 4, 5, 6, 7, 8
+    OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING, OPT_ACCUMULATE = 1, 2, 3, 4, 5, 6, 7, 8, 9
 
 STATUS = {0: "RTX_OK", 1: "RTX_ERR_INVALID", 2: "RTX_ERR_CUDA", 3: "RTX_ERR_NOMEM",
           4: "RTX_ERR_NO_SCENE", 5: "RTX_ERR_DEVICE"}
@@ -28,7 +28,7 @@ STATUS = {0: "RTX_OK", 1: "RTX_ERR_INVALID", 2: "RTX_ERR_CUDA", 3: "RTX_ERR_NOME
 EXPORTS = [
     "rtx_create", "rtx_destroy", "rtx_last_error", "rtx_version", "rtx_set_option",
     "rtx_get_option", "rtx_get_stream", "rtx_set_stream", "rtx_synchronize", "rtx_get_stats",
-    "rtx_scene_upload", "rtx_scene_emitters", "rtx_render_pt", "rtx_trace_paths",
+    "rtx_scene_upload", "rtx_scene_emitters", "rtx_scene_set_emitters", "rtx_render_pt", "rtx_trace_paths",
     "rtx_render_aov", "rtx_primary_hits", "rtx_intersect", "rtx_image_convolve",
     "rtx_image_gaussian_blur", "rtx_image_edge_detect", "rtx_image_bloom",
 ]
@@ -48,7 +48,7 @@ class Stats(C.Structure):
                 ("last_gpu_ms", C.c_double), ("extend_ms", C.c_double), ("shade_ms", C.c_double),
                 ("connect_ms", C.c_double), ("bvh_build_ms", C.c_double), ("bvh_nodes", C.c_int32), ("bvh_leaves", C.c_int32),
                 ("bvh_depth", C.c_int32), ("node_bytes", C.c_int32), ("tri_bytes", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("ext_rays_by_depth", C.c_uint64 * 16)]
 
 
 _lib = None
@@ -76,6 +76,7 @@ def lib() -> C.CDLL:
         "rtx_get_stats": (i, [vp, C.POINTER(Stats)]),
         "rtx_scene_upload": (i, [vp, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp]),
         "rtx_scene_emitters": (i, [vp, vp, i, C.POINTER(i)]),
+        "rtx_scene_set_emitters": (i, [vp, vp, i]),
         "rtx_render_pt": (i, [vp, vp, i, i, i, i, u64, vp]),
         "rtx_trace_paths": (i, [vp, vp, i, i, i, i, i, u64, vp]),
         "rtx_render_aov": (i, [vp, vp, i, i, f, f, vp, vp, vp]),
@@ -159,7 +160,9 @@ class Context:
     def stats(self) -> dict:
         s = Stats()
         self._check(self.L.rtx_get_stats(self.h, C.byref(s)))
-        return {k: getattr(s, k) for k, _ in Stats._fields_ if k != "reserved"}
+        d = {k: getattr(s, k) for k, _ in Stats._fields_ if k not in ("reserved", "ext_rays_by_depth")}
+        d["ext_rays_by_depth"] = list(s.ext_rays_by_depth)
+        return d
 
     # -- scene ---------------------------------------------------------------
     def upload(self, sc):
@@ -179,6 +182,10 @@ class Context:
         out = np.zeros(max(n.value, 1), np.int32)
         self._check(self.L.rtx_scene_emitters(self.h, _ptr(out), len(out), C.byref(n)))
         return out[:n.value]
+
+    def set_emitters(self, ids):
+        ids = np.ascontiguousarray(ids, np.int32)
+        self._check(self.L.rtx_scene_set_emitters(self.h, _ptr(ids), len(ids)))
 
     def _cam(self, camera):
         return _f32(self.scene.camera if camera is None else camera)

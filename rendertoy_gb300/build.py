@@ -21,6 +21,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librtx.so")
+COMPAT_LIB = os.path.join(HERE, "librendertoy_compat.so")
+COMPAT_INC = os.path.join(HERE, "compat", "include")
+COMPAT_SRC = os.path.join(HERE, "compat", "src")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -48,6 +51,31 @@ def _compile(cmd):
     if r.returncode != 0:
         raise RuntimeError("compile failed:\n" + " ".join(cmd) + "\n" + r.stdout)
     return r.stdout
+
+
+def build_compat(force: bool = False) -> str:
+    """The RenderToy-compatible C++ API (compat/) as librendertoy_compat.so,
+    linked against librtx.so."""
+    build(force=force)
+    srcs = [os.path.join(COMPAT_SRC, f) for f in sorted(os.listdir(COMPAT_SRC)) if f.endswith(".cpp")]
+    deps = srcs + [os.path.join(COMPAT_INC, "RenderToy", f) for f in os.listdir(os.path.join(COMPAT_INC, "RenderToy"))]
+    if not force and os.path.exists(COMPAT_LIB) and \
+            os.path.getmtime(COMPAT_LIB) >= max(max(os.path.getmtime(d) for d in deps), os.path.getmtime(LIB)):
+        return COMPAT_LIB
+    tmp = COMPAT_LIB + ".tmp"
+    _compile(["g++", "-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-o", tmp,
+              "-I" + COMPAT_INC, *srcs, "-L" + HERE, "-lrtx", "-Wl,-rpath,$ORIGIN",
+              "-Wl,--no-undefined"])
+    os.replace(tmp, COMPAT_LIB)
+    return COMPAT_LIB
+
+
+def compile_app(src: str, out: str) -> str:
+    """Compile a RenderToy application against the compatible API."""
+    build_compat()
+    _compile(["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-I" + COMPAT_INC, src, "-o", out,
+              "-L" + HERE, "-lrendertoy_compat", "-lrtx", "-Wl,-rpath," + HERE])
+    return out
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -86,3 +114,4 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_compat())

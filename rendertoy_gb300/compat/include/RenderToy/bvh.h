@@ -1,0 +1,47 @@
+// RenderToy/bvh.h — BVH is the GPU-resident scene of a RenderContext (in
+// RenderToy, include/RenderToy/bvh.h:74-86, the CPU octree).  It owns one
+// librtx context; Intersect traces rays on the GPU.
+#ifndef RTX_COMPAT_BVH_H
+#define RTX_COMPAT_BVH_H
+#include <cstdint>
+#include <vector>
+
+#include "ray.h"
+#include "rtmath.h"
+
+struct rtx_context;
+
+namespace RenderToy {
+class Triangle;
+struct World;
+
+struct BoundingBox {
+  Vector3f vmin, vmax;
+  BoundingBox() : vmin(Vector3f::O), vmax(Vector3f::O) {}
+  BoundingBox(const Vector3f& a, const Vector3f& b) : vmin(a), vmax(b) {}
+};
+
+class BVH {
+ public:
+  // Uploads the world's triangles (World::triangles order), materials and
+  // emitters.
+  explicit BVH(World* world);
+  BVH(const BVH&) = delete;
+  ~BVH();
+  // Closest hit of one ray (BVH::Intersect): the triangle or nullptr.
+  const Triangle* Intersect(const Ray& ray, Vector3f& position, float& t, float& u, float& v,
+                            const Triangle* const exclude) const;
+  rtx_context* Device() const { return ctx; }
+  // Re-upload when the world's materials or emitters changed
+  void Refresh();
+
+ private:
+  friend struct RenderContext;
+  World* world;
+  rtx_context* ctx = nullptr;
+  std::vector<float> snapshot;  // materials, mesh table and emitters as uploaded
+  void Upload();
+  std::vector<float> Signature() const;
+};
+}  // namespace RenderToy
+#endif

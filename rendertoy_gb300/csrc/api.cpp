@@ -76,6 +76,7 @@ struct rtx_context {
   bool count_visits = false;
   int leaf_size = 4;
   bool primary_cache = false;
+  bool accumulate = false;
   KernelTimer timer;
   // scene
   bool has_scene = false;
@@ -337,6 +338,7 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
       return RTX_OK;
     case RTX_OPT_PRIMARY_CACHE: c->primary_cache = v != 0; return RTX_OK;
     case RTX_OPT_KERNEL_TIMING: c->timer.on = v != 0; return RTX_OK;
+    case RTX_OPT_ACCUMULATE: c->accumulate = v != 0; return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -352,6 +354,7 @@ int rtx_get_option(rtx_context* c, int option, int64_t* v) {
     case RTX_OPT_LEAF_SIZE: *v = c->leaf_size; return RTX_OK;
     case RTX_OPT_PRIMARY_CACHE: *v = c->primary_cache; return RTX_OK;
     case RTX_OPT_KERNEL_TIMING: *v = c->timer.on; return RTX_OK;
+    case RTX_OPT_ACCUMULATE: *v = c->accumulate; return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -396,6 +399,7 @@ int rtx_get_stats(rtx_context* c, rtx_stats* out) {
   c->stats.ext_tri_tests = h.ext_tri_tests;
   c->stats.shadow_node_visits = h.sh_node_visits;
   c->stats.shadow_tri_tests = h.sh_tri_tests;
+  for (int d = 0; d < 16; ++d) c->stats.ext_rays_by_depth[d] = h.ext_rays_by_depth[d];
   RTX_CUDA(c->timer.collect(), "kernel timing");
   c->stats.extend_ms = c->timer.ms[0];
   c->stats.shade_ms = c->timer.ms[1];
@@ -510,6 +514,22 @@ int rtx_scene_emitters(rtx_context* c, int32_t* out, int cap, int* n_out) {
   return RTX_OK;
 }
 
+int rtx_scene_set_emitters(rtx_context* c, const int32_t* ids, int n) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!c->has_scene) return fail(c, RTX_ERR_NO_SCENE, "no scene uploaded");
+  if (n < 0 || (n > 0 && !ids)) return fail(c, RTX_ERR_INVALID, "bad emitter list");
+  for (int i = 0; i < n; ++i)
+    if (ids[i] < 0 || ids[i] >= c->ds.n_tris) return fail(c, RTX_ERR_INVALID, "emitter id out of range");
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  c->emitters.assign(ids, ids + n);
+  RTX_CUDA(c->emit.ensure((size_t)n * sizeof(int32_t)), "emitter alloc");
+  if (n) RTX_CUDA(cudaMemcpy(c->emit.p, ids, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice), "emitter upload");
+  c->ds.emitters = (const int*)c->emit.p;
+  c->ds.n_emitters = n;
+  return RTX_OK;
+}
+
 static int render_paths(rtx_context* c, const float* cam, int W, int H, int first, int n_samples,
                         int spp, int max_depth, uint64_t seed, float* out, bool per_path) {
   if (!c) return RTX_ERR_INVALID;
@@ -522,7 +542,14 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   size_t out_elems = per_path ? npix * (size_t)n_samples : npix;
   if ((r = begin(c))) return r;
   Arg o;
-  if ((r = bind_out(c, out, out_elems * 3 * sizeof(float), 0, o))) return r;
+  bool acc = c->accumulate && !per_path;
+  if (acc) {
+    // the caller's image is read as well as written
+    if ((r = bind_in(c, out, out_elems * 3 * sizeof(float), 0, o))) return r;
+    if (!is_device_ptr(out)) o.host = out;
+  } else if ((r = bind_out(c, out, out_elems * 3 * sizeof(float), 0, o))) {
+    return r;
+  }
   CamParams cp = make_cam_params(cam, W, H);
   PtParams p;
   p.W = W;
@@ -535,6 +562,7 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   p.wave_paths = (int)c->wave_paths;
   p.block = c->block;
   p.per_path = per_path;
+  p.accumulate = acc;
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
   RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");

@@ -344,6 +344,7 @@ __global__ void k_tally(const int* counts, const int* shadow_counts, int max_dep
   for (int d = 0; d < max_depth; ++d) {
     e += (unsigned)counts[d];
     sh += (unsigned)shadow_counts[d];
+    if (d < 16) c->ext_rays_by_depth[d] += (unsigned)counts[d];
   }
   c->ext_rays += e;
   c->shadow_rays += sh;
@@ -388,7 +389,8 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
   }
   long long npix = (long long)p.W * p.H;
   long long total = npix * p.n_samples;
-  if (!p.per_path && (e = cudaMemsetAsync(d_out, 0, (size_t)npix * 3 * sizeof(float), st)))
+  if (!p.per_path && !p.accumulate &&
+      (e = cudaMemsetAsync(d_out, 0, (size_t)npix * 3 * sizeof(float), st)))
     return e;
   if (total == 0) return cudaSuccess;
   long long wave = p.wave_paths > 0 ? p.wave_paths : (1LL << 22);

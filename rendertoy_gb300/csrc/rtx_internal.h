@@ -83,6 +83,7 @@ struct Counters {
   unsigned long long sh_tri_tests;
   unsigned long long ext_rays;
   unsigned long long shadow_rays;
+  unsigned long long ext_rays_by_depth[16];
 };
 
 // Per-kernel CUDA-event timing of a render (RTX_OPT_KERNEL_TIMING)
@@ -118,6 +119,7 @@ struct PtParams {
   int wave_paths;  // paths per wave (<= capacity)
   int block;
   bool per_path;   // write L(p, s) instead of accumulating
+  bool accumulate; // add the mean to the output instead of overwriting it
   bool count_visits;
   bool primary_cache;
 };

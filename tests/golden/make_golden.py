@@ -184,6 +184,52 @@ def rng_case(ref, orc):
     np.savez_compressed(os.path.join(OUT, "rng.npz"), **out)
 
 
+def write_scene_file(sc, path):
+    """Scene file read by tests/compat/demo_cornell.cpp."""
+    with open(path, "wb") as f:
+        np.array([sc.n_tris, len(sc.mesh_mat), len(sc.mats)], np.int32).tofile(f)
+        np.ascontiguousarray(sc.verts, np.float32).tofile(f)
+        np.ascontiguousarray(sc.norms, np.float32).tofile(f)
+        np.ascontiguousarray(sc.tri_mesh, np.int32).tofile(f)
+        np.ascontiguousarray(sc.mesh_mat, np.int32).tofile(f)
+        np.ascontiguousarray(sc.mesh_smooth, np.uint8).tofile(f)
+        np.ascontiguousarray(sc.mats, np.float32).tofile(f)
+        np.ascontiguousarray(sc.camera, np.float32).tofile(f)
+
+
+def read_demo_output(path):
+    with open(path, "rb") as f:
+        W, H, n = np.fromfile(f, np.int32, 3)
+        return np.fromfile(f, np.float32).reshape(n, H, W, 3)
+
+
+DEMO_W, DEMO_H, DEMO_SPP = 40, 32, 256
+
+
+def demo_case(ref_root):
+    """tests/compat/demo_cornell.cpp built against RenderToy's own headers and
+    sources (serially: no OpenMP), run on the mixed-material scene."""
+    rdir = os.path.join(ROOT, "oracle", "_ref")
+    os.makedirs(rdir, exist_ok=True)
+    exe = os.path.join(rdir, "demo_cornell_ref")
+    srcs = [os.path.join(ref_root, "src", f + ".cpp") for f in
+            ("bvh", "object", "material", "rtmath", "surfacepoint", "world", "ray", "compositor",
+             "exception", "procedural", "importer", "exporter", "renderer")]
+    subprocess.check_call(["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-include", "functional",
+                           "-include", "vector", "-include", "cstdint", "-include", "optional",
+                           "-include", "algorithm", "-I" + os.path.join(ref_root, "include"),
+                           os.path.join(ROOT, "tests", "compat", "demo_cornell.cpp"), *srcs, "-o", exe])
+    sc = scenes.cornell_mixed()
+    scene_file = os.path.join(rdir, "demo_scene.bin")
+    write_scene_file(sc, scene_file)
+    out_file = os.path.join(rdir, "demo_out_ref.bin")
+    subprocess.check_call([exe, scene_file, out_file, str(DEMO_W), str(DEMO_H), str(DEMO_SPP)])
+    out = read_demo_output(out_file)
+    np.savez_compressed(os.path.join(OUT, "demo_cornell.npz"), buffers=out, W=DEMO_W, H=DEMO_H,
+                        spp=DEMO_SPP)
+    print(f"  demo_cornell (reference build): {out.shape[0]} buffers")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -201,6 +247,8 @@ def main():
     compositor_case(ref, orc)
     print("rng:")
     rng_case(ref, orc)
+    print("drop-in application:")
+    demo_case(args.ref)
     print("written to", OUT)
 
 
