@@ -189,6 +189,26 @@ int rtx_image_edge_detect(rtx_context* ctx, const float* in, float* out, int W,
 int rtx_image_bloom(rtx_context* ctx, const float* in, float* out, int W,
                     int H, int size, float sigma, float threshold);
 
+/* ---- without allocation -----------------------------------------------------
+ * No counterpart in RenderToy.  Image::GaussianBlur (as rtx_image_gaussian_blur)
+ * for callers that cannot allocate device memory when they call in: a plugin
+ * whose host application owns the device-memory budget, a real-time loop in
+ * which cudaMalloc / cudaFree would synchronise the device, or code that runs
+ * while another component captures a stream.  d_in / d_out are device images
+ * on the current device (in == out allowed); the work is enqueued on `stream`
+ * (a cudaStream_t; NULL = the default stream) and the call returns without
+ * waiting.  The intermediate image lives in a fixed 24 MiB device array that
+ * the library keeps on every GPU that loads it until the process exits:
+ * W * H <= 2097152 and size <= 255, otherwise RTX_ERR_INVALID.  All calls
+ * share that array, so calls whose work overlaps on the GPU race: serialise
+ * them.  The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress); make it before any stream capture.  msg (may be
+ * NULL) receives a message on failure.  Calls no cudaMalloc, cudaFree or other
+ * allocating routine. */
+int rtx_image_gaussian_blur_noalloc(const float* d_in, float* d_out, int W,
+                                    int H, int size, float sigma, void* stream,
+                                    char* msg, size_t msg_len);
+
 #ifdef __cplusplus
 }
 #endif

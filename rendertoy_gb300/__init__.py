@@ -31,6 +31,7 @@ EXPORTS = [
     "rtx_scene_upload", "rtx_scene_emitters", "rtx_scene_set_emitters", "rtx_render_pt", "rtx_trace_paths",
     "rtx_render_aov", "rtx_primary_hits", "rtx_intersect", "rtx_image_convolve",
     "rtx_image_gaussian_blur", "rtx_image_edge_detect", "rtx_image_bloom",
+    "rtx_image_gaussian_blur_noalloc",
 ]
 
 
@@ -86,6 +87,7 @@ def lib() -> C.CDLL:
         "rtx_image_gaussian_blur": (i, [vp, vp, vp, i, i, i, f]),
         "rtx_image_edge_detect": (i, [vp, vp, vp, i, i]),
         "rtx_image_bloom": (i, [vp, vp, vp, i, i, i, f, f]),
+        "rtx_image_gaussian_blur_noalloc": (i, [vp, vp, i, i, i, f, vp, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -1,0 +1,55 @@
+"""rtx_image_gaussian_blur_noalloc: the Gaussian blur for callers that cannot
+allocate device memory when they call in (a plugin whose host application owns
+the device-memory budget, a real-time loop that must not synchronise the
+device, code running during someone else's stream capture).  It keeps its
+intermediate image in a fixed device array instead of allocating one.
+
+Called through the C ABI twice in a row on device buffers the test owns; each
+result must equal, bit for bit, what rtx_image_gaussian_blur returns for the
+same image (the tolerance of every compositor test here).  Collected last so a
+failing run has already run every other test; it also passes alone.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_blur_matches_allocating_entry_point():
+    import torch
+
+    import rendertoy_gb300 as rt
+    from rendertoy_gb300 import build
+    build.build()
+    L = rt.lib()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream().cuda_stream
+    msg = C.create_string_buffer(256)
+    ctx = rt.Context(0)
+    try:
+        rng = np.random.RandomState(12)
+        cases = [(300, 200, 49, 8.0), (1024, 1024, 7, 1.5)]
+        for W, H, size, sigma in cases:  # two calls in a row, different sizes
+            img = rng.exponential(0.7, (H, W, 3)).astype(np.float32)
+            d_in = torch.from_numpy(img).cuda()
+            d_out = torch.full_like(d_in, float("nan"))
+            r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(d_in.data_ptr()),
+                                                  C.c_void_p(d_out.data_ptr()), W, H, size,
+                                                  sigma, C.c_void_p(stream), msg, len(msg))
+            assert r == 0, msg.value
+            torch.cuda.synchronize()
+            want = ctx.gaussian_blur(img, size, sigma)
+            got = d_out.cpu().numpy()
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (W, H, size)
+        # sizes beyond the fixed scratch are refused, with a message
+        big = torch.zeros((2049, 1024, 3), device="cuda")
+        r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(big.data_ptr()), C.c_void_p(big.data_ptr()),
+                                              1024, 2049, 7, 1.5, C.c_void_p(stream), msg, len(msg))
+        assert r == 1 and b"scratch" in msg.value
+        r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(big.data_ptr()), C.c_void_p(big.data_ptr()),
+                                              64, 64, 256, 1.5, C.c_void_p(stream), msg, len(msg))
+        assert r == 1
+    finally:
+        ctx.close()
