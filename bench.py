@@ -121,14 +121,21 @@ def dist_env():
     return ws, rank, local
 
 
-def reduce_max(x, ws):
+def reduce_max(x, ws, device="cuda"):
+    """Max over ranks of a per-rank timing (the only collective: control plane)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_rate(units_per_rank, slowest_seconds, ws):
+    """Whole-job throughput: every rank processes its own units (weak scaling),
+    the job takes as long as the slowest rank."""
+    return units_per_rank * ws / slowest_seconds
 
 
 def cpu_sample_rate(sc, seconds=12.0, threads=0, kind="oracle"):
@@ -282,7 +289,7 @@ def main():
             rays_s += s["shadow_rays"]
     total_ms = reduce_max(sum(step_ms), ws)
     samples = RES * RES * SPP * args.steps
-    value = samples * ws / (total_ms / 1e3) / 1e6
+    value = job_rate(samples, total_ms / 1e3, ws) / 1e6
     mrays = (rays_e + rays_s) * ws / (total_ms / 1e3) / 1e6
 
     # instrumented run (untimed): node visits and triangle tests per frame

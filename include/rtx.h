@@ -67,7 +67,9 @@ enum rtx_status {
 
 enum rtx_option {
   RTX_OPT_ASYNC = 1,          /* 0/1: return before device-only work ends */
-  RTX_OPT_WAVE_PATHS = 2,     /* max paths in flight per wavefront (0 = auto) */
+  RTX_OPT_WAVE_PATHS = 2,     /* max paths in flight per wavefront (0 = auto:
+                                 the whole render up to 2^26 paths and a
+                                 quarter of the free device memory) */
   RTX_OPT_BLOCK = 3,          /* threads per block of the wavefront kernels */
   RTX_OPT_SORT_MATERIAL = 4,  /* 0/1: sort hits by material before shading */
   RTX_OPT_COUNT_VISITS = 5,   /* 0/1: count node visits and triangle tests */
@@ -75,9 +77,15 @@ enum rtx_option {
   RTX_OPT_PRIMARY_CACHE = 7,  /* 0/1: trace each pixel's primary ray once */
   RTX_OPT_KERNEL_TIMING = 8,  /* 0/1: CUDA events around each traversal and
                                  shading launch (rtx_stats.*_ms) */
-  RTX_OPT_ACCUMULATE = 9      /* 0/1: rtx_render_pt adds its mean to out_rgb
+  RTX_OPT_ACCUMULATE = 9,     /* 0/1: rtx_render_pt adds its mean to out_rgb
                                  (RenderToy's buffer +=, renderer.cpp:261)
                                  instead of overwriting it */
+  RTX_OPT_TRAVERSAL = 10,     /* traversal kernels: 0 (default) = binary tree, one ray
+                                 per lane until the warp's batch is done;
+                                 1 = binary tree, lanes take new rays as theirs
+                                 finish (while-while); 2 = 4-wide tree, batch */
+  RTX_OPT_MIN_BUSY = 11       /* with RTX_OPT_TRAVERSAL = 1: refill a warp once
+                                 fewer lanes than this are traversing (0..32) */
 };
 
 typedef struct rtx_context rtx_context;
@@ -188,6 +196,12 @@ int rtx_image_edge_detect(rtx_context* ctx, const float* in, float* out, int W,
 /* Image::Bloom(size, sigma, threshold) */
 int rtx_image_bloom(rtx_context* ctx, const float* in, float* out, int W,
                     int H, int size, float sigma, float threshold);
+
+/* ---- denoiser building blocks (no RenderToy counterpart) --------------------
+ * C[M x N] (FP32) = A[M x K] * B[N x K]^T on the tcgen05 tensor cores, A and
+ * B row-major BF16 (K contiguous); K must be a multiple of 8. */
+int rtx_nn_gemm_bf16(rtx_context* ctx, int M, int N, int K, const void* A,
+                     const void* B, float* C);
 
 /* ---- without allocation -----------------------------------------------------
  * No counterpart in RenderToy.  Image::GaussianBlur (as rtx_image_gaussian_blur)

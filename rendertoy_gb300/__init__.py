@@ -19,7 +19,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "librtx.so")
 
 OPT_ASYNC, OPT_WAVE_PATHS, OPT_BLOCK, OPT_SORT_MATERIAL, OPT_COUNT_VISITS, OPT_LEAF_SIZE, \
-    OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING, OPT_ACCUMULATE = 1, 2, 3, 4, 5, 6, 7, 8, 9
+    OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING, OPT_ACCUMULATE, OPT_TRAVERSAL, OPT_MIN_BUSY = \
+    1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11
 
 STATUS = {0: "RTX_OK", 1: "RTX_ERR_INVALID", 2: "RTX_ERR_CUDA", 3: "RTX_ERR_NOMEM",
           4: "RTX_ERR_NO_SCENE", 5: "RTX_ERR_DEVICE"}
@@ -31,7 +32,7 @@ EXPORTS = [
     "rtx_scene_upload", "rtx_scene_emitters", "rtx_scene_set_emitters", "rtx_render_pt", "rtx_trace_paths",
     "rtx_render_aov", "rtx_primary_hits", "rtx_intersect", "rtx_image_convolve",
     "rtx_image_gaussian_blur", "rtx_image_edge_detect", "rtx_image_bloom",
-    "rtx_image_gaussian_blur_noalloc",
+    "rtx_image_gaussian_blur_noalloc", "rtx_nn_gemm_bf16",
 ]
 
 
@@ -88,6 +89,7 @@ def lib() -> C.CDLL:
         "rtx_image_edge_detect": (i, [vp, vp, vp, i, i]),
         "rtx_image_bloom": (i, [vp, vp, vp, i, i, i, f, f]),
         "rtx_image_gaussian_blur_noalloc": (i, [vp, vp, i, i, i, f, vp, C.c_char_p, C.c_size_t]),
+        "rtx_nn_gemm_bf16": (i, [vp, i, i, i, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -230,6 +232,16 @@ class Context:
         tuv = np.zeros((n, 3), np.float32)
         self._check(self.L.rtx_intersect(self.h, n, _ptr(rays), _ptr(ex), _ptr(tri), _ptr(tuv)))
         return tri, tuv
+
+    # -- denoiser building blocks ---------------------------------------------
+    def gemm_bf16(self, A, B, out=None):
+        """C = A @ B.T on the tensor cores; A, B are uint16 arrays of BF16 bits
+        (or device tensors of dtype bfloat16)."""
+        M, K = A.shape
+        N = B.shape[0]
+        C_ = np.zeros((M, N), np.float32) if out is None else out
+        self._check(self.L.rtx_nn_gemm_bf16(self.h, M, N, K, _ptr(A), _ptr(B), _ptr(C_)))
+        return C_
 
     # -- compositor -------------------------------------------------------------
     @staticmethod

@@ -90,7 +90,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for f in cu:
         o = os.path.join(OBJ, f + ".o")
         objs.append(o)
-        cmds.append([_nvcc(), *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17",
+        extra = os.environ.get("RTX_NVCC_FLAGS", "").split()
+        cmds.append([_nvcc(), *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", *extra,
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3",
                      *inc, "-c", os.path.join(CSRC, f), "-o", o])
     for f in cpp:

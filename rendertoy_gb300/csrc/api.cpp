@@ -75,13 +75,15 @@ struct rtx_context {
   bool sort_material = false;
   bool count_visits = false;
   int leaf_size = 4;
-  bool primary_cache = false;
+  bool primary_cache = true;
   bool accumulate = false;
+  int traversal = 0;
+  int min_busy = 20;
   KernelTimer timer;
   // scene
   bool has_scene = false;
   DeviceScene ds{};
-  DevBuf nodes, tris, shade, geo, mats, emit;
+  DevBuf nodes, nodes4, tris, shade, geo, mats, emit;
   std::vector<int32_t> emitters;
   // device scratch
   int* d_err = nullptr;
@@ -151,6 +153,7 @@ int finish(rtx_context* c, bool may_async) {
     if (herr & kErrStackOverflow) m += " traversal stack overflow";
     if (herr & kErrQueueOverflow) m += " queue overflow";
     if (herr & kErrBadIndex) m += " index out of range";
+    if (herr & 8) m += " tensor-core barrier wait timed out";
     return fail(c, RTX_ERR_DEVICE, m);
   }
   return RTX_OK;
@@ -300,6 +303,7 @@ void rtx_destroy(rtx_context* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->nodes.release();
+  c->nodes4.release();
   c->tris.release();
   c->shade.release();
   c->geo.release();
@@ -339,6 +343,14 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
     case RTX_OPT_PRIMARY_CACHE: c->primary_cache = v != 0; return RTX_OK;
     case RTX_OPT_KERNEL_TIMING: c->timer.on = v != 0; return RTX_OK;
     case RTX_OPT_ACCUMULATE: c->accumulate = v != 0; return RTX_OK;
+    case RTX_OPT_TRAVERSAL:
+      if (v < 0 || v > 2) return fail(c, RTX_ERR_INVALID, "traversal must be 0, 1 or 2");
+      c->traversal = (int)v;
+      return RTX_OK;
+    case RTX_OPT_MIN_BUSY:
+      if (v < 0 || v > 32) return fail(c, RTX_ERR_INVALID, "min busy lanes must be in [0, 32]");
+      c->min_busy = (int)v;
+      return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -355,6 +367,8 @@ int rtx_get_option(rtx_context* c, int option, int64_t* v) {
     case RTX_OPT_PRIMARY_CACHE: *v = c->primary_cache; return RTX_OK;
     case RTX_OPT_KERNEL_TIMING: *v = c->timer.on; return RTX_OK;
     case RTX_OPT_ACCUMULATE: *v = c->accumulate; return RTX_OK;
+    case RTX_OPT_TRAVERSAL: *v = c->traversal; return RTX_OK;
+    case RTX_OPT_MIN_BUSY: *v = c->min_busy; return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -474,6 +488,7 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   };
   int r;
   if ((r = up(c->nodes, b.nodes.data(), b.nodes.size() * sizeof(float4), "upload nodes"))) return r;
+  if ((r = up(c->nodes4, b.nodes4.data(), b.nodes4.size() * sizeof(float4), "upload nodes4"))) return r;
   if ((r = up(c->tris, b.tris.data(), b.tris.size() * sizeof(float4), "upload tris"))) return r;
   if ((r = up(c->shade, shade.data(), shade.size() * sizeof(float4), "upload shade"))) return r;
   if ((r = up(c->geo, geo.data(), geo.size() * sizeof(float4), "upload geo"))) return r;
@@ -482,6 +497,8 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
 
   DeviceScene& s = c->ds;
   s.nodes = (const float4*)c->nodes.p;
+  s.nodes4 = (const float4*)c->nodes4.p;
+  s.root4 = b.root4;
   s.tris = (const float4*)c->tris.p;
   s.shade = (const float4*)c->shade.p;
   s.geo = (const float4*)c->geo.p;
@@ -565,6 +582,8 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   p.accumulate = acc;
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
+  p.traversal = c->traversal;
+  p.min_busy = c->min_busy;
   RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
   int launches = 0, ext_launches = 0;
   std::string why;
@@ -733,6 +752,23 @@ int rtx_image_gaussian_blur(rtx_context* c, const float* in, float* out, int W, 
 int rtx_image_bloom(rtx_context* c, const float* in, float* out, int W, int H, int size,
                     float sigma, float threshold) {
   return gaussian_common(c, in, out, W, H, size, sigma, true, threshold);
+}
+
+int rtx_nn_gemm_bf16(rtx_context* c, int M, int N, int K, const void* A, const void* B, float* C) {
+  if (!c) return RTX_ERR_INVALID;
+  if (M <= 0 || N <= 0 || K <= 0 || K % 8) return fail(c, RTX_ERR_INVALID, "M, N, K must be positive and K % 8 == 0");
+  if (!A || !B || !C) return fail(c, RTX_ERR_INVALID, "NULL operand");
+  int r;
+  if ((r = begin(c))) return r;
+  Arg aa, ab, ac;
+  if ((r = bind_in(c, A, (size_t)M * K * 2, 0, aa))) return r;
+  if ((r = bind_in(c, B, (size_t)N * K * 2, 1, ab))) return r;
+  if ((r = bind_out(c, C, (size_t)M * N * 4, 2, ac))) return r;
+  cudaError_t e = launch_gemm_bf16(aa.dev, ab.dev, (float*)ac.dev, M, N, K, c->d_err, c->stream);
+  c->stats.kernel_launches = 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "gemm kernel");
+  if ((r = copy_back(c, ac))) return r;
+  return finish(c, all_device({&aa, &ab, &ac}));
 }
 
 int rtx_image_edge_detect(rtx_context* c, const float* in, float* out, int W, int H) {

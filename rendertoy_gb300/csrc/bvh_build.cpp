@@ -181,6 +181,80 @@ struct Builder {
   }
 };
 
+// Collapse the binary tree into a 4-wide one: a 4-wide node takes a binary
+// node's two children and keeps replacing its largest-area inner child by
+// that child's two children until it has four (or only leaves remain).
+struct Collapser {
+  const std::vector<float4>& bin;
+  std::vector<float4>& out;
+  int max_depth = 0;
+
+  struct Child {
+    float lo[3], hi[3];
+    int ref;
+  };
+
+  Child child_of(int b, int k) const {
+    const float4* n = &bin[4 * (size_t)b];
+    Child c;
+    if (k == 0) {
+      c.lo[0] = n[0].x; c.hi[0] = n[0].y; c.lo[1] = n[0].z; c.hi[1] = n[0].w;
+      c.lo[2] = n[2].x; c.hi[2] = n[2].y;
+      std::memcpy(&c.ref, &n[3].x, 4);
+    } else {
+      c.lo[0] = n[1].x; c.hi[0] = n[1].y; c.lo[1] = n[1].z; c.hi[1] = n[1].w;
+      c.lo[2] = n[2].z; c.hi[2] = n[2].w;
+      std::memcpy(&c.ref, &n[3].y, 4);
+    }
+    return c;
+  }
+
+  static float area(const Child& c) {
+    float d0 = c.hi[0] - c.lo[0], d1 = c.hi[1] - c.lo[1], d2 = c.hi[2] - c.lo[2];
+    return d0 * d1 + d1 * d2 + d2 * d0;
+  }
+
+  int collapse(int b, int depth) {
+    max_depth = std::max(max_depth, depth);
+    int idx = (int)(out.size() / 7);
+    out.resize(out.size() + 7);
+    Child ch[4];
+    int n = 2;
+    ch[0] = child_of(b, 0);
+    ch[1] = child_of(b, 1);
+    while (n < 4) {
+      int best = -1;
+      float best_area = -1.0f;
+      for (int k = 0; k < n; ++k)
+        if (ch[k].ref >= 0 && area(ch[k]) > best_area) {
+          best = k;
+          best_area = area(ch[k]);
+        }
+      if (best < 0) break;
+      int bb = ch[best].ref;
+      ch[best] = child_of(bb, 0);
+      ch[n++] = child_of(bb, 1);
+    }
+    int refs[4];
+    for (int k = 0; k < 4; ++k) refs[k] = k < n ? (ch[k].ref >= 0 ? collapse(ch[k].ref, depth + 1) : ch[k].ref) : 0;
+    float4* nd = &out[7 * (size_t)idx];
+    float v[6][4];
+    for (int k = 0; k < 4; ++k)
+      for (int a = 0; a < 3; ++a) {
+        v[2 * a][k] = k < n ? ch[k].lo[a] : 1e30f;
+        v[2 * a + 1][k] = k < n ? ch[k].hi[a] : 1e30f;
+      }
+    for (int r = 0; r < 6; ++r) nd[r] = make_float4(v[r][0], v[r][1], v[r][2], v[r][3]);
+    float4 m;
+    std::memcpy(&m.x, &refs[0], 4);
+    std::memcpy(&m.y, &refs[1], 4);
+    std::memcpy(&m.z, &refs[2], 4);
+    std::memcpy(&m.w, &refs[3], 4);
+    nd[6] = m;
+    return idx;
+  }
+};
+
 }  // namespace
 
 BvhBuildResult build_bvh(const float* verts, int n, int max_leaf) {
@@ -214,6 +288,15 @@ BvhBuildResult build_bvh(const float* verts, int n, int max_leaf) {
   res.n_nodes = (int)(res.nodes.size() / 4);
   res.n_leaves = b.n_leaves;
   res.depth = b.max_depth;
+  if (res.root >= 0) {
+    Collapser col{res.nodes, res.nodes4};
+    res.nodes4.reserve(res.nodes.size() * 7 / 4 / 2 + 7);
+    res.root4 = col.collapse(res.root, 0);
+    res.depth4 = col.max_depth;
+  } else {
+    res.root4 = res.root;
+  }
+  res.n_nodes4 = (int)(res.nodes4.size() / 7);
   res.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return res;
 }

@@ -15,6 +15,14 @@
 namespace rtx {
 
 #define RTX_DEV __device__ __forceinline__
+// The BSDF lobes are called from both Eval and Sample; compiling them once
+// (not inlined twice) keeps the shading kernel small enough for the
+// instruction cache.
+#ifndef RTX_LOBE_INLINE
+#define RTX_LOBE static __device__ __noinline__
+#else
+#define RTX_LOBE RTX_DEV
+#endif
 
 struct F3 {
   float x, y, z;
@@ -100,21 +108,25 @@ struct Mat {
 };
 
 RTX_DEV Mat load_mat(const float* __restrict__ m) {
+  // the 24-float record is 16-byte aligned: six vector loads
+  const float4* q = reinterpret_cast<const float4*>(m);
+  float4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3), e = __ldg(q + 4);
+  float4 f = __ldg(q + 5);
   Mat r;
-  r.base_color = f3(__ldg(m + 0), __ldg(m + 1), __ldg(m + 2));
-  r.emission = f3(__ldg(m + 3), __ldg(m + 4), __ldg(m + 5));
-  r.roughness = __ldg(m + 6);
-  r.metallic = __ldg(m + 7);
-  r.subsurface = __ldg(m + 9);
-  r.specular_tint = __ldg(m + 10);
-  r.sheen = __ldg(m + 11);
-  r.sheen_tint = __ldg(m + 12);
-  r.clearcoat = __ldg(m + 13);
-  r.clearcoat_roughness = __ldg(m + 14);
-  r.spec_trans = __ldg(m + 15);
-  r.ior = __ldg(m + 16);
-  r.at_distance = __ldg(m + 17);
-  r.extinction = f3(__ldg(m + 18), __ldg(m + 19), __ldg(m + 20));
+  r.base_color = f3(a.x, a.y, a.z);
+  r.emission = f3(a.w, b.x, b.y);
+  r.roughness = b.z;
+  r.metallic = b.w;
+  r.subsurface = c.y;
+  r.specular_tint = c.z;
+  r.sheen = c.w;
+  r.sheen_tint = d.x;
+  r.clearcoat = d.y;
+  r.clearcoat_roughness = d.z;
+  r.spec_trans = d.w;
+  r.ior = e.x;
+  r.at_distance = e.y;
+  r.extinction = f3(e.z, e.w, f.x);
   return r;
 }
 
@@ -144,7 +156,7 @@ RTX_DEV float GTR2(float NdotH, float a) {
   float t = 1.0f + (a2 - 1.0f) * NdotH * NdotH;
   return a2 / (kPi * t * t);
 }
-RTX_DEV F3 SampleGGXVNDF(F3 V, float rgh, float r1, float r2) {
+RTX_LOBE F3 SampleGGXVNDF(F3 V, float rgh, float r1, float r2) {
   F3 Vh = normalized(f3(rgh * V.x, rgh * V.y, V.z));
   float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
   F3 T1 = lensq > 0.0f ? f3(-Vh.y, Vh.x, 0.0f) * (1.0f / sqrtf(lensq)) : f3(1.0f, 0.0f, 0.0f);
@@ -214,7 +226,7 @@ RTX_DEV float FresnelMix(const Mat& m, float eta, float VdotH) {
   float df = DielectricFresnel(VdotH, eta);
   return lerp(df, mf, m.metallic);
 }
-RTX_DEV F3 EvalDiffuse(const Mat& m, F3 Csheen, F3 V, F3 L, F3 H, float& pdf) {
+RTX_LOBE F3 EvalDiffuse(const Mat& m, F3 Csheen, F3 V, F3 L, F3 H, float& pdf) {
   pdf = 0.0f;
   if (L.z <= 0.0f) return f3s(0.0f);
   float FL = SchlickFresnel(L.z);
@@ -233,7 +245,7 @@ RTX_DEV F3 EvalDiffuse(const Mat& m, F3 Csheen, F3 V, F3 L, F3 H, float& pdf) {
   r = r * (1.0f - m.spec_trans);
   return r;
 }
-RTX_DEV F3 EvalSpecReflection(const Mat& m, float eta, F3 specCol, F3 V, F3 L, F3 H,
+RTX_LOBE F3 EvalSpecReflection(const Mat& m, float eta, F3 specCol, F3 V, F3 L, F3 H,
                               float& pdf) {
   pdf = 0.0f;
   if (L.z <= 0.0f) return f3s(0.0f);
@@ -248,7 +260,7 @@ RTX_DEV F3 EvalSpecReflection(const Mat& m, float eta, F3 specCol, F3 V, F3 L, F
   r = r * G2;
   return r / (4.0f * L.z * V.z);
 }
-RTX_DEV F3 EvalSpecRefraction(const Mat& m, float eta, F3 V, F3 L, F3 H, float& pdf) {
+RTX_LOBE F3 EvalSpecRefraction(const Mat& m, float eta, F3 V, F3 L, F3 H, float& pdf) {
   pdf = 0.0f;
   if (L.z >= 0.0f) return f3s(0.0f);
   float F = DielectricFresnel(fabsf(dot(V, H)), eta);
@@ -272,7 +284,7 @@ RTX_DEV F3 EvalSpecRefraction(const Mat& m, float eta, F3 V, F3 L, F3 H, float& 
   r = r * eta;
   return r / (denom * fabsf(L.z) * fabsf(V.z));
 }
-RTX_DEV F3 EvalClearcoat(const Mat& m, F3 V, F3 L, F3 H, float& pdf) {
+RTX_LOBE F3 EvalClearcoat(const Mat& m, F3 V, F3 L, F3 H, float& pdf) {
   pdf = 0.0f;
   if (L.z <= 0.0f) return f3s(0.0f);
   float FH = DielectricFresnel(dot(V, H), 1.0f / 1.5f);
@@ -307,21 +319,34 @@ RTX_DEV void GetLobeProbabilities(const Mat& m, F3 spec_col, float af, float& dw
   strw /= total;
   cw /= total;
 }
-RTX_DEV F3 BsdfEval(const Mat& m, float eta, F3 V, F3 N, F3 L, float& bsdf_pdf) {
+// What Eval and Sample both derive from the shading normal, the outgoing
+// direction and the material: the same operations, done once per vertex.
+struct ShadingFrame {
+  F3 T, B, N, V;  // tangent frame and the outgoing direction in it
+  F3 spec_col, sheen_col;
+};
+
+RTX_DEV ShadingFrame make_frame(const Mat& m, float eta, F3 N, F3 V) {
+  ShadingFrame fr;
+  Onb(N, fr.T, fr.B);
+  fr.N = N;
+  fr.V = ToLocal(fr.T, fr.B, N, V);
+  GetSpecColor(m, eta, fr.spec_col, fr.sheen_col);
+  return fr;
+}
+
+RTX_DEV F3 BsdfEvalFrame(const Mat& m, float eta, const ShadingFrame& fr, F3 L, float& bsdf_pdf) {
   bsdf_pdf = 0.0f;
   F3 f = f3s(0.0f);
-  F3 T, B;
-  Onb(N, T, B);
-  V = ToLocal(T, B, N, V);
-  L = ToLocal(T, B, N, L);
+  F3 V = fr.V;
+  L = ToLocal(fr.T, fr.B, fr.N, L);
   F3 H;
   if (L.z > 0.0f)
     H = normalized(L + V);
   else
     H = normalized(L + V * eta);
   if (H.z < 0.0f) H = -H;
-  F3 spec_color, sheen_color;
-  GetSpecColor(m, eta, spec_color, sheen_color);
+  F3 spec_color = fr.spec_col, sheen_color = fr.sheen_col;
   float dw, srw, strw, cw;
   float fresnel = FresnelMix(m, eta, dot(V, H));
   GetLobeProbabilities(m, spec_color, fresnel, dw, srw, strw, cw);
@@ -344,16 +369,13 @@ RTX_DEV F3 BsdfEval(const Mat& m, float eta, F3 V, F3 N, F3 L, float& bsdf_pdf) 
   }
   return f * fabsf(L.z);
 }
-RTX_DEV bool BsdfSample(const Mat& m, float eta, F3 N, F3 in_dir, float r1, float r2,
-                        F3& out_dir, F3& color_o, float& pdf) {
+RTX_DEV bool BsdfSampleFrame(const Mat& m, float eta, const ShadingFrame& fr, float r1, float r2,
+                             F3& out_dir, F3& color_o, float& pdf) {
   pdf = 0.0f;
   F3 f = f3s(0.0f);
-  F3 V = in_dir;
-  F3 T, B;
-  Onb(N, T, B);
-  V = ToLocal(T, B, N, V);
-  F3 specCol, sheenCol;
-  GetSpecColor(m, eta, specCol, sheenCol);
+  F3 V = fr.V;
+  F3 T = fr.T, B = fr.B, N = fr.N;
+  F3 specCol = fr.spec_col, sheenCol = fr.sheen_col;
   float dw, srw, strw, cw;
   float approxFresnel = FresnelMix(m, eta, V.z);
   GetLobeProbabilities(m, specCol, approxFresnel, dw, srw, strw, cw);
@@ -393,6 +415,15 @@ RTX_DEV bool BsdfSample(const Mat& m, float eta, F3 N, F3 in_dir, float r1, floa
   out_dir = ToWorld(T, B, N, out_dir);
   color_o = f * fabsf(dot(N, out_dir));
   return !eq_zero_eps(out_dir);
+}
+
+// PrincipledBSDF::Eval / Sample with their own frame (material.cpp:143, 206)
+RTX_DEV F3 BsdfEval(const Mat& m, float eta, F3 V, F3 N, F3 L, float& bsdf_pdf) {
+  return BsdfEvalFrame(m, eta, make_frame(m, eta, N, V), L, bsdf_pdf);
+}
+RTX_DEV bool BsdfSample(const Mat& m, float eta, F3 N, F3 in_dir, float r1, float r2,
+                        F3& out_dir, F3& color_o, float& pdf) {
+  return BsdfSampleFrame(m, eta, make_frame(m, eta, N, in_dir), r1, r2, out_dir, color_o, pdf);
 }
 
 }  // namespace rtx

@@ -27,9 +27,20 @@
 namespace rtx {
 
 constexpr int kMaxDepthSlots = 64;
+// minimum resident blocks of 128 threads per SM (register budget)
+#ifndef RTX_SHADE_MINB
+#define RTX_SHADE_MINB 8
+#endif
+#ifndef RTX_TRACE_MINB
+#define RTX_TRACE_MINB 1
+#endif
+// path state 6 x 16 B + shadow record 4 x 16 B + two queue entries
+constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 2 * 4;
 
 struct PtWorkspace {
   size_t cap = 0;
+  float4* prim = nullptr;  // per-pixel primary hits
+  size_t prim_cap = 0;
   float4 *ray_o = nullptr, *ray_d = nullptr, *thr = nullptr, *rad = nullptr, *absb = nullptr,
          *hit = nullptr;
   int* queue[2] = {nullptr, nullptr};
@@ -57,6 +68,7 @@ static void ws_free(PtWorkspace* w) {
 void pt_workspace_destroy(PtWorkspace* ws) {
   if (!ws) return;
   ws_free(ws);
+  if (ws->prim) cudaFree(ws->prim);
   delete ws;
 }
 
@@ -82,7 +94,7 @@ struct PtArgs {
   int* err;
   Counters* ctr;
   long long q0;
-  int n_wave, npix, W, first_sample, max_depth, depth;
+  int n_wave, npix, W, first_sample, max_depth, depth, min_busy;
   uint32_t k0, k1;
 };
 
@@ -105,12 +117,13 @@ RTX_DEV int warp_fetch(int* work) {
   return __shfl_sync(0xffffffffu, base, 0);
 }
 
-__global__ void k_raygen(PtArgs a, CamParams cam) {
+__global__ void k_raygen(PtArgs a, CamParams cam, const float4* __restrict__ prim) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) a.counts[0] = a.n_wave;
   if (i >= a.n_wave) return;
   long long q = a.q0 + i;
   int pix = (int)(q % a.npix);
+  if (prim) a.hit[i] = prim[pix];
   F3 o, d;
   camera_ray(cam, pix % a.W, pix / a.W, o, d);
   a.ray_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
@@ -121,9 +134,64 @@ __global__ void k_raygen(PtArgs a, CamParams cam) {
   a.queue_in[i] = i;
 }
 
+// Lanes of a warp that need a ray take the next ones from the queue; a lane
+// finds none left when the queue is exhausted.
+RTX_DEV int warp_refill(bool need, int* work, int n, bool& retired) {
+  unsigned m = __ballot_sync(0xffffffffu, need);
+  int item = -1;
+  if (m) {
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(work, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need) {
+      int i = base + __popc(m & ((1u << lane) - 1u));
+      if (i < n)
+        item = i;
+      else
+        retired = true;
+    }
+  }
+  return item;
+}
+
+// Closest hit of every live path (BVH::Intersect, renderer.cpp:282): persistent
+// warps; a lane whose ray finishes takes a new one (dynamic fetch).
 template <bool kCount>
-__global__ void k_extend(PtArgs a, DeviceScene s) {
-  int n = a.counts[a.depth];
+__global__ void __launch_bounds__(128) k_extend(PtArgs a, DeviceScene s) {
+  const int n = a.counts[a.depth];
+  int* work = a.work + 2 * a.depth;
+  VisitCount vc;
+  Trav r;
+  int stack[kStackSize];
+  int p = -1;
+  bool retired = false;
+  while (true) {
+    int i = warp_refill(p < 0 && !retired, work, n, retired);
+    if (i >= 0) {
+      p = a.queue_in[i];
+      float4 ro = a.ray_o[p], rd = a.ray_d[p];
+      trav_begin(r, stack, s, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z), __float_as_int(rd.w), -1,
+                 kInf);
+    }
+    if (__all_sync(0xffffffffu, p < 0)) break;
+    if (p >= 0 && trav_run<false, kCount>(r, stack, s, a.err, vc, a.min_busy)) {
+      a.hit[p] = make_float4(__int_as_float(r.best), r.tmax, r.u, r.v);
+      p = -1;
+    }
+  }
+  if (kCount) {
+    atomicAdd(&a.ctr->ext_node_visits, (unsigned long long)vc.nodes);
+    atomicAdd(&a.ctr->ext_tri_tests, (unsigned long long)vc.tris);
+  }
+}
+
+// Variant: a warp takes 32 rays at a time and each lane traces its ray to the
+// end before the warp takes the next batch.
+template <bool kCount, bool kWide>
+__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_extend_batch(PtArgs a, DeviceScene s) {
+  const int n = a.counts[a.depth];
   VisitCount vc;
   int lane = threadIdx.x & 31;
   while (true) {
@@ -134,8 +202,10 @@ __global__ void k_extend(PtArgs a, DeviceScene s) {
       int p = a.queue_in[i];
       float4 ro = a.ray_o[p], rd = a.ray_d[p];
       float t, u, v;
-      int h = closest_hit<kCount>(s, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z),
-                                  __float_as_int(rd.w), t, u, v, a.err, vc);
+      int h = kWide ? trace4<false, kCount>(s, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z),
+                                            __float_as_int(rd.w), -1, t, u, v, a.err, vc)
+                    : closest_hit<kCount>(s, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z),
+                                          __float_as_int(rd.w), t, u, v, a.err, vc);
       a.hit[p] = make_float4(__int_as_float(h), t, u, v);
     }
   }
@@ -145,7 +215,27 @@ __global__ void k_extend(PtArgs a, DeviceScene s) {
   }
 }
 
-__global__ void k_shade(PtArgs a, DeviceScene s) {
+// Primary hits of every pixel, traced once per render: all samples of a pixel
+// share its primary ray (renderer.cpp:255-259 has no per-sample jitter).
+__global__ void __launch_bounds__(64) k_primary_cache(DeviceScene s, CamParams cam, float4* out,
+                                                      int* err, Counters* ctr) {
+  int tiles_x = (cam.W + 7) >> 3;
+  int x = (blockIdx.x % tiles_x) * 8 + (threadIdx.x & 7);
+  int y = (blockIdx.x / tiles_x) * 8 + (threadIdx.x >> 3);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&ctr->ext_rays, (unsigned long long)cam.W * cam.H);
+    atomicAdd(&ctr->ext_rays_by_depth[0], (unsigned long long)cam.W * cam.H);
+  }
+  if (x >= cam.W || y >= cam.H) return;
+  F3 o, d;
+  camera_ray(cam, x, y, o, d);
+  float t, u, v;
+  VisitCount vc;
+  int h = closest_hit<false>(s, o, d, -1, t, u, v, err, vc);
+  out[(size_t)y * cam.W + x] = make_float4(__int_as_float(h), t, u, v);
+}
+
+__global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceScene s) {
   int n = a.counts[a.depth];
   const int depth = a.depth;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -191,7 +281,10 @@ __global__ void k_shade(PtArgs a, DeviceScene s) {
     acc = acc + T * E;
     float dist = length(pos - o);
     F3 expo = (-absorption) * dist;
-    F3 br = f3(powf(kE, expo.x), powf(kE, expo.y), powf(kE, expo.z));
+    // pow(e, +-0) is exactly 1: skip the call for the common no-absorption case
+    F3 br = f3(expo.x == 0.0f ? 1.0f : powf(kE, expo.x), expo.y == 0.0f ? 1.0f : powf(kE, expo.y),
+               expo.z == 0.0f ? 1.0f : powf(kE, expo.z));
+    ShadingFrame fr = make_frame(m, eta, ff, -d);
 
     long long q = a.q0 + p;
     Rng rng{a.k0, a.k1, (uint32_t)(q % a.npix), (uint32_t)(a.first_sample + q / a.npix),
@@ -208,7 +301,7 @@ __global__ void k_shade(PtArgs a, DeviceScene s) {
       F3 emit_pos = (f3(g1.x, g1.y, g1.z) * aa + f3(g2.x, g2.y, g2.z) * bb) + f3(g0.x, g0.y, g0.z);
       F3 dl = normalized(emit_pos - pos);
       float bpdf;
-      F3 f = BsdfEval(m, eta, -d, ff, dl, bpdf);
+      F3 f = BsdfEvalFrame(m, eta, fr, dl, bpdf);
       if (bpdf > 0.0f) {
         int slot = warp_append(a.shadow_counts + depth);
         F3 tb = T * br;
@@ -224,9 +317,12 @@ __global__ void k_shade(PtArgs a, DeviceScene s) {
     F3 nd, color;
     float pdf;
     bool cont = false;
-    if (BsdfSample(m, eta, ff, -d, r1, r2, nd, color, pdf)) {
-      absorption = f3(-logf(m.extinction.x), -logf(m.extinction.y), -logf(m.extinction.z)) /
-                   m.at_distance;
+    if (BsdfSampleFrame(m, eta, fr, r1, r2, nd, color, pdf)) {
+      // log(1) is exactly +0: skip the call for the default extinction
+      F3 lg = f3(m.extinction.x == 1.0f ? 0.0f : logf(m.extinction.x),
+                 m.extinction.y == 1.0f ? 0.0f : logf(m.extinction.y),
+                 m.extinction.z == 1.0f ? 0.0f : logf(m.extinction.z));
+      absorption = (-lg) / m.at_distance;
       if (pdf > 0.0f) {
         F3 w = (br * color) / pdf;
         if (depth + 1 < a.max_depth) {
@@ -251,9 +347,36 @@ __global__ void k_shade(PtArgs a, DeviceScene s) {
   }
 }
 
-template <bool kCount>
-__global__ void k_connect(PtArgs a, DeviceScene s) {
-  int n = a.shadow_counts[a.depth];
+// Emitter's own exact test for a shadow record: the emitter is the target of
+// the occlusion query when the ray reaches it (t < 1e7); otherwise any hit
+// occludes.
+RTX_DEV bool emitter_hit(const DeviceScene& s, F3 pos, F3 dir, int e, int ex, float& te, float& ue,
+                         float& ve) {
+  te = kInf;
+  ue = 0.0f;
+  ve = 0.0f;
+  if (e == ex) return false;
+  const float4* g = s.geo + 3 * (size_t)e;
+  float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2);
+  float tt, uu, vv;
+  if (tri_hit(pos, dir, f3(g0.x, g0.y, g0.z), f3(g1.x, g1.y, g1.z), f3(g2.x, g2.y, g2.z), tt, uu, vv) &&
+      tt < kInf) {
+    te = tt;
+    ue = uu;
+    ve = vv;
+    return true;
+  }
+  return false;
+}
+
+// Visibility of each light sample (renderer.cpp:352-354: the light is seen
+// when the closest hit is the sampled emitter or nothing) as an occlusion
+// query, then the MIS-weighted contribution (renderer.cpp:356-379).
+RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec);
+
+template <bool kCount, bool kWide>
+__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_connect_batch(PtArgs a, DeviceScene s) {
+  const int n = a.shadow_counts[a.depth];
   VisitCount vc;
   int lane = threadIdx.x & 31;
   while (true) {
@@ -261,54 +384,89 @@ __global__ void k_connect(PtArgs a, DeviceScene s) {
     if (base >= n) break;
     int i = base + lane;
     if (i >= n) continue;
-    const float4* r = a.shadow + 4 * (size_t)i;
-    float4 r0 = r[0], r1 = r[1], r2 = r[2], r3 = r[3];
-    F3 pos = f3(r0.x, r0.y, r0.z), emit_pos = f3(r1.x, r1.y, r1.z);
-    int p = __float_as_int(r0.w), e = __float_as_int(r1.w), ex = __float_as_int(r3.w);
-    F3 dir = normalized(emit_pos - pos);
-    // Closest-hit visibility of renderer.cpp:352-354 as an occlusion query:
-    // the light is seen when no other triangle lies nearer than the emitter
-    // (or, when the emitter itself is missed, when nothing is hit at all).
-    float te = kInf, ue = 0.0f, ve = 0.0f;
-    bool he = false;
-    if (e != ex) {
-      const float4* g = s.geo + 3 * (size_t)e;
-      float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2);
-      float tt, uu, vv;
-      if (tri_hit(pos, dir, f3(g0.x, g0.y, g0.z), f3(g1.x, g1.y, g1.z), f3(g2.x, g2.y, g2.z), tt,
-                  uu, vv) &&
-          tt < kInf) {
-        he = true;
-        te = tt;
-        ue = uu;
-        ve = vv;
-      }
+    const float4* q = a.shadow + 4 * (size_t)i;
+    float4 q0 = q[0], q1 = q[1], q3 = q[3];
+    F3 pos = f3(q0.x, q0.y, q0.z);
+    F3 dir = normalized(f3(q1.x, q1.y, q1.z) - pos);
+    int e = __float_as_int(q1.w), ex = __float_as_int(q3.w);
+    float te, ue, ve;
+    bool he = emitter_hit(s, pos, dir, e, ex, te, ue, ve);
+    bool occ;
+    if (kWide) {
+      float uu, vv;
+      occ = trace4<true, kCount>(s, pos, dir, ex, he ? e : -1, te, uu, vv, a.err, vc) == 1;
+    } else {
+      occ = occluded<kCount>(s, pos, dir, ex, he ? e : -1, te, a.err, vc);
     }
-    bool occ = he ? occluded<kCount>(s, pos, dir, ex, e, te, a.err, vc)
-                  : occluded<kCount>(s, pos, dir, ex, -1, kInf, a.err, vc);
-    if (occ) continue;
-    float4 s0 = __ldg(s.shade + 4 * (size_t)e), s1 = __ldg(s.shade + 4 * (size_t)e + 1);
-    int info = __float_as_int(s1.w);
-    F3 Ne = shading_normal(s, e, ue, ve, s0, s1, info < 0);
-    F3 rv = pos - emit_pos;
-    float d2 = dot(rv, rv);
-    float cos_area = dot(-dir, Ne) * s0.w;
-    float lpdf = fabsf(d2 / cos_area);
-    const float* me = s.mats + 24 * (size_t)(info & 0x7fffffff);
-    F3 Le = f3(__ldg(me + 3), __ldg(me + 4), __ldg(me + 5));
-    float w = PowerHeuristic(lpdf, r2.w);
-    F3 c = f3(r2.x, r2.y, r2.z) * w;
-    c = c * Le;
-    c = c * (float)s.n_emitters;
-    c = c / lpdf;
-    float4 acc = a.rad[p];
-    F3 tb = f3(r3.x, r3.y, r3.z) * c;
-    a.rad[p] = make_float4(acc.x + tb.x, acc.y + tb.y, acc.z + tb.z, 0.0f);
+    if (!occ) add_light(a, s, i);
   }
   if (kCount) {
     atomicAdd(&a.ctr->sh_node_visits, (unsigned long long)vc.nodes);
     atomicAdd(&a.ctr->sh_tri_tests, (unsigned long long)vc.tris);
   }
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(128) k_connect(PtArgs a, DeviceScene s) {
+  const int n = a.shadow_counts[a.depth];
+  int* work = a.work + 2 * a.depth + 1;
+  VisitCount vc;
+  Trav r;
+  int stack[kStackSize];
+  int rec = -1;
+  bool retired = false;
+  while (true) {
+    int i = warp_refill(rec < 0 && !retired, work, n, retired);
+    if (i >= 0) {
+      rec = i;
+      const float4* q = a.shadow + 4 * (size_t)rec;
+      float4 q0 = q[0], q1 = q[1], q3 = q[3];
+      F3 pos = f3(q0.x, q0.y, q0.z);
+      F3 dir = normalized(f3(q1.x, q1.y, q1.z) - pos);
+      int e = __float_as_int(q1.w), ex = __float_as_int(q3.w);
+      float te, ue, ve;
+      bool he = emitter_hit(s, pos, dir, e, ex, te, ue, ve);
+      trav_begin(r, stack, s, pos, dir, ex, he ? e : -1, te);
+    }
+    if (__all_sync(0xffffffffu, rec < 0)) break;
+    if (rec >= 0 && trav_run<true, kCount>(r, stack, s, a.err, vc, a.min_busy)) {
+      if (r.best != 1) add_light(a, s, rec);
+      rec = -1;
+    }
+  }
+  if (kCount) {
+    atomicAdd(&a.ctr->sh_node_visits, (unsigned long long)vc.nodes);
+    atomicAdd(&a.ctr->sh_tri_tests, (unsigned long long)vc.tris);
+  }
+}
+
+// MIS-weighted light contribution of a visible light sample
+// (renderer.cpp:356-379), added to its path's radiance.
+RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec) {
+  const float4* q = a.shadow + 4 * (size_t)rec;
+  float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+  F3 pos = f3(q0.x, q0.y, q0.z), emit_pos = f3(q1.x, q1.y, q1.z);
+  int p = __float_as_int(q0.w), e = __float_as_int(q1.w), ex = __float_as_int(q3.w);
+  F3 dir = normalized(emit_pos - pos);
+  float te, ue, ve;
+  emitter_hit(s, pos, dir, e, ex, te, ue, ve);  // (u, v) of the emitter hit, or (0, 0)
+  float4 s0 = __ldg(s.shade + 4 * (size_t)e), s1 = __ldg(s.shade + 4 * (size_t)e + 1);
+  int info = __float_as_int(s1.w);
+  F3 Ne = shading_normal(s, e, ue, ve, s0, s1, info < 0);
+  F3 rv = pos - emit_pos;
+  float d2 = dot(rv, rv);
+  float cos_area = dot(-dir, Ne) * s0.w;
+  float lpdf = fabsf(d2 / cos_area);
+  const float* me = s.mats + 24 * (size_t)(info & 0x7fffffff);
+  F3 Le = f3(__ldg(me + 3), __ldg(me + 4), __ldg(me + 5));
+  float w = PowerHeuristic(lpdf, q2.w);
+  F3 c = f3(q2.x, q2.y, q2.z) * w;
+  c = c * Le;
+  c = c * (float)s.n_emitters;
+  c = c / lpdf;
+  float4 acc = a.rad[p];
+  F3 tb = f3(q3.x, q3.y, q3.z) * c;
+  a.rad[p] = make_float4(acc.x + tb.x, acc.y + tb.y, acc.z + tb.z, 0.0f);
 }
 
 __global__ void k_accumulate(const float4* rad, long long q0, int n_wave, int npix, float spp,
@@ -338,12 +496,14 @@ __global__ void k_accumulate(const float4* rad, long long q0, int n_wave, int np
   o[2] = acc.z;
 }
 
-__global__ void k_tally(const int* counts, const int* shadow_counts, int max_depth, Counters* c) {
+__global__ void k_tally(const int* counts, const int* shadow_counts, int max_depth, int first_traced,
+                        Counters* c) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   unsigned long long e = 0, sh = 0;
   for (int d = 0; d < max_depth; ++d) {
-    e += (unsigned)counts[d];
     sh += (unsigned)shadow_counts[d];
+    if (d < first_traced) continue;  // primary hits came from the per-pixel cache
+    e += (unsigned)counts[d];
     if (d < 16) c->ext_rays_by_depth[d] += (unsigned)counts[d];
   }
   c->ext_rays += e;
@@ -393,7 +553,16 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
       (e = cudaMemsetAsync(d_out, 0, (size_t)npix * 3 * sizeof(float), st)))
     return e;
   if (total == 0) return cudaSuccess;
-  long long wave = p.wave_paths > 0 ? p.wave_paths : (1LL << 22);
+  // Paths in flight: the whole render when it fits (every vertex launch has an
+  // idle tail, so fewer, larger waves are faster), at most 2^26 paths and a
+  // quarter of the free device memory (176 B of path state per path).
+  long long wave = p.wave_paths;
+  if (wave <= 0) {
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    long long fit = (long long)(free_b / 4 / kPathBytes);
+    wave = std::max(1LL << 20, std::min(1LL << 26, fit));
+  }
   wave = std::min(wave, total);
   if ((e = ws_reserve(ws, (size_t)wave)) != cudaSuccess) return e;
   int block = p.block > 0 ? p.block : 128;
@@ -401,9 +570,18 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     int dev;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_extend, k_extend<false>, block, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_connect, k_connect<false>, block, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade, block, 0);
+    int o1 = 0, o2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_extend, k_extend<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, false>, 128, 0);
+    ws->occ_extend = std::min(ws->occ_extend, o1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, true>, 128, 0);
+    ws->occ_extend = std::min(ws->occ_extend, o1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_connect, k_connect<false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, false>, 128, 0);
+    ws->occ_connect = std::min(ws->occ_connect, o2);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, true>, 128, 0);
+    ws->occ_connect = std::min(ws->occ_connect, o2);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade, 128, 0);
     ws->block_cached = block;
   }
   int grid_ext = ws->num_sms * std::max(ws->occ_extend, 1);
@@ -429,7 +607,23 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
   a.max_depth = p.max_depth;
   a.k0 = (uint32_t)p.seed;
   a.k1 = (uint32_t)(p.seed >> 32);
+  a.min_busy = p.min_busy;
   float spp = (float)p.spp;
+
+  const float4* prim = nullptr;
+  if (p.primary_cache) {
+    if (ws->prim_cap < (size_t)npix) {
+      if (ws->prim) cudaFree(ws->prim);
+      ws->prim = nullptr;
+      ws->prim_cap = 0;
+      if ((e = cudaMalloc(&ws->prim, (size_t)npix * sizeof(float4))) != cudaSuccess) return e;
+      ws->prim_cap = (size_t)npix;
+    }
+    int tiles = ((p.W + 7) >> 3) * ((p.H + 7) >> 3);
+    k_primary_cache<<<tiles, 64, 0, st>>>(s, cam, ws->prim, err, d_counters);
+    ++*launches;
+    prim = ws->prim;
+  }
 
   for (long long q0 = 0; q0 < total; q0 += wave) {
     int nw = (int)std::min(wave, total - q0);
@@ -439,34 +633,59 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     a.queue_in = ws->queue[0];
     a.queue_out = ws->queue[1];
     a.depth = 0;
-    k_raygen<<<(nw + 255) / 256, 256, 0, st>>>(a, cam);
+    k_raygen<<<(nw + 255) / 256, 256, 0, st>>>(a, cam, prim);
     ++*launches;
     for (int depth = 0; depth < p.max_depth; ++depth) {
       a.depth = depth;
       a.queue_in = ws->queue[depth & 1];
       a.queue_out = ws->queue[(depth + 1) & 1];
-      if ((e = timer->mark(0, st, true))) return e;
-      if (p.count_visits)
-        k_extend<true><<<grid_ext, block, 0, st>>>(a, s);
-      else
-        k_extend<false><<<grid_ext, block, 0, st>>>(a, s);
-      if ((e = timer->mark(0, st, false))) return e;
+      if (!(prim && depth == 0)) {
+        if ((e = timer->mark(0, st, true))) return e;
+        if (p.traversal == 2) {
+          if (p.count_visits)
+            k_extend_batch<true, true><<<grid_ext, 128, 0, st>>>(a, s);
+          else
+            k_extend_batch<false, true><<<grid_ext, 128, 0, st>>>(a, s);
+        } else if (p.traversal == 0) {
+          if (p.count_visits)
+            k_extend_batch<true, false><<<grid_ext, 128, 0, st>>>(a, s);
+          else
+            k_extend_batch<false, false><<<grid_ext, 128, 0, st>>>(a, s);
+        } else if (p.count_visits) {
+          k_extend<true><<<grid_ext, 128, 0, st>>>(a, s);
+        } else {
+          k_extend<false><<<grid_ext, 128, 0, st>>>(a, s);
+        }
+        if ((e = timer->mark(0, st, false))) return e;
+        ++*extend_launches;
+        ++*launches;
+      }
       if ((e = timer->mark(1, st, true))) return e;
-      k_shade<<<grid_sh, block, 0, st>>>(a, s);
+      k_shade<<<grid_sh, 128, 0, st>>>(a, s);
       if ((e = timer->mark(1, st, false))) return e;
       if ((e = timer->mark(2, st, true))) return e;
-      if (p.count_visits)
-        k_connect<true><<<grid_con, block, 0, st>>>(a, s);
-      else
-        k_connect<false><<<grid_con, block, 0, st>>>(a, s);
+      if (p.traversal == 2) {
+        if (p.count_visits)
+          k_connect_batch<true, true><<<grid_con, 128, 0, st>>>(a, s);
+        else
+          k_connect_batch<false, true><<<grid_con, 128, 0, st>>>(a, s);
+      } else if (p.traversal == 0) {
+        if (p.count_visits)
+          k_connect_batch<true, false><<<grid_con, 128, 0, st>>>(a, s);
+        else
+          k_connect_batch<false, false><<<grid_con, 128, 0, st>>>(a, s);
+      } else if (p.count_visits) {
+        k_connect<true><<<grid_con, 128, 0, st>>>(a, s);
+      } else {
+        k_connect<false><<<grid_con, 128, 0, st>>>(a, s);
+      }
       if ((e = timer->mark(2, st, false))) return e;
-      *launches += 3;
-      ++*extend_launches;
+      *launches += 2;
     }
     int acc_n = p.per_path ? nw : (int)npix;
     k_accumulate<<<(acc_n + 255) / 256, 256, 0, st>>>(ws->rad, q0, nw, (int)npix, spp, d_out,
                                                      p.per_path ? 1 : 0);
-    k_tally<<<1, 32, 0, st>>>(a.counts, a.shadow_counts, p.max_depth, d_counters);
+    k_tally<<<1, 32, 0, st>>>(a.counts, a.shadow_counts, p.max_depth, prim ? 1 : 0, d_counters);
     *launches += 2;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }

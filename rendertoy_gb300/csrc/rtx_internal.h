@@ -15,6 +15,10 @@
 //   shade   : per triangle id, 4 x float4 = 64 B:
 //             (flat normal.xyz, area) (n0.xyz, info) (n1.xyz, 0) (n2.xyz, 0)
 //             info = material index | 0x80000000 when the mesh is smooth
+//   nodes4  : the same tree collapsed to 4 children per node, 7 x float4 =
+//             112 B per node: lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4]
+//             and the four child refs (int bits, as above); an unused slot
+//             holds a degenerate box at 1e30 that no ray reaches before 1e7
 //   geo     : per triangle id, 3 x float4 (v0, e1, e2): emitter sampling
 //   mats    : 24 floats per material; emitters: triangle ids.
 #pragma once
@@ -41,6 +45,8 @@ enum DeviceError : int {
 
 struct DeviceScene {
   const float4* __restrict__ nodes;
+  const float4* __restrict__ nodes4;
+  int root4;  // root of nodes4 (>= 0), a leaf ref (< 0) or kEmptyRoot
   const float4* __restrict__ tris;
   const float4* __restrict__ shade;
   const float4* __restrict__ geo;
@@ -62,10 +68,12 @@ struct CamParams {
 };
 
 struct BvhBuildResult {
-  std::vector<float4> nodes;  // 4 per node
-  std::vector<float4> tris;   // 3 per triangle, leaf order
+  std::vector<float4> nodes;   // 4 per node
+  std::vector<float4> nodes4;  // 7 per 4-wide node
+  std::vector<float4> tris;    // 3 per triangle, leaf order
   int root = kEmptyRoot;
-  int n_nodes = 0, n_leaves = 0, depth = 0;
+  int root4 = kEmptyRoot;
+  int n_nodes = 0, n_nodes4 = 0, n_leaves = 0, depth = 0, depth4 = 0;
   double ms = 0.0;
 };
 
@@ -122,6 +130,8 @@ struct PtParams {
   bool accumulate; // add the mean to the output instead of overwriting it
   bool count_visits;
   bool primary_cache;
+  int traversal;  // RTX_OPT_TRAVERSAL
+  int min_busy;   // RTX_OPT_MIN_BUSY
 };
 PtWorkspace* pt_workspace_create();
 void pt_workspace_destroy(PtWorkspace* ws);
@@ -137,5 +147,7 @@ cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out
                             cudaStream_t st, int* launches);
 cudaError_t launch_edge(const float* in, float* out, int W, int H, cudaStream_t st,
                         int* launches);
+cudaError_t launch_gemm_bf16(const void* A, const void* B, float* C, int M, int N, int K, int* err,
+                             cudaStream_t st);
 
 }  // namespace rtx

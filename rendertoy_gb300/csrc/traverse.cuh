@@ -49,8 +49,10 @@ RTX_DEV bool tri_hit(F3 o, F3 d, F3 v0, F3 e1, F3 e2, float& t, float& u, float&
   return false;
 }
 
+// Slab-test form of a ray: t = plane * inv - origin * inv, one FMA per plane.
+// The box test need not be exact: boxes are widened far beyond its rounding.
 struct RayBox {
-  float ox, oy, oz, ix, iy, iz;
+  float ox, oy, oz, ix, iy, iz;  // ox.. hold -origin * inv
 };
 
 RTX_DEV float safe_inv(float d) {
@@ -59,20 +61,21 @@ RTX_DEV float safe_inv(float d) {
 }
 
 RTX_DEV RayBox make_raybox(F3 o, F3 d) {
-  return RayBox{o.x, o.y, o.z, safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+  float ix = safe_inv(d.x), iy = safe_inv(d.y), iz = safe_inv(d.z);
+  return RayBox{-o.x * ix, -o.y * iy, -o.z * iz, ix, iy, iz};
 }
 
 // Slab test of the two children stored in one node; returns entry distances.
 RTX_DEV void box2(const RayBox& r, float4 n0, float4 n1, float4 n2, float tmax, bool& h0,
                   bool& h1, float& t0, float& t1) {
-  float a0 = (n0.x - r.ox) * r.ix, a1 = (n0.y - r.ox) * r.ix;
-  float b0 = (n0.z - r.oy) * r.iy, b1 = (n0.w - r.oy) * r.iy;
-  float c0 = (n2.x - r.oz) * r.iz, c1 = (n2.y - r.oz) * r.iz;
+  float a0 = __fmaf_rn(n0.x, r.ix, r.ox), a1 = __fmaf_rn(n0.y, r.ix, r.ox);
+  float b0 = __fmaf_rn(n0.z, r.iy, r.oy), b1 = __fmaf_rn(n0.w, r.iy, r.oy);
+  float c0 = __fmaf_rn(n2.x, r.iz, r.oz), c1 = __fmaf_rn(n2.y, r.iz, r.oz);
   float lo0 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
   float hi0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tmax));
-  float d0 = (n1.x - r.ox) * r.ix, d1 = (n1.y - r.ox) * r.ix;
-  float e0 = (n1.z - r.oy) * r.iy, e1 = (n1.w - r.oy) * r.iy;
-  float f0 = (n2.z - r.oz) * r.iz, f1 = (n2.w - r.oz) * r.iz;
+  float d0 = __fmaf_rn(n1.x, r.ix, r.ox), d1 = __fmaf_rn(n1.y, r.ix, r.ox);
+  float e0 = __fmaf_rn(n1.z, r.iy, r.oy), e1 = __fmaf_rn(n1.w, r.iy, r.oy);
+  float f0 = __fmaf_rn(n2.z, r.iz, r.oz), f1 = __fmaf_rn(n2.w, r.iz, r.oz);
   float lo1 = fmaxf(fmaxf(fminf(d0, d1), fminf(e0, e1)), fmaxf(fminf(f0, f1), 0.0f));
   float hi1 = fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1)), fminf(fmaxf(f0, f1), tmax));
   h0 = lo0 <= hi0;
@@ -213,6 +216,242 @@ RTX_DEV bool occluded(const DeviceScene& s, F3 o, F3 d, int exclude, int target,
     node = stack[--sp];
   }
   return false;
+}
+
+// ---------------------------------------------------------------------------
+// 4-wide tree: one node = seven 16-byte loads, four slab tests; the children
+// hit are visited nearest first (sorted by entry distance).
+// ---------------------------------------------------------------------------
+RTX_DEV void cswap(float& ka, int& ra, float& kb, int& rb) {
+  if (kb < ka) {
+    float tk = ka;
+    ka = kb;
+    kb = tk;
+    int tr = ra;
+    ra = rb;
+    rb = tr;
+  }
+}
+
+RTX_DEV float slab(float lo, float hi, float oi, float inv, float& tfar) {
+  float a = __fmaf_rn(lo, inv, oi), b = __fmaf_rn(hi, inv, oi);
+  tfar = fmaxf(a, b);
+  return fminf(a, b);
+}
+
+// Children of a 4-wide node hit before tmax, sorted by entry distance;
+// returns how many.
+RTX_DEV int node4(const RayBox& r, const float4* n, float tmax, int& c0, int& c1, int& c2, int& c3) {
+  float4 lx = __ldg(n), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3);
+  float4 lz = __ldg(n + 4), hz = __ldg(n + 5), rf = __ldg(n + 6);
+  const float kMiss = __int_as_float(0x7f800000);
+  float k[4];
+  const float* LX = &lx.x;
+  const float* HX = &hx.x;
+  const float* LY = &ly.x;
+  const float* HY = &hy.x;
+  const float* LZ = &lz.x;
+  const float* HZ = &hz.x;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float fx, fy, fz;
+    float nx = slab(LX[i], HX[i], r.ox, r.ix, fx);
+    float ny = slab(LY[i], HY[i], r.oy, r.iy, fy);
+    float nz = slab(LZ[i], HZ[i], r.oz, r.iz, fz);
+    float tn = fmaxf(fmaxf(nx, ny), fmaxf(nz, 0.0f));
+    float tf = fminf(fminf(fx, fy), fminf(fz, tmax));
+    k[i] = tn <= tf ? tn : kMiss;
+  }
+  float k0 = k[0], k1 = k[1], k2 = k[2], k3 = k[3];
+  c0 = __float_as_int(rf.x);
+  c1 = __float_as_int(rf.y);
+  c2 = __float_as_int(rf.z);
+  c3 = __float_as_int(rf.w);
+  cswap(k0, c0, k1, c1);
+  cswap(k2, c2, k3, c3);
+  cswap(k0, c0, k2, c2);
+  cswap(k1, c1, k3, c3);
+  cswap(k1, c1, k2, c2);
+  return (k0 < kMiss) + (k1 < kMiss) + (k2 < kMiss) + (k3 < kMiss);
+}
+
+// Closest hit over the 4-wide tree; same result as closest_hit.
+template <bool kAnyHit, bool kCount>
+RTX_DEV int trace4(const DeviceScene& s, F3 o, F3 d, int exclude, int target, float& t, float& u,
+                   float& v, int* err, VisitCount& vc) {
+  // closest hit: t starts at 1e7, returns the triangle; occlusion: t is the
+  // limit, returns 1 when occluded, -1 otherwise
+  if (!kAnyHit) t = kInf;
+  u = 0.0f;
+  v = 0.0f;
+  int best = -1;
+  int node = s.root4;
+  if (node == kEmptyRoot) return -1;
+  RayBox rb = make_raybox(o, d);
+  int stack[kStackSize];
+  int sp = 0;
+  while (true) {
+    if (node >= 0) {
+      if (kCount) vc.nodes++;
+      int c0, c1, c2, c3;
+      int nh = node4(rb, s.nodes4 + 7 * (size_t)node, t, c0, c1, c2, c3);
+      if (nh > 0) {
+        if (sp + 3 > kStackSize) {
+          atomicOr(err, kErrStackOverflow);
+          return kAnyHit ? 1 : best;
+        }
+        if (nh >= 4) stack[sp++] = c3;
+        if (nh >= 3) stack[sp++] = c2;
+        if (nh >= 2) stack[sp++] = c1;
+        node = c0;
+        continue;
+      }
+    } else {
+      int ref = ~node;
+      int first = ref >> 3, cnt = (ref & 7) + 1;
+      for (int k = 0; k < cnt; ++k) {
+        const float4* tp = s.tris + 3 * (size_t)(first + k);
+        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        if (kCount) vc.tris++;
+        int id = __float_as_int(a.w);
+        if (id == exclude || (kAnyHit && id == target)) continue;
+        float tt, uu, vv;
+        if (tri_hit(o, d, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), f3(c.x, c.y, c.z), tt, uu, vv)) {
+          if (kAnyHit) {
+            if (tt < t || (tt == t && id < target)) return 1;
+          } else if (tt < t || (tt == t && id < best)) {
+            t = tt;
+            u = uu;
+            v = vv;
+            best = id;
+          }
+        }
+      }
+    }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+  return best;
+}
+
+// ---------------------------------------------------------------------------
+// Resumable traversal for persistent kernels (Aila & Laine, HPG 2009:
+// while-while loop, speculative postponement of the first leaf, and an exit
+// when too few lanes of the warp are still busy so that the kernel can hand
+// finished lanes new rays).  One lane's ray lives in a Trav; trav_run advances
+// it and returns true once it has finished.
+// ---------------------------------------------------------------------------
+constexpr int kSentinel = 0x76543210;  // bottom of the stack: "nothing left"
+
+struct Trav {
+  F3 o, d;
+  RayBox rb;
+  float tmax;  // closest hit: the nearest t so far; occlusion: the fixed limit
+  float u, v;
+  int best;    // closest hit: triangle id (-1); occlusion: 1 once occluded
+  int exclude, target;
+  int node, leaf, sp;
+};
+
+// `stack` is the lane's traversal stack (kStackSize ints, kept apart from the
+// scalar state so that the latter stays in registers).
+RTX_DEV void trav_begin(Trav& r, int* stack, const DeviceScene& s, F3 o, F3 d, int exclude,
+                        int target, float tmax) {
+  r.o = o;
+  r.d = d;
+  r.rb = make_raybox(o, d);
+  r.exclude = exclude;
+  r.target = target;
+  r.tmax = tmax;
+  r.u = 0.0f;
+  r.v = 0.0f;
+  r.best = -1;
+  r.sp = 0;
+  stack[0] = kSentinel;
+  r.leaf = 0;
+  r.node = s.root;
+  if (s.root == kEmptyRoot) {
+    r.node = kSentinel;
+  } else if (s.root < 0) {  // the whole tree is one leaf
+    r.leaf = s.root;
+    r.node = kSentinel;
+  }
+}
+
+template <bool kAnyHit, bool kCount>
+RTX_DEV bool trav_run(Trav& r, int* stack, const DeviceScene& s, int* err, VisitCount& vc,
+                      int min_busy) {
+  do {
+    // inner nodes: 0 <= node < kSentinel
+    while ((unsigned)r.node < (unsigned)kSentinel) {
+      const float4* n = s.nodes + 4 * (size_t)r.node;
+      float4 n0 = __ldg(n), n1 = __ldg(n + 1), n2 = __ldg(n + 2), n3 = __ldg(n + 3);
+      if (kCount) vc.nodes++;
+      bool h0, h1;
+      float t0, t1;
+      box2(r.rb, n0, n1, n2, r.tmax, h0, h1, t0, t1);
+      int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      if (!h0 && !h1) {
+        r.node = stack[r.sp--];
+      } else {
+        r.node = h0 ? c0 : c1;
+        if (h0 && h1) {
+          int farc = c1;
+          if (t1 < t0) {
+            r.node = c1;
+            farc = c0;
+          }
+          if (r.sp + 1 >= kStackSize) {
+            atomicOr(err, kErrStackOverflow);
+            r.node = kSentinel;
+            r.leaf = 0;
+            return true;
+          }
+          stack[++r.sp] = farc;
+        }
+      }
+      if (r.node < 0 && r.leaf >= 0) {  // first leaf: postpone it, keep descending
+        r.leaf = r.node;
+        r.node = stack[r.sp--];
+      }
+      if (!__any_sync(__activemask(), r.leaf >= 0)) break;  // every busy lane holds a leaf
+    }
+    // postponed leaves
+    while (r.leaf < 0) {
+      int ref = ~r.leaf;
+      int first = ref >> 3, cnt = (ref & 7) + 1;
+      for (int k = 0; k < cnt; ++k) {
+        const float4* tp = s.tris + 3 * (size_t)(first + k);
+        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        if (kCount) vc.tris++;
+        int id = __float_as_int(a.w);
+        if (id == r.exclude || (kAnyHit && id == r.target)) continue;
+        float tt, uu, vv;
+        if (tri_hit(r.o, r.d, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), f3(c.x, c.y, c.z), tt, uu, vv)) {
+          if (kAnyHit) {
+            if (tt < r.tmax || (tt == r.tmax && id < r.target)) {
+              r.best = 1;
+              r.node = kSentinel;
+              break;
+            }
+          } else if (tt < r.tmax || (tt == r.tmax && id < r.best)) {
+            r.tmax = tt;
+            r.u = uu;
+            r.v = vv;
+            r.best = id;
+          }
+        }
+      }
+      if (kAnyHit && r.best == 1) {
+        r.leaf = 0;
+        break;
+      }
+      r.leaf = r.node;
+      if (r.node < 0) r.node = stack[r.sp--];
+    }
+    if (__popc(__activemask()) < min_busy) break;  // let the warp refill idle lanes
+  } while (r.node != kSentinel);
+  return r.node == kSentinel;
 }
 
 // Shading normal (Triangle::NormalC, src/object.cpp:207-217)
