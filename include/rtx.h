@@ -198,10 +198,79 @@ int rtx_image_bloom(rtx_context* ctx, const float* in, float* out, int W,
                     int H, int size, float sigma, float threshold);
 
 /* ---- denoiser building blocks (no RenderToy counterpart) --------------------
- * C[M x N] (FP32) = A[M x K] * B[N x K]^T on the tcgen05 tensor cores, A and
- * B row-major BF16 (K contiguous); K must be a multiple of 8. */
+ * C[M x N] (FP32) = A * B^T on the tcgen05 tensor cores with BF16 operands:
+ * A is M x K row-major (K contiguous), or K x M (M contiguous) when a_mn;
+ * B is N x K, or K x N when b_mn.  The contiguous dimension must be a
+ * multiple of 8. */
 int rtx_nn_gemm_bf16(rtx_context* ctx, int M, int N, int K, const void* A,
-                     const void* B, float* C);
+                     const void* B, float* C, int a_mn, int b_mn);
+
+/* One 3 x 3 "same" convolution of the denoiser, for validating its kernels
+ * operator by operator.  Tensors are NHWC BF16 (uint16 bit patterns): the
+ * input is the channel concatenation of x1 (C1 channels; stored at half
+ * resolution and read upsampled by nearest neighbour when up1 != 0) and x2
+ * (C2 channels, may be NULL with C2 = 0); Cin = C1 + C2.  C1, C2 multiples
+ * of 8; Cout a multiple of 16 and <= 256.
+ *   fwd  : out[P][Cout] (FP32) = relu?(bias + conv(x, w)), w [Cout][9][Cin]
+ *   dgrad: din[P][Cin] (BF16) = conv^T(dout, wt) * (x > 0 if mask_relu),
+ *          wt [Cin][9][Cout], Cin a multiple of 16
+ *   wgrad: dw[Cout][9][Cin] (FP32) = sum_p dout[p] x[p + tap]
+ * P = N * H * W at the convolution's resolution. */
+int rtx_nn_conv3x3_fwd(rtx_context* ctx, int N, int H, int W, const void* x1,
+                       int C1, int up1, const void* x2, int C2, const void* w,
+                       const float* bias, int Cout, int relu, float* out);
+int rtx_nn_conv3x3_dgrad(rtx_context* ctx, int N, int H, int W,
+                         const void* dout, int Cout, const void* wt,
+                         const void* x1, int C1, int up1, const void* x2,
+                         int C2, int mask_relu, void* din);
+int rtx_nn_conv3x3_wgrad(rtx_context* ctx, int N, int H, int W,
+                         const void* dout, int Cout, const void* x1, int C1,
+                         int up1, const void* x2, int C2, float* dw);
+
+/* ---- learned denoiser -------------------------------------------------------
+ * No counterpart in RenderToy: its demos hand the path tracer's buffer to
+ * Intel OIDN, a closed binary (demo/WithOIDN/main.cpp:60).  This is a 5-level
+ * U-Net (3 x 3 convolutions of 32 / 64 / 96 / 128 / 160 channels, 2 x 2
+ * average pooling, nearest upsampling, skip concatenation; 14 layers), run
+ * and trained on the tensor cores in BF16 with FP32 accumulation.
+ * Input, per pixel, 10 FP32 channels: radiance RGB, albedo RGB, normal RGB
+ * (encoded (n + 1) / 2 as the normal pass writes it), depth; the network
+ * predicts log(1 + radiance) and is trained with an L1 loss on
+ * log(1 + target) and Adam (beta 0.9 / 0.999, eps 1e-8).
+ * Batches are [N][H][W][10] with H and W multiples of 16.  Parameters are one
+ * FP32 array in the padded layout rtx_dn_layer describes. */
+int rtx_dn_init(rtx_context* ctx, uint64_t seed);
+/* n_params: FP32 entries of the padded array; n_real: parameters of the
+ * network proper; n_layers: 14; step: Adam steps taken */
+int rtx_dn_info(rtx_context* ctx, int64_t* n_params, int64_t* n_real,
+                int* n_layers, int* step);
+/* info[11] = cout_pad, cout, cin_pad, cin, c1_pad (channels of the first
+ * source; the rest come from the skip connection), up1 (first source read
+ * upsampled), relu, level (resolution = full >> level), w_off, b_off (float
+ * offsets of w [cout_pad][9][cin_pad] and b [cout_pad]), first source id */
+int rtx_dn_layer(rtx_context* ctx, int layer, int64_t info[11]);
+int rtx_dn_get_params(rtx_context* ctx, float* out);
+int rtx_dn_set_params(rtx_context* ctx, const float* in);
+int rtx_dn_get_grads(rtx_context* ctx, float* out);
+int rtx_dn_get_adam(rtx_context* ctx, float* m, float* v);
+int rtx_dn_set_adam(rtx_context* ctx, const float* m, const float* v,
+                    int step);
+/* forward + loss + backward without an update (the gradients stay readable
+ * with rtx_dn_get_grads) */
+int rtx_dn_loss_grads(rtx_context* ctx, const float* input, const float* target,
+                      int N, int H, int W, double* loss);
+/* one Adam step on a minibatch; *loss = the minibatch loss before the step */
+int rtx_dn_train_step(rtx_context* ctx, const float* input, const float* target,
+                      int N, int H, int W, float lr, double* loss);
+/* out [N][H][W][3] = exp(prediction) - 1 */
+int rtx_dn_infer(rtx_context* ctx, const float* input, float* out, int N, int H,
+                 int W);
+/* Denoise one frame from the renderer's passes, each W x H RGB FP32 as
+ * rtx_render_pt / rtx_render_aov write them (depth: channel 0 is used).  Any
+ * W, H: the frame is padded with zeros to multiples of 16 on the device. */
+int rtx_denoise(rtx_context* ctx, const float* radiance, const float* albedo,
+                const float* normal, const float* depth, float* out, int W,
+                int H);
 
 /* ---- without allocation -----------------------------------------------------
  * No counterpart in RenderToy.  Image::GaussianBlur (as rtx_image_gaussian_blur)

@@ -95,3 +95,170 @@ def adam(p, g, m, v, step, lr=3e-4, b1=0.9, b2=0.999, eps=1e-8):
     mh = m / (1 - b1 ** step)
     vh = v / (1 - b2 ** step)
     return p - lr * mh / (np.sqrt(vh) + eps), m, v
+
+
+# ---------------------------------------------------------------------------
+# The whole network, in FP64.
+#
+# Architecture (the denoiser's definition): 3 x 3 convolutions with ReLU
+# except the last, 2 x 2 average pooling, nearest upsampling, skip
+# concatenation after the upsampled channels.  Tensors carry padded channel
+# counts (multiples of 8; the 10-channel input is padded to 16, the 3-channel
+# output to 16), and the parameters live in one flat array:
+# per layer w [cout_pad][9][cin_pad] then b [cout_pad], each start aligned to
+# 4 floats.  With bf16=True every value the GPU stores in BF16 (the encoded
+# input, the weights, activations, data gradients) is rounded to BF16
+# (round-to-nearest-even) at the same point, so that only the accumulation
+# order separates the two.
+# ---------------------------------------------------------------------------
+
+# tensor: (channels, level); level l has resolution full >> l
+TENSORS = {
+    "X": (16, 0), "A0a": (32, 0), "S0": (32, 0), "P1": (32, 1), "A1a": (64, 1), "S1": (64, 1),
+    "P2": (64, 2), "A2a": (96, 2), "S2": (96, 2), "P3": (96, 3), "A3a": (128, 3), "S3": (128, 3),
+    "P4": (128, 4), "B": (160, 4), "U3": (128, 3), "U2": (96, 2), "U1": (64, 1), "U0": (32, 0),
+}
+POOLED = {"P1": "S0", "P2": "S1", "P3": "S2", "P4": "S3"}
+# (s1, s1 upsampled, s2, out, cout_pad, cout, cin, relu)
+LAYERS = [
+    ("X", 0, None, "A0a", 32, 32, 10, 1), ("A0a", 0, None, "S0", 32, 32, 32, 1),
+    ("P1", 0, None, "A1a", 64, 64, 32, 1), ("A1a", 0, None, "S1", 64, 64, 64, 1),
+    ("P2", 0, None, "A2a", 96, 96, 64, 1), ("A2a", 0, None, "S2", 96, 96, 96, 1),
+    ("P3", 0, None, "A3a", 128, 128, 96, 1), ("A3a", 0, None, "S3", 128, 128, 128, 1),
+    ("P4", 0, None, "B", 160, 160, 128, 1), ("B", 1, "S3", "U3", 128, 128, 288, 1),
+    ("U3", 1, "S2", "U2", 96, 96, 224, 1), ("U2", 1, "S1", "U1", 64, 64, 160, 1),
+    ("U1", 1, "S0", "U0", 32, 32, 96, 1), ("U0", 0, None, None, 16, 3, 32, 0),
+]
+
+
+def layer_table():
+    """Per layer: cout_pad, cout, cin_pad, cin, c1_pad, up1, relu, level,
+    w_off, b_off (the layout of the flat parameter array); and its size."""
+    rows, off = [], 0
+    a4 = lambda n: (n + 3) // 4 * 4  # noqa: E731
+    for s1, up, s2, out, cop, co, ci, relu in LAYERS:
+        c1 = TENSORS[s1][0]
+        cip = c1 + (TENSORS[s2][0] if s2 else 0)
+        level = TENSORS[out][1] if out else 0
+        w_off = off
+        off = a4(off + cop * 9 * cip)
+        b_off = off
+        off = a4(off + cop)
+        rows.append(dict(cout_pad=cop, cout=co, cin_pad=cip, cin=ci, c1_pad=c1, up1=up, relu=relu,
+                         level=level, w_off=w_off, b_off=b_off))
+    return rows, off
+
+
+def real_param_count():
+    return sum(co * 9 * ci + co for _, _, _, _, _, co, ci, _ in LAYERS)
+
+
+def to_bf16(x):
+    """Round to the nearest BF16 (ties to even), returned as float64."""
+    f = np.asarray(x, np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16 << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def init_params(seed=0):
+    """He-normal weights on the real entries, zero padding and biases (the
+    values differ from the GPU initialiser's; tests set parameters
+    explicitly)."""
+    rng = np.random.RandomState(seed)
+    rows, n = layer_table()
+    p = np.zeros(n)
+    for r in rows:
+        w = np.zeros((r["cout_pad"], 9, r["cin_pad"]))
+        real_in = r["cin"] if r["cin_pad"] == r["c1_pad"] else r["cin_pad"]
+        w[:r["cout"], :, :real_in] = rng.normal(0, np.sqrt(2.0 / (9 * r["cin"])), (r["cout"], 9, real_in))
+        p[r["w_off"]:r["w_off"] + w.size] = w.ravel()
+    return p
+
+
+def encode_input(raw):
+    """raw [N][H][W][10] -> [N][H][W][16]: log(1 + max(radiance, 0)), the
+    other 7 channels as they are, 6 zero channels."""
+    raw = np.asarray(raw, np.float64)
+    x = np.zeros(raw.shape[:3] + (16,))
+    x[..., :3] = np.log1p(np.maximum(raw[..., :3], 0.0))
+    x[..., 3:10] = raw[..., 3:10]
+    return x
+
+
+class UNet:
+    """Forward / backward of the denoiser on a flat parameter array."""
+
+    def __init__(self, params, bf16=False):
+        self.rows, n = layer_table()
+        assert params.size == n
+        self.p = np.asarray(params, np.float64)
+        self.bf16 = bf16
+        self.r = to_bf16 if bf16 else (lambda a: a)
+
+    def _wb(self, i):
+        r = self.rows[i]
+        w = self.p[r["w_off"]:r["w_off"] + r["cout_pad"] * 9 * r["cin_pad"]].reshape(r["cout_pad"], 3, 3, r["cin_pad"])
+        b = self.p[r["b_off"]:r["b_off"] + r["cout_pad"]]
+        return self.r(w), b
+
+    def _input(self, i, act):
+        s1, up, s2 = LAYERS[i][:3]
+        x = upsample2(act[s1]) if up else act[s1]
+        return np.concatenate([x, act[s2]], axis=3) if s2 else x
+
+    def forward(self, raw):
+        act = {"X": self.r(encode_input(raw))}
+        for i, (s1, up, s2, out, *_rest) in enumerate(LAYERS):
+            if s1 in POOLED:
+                act[s1] = self.r(avgpool2(act[POOLED[s1]]))
+            w, b = self._wb(i)
+            z = conv3x3(self._input(i, act), w, b)
+            if out is None:
+                act["pred"] = z
+            else:
+                act[out] = self.r(relu(z))
+        self.act = act
+        return act["pred"]
+
+    def loss_and_grads(self, raw, target):
+        """L1 on log(1 + target) of the first 3 output channels; returns the
+        loss and the gradient of the flat parameter array."""
+        pred = self.forward(raw)
+        act = self.act
+        P = pred.shape[0] * pred.shape[1] * pred.shape[2]
+        t = np.log1p(np.maximum(np.asarray(target, np.float64), 0.0))
+        d = pred[..., :3] - t
+        loss = np.abs(d).mean()
+        inv = float(np.float32(1.0) / np.float32(3.0 * P))
+        if self.bf16:
+            inv = float(to_bf16(inv))
+        dpred = np.zeros_like(pred)
+        dpred[..., :3] = np.sign(d) * inv
+        grad = np.zeros_like(self.p)
+        dact = {}
+        for i in range(len(LAYERS) - 1, -1, -1):
+            s1, up, s2, out, cop, co, ci, rl = LAYERS[i]
+            r = self.rows[i]
+            dout = dpred if out is None else dact[out]
+            x = self._input(i, act)
+            dw, db = conv3x3_wgrad(x, dout)
+            grad[r["w_off"]:r["w_off"] + dw.size] = dw.reshape(cop, 9, -1).ravel()
+            grad[r["b_off"]:r["b_off"] + cop] = db
+            if i == 0:
+                break
+            w, _ = self._wb(i)
+            din = conv3x3_dgrad(dout, w)
+            if s1 not in POOLED:
+                din = np.where(x > 0.0, din, 0.0)  # the sources are ReLU outputs
+            din = self.r(din)
+            c1 = TENSORS[s1][0]
+            if s2:
+                dact[s1] = self.r(upsample2_grad(din[..., :c1]))
+                dact[s2] = din[..., c1:]
+            elif s1 in POOLED:
+                skip = POOLED[s1]
+                dact[skip] = self.r(dact[skip] + np.where(act[skip] > 0.0, 0.25 * upsample2(din), 0.0))
+            else:
+                dact[s1] = din
+        return loss, grad

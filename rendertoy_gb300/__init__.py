@@ -32,7 +32,10 @@ EXPORTS = [
     "rtx_scene_upload", "rtx_scene_emitters", "rtx_scene_set_emitters", "rtx_render_pt", "rtx_trace_paths",
     "rtx_render_aov", "rtx_primary_hits", "rtx_intersect", "rtx_image_convolve",
     "rtx_image_gaussian_blur", "rtx_image_edge_detect", "rtx_image_bloom",
-    "rtx_image_gaussian_blur_noalloc", "rtx_nn_gemm_bf16",
+    "rtx_image_gaussian_blur_noalloc", "rtx_nn_gemm_bf16", "rtx_nn_conv3x3_fwd",
+    "rtx_nn_conv3x3_dgrad", "rtx_nn_conv3x3_wgrad", "rtx_dn_init", "rtx_dn_info", "rtx_dn_layer",
+    "rtx_dn_get_params", "rtx_dn_set_params", "rtx_dn_get_grads", "rtx_dn_get_adam", "rtx_dn_set_adam",
+    "rtx_dn_loss_grads", "rtx_dn_train_step", "rtx_dn_infer", "rtx_denoise",
 ]
 
 
@@ -89,7 +92,22 @@ def lib() -> C.CDLL:
         "rtx_image_edge_detect": (i, [vp, vp, vp, i, i]),
         "rtx_image_bloom": (i, [vp, vp, vp, i, i, i, f, f]),
         "rtx_image_gaussian_blur_noalloc": (i, [vp, vp, i, i, i, f, vp, C.c_char_p, C.c_size_t]),
-        "rtx_nn_gemm_bf16": (i, [vp, i, i, i, vp, vp, vp]),
+        "rtx_nn_gemm_bf16": (i, [vp, i, i, i, vp, vp, vp, i, i]),
+        "rtx_nn_conv3x3_fwd": (i, [vp, i, i, i, vp, i, i, vp, i, vp, vp, i, i, vp]),
+        "rtx_nn_conv3x3_dgrad": (i, [vp, i, i, i, vp, i, vp, vp, i, i, vp, i, i, vp]),
+        "rtx_nn_conv3x3_wgrad": (i, [vp, i, i, i, vp, i, vp, i, i, vp, i, vp]),
+        "rtx_dn_init": (i, [vp, u64]),
+        "rtx_dn_info": (i, [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(i), C.POINTER(i)]),
+        "rtx_dn_layer": (i, [vp, i, C.POINTER(C.c_int64)]),
+        "rtx_dn_get_params": (i, [vp, vp]),
+        "rtx_dn_set_params": (i, [vp, vp]),
+        "rtx_dn_get_grads": (i, [vp, vp]),
+        "rtx_dn_get_adam": (i, [vp, vp, vp]),
+        "rtx_dn_set_adam": (i, [vp, vp, vp, i]),
+        "rtx_dn_loss_grads": (i, [vp, vp, vp, i, i, i, C.POINTER(C.c_double)]),
+        "rtx_dn_train_step": (i, [vp, vp, vp, i, i, i, f, C.POINTER(C.c_double)]),
+        "rtx_dn_infer": (i, [vp, vp, vp, i, i, i]),
+        "rtx_denoise": (i, [vp, vp, vp, vp, vp, vp, i, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -234,14 +252,139 @@ class Context:
         return tri, tuv
 
     # -- denoiser building blocks ---------------------------------------------
-    def gemm_bf16(self, A, B, out=None):
+    def gemm_bf16(self, A, B, a_mn=False, b_mn=False, out=None):
         """C = A @ B.T on the tensor cores; A, B are uint16 arrays of BF16 bits
-        (or device tensors of dtype bfloat16)."""
-        M, K = A.shape
-        N = B.shape[0]
+        (or device bfloat16 tensors), M x K and N x K, or K x M / K x N when
+        a_mn / b_mn."""
+        M, K = (A.shape[1], A.shape[0]) if a_mn else A.shape
+        N = B.shape[1] if b_mn else B.shape[0]
         C_ = np.zeros((M, N), np.float32) if out is None else out
-        self._check(self.L.rtx_nn_gemm_bf16(self.h, M, N, K, _ptr(A), _ptr(B), _ptr(C_)))
+        self._check(self.L.rtx_nn_gemm_bf16(self.h, M, N, K, _ptr(A), _ptr(B), _ptr(C_), int(a_mn),
+                                            int(b_mn)))
         return C_
+
+    # -- denoiser operators -------------------------------------------------------
+    def conv3x3_fwd(self, x1, w, Cout, x2=None, up1=False, bias=None, relu=False, out=None):
+        """One convolution of the denoiser: x1 [N][h][w][C1] (half resolution
+        when up1), x2 [N][H][W][C2], w [Cout][9][C1 + C2], all BF16 bits
+        (uint16) or device bfloat16 tensors; returns FP32 [N][H][W][Cout]."""
+        N, H, W, C1 = x1.shape
+        if up1:
+            H, W = 2 * H, 2 * W
+        C2 = 0 if x2 is None else x2.shape[3]
+        if out is None:
+            out = np.zeros((N, H, W, Cout), np.float32)
+        b = None if bias is None else (bias if hasattr(bias, "data_ptr") else _f32(bias))
+        self._check(self.L.rtx_nn_conv3x3_fwd(self.h, N, H, W, _ptr(x1), C1, int(up1), _ptr(x2), C2, _ptr(w),
+                                              _ptr(b), Cout, int(relu), _ptr(out)))
+        return out
+
+    def conv3x3_dgrad(self, dout, wt, x1, x2=None, up1=False, mask_relu=False, out=None):
+        """din [N][H][W][C1 + C2] (BF16 bits) of a convolution; wt [Cin][9][Cout]."""
+        N, H, W, Cout = dout.shape
+        C1 = x1.shape[3]
+        C2 = 0 if x2 is None else x2.shape[3]
+        if out is None:
+            out = np.zeros((N, H, W, C1 + C2), np.uint16)
+        self._check(self.L.rtx_nn_conv3x3_dgrad(self.h, N, H, W, _ptr(dout), Cout, _ptr(wt), _ptr(x1), C1,
+                                                int(up1), _ptr(x2), C2, int(mask_relu), _ptr(out)))
+        return out
+
+    def conv3x3_wgrad(self, dout, x1, x2=None, up1=False, out=None):
+        """dw [Cout][9][C1 + C2] (FP32) of a convolution."""
+        N, H, W, Cout = dout.shape
+        C1 = x1.shape[3]
+        C2 = 0 if x2 is None else x2.shape[3]
+        if out is None:
+            out = np.zeros((Cout, 9, C1 + C2), np.float32)
+        self._check(self.L.rtx_nn_conv3x3_wgrad(self.h, N, H, W, _ptr(dout), Cout, _ptr(x1), C1, int(up1),
+                                                _ptr(x2), C2, _ptr(out)))
+        return out
+
+    # -- denoiser ---------------------------------------------------------------
+    def dn_init(self, seed=0):
+        self._check(self.L.rtx_dn_init(self.h, seed))
+
+    def dn_info(self):
+        n, r, nl, st = C.c_int64(), C.c_int64(), C.c_int(), C.c_int()
+        self._check(self.L.rtx_dn_info(self.h, C.byref(n), C.byref(r), C.byref(nl), C.byref(st)))
+        return {"n_params": n.value, "n_real": r.value, "n_layers": nl.value, "step": st.value}
+
+    DN_LAYER_KEYS = ("cout_pad", "cout", "cin_pad", "cin", "c1_pad", "up1", "relu", "level", "w_off",
+                     "b_off", "src1")
+
+    def dn_layers(self):
+        out = []
+        for i in range(self.dn_info()["n_layers"]):
+            a = (C.c_int64 * 11)()
+            self._check(self.L.rtx_dn_layer(self.h, i, a))
+            out.append(dict(zip(self.DN_LAYER_KEYS, list(a))))
+        return out
+
+    def dn_get_params(self):
+        p = np.zeros(self.dn_info()["n_params"], np.float32)
+        self._check(self.L.rtx_dn_get_params(self.h, _ptr(p)))
+        return p
+
+    def dn_set_params(self, p):
+        p = _f32(p)
+        assert p.size == self.dn_info()["n_params"]
+        self._check(self.L.rtx_dn_set_params(self.h, _ptr(p)))
+
+    def dn_get_grads(self):
+        g = np.zeros(self.dn_info()["n_params"], np.float32)
+        self._check(self.L.rtx_dn_get_grads(self.h, _ptr(g)))
+        return g
+
+    def dn_get_adam(self):
+        n = self.dn_info()["n_params"]
+        m, v = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        self._check(self.L.rtx_dn_get_adam(self.h, _ptr(m), _ptr(v)))
+        return m, v
+
+    def dn_set_adam(self, m, v, step):
+        m, v = _f32(m), _f32(v)
+        self._check(self.L.rtx_dn_set_adam(self.h, _ptr(m), _ptr(v), int(step)))
+
+    @staticmethod
+    def _batch(x):
+        if x.ndim == 3:
+            x = x[None]
+        return x if hasattr(x, "data_ptr") else _f32(x)
+
+    def dn_loss_grads(self, inp, target):
+        """Loss of a batch (inp [N][H][W][10], target [N][H][W][3]); the
+        gradients are then read with dn_get_grads."""
+        inp, target = self._batch(inp), self._batch(target)
+        N, H, W = inp.shape[:3]
+        l = C.c_double()
+        self._check(self.L.rtx_dn_loss_grads(self.h, _ptr(inp), _ptr(target), N, H, W, C.byref(l)))
+        return l.value
+
+    def dn_train_step(self, inp, target, lr=3e-4):
+        inp, target = self._batch(inp), self._batch(target)
+        N, H, W = inp.shape[:3]
+        l = C.c_double()
+        self._check(self.L.rtx_dn_train_step(self.h, _ptr(inp), _ptr(target), N, H, W, float(lr),
+                                             C.byref(l)))
+        return l.value
+
+    def dn_infer(self, inp, out=None):
+        inp = self._batch(inp)
+        N, H, W = inp.shape[:3]
+        if out is None:
+            out = np.zeros((N, H, W, 3), np.float32)
+        self._check(self.L.rtx_dn_infer(self.h, _ptr(inp), _ptr(out), N, H, W))
+        return out
+
+    def denoise(self, radiance, albedo, normal, depth, out=None):
+        """Denoise a frame from its passes (each H x W x 3 FP32)."""
+        rad, alb, nrm, dep = (x if hasattr(x, "data_ptr") else _f32(x) for x in (radiance, albedo, normal, depth))
+        H, W = rad.shape[:2]
+        if out is None:
+            out = np.zeros((H, W, 3), np.float32)
+        self._check(self.L.rtx_denoise(self.h, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(dep), _ptr(out), W, H))
+        return out
 
     # -- compositor -------------------------------------------------------------
     @staticmethod

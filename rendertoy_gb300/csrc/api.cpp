@@ -16,6 +16,9 @@
 #include <string>
 #include <vector>
 
+#include "nn.h"
+#include "nn_ops.h"
+#include "nn_unet.h"
 #include "rtx_internal.h"
 
 using namespace rtx;
@@ -89,7 +92,8 @@ struct rtx_context {
   int* d_err = nullptr;
   Counters* d_counters = nullptr;
   PtWorkspace* pt = nullptr;
-  DevBuf stage[4];
+  DevBuf stage[8];
+  rtx::nn::UNet* dn = nullptr;
   DevBuf weights;
   std::vector<float> host_weights;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -310,6 +314,7 @@ void rtx_destroy(rtx_context* c) {
   c->mats.release();
   c->emit.release();
   for (auto& s : c->stage) s.release();
+  delete c->dn;
   c->weights.release();
   if (c->pt) pt_workspace_destroy(c->pt);
   if (c->d_err) cudaFree(c->d_err);
@@ -754,9 +759,12 @@ int rtx_image_bloom(rtx_context* c, const float* in, float* out, int W, int H, i
   return gaussian_common(c, in, out, W, H, size, sigma, true, threshold);
 }
 
-int rtx_nn_gemm_bf16(rtx_context* c, int M, int N, int K, const void* A, const void* B, float* C) {
+int rtx_nn_gemm_bf16(rtx_context* c, int M, int N, int K, const void* A, const void* B, float* C,
+                     int a_mn, int b_mn) {
   if (!c) return RTX_ERR_INVALID;
-  if (M <= 0 || N <= 0 || K <= 0 || K % 8) return fail(c, RTX_ERR_INVALID, "M, N, K must be positive and K % 8 == 0");
+  if (M <= 0 || N <= 0 || K <= 0) return fail(c, RTX_ERR_INVALID, "M, N, K must be positive");
+  if ((a_mn ? M : K) % 8 || (b_mn ? N : K) % 8)
+    return fail(c, RTX_ERR_INVALID, "the contiguous dimension of each operand must be a multiple of 8");
   if (!A || !B || !C) return fail(c, RTX_ERR_INVALID, "NULL operand");
   int r;
   if ((r = begin(c))) return r;
@@ -764,11 +772,324 @@ int rtx_nn_gemm_bf16(rtx_context* c, int M, int N, int K, const void* A, const v
   if ((r = bind_in(c, A, (size_t)M * K * 2, 0, aa))) return r;
   if ((r = bind_in(c, B, (size_t)N * K * 2, 1, ab))) return r;
   if ((r = bind_out(c, C, (size_t)M * N * 4, 2, ac))) return r;
-  cudaError_t e = launch_gemm_bf16(aa.dev, ab.dev, (float*)ac.dev, M, N, K, c->d_err, c->stream);
+  cudaError_t e = launch_gemm_bf16(aa.dev, ab.dev, (float*)ac.dev, M, N, K, a_mn, b_mn, c->d_err, c->stream);
   c->stats.kernel_launches = 1;
   if (e != cudaSuccess) return cuda_fail(c, e, "gemm kernel");
   if ((r = copy_back(c, ac))) return r;
   return finish(c, all_device({&aa, &ab, &ac}));
+}
+
+// ---- denoiser operators ------------------------------------------------------
+static int check_conv_srcs(rtx_context* c, int N, int H, int W, const void* x1, int C1, int up1,
+                           const void* x2, int C2) {
+  if (N <= 0 || H <= 0 || W <= 0) return fail(c, RTX_ERR_INVALID, "N, H, W must be positive");
+  if ((long long)N * H * W > (1LL << 31)) return fail(c, RTX_ERR_INVALID, "tensor too large");
+  if (!x1 || C1 <= 0 || C1 % 8) return fail(c, RTX_ERR_INVALID, "x1 must be given with C1 a multiple of 8");
+  if (C2 < 0 || C2 % 8 || (C2 > 0) != (x2 != nullptr))
+    return fail(c, RTX_ERR_INVALID, "x2 must be given exactly when C2 > 0, C2 a multiple of 8");
+  if (up1 && (H % 2 || W % 2)) return fail(c, RTX_ERR_INVALID, "an upsampled source needs even H and W");
+  return RTX_OK;
+}
+
+static int bind_srcs(rtx_context* c, int N, int H, int W, const void* x1, int C1, int up1, const void* x2,
+                     int C2, int slot, Arg& a1, Arg& a2, rtx::nn::Src& s1, rtx::nn::Src& s2) {
+  int r;
+  size_t p1 = up1 ? (size_t)N * (H / 2) * (W / 2) : (size_t)N * H * W;
+  if ((r = bind_in(c, x1, p1 * C1 * 2, slot, a1))) return r;
+  if ((r = bind_in(c, x2, (size_t)N * H * W * C2 * 2, slot + 1, a2))) return r;
+  s1 = rtx::nn::Src{(const rtx::nn::bf16*)a1.dev, C1, up1 ? 1 : 0};
+  s2 = rtx::nn::Src{(const rtx::nn::bf16*)a2.dev, C2, 0};
+  return RTX_OK;
+}
+
+int rtx_nn_conv3x3_fwd(rtx_context* c, int N, int H, int W, const void* x1, int C1, int up1,
+                       const void* x2, int C2, const void* w, const float* bias, int Cout, int relu,
+                       float* out) {
+  if (!c) return RTX_ERR_INVALID;
+  int r;
+  if ((r = check_conv_srcs(c, N, H, W, x1, C1, up1, x2, C2))) return r;
+  if (Cout <= 0 || Cout % 16 || Cout > 256) return fail(c, RTX_ERR_INVALID, "Cout must be a multiple of 16, <= 256");
+  if (!w || !out) return fail(c, RTX_ERR_INVALID, "NULL weight or output");
+  const int Cin = C1 + C2;
+  const size_t P = (size_t)N * H * W;
+  if ((r = begin(c))) return r;
+  Arg a1, a2, aw, ab, ao;
+  rtx::nn::Src s1, s2;
+  if ((r = bind_srcs(c, N, H, W, x1, C1, up1, x2, C2, 0, a1, a2, s1, s2))) return r;
+  if ((r = bind_in(c, w, (size_t)Cout * 9 * Cin * 2, 2, aw))) return r;
+  if ((r = bind_in(c, bias, bias ? (size_t)Cout * 4 : 0, 3, ab))) return r;
+  if ((r = bind_out(c, out, P * Cout * 4, 4, ao))) return r;
+  rtx::nn::ConvFwd a{};
+  a.s1 = s1;
+  a.s2 = s2;
+  a.N = N;
+  a.H = H;
+  a.W = W;
+  a.Cin = Cin;
+  a.Cout = Cout;
+  a.w = (const rtx::nn::bf16*)aw.dev;
+  a.bias = (const float*)ab.dev;
+  a.relu = relu;
+  a.out = nullptr;
+  a.out_f32 = (float*)ao.dev;
+  a.err = c->d_err;
+  cudaError_t e = rtx::nn::conv_fwd(a, c->stream);
+  c->stats.kernel_launches = 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "conv forward kernel");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&a1, &a2, &aw, &ab, &ao}));
+}
+
+int rtx_nn_conv3x3_dgrad(rtx_context* c, int N, int H, int W, const void* dout, int Cout, const void* wt,
+                         const void* x1, int C1, int up1, const void* x2, int C2, int mask_relu,
+                         void* din) {
+  if (!c) return RTX_ERR_INVALID;
+  int r;
+  if ((r = check_conv_srcs(c, N, H, W, x1, C1, up1, x2, C2))) return r;
+  const int Cin = C1 + C2;
+  if (Cin % 16) return fail(c, RTX_ERR_INVALID, "C1 + C2 must be a multiple of 16");
+  if (Cout <= 0 || Cout % 8) return fail(c, RTX_ERR_INVALID, "Cout must be a positive multiple of 8");
+  if (!dout || !wt || !din) return fail(c, RTX_ERR_INVALID, "NULL gradient, weight or output");
+  const size_t P = (size_t)N * H * W;
+  if ((r = begin(c))) return r;
+  Arg a1, a2, ad, aw, ao;
+  rtx::nn::Src s1, s2;
+  if ((r = bind_srcs(c, N, H, W, x1, C1, up1, x2, C2, 0, a1, a2, s1, s2))) return r;
+  if ((r = bind_in(c, dout, P * Cout * 2, 2, ad))) return r;
+  if ((r = bind_in(c, wt, (size_t)Cin * 9 * Cout * 2, 3, aw))) return r;
+  if ((r = bind_out(c, din, P * Cin * 2, 4, ao))) return r;
+  rtx::nn::ConvDgrad a{};
+  a.dout = (const rtx::nn::bf16*)ad.dev;
+  a.Cout = Cout;
+  a.wt = (const rtx::nn::bf16*)aw.dev;
+  a.N = N;
+  a.H = H;
+  a.W = W;
+  a.Cin = Cin;
+  a.s1 = s1;
+  a.s2 = s2;
+  a.mask_relu = mask_relu;
+  a.din = (rtx::nn::bf16*)ao.dev;
+  a.err = c->d_err;
+  cudaError_t e = rtx::nn::conv_dgrad(a, c->stream);
+  c->stats.kernel_launches = 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "conv data-gradient kernel");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&a1, &a2, &ad, &aw, &ao}));
+}
+
+int rtx_nn_conv3x3_wgrad(rtx_context* c, int N, int H, int W, const void* dout, int Cout, const void* x1,
+                         int C1, int up1, const void* x2, int C2, float* dw) {
+  if (!c) return RTX_ERR_INVALID;
+  int r;
+  if ((r = check_conv_srcs(c, N, H, W, x1, C1, up1, x2, C2))) return r;
+  if (Cout <= 0 || Cout % 8) return fail(c, RTX_ERR_INVALID, "Cout must be a positive multiple of 8");
+  if (!dout || !dw) return fail(c, RTX_ERR_INVALID, "NULL gradient or output");
+  const int Cin = C1 + C2;
+  const long long P = (long long)N * H * W;
+  if ((r = begin(c))) return r;
+  Arg a1, a2, ad, ao;
+  rtx::nn::Src s1, s2;
+  if ((r = bind_srcs(c, N, H, W, x1, C1, up1, x2, C2, 0, a1, a2, s1, s2))) return r;
+  if ((r = bind_in(c, dout, (size_t)P * Cout * 2, 2, ad))) return r;
+  if ((r = bind_out(c, dw, (size_t)Cout * 9 * Cin * 4, 4, ao))) return r;
+  RTX_CUDA(cudaMemsetAsync(ao.dev, 0, ao.bytes, c->stream), "zero dw");
+  rtx::nn::ConvWgrad a{};
+  a.dout = (const rtx::nn::bf16*)ad.dev;
+  a.Cout = Cout;
+  a.s1 = s1;
+  a.s2 = s2;
+  a.N = N;
+  a.H = H;
+  a.W = W;
+  a.Cin = Cin;
+  a.pix_per_cta = rtx::nn::wgrad_pixels_per_cta(P, Cout, Cin);
+  a.dw = (float*)ao.dev;
+  a.err = c->d_err;
+  cudaError_t e = rtx::nn::conv_wgrad(a, c->stream);
+  c->stats.kernel_launches = 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "conv weight-gradient kernel");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&a1, &a2, &ad, &ao}));
+}
+
+// ---- denoiser ------------------------------------------------------------------
+static int need_dn(rtx_context* c) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!c->dn) return fail(c, RTX_ERR_INVALID, "denoiser not initialised (rtx_dn_init)");
+  return RTX_OK;
+}
+
+static int check_batch(rtx_context* c, int N, int H, int W) {
+  if (N <= 0 || H <= 0 || W <= 0) return fail(c, RTX_ERR_INVALID, "N, H, W must be positive");
+  if (H % 16 || W % 16) return fail(c, RTX_ERR_INVALID, "H and W must be multiples of 16");
+  if ((long long)N * H * W > (1LL << 28)) return fail(c, RTX_ERR_INVALID, "batch too large");
+  return RTX_OK;
+}
+
+int rtx_dn_init(rtx_context* c, uint64_t seed) {
+  if (!c) return RTX_ERR_INVALID;
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  delete c->dn;
+  c->dn = new (std::nothrow) rtx::nn::UNet();
+  if (!c->dn) return fail(c, RTX_ERR_NOMEM, "host allocation");
+  cudaError_t e = c->dn->init(seed, c->stream);
+  if (e != cudaSuccess) {
+    delete c->dn;
+    c->dn = nullptr;
+    return cuda_fail(c, e, "denoiser init");
+  }
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return RTX_OK;
+}
+
+int rtx_dn_info(rtx_context* c, int64_t* n_params, int64_t* n_real, int* n_layers, int* step) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (n_params) *n_params = c->dn->num_params();
+  if (n_real) *n_real = c->dn->num_real_params();
+  if (n_layers) *n_layers = rtx::nn::UNet::num_layers();
+  if (step) *step = c->dn->step();
+  return RTX_OK;
+}
+
+int rtx_dn_layer(rtx_context* c, int layer, int64_t info[11]) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (layer < 0 || layer >= rtx::nn::UNet::num_layers() || !info)
+    return fail(c, RTX_ERR_INVALID, "layer out of range");
+  c->dn->layer_info(layer, info);
+  return RTX_OK;
+}
+
+int rtx_dn_get_params(rtx_context* c, float* out) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (!out || is_device_ptr(out)) return fail(c, RTX_ERR_INVALID, "out must be a host buffer");
+  RTX_CUDA(c->dn->get_params(out, c->stream), "get params");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return RTX_OK;
+}
+
+int rtx_dn_set_params(rtx_context* c, const float* in) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (!in || is_device_ptr(in)) return fail(c, RTX_ERR_INVALID, "in must be a host buffer");
+  RTX_CUDA(c->dn->set_params(in, c->stream), "set params");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return RTX_OK;
+}
+
+int rtx_dn_get_grads(rtx_context* c, float* out) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (!out || is_device_ptr(out)) return fail(c, RTX_ERR_INVALID, "out must be a host buffer");
+  RTX_CUDA(c->dn->get_grads(out, c->stream), "get grads");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return RTX_OK;
+}
+
+int rtx_dn_get_adam(rtx_context* c, float* m, float* v) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (!m || !v || is_device_ptr(m) || is_device_ptr(v))
+    return fail(c, RTX_ERR_INVALID, "m and v must be host buffers");
+  RTX_CUDA(c->dn->get_state(m, v, c->stream), "get Adam state");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return RTX_OK;
+}
+
+int rtx_dn_set_adam(rtx_context* c, const float* m, const float* v, int step) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (!m || !v || is_device_ptr(m) || is_device_ptr(v))
+    return fail(c, RTX_ERR_INVALID, "m and v must be host buffers");
+  if (step < 0) return fail(c, RTX_ERR_INVALID, "step must be >= 0");
+  RTX_CUDA(c->dn->set_state(m, v, step, c->stream), "set Adam state");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return RTX_OK;
+}
+
+static int dn_run(rtx_context* c, const float* input, const float* target, int N, int H, int W, bool update,
+                  float lr, double* loss) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if ((r = check_batch(c, N, H, W))) return r;
+  if (!input || !target) return fail(c, RTX_ERR_INVALID, "NULL input or target");
+  const size_t P = (size_t)N * H * W;
+  if ((r = begin(c))) return r;
+  Arg ai, at;
+  if ((r = bind_in(c, input, P * 40, 0, ai))) return r;
+  if ((r = bind_in(c, target, P * 12, 1, at))) return r;
+  RTX_CUDA(c->dn->reserve((long long)P), "denoiser buffers");
+  double l = 0.0;
+  cudaError_t e = update ? c->dn->train_step((const float*)ai.dev, (const float*)at.dev, N, H, W, lr, &l,
+                                             c->d_err, c->stream)
+                         : c->dn->loss_and_grads((const float*)ai.dev, (const float*)at.dev, N, H, W, &l,
+                                                 c->d_err, c->stream);
+  c->stats.kernel_launches = c->dn->last_launches();
+  if (e != cudaSuccess) return cuda_fail(c, e, update ? "denoiser train step" : "denoiser gradients");
+  if ((r = finish(c, false))) return r;
+  if (loss) *loss = l;
+  return RTX_OK;
+}
+
+int rtx_dn_loss_grads(rtx_context* c, const float* input, const float* target, int N, int H, int W,
+                      double* loss) {
+  return dn_run(c, input, target, N, H, W, false, 0.0f, loss);
+}
+
+int rtx_dn_train_step(rtx_context* c, const float* input, const float* target, int N, int H, int W, float lr,
+                      double* loss) {
+  if (c && !(lr > 0.0f)) return fail(c, RTX_ERR_INVALID, "lr must be positive");
+  return dn_run(c, input, target, N, H, W, true, lr, loss);
+}
+
+int rtx_dn_infer(rtx_context* c, const float* input, float* out, int N, int H, int W) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if ((r = check_batch(c, N, H, W))) return r;
+  if (!input || !out) return fail(c, RTX_ERR_INVALID, "NULL input or output");
+  const size_t P = (size_t)N * H * W;
+  if ((r = begin(c))) return r;
+  Arg ai, ao;
+  if ((r = bind_in(c, input, P * 40, 0, ai))) return r;
+  if ((r = bind_out(c, out, P * 12, 1, ao))) return r;
+  RTX_CUDA(c->dn->reserve((long long)P), "denoiser buffers");
+  cudaError_t e = c->dn->forward((const float*)ai.dev, N, H, W, c->d_err, c->stream);
+  if (e == cudaSuccess) e = c->dn->decode((float*)ao.dev, (long long)P, c->stream);
+  c->stats.kernel_launches = c->dn->last_launches() + 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "denoiser inference");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&ai, &ao}));
+}
+
+int rtx_denoise(rtx_context* c, const float* radiance, const float* albedo, const float* normal,
+                const float* depth, float* out, int W, int H) {
+  int r;
+  if ((r = need_dn(c))) return r;
+  if (W <= 0 || H <= 0 || (long long)W * H > (1LL << 28)) return fail(c, RTX_ERR_INVALID, "bad image size");
+  if (!radiance || !albedo || !normal || !depth || !out) return fail(c, RTX_ERR_INVALID, "NULL image");
+  const int Wp = (W + 15) / 16 * 16, Hp = (H + 15) / 16 * 16;
+  const size_t bytes = (size_t)W * H * 12;
+  if ((r = begin(c))) return r;
+  Arg ar, aa, an, ad, ao;
+  if ((r = bind_in(c, radiance, bytes, 0, ar))) return r;
+  if ((r = bind_in(c, albedo, bytes, 1, aa))) return r;
+  if ((r = bind_in(c, normal, bytes, 2, an))) return r;
+  if ((r = bind_in(c, depth, bytes, 3, ad))) return r;
+  if ((r = bind_out(c, out, bytes, 4, ao))) return r;
+  RTX_CUDA(c->stage[5].ensure((size_t)Wp * Hp * 40), "stage alloc");
+  RTX_CUDA(c->dn->reserve((long long)Wp * Hp), "denoiser buffers");
+  float* raw = (float*)c->stage[5].p;
+  cudaError_t e = rtx::nn::pack_passes((const float*)ar.dev, (const float*)aa.dev, (const float*)an.dev,
+                                       (const float*)ad.dev, raw, W, H, Wp, Hp, c->stream);
+  if (e == cudaSuccess) e = c->dn->forward(raw, 1, Hp, Wp, c->d_err, c->stream);
+  if (e == cudaSuccess) e = rtx::nn::decode_crop(c->dn->prediction(), (float*)ao.dev, W, H, Wp, c->stream);
+  c->stats.kernel_launches = c->dn->last_launches() + 2;
+  if (e != cudaSuccess) return cuda_fail(c, e, "denoise");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&ar, &aa, &an, &ad, &ao}));
 }
 
 int rtx_image_edge_detect(rtx_context* c, const float* in, float* out, int W, int H) {

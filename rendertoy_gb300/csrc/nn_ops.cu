@@ -1,0 +1,301 @@
+// nn_ops.cu — the denoiser's memory-bound operators: input encoding, 2 x 2
+// average pooling and its gradient, the gradient of nearest upsampling and of
+// channel concatenation, the L1-on-log loss, bias gradients, Adam and the
+// BF16 weight layouts the convolutions read.  One thread per 8 channels of a
+// pixel (16-byte BF16 accesses) unless noted.
+#include "nn.h"
+#include "nn_ops.h"
+
+namespace rtx {
+namespace nn {
+
+namespace {
+
+__device__ __forceinline__ void ld8(const bf16* p, float* f) {
+  uint4 u = *reinterpret_cast<const uint4*>(p);
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float2 t = __bfloat1622float2(h[i]);
+    f[2 * i] = t.x;
+    f[2 * i + 1] = t.y;
+  }
+}
+
+__device__ __forceinline__ void st8(bf16* p, const float* f) {
+  uint4 u;
+  __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+  *reinterpret_cast<uint4*>(p) = u;
+}
+
+unsigned blocks(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+// raw [P][10] (radiance 3, albedo 3, normal 3, depth 1) -> [P][16] BF16,
+// radiance as log(1 + max(x, 0)), channels 10..15 zero
+__global__ void k_encode_input(const float* __restrict__ raw, bf16* __restrict__ x, long long P) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const float* r = raw + 10 * p;
+  float f[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) f[i] = 0.0f;
+  for (int i = 0; i < 3; ++i) f[i] = log1pf(fmaxf(r[i], 0.0f));
+  for (int i = 3; i < 10; ++i) f[i] = r[i];
+  st8(x + 16 * p, f);
+  st8(x + 16 * p + 8, f + 8);
+}
+
+__global__ void k_avgpool(const bf16* __restrict__ in, bf16* __restrict__ out, int N, int H, int W, int C) {
+  int h = H >> 1, w = W >> 1, c8 = C >> 3;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long total = (long long)N * h * w * c8;
+  if (i >= total) return;
+  int c = (int)(i % c8) * 8;
+  long long q = i / c8;
+  int x = (int)(q % w);
+  long long r = q / w;
+  int y = (int)(r % h);
+  int n = (int)(r / h);
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
+  for (int dy = 0; dy < 2; ++dy)
+    for (int dx = 0; dx < 2; ++dx) {
+      ld8(in + (((size_t)n * H + 2 * y + dy) * W + 2 * x + dx) * C + c, v);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) acc[k] += v[k];
+    }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k] *= 0.25f;
+  st8(out + q * C + c, acc);
+}
+
+// d_low[n, y, x, c] = sum over the 2 x 2 block of dcat[.., c0 + c] (nearest
+// upsampling's gradient), channels [c0, c0 + C) of a Ccat-channel tensor
+__global__ void k_upsample_grad(const bf16* __restrict__ dcat, int Ccat, int c0, bf16* __restrict__ dlow,
+                                int N, int H, int W, int C) {
+  int h = H >> 1, w = W >> 1, c8 = C >> 3;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long total = (long long)N * h * w * c8;
+  if (i >= total) return;
+  int c = (int)(i % c8) * 8;
+  long long q = i / c8;
+  int x = (int)(q % w);
+  long long r = q / w;
+  int y = (int)(r % h);
+  int n = (int)(r / h);
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
+  for (int dy = 0; dy < 2; ++dy)
+    for (int dx = 0; dx < 2; ++dx) {
+      ld8(dcat + (((size_t)n * H + 2 * y + dy) * W + 2 * x + dx) * Ccat + c0 + c, v);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) acc[k] += v[k];
+    }
+  st8(dlow + q * C + c, acc);
+}
+
+// dst[p, c] = dcat[p, c0 + c] (a skip connection's share of a concatenation)
+__global__ void k_take_channels(const bf16* __restrict__ dcat, int Ccat, int c0, bf16* __restrict__ dst,
+                                long long P, int C) {
+  int c8 = C >> 3;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= P * c8) return;
+  long long p = i / c8;
+  int c = (int)(i % c8) * 8;
+  *reinterpret_cast<uint4*>(dst + p * C + c) = *reinterpret_cast<const uint4*>(dcat + p * Ccat + c0 + c);
+}
+
+// dskip[p, c] += (skip[p, c] > 0) * 0.25 * dpool[p / 2, c]: the pooled path's
+// gradient reaching a ReLU output
+__global__ void k_pool_grad_acc(const bf16* __restrict__ dpool, const bf16* __restrict__ skip,
+                                bf16* __restrict__ dskip, int N, int H, int W, int C) {
+  int c8 = C >> 3;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long total = (long long)N * H * W * c8;
+  if (i >= total) return;
+  int c = (int)(i % c8) * 8;
+  long long p = i / c8;
+  int x = (int)(p % W);
+  long long r = p / W;
+  int y = (int)(r % H);
+  int n = (int)(r / H);
+  float d[8], s[8], g[8];
+  ld8(dpool + (((size_t)n * (H >> 1) + (y >> 1)) * (W >> 1) + (x >> 1)) * C + c, d);
+  ld8(skip + p * C + c, s);
+  ld8(dskip + p * C + c, g);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) g[k] += s[k] > 0.0f ? 0.25f * d[k] : 0.0f;
+  st8(dskip + p * C + c, g);
+}
+
+// L1 on log(1 + target): pred [P][16] FP32 (channels 0..2), target [P][3];
+// d_pred = sign(pred - log1p(target)) / (3P) as BF16 [P][16]; loss summed
+// into *loss (FP64)
+__global__ void k_l1log_loss(const float* __restrict__ pred, const float* __restrict__ target,
+                             bf16* __restrict__ dpred, long long P, double* loss) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float part = 0.0f;
+  if (p < P) {
+    float g[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) g[i] = 0.0f;
+    float inv = 1.0f / (3.0f * (float)P);
+    for (int i = 0; i < 3; ++i) {
+      float d = pred[16 * p + i] - log1pf(fmaxf(target[3 * p + i], 0.0f));
+      part += fabsf(d);
+      g[i] = d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f);
+    }
+    st8(dpred + 16 * p, g);
+    st8(dpred + 16 * p + 8, g + 8);
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)part);
+}
+
+// db[c] += sum_p dout[p, c]; a block sums 256 pixels of one 8-channel group
+__global__ void k_bias_grad(const bf16* __restrict__ dout, long long P, int C, float* __restrict__ db) {
+  int c = blockIdx.y * 8;
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (p < P) ld8(dout + p * C + c, v);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    float s = v[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(db + c + k, s);
+  }
+}
+
+// Adam (Kingma & Ba) on the FP32 master parameters
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, long long n, float lr, float b1, float b2, float eps,
+                       float c1, float c2) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float gi = g[i];
+  float mi = b1 * m[i] + (1.0f - b1) * gi;
+  float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// master [Cout][9][Cin] FP32 -> w [Cout][9][Cin] and wt [Cin][9][Cout] BF16
+__global__ void k_weights_bf16(const float* __restrict__ master, bf16* __restrict__ w, bf16* __restrict__ wt,
+                               int Cout, int Cin) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long n = (long long)Cout * 9 * Cin;
+  if (i >= n) return;
+  int c = (int)(i % Cin);
+  long long r = i / Cin;
+  int t = (int)(r % 9);
+  int o = (int)(r / 9);
+  bf16 b = __float2bfloat16_rn(master[i]);
+  w[i] = b;
+  if (wt) wt[((size_t)c * 9 + t) * Cout + o] = b;
+}
+
+// prediction (log space) [P][16] -> radiance [P][3] = exp(pred) - 1
+__global__ void k_decode_output(const float* __restrict__ pred, float* __restrict__ out, long long P) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  for (int i = 0; i < 3; ++i) out[3 * p + i] = expm1f(pred[16 * p + i]);
+}
+
+// the renderer's passes (W x H RGB FP32 each) -> raw [Hp][Wp][10], zero
+// outside the W x H frame
+__global__ void k_pack_passes(const float* __restrict__ rad, const float* __restrict__ alb,
+                              const float* __restrict__ nrm, const float* __restrict__ dep,
+                              float* __restrict__ raw, int W, int H, int Wp, int Hp) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)Wp * Hp) return;
+  int x = (int)(i % Wp), y = (int)(i / Wp);
+  float* r = raw + 10 * i;
+  if (x >= W || y >= H) {
+    for (int k = 0; k < 10; ++k) r[k] = 0.0f;
+    return;
+  }
+  long long s = ((long long)y * W + x) * 3;
+  for (int k = 0; k < 3; ++k) {
+    r[k] = rad[s + k];
+    r[3 + k] = alb[s + k];
+    r[6 + k] = nrm[s + k];
+  }
+  r[9] = dep[s];
+}
+
+// prediction [Hp][Wp][16] (log space) -> radiance W x H RGB
+__global__ void k_decode_crop(const float* __restrict__ pred, float* __restrict__ out, int W, int H, int Wp) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)W * H) return;
+  int x = (int)(i % W), y = (int)(i / W);
+  const float* q = pred + 16 * ((long long)y * Wp + x);
+  for (int k = 0; k < 3; ++k) out[3 * i + k] = expm1f(q[k]);
+}
+
+// ---- launchers ------------------------------------------------------------
+cudaError_t encode_input(const float* raw, bf16* x, long long P, cudaStream_t st) {
+  k_encode_input<<<blocks(P), 256, 0, st>>>(raw, x, P);
+  return cudaGetLastError();
+}
+cudaError_t avgpool(const bf16* in, bf16* out, int N, int H, int W, int C, cudaStream_t st) {
+  long long n = (long long)N * (H / 2) * (W / 2) * (C / 8);
+  k_avgpool<<<blocks(n), 256, 0, st>>>(in, out, N, H, W, C);
+  return cudaGetLastError();
+}
+cudaError_t upsample_grad(const bf16* dcat, int Ccat, int c0, bf16* dlow, int N, int H, int W, int C,
+                          cudaStream_t st) {
+  long long n = (long long)N * (H / 2) * (W / 2) * (C / 8);
+  k_upsample_grad<<<blocks(n), 256, 0, st>>>(dcat, Ccat, c0, dlow, N, H, W, C);
+  return cudaGetLastError();
+}
+cudaError_t take_channels(const bf16* dcat, int Ccat, int c0, bf16* dst, long long P, int C, cudaStream_t st) {
+  k_take_channels<<<blocks(P * (C / 8)), 256, 0, st>>>(dcat, Ccat, c0, dst, P, C);
+  return cudaGetLastError();
+}
+cudaError_t pool_grad_acc(const bf16* dpool, const bf16* skip, bf16* dskip, int N, int H, int W, int C,
+                          cudaStream_t st) {
+  long long n = (long long)N * H * W * (C / 8);
+  k_pool_grad_acc<<<blocks(n), 256, 0, st>>>(dpool, skip, dskip, N, H, W, C);
+  return cudaGetLastError();
+}
+cudaError_t l1log_loss(const float* pred, const float* target, bf16* dpred, long long P, double* loss,
+                       cudaStream_t st) {
+  k_l1log_loss<<<blocks(P), 256, 0, st>>>(pred, target, dpred, P, loss);
+  return cudaGetLastError();
+}
+cudaError_t bias_grad(const bf16* dout, long long P, int C, float* db, cudaStream_t st) {
+  dim3 g(blocks(P), C / 8);
+  k_bias_grad<<<g, 256, 0, st>>>(dout, P, C, db);
+  return cudaGetLastError();
+}
+cudaError_t adam(float* p, const float* g, float* m, float* v, long long n, float lr, int step,
+                 cudaStream_t st) {
+  const float b1 = 0.9f, b2 = 0.999f;
+  float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+  k_adam<<<blocks(n), 256, 0, st>>>(p, g, m, v, n, lr, b1, b2, 1e-8f, c1, c2);
+  return cudaGetLastError();
+}
+cudaError_t weights_bf16(const float* master, bf16* w, bf16* wt, int Cout, int Cin, cudaStream_t st) {
+  k_weights_bf16<<<blocks((long long)Cout * 9 * Cin), 256, 0, st>>>(master, w, wt, Cout, Cin);
+  return cudaGetLastError();
+}
+cudaError_t decode_output(const float* pred, float* out, long long P, cudaStream_t st) {
+  k_decode_output<<<blocks(P), 256, 0, st>>>(pred, out, P);
+  return cudaGetLastError();
+}
+
+cudaError_t pack_passes(const float* rad, const float* alb, const float* nrm, const float* dep, float* raw,
+                        int W, int H, int Wp, int Hp, cudaStream_t st) {
+  k_pack_passes<<<blocks((long long)Wp * Hp), 256, 0, st>>>(rad, alb, nrm, dep, raw, W, H, Wp, Hp);
+  return cudaGetLastError();
+}
+cudaError_t decode_crop(const float* pred, float* out, int W, int H, int Wp, cudaStream_t st) {
+  k_decode_crop<<<blocks((long long)W * H), 256, 0, st>>>(pred, out, W, H, Wp);
+  return cudaGetLastError();
+}
+
+}  // namespace nn
+}  // namespace rtx

@@ -147,7 +147,7 @@ cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out
                             cudaStream_t st, int* launches);
 cudaError_t launch_edge(const float* in, float* out, int W, int H, cudaStream_t st,
                         int* launches);
-cudaError_t launch_gemm_bf16(const void* A, const void* B, float* C, int M, int N, int K, int* err,
-                             cudaStream_t st);
+cudaError_t launch_gemm_bf16(const void* A, const void* B, float* C, int M, int N, int K, int a_mn,
+                             int b_mn, int* err, cudaStream_t st);
 
 }  // namespace rtx

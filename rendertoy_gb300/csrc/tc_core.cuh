@@ -35,10 +35,12 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
-// Instruction descriptor for kind::f16: FP32 accumulator, BF16 A and B, both
-// K-major, shape M x N (x 16).
-__host__ __device__ constexpr uint32_t make_idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor for kind::f16: FP32 accumulator, BF16 A and B,
+// shape M x N (x 16); a_mn / b_mn select MN-major instead of K-major operands.
+__host__ __device__ constexpr uint32_t make_idesc_bf16(int M, int N, bool a_mn = false,
+                                                       bool b_mn = false) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* smem_slot, uint32_t ncols) {
@@ -114,9 +116,16 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
 }
 
 // Byte offset of element (row, k) in a K-major no-swizzle tile whose rows
-// hold kdim elements (kdim a multiple of 8).
+// hold kdim elements (kdim a multiple of 8): LBO = 128, SBO = 16 * kdim.
 __host__ __device__ constexpr uint32_t tile_offset(int row, int k, int kdim) {
   return (uint32_t)(((row >> 3) * (kdim >> 3) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// Byte offset of element (row, k) in an MN-major no-swizzle tile of `rows`
+// rows (a multiple of 8): a core matrix holds 8 K-steps x 8 consecutive rows;
+// SBO (next 8 rows) = 128, LBO (next 8 K-steps) = 16 * rows.
+__host__ __device__ constexpr uint32_t tile_offset_mn(int row, int k, int rows) {
+  return (uint32_t)(((k >> 3) * (rows >> 3) + (row >> 3)) * 128 + (k & 7) * 16 + (row & 7) * 2);
 }
 
 }  // namespace tc

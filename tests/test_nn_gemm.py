@@ -17,12 +17,15 @@ def from_bf16(b):
     return (b.astype(np.uint32) << 16).view(np.float32)
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (200, 144, 96), (37, 16, 8), (256, 300, 200)])
-def test_gemm_bf16(ctx, M, N, K):
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (200, 144, 96), (40, 16, 8), (256, 304, 200)])
+@pytest.mark.parametrize("a_mn,b_mn", [(False, False), (True, False), (False, True), (True, True)])
+def test_gemm_bf16(ctx, M, N, K, a_mn, b_mn):
     rng = np.random.RandomState(M + N + K)
     A = to_bf16(rng.normal(size=(M, K)))
     B = to_bf16(rng.normal(size=(N, K)))
-    C = ctx.gemm_bf16(A, B)
+    Aa = np.ascontiguousarray(A.T) if a_mn else A
+    Bb = np.ascontiguousarray(B.T) if b_mn else B
+    C = ctx.gemm_bf16(Aa, Bb, a_mn=a_mn, b_mn=b_mn)
     ref = from_bf16(A).astype(np.float64) @ from_bf16(B).astype(np.float64).T
     err = np.abs(C - ref).max() / max(np.abs(ref).max(), 1e-6)
     assert err < 1e-5, err

@@ -46,3 +46,66 @@ def test_pool_upsample_loss_adam():
     assert np.allclose(g, _fd(lambda: U.l1_log_loss(x, t)[0], x), atol=1e-6)
     p, m, v = U.adam(np.ones(3), np.array([1.0, -2.0, 0.0]), np.zeros(3), np.zeros(3), 1)
     assert np.allclose(p, [1 - 3e-4, 1 + 3e-4, 1.0])
+
+
+def test_bf16_rounding_is_nearest_even():
+    e = 2.0 ** -7  # BF16 spacing at 1.0 (7 stored mantissa bits)
+    vals = np.array([1.0, 1 + e / 2, 1 + 3 * e / 2, 1 + e / 2 + 1e-6, -2.5, 0.0, 3.0e38])
+    got = U.to_bf16(vals)
+    assert got[0] == 1.0 and got[1] == 1.0  # tie -> even
+    assert got[2] == 1 + 2 * e               # tie -> even (upwards)
+    assert got[3] == 1 + e                   # above the tie
+    assert got[4] == -2.5 and got[5] == 0.0
+    assert np.isfinite(got[6])
+
+
+def test_layer_table_layout():
+    rows, n = U.layer_table()
+    assert len(rows) == 14
+    end = 0
+    for r in rows:
+        assert r["w_off"] % 4 == 0 and r["b_off"] % 4 == 0 and r["w_off"] >= end
+        assert r["cin_pad"] % 16 == 0 and r["cout_pad"] % 16 == 0
+        end = r["b_off"] + r["cout_pad"]
+    assert end <= n
+    # 32 / 64 / 96 / 128 / 160 channels, about 1.3M parameters
+    assert [r["cout"] for r in rows] == [32, 32, 64, 64, 96, 96, 128, 128, 160, 128, 96, 64, 32, 3]
+    assert 1.2e6 < U.real_param_count() < 1.4e6
+
+
+def test_network_gradients_match_finite_differences():
+    """The whole U-Net (FP64, no rounding): the analytic gradient of the L1-log
+    loss against central differences, for weights and biases of every layer."""
+    rng = np.random.RandomState(3)
+    p = U.init_params(5)
+    rows, _ = U.layer_table()
+    for r in rows:  # non-zero biases so that every bias gradient is exercised
+        p[r["b_off"]:r["b_off"] + r["cout"]] = rng.normal(0, 0.05, r["cout"])
+    raw = rng.uniform(0, 1, (1, 16, 16, 10))
+    raw[..., :3] *= 4.0
+    target = rng.uniform(0, 3, (1, 16, 16, 3))
+    net = U.UNet(p)
+    loss, g = net.loss_and_grads(raw, target)
+    assert np.isfinite(loss)
+
+    def f():
+        return np.abs(U.UNet(p).forward(raw)[..., :3] - np.log1p(target)).mean()
+
+    picks = []
+    for r in rows:
+        w = r["w_off"]
+        ci = r["cin"] if r["cin_pad"] == r["c1_pad"] else r["cin_pad"]
+        for _ in range(2):
+            o, t, c = rng.randint(r["cout"]), rng.randint(9), rng.randint(ci)
+            picks.append(w + (o * 9 + t) * r["cin_pad"] + c)
+        picks.append(r["b_off"] + rng.randint(r["cout"]))
+    eps = 1e-6
+    for k in picks:
+        old = p[k]
+        p[k] = old + eps
+        a = f()
+        p[k] = old - eps
+        b = f()
+        p[k] = old
+        fd = (a - b) / (2 * eps)
+        assert abs(fd - g[k]) <= 1e-6 + 1e-4 * abs(fd), (k, fd, g[k])
