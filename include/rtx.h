@@ -26,7 +26,16 @@
  *       [8] anisotropic (unused by the BSDF, as in the reference)
  *       [9] subsurface  [10] specular_tint  [11] sheen  [12] sheen_tint
  *       [13] clearcoat  [14] clearcoat_roughness  [15] spec_trans  [16] ior
- *       [17] at_distance  [18..20] extinction  [21..23] padding
+ *       [17] at_distance  [18..20] extinction
+ *       [21] texture kind: 0 none, 1 checkerboard, 2 wave, 3 Perlin
+ *       [22] the texture's parameter (CheckerBoard::scale, an integer;
+ *            Wave::period; PerlinNoise::scale)  [23] texture units per world
+ *            unit.  A textured material's base_color is scaled by
+ *            0.25 + 0.75 * Sample(p), p = the hit point's two world
+ *            coordinates across the dominant axis of the shading normal
+ *            (x: (y, z); y: (x, z); z: (x, y)) times [23].  RenderToy's
+ *            textures (src/procedural.cpp) only rasterise to images; this
+ *            binding is an extension.  Zero in all three = untextured.
  *   camera (RTX_CAMERA_FLOATS = 21 floats) — Camera,
  *     include/RenderToy/object.h:69-95:
  *       [0..15] object-to-world 4x4, row-major  [16] focal length (mm)
@@ -149,6 +158,16 @@ int rtx_scene_emitters(rtx_context* ctx, int32_t* out, int cap, int* n_out);
  * World::PrepareDirectLightSampling left it (src/world.cpp:24-37); n = 0
  * disables light sampling, as in a World where it was never called. */
 int rtx_scene_set_emitters(rtx_context* ctx, const int32_t* ids, int n);
+/* The 256-entry permutation the Perlin texture hashes through
+ * (siv::BasicPerlinNoise's m_permutation; default: a fixed seeded shuffle).
+ * Applies to the current and later scenes of the context. */
+int rtx_scene_set_texture_table(rtx_context* ctx, const uint8_t* perm);
+/* RenderToy's ProceduralTexture samplers at n points (uv: n x 2 floats):
+ * kind 1 CheckerBoard(scale = (int)param), 2 Wave(period = param),
+ * 3 PerlinNoise with scale = param, time 0, 4 octaves (src/procedural.cpp:
+ * 8-46), evaluated by the device code that shades textured materials. */
+int rtx_texture_sample(rtx_context* ctx, int kind, float param, int n,
+                       const float* uv, float* out);
 
 /* ---- renderers ------------------------------------------------------------
  * PathTracingRenderer::Render (src/renderer.cpp:236-270): out_rgb[p] =
@@ -177,6 +196,42 @@ int rtx_primary_hits(rtx_context* ctx, const float* camera, int W, int H,
  * exclude may be NULL). */
 int rtx_intersect(rtx_context* ctx, int n, const float* rays,
                   const int32_t* exclude, int32_t* out_tri, float* out_tuv);
+
+/* rtx_render_pt, and in the same pass as the last accumulation the display
+ * resolve of the mean (see rtx_image_resolve): display (W x H RGB FP32) and
+ * bytes (format as rtx_image_resolve) may each be NULL; out is the radiance. */
+int rtx_render_pt_resolved(rtx_context* ctx, const float* camera, int W, int H,
+                           int spp, int max_depth, uint64_t seed, float* out,
+                           float limit, float gamma, float* display,
+                           uint8_t* bytes, int format);
+
+/* ---- display resolve and image files ----------------------------------------
+ * Image::Tonemap<kITURBT709>(limit): p * 1 / (1 + Luma709(p) / limit)
+ * (include/RenderToy/compositor.h:220-226, rtmath.h:1142-1177), then
+ * Image::GammaCorrection(gamma): p^(1 / gamma) per channel
+ * (src/compositor.cpp:94-100), then the exporters' quantisation
+ * int(255.99 * clamp(x, 0, 1)), NaN -> 0 (src/exporter.cpp:8-95).
+ * limit <= 0 skips the tonemap and gamma <= 0 the gamma correction. */
+#define RTX_BYTES_BMP 0 /* BMP pixel array: rows of B, G, R bytes, buffer row 0
+                           first, each row zero-padded to a multiple of 4 */
+#define RTX_BYTES_RGB 1 /* R, G, B bytes per pixel in buffer order */
+int rtx_image_resolve(rtx_context* ctx, const float* in, int W, int H,
+                      float limit, float gamma, float* display, uint8_t* bytes,
+                      int format);
+int rtx_image_tonemap(rtx_context* ctx, const float* in, float* out, int W,
+                      int H, float limit);
+int rtx_image_gamma(rtx_context* ctx, const float* in, float* out, int W, int H,
+                    float gamma);
+/* BMPExporter::Export (src/exporter.cpp:38-95) into memory: 54-byte header +
+ * the BMP pixel array of the image (quantised as above, no tonemap).  The
+ * padding bytes are zeros (the reference writes them from a null pointer)
+ * and the header's file size counts them.  file = NULL queries *size. */
+int rtx_encode_bmp(rtx_context* ctx, const float* in, int W, int H,
+                   uint8_t* file, size_t cap, size_t* size);
+/* PPMExporter::Export (src/exporter.cpp:8-29) into memory: "P3" text, one
+ * "r g b" line per pixel, buffer row 0 first.  file = NULL queries *size. */
+int rtx_encode_ppm(rtx_context* ctx, const float* in, int W, int H, char* file,
+                   size_t cap, size_t* size);
 
 /* ---- compositor ------------------------------------------------------------
  * Image operations (include/RenderToy/compositor.h:107-178,
@@ -214,7 +269,8 @@ int rtx_nn_gemm_bf16(rtx_context* ctx, int M, int N, int K, const void* A,
  *   fwd  : out[P][Cout] (FP32) = relu?(bias + conv(x, w)), w [Cout][9][Cin]
  *   dgrad: din[P][Cin] (BF16) = conv^T(dout, wt) * (x > 0 if mask_relu),
  *          wt [Cin][9][Cout], Cin a multiple of 16
- *   wgrad: dw[Cout][9][Cin] (FP32) = sum_p dout[p] x[p + tap]
+ *   wgrad: dw[Cout][9][Cin] (FP32) = sum_p dout[p] x[p + tap]; Cout a
+ *          multiple of 16 and <= 256
  * P = N * H * W at the convolution's resolution. */
 int rtx_nn_conv3x3_fwd(rtx_context* ctx, int N, int H, int W, const void* x1,
                        int C1, int up1, const void* x2, int C2, const void* w,

@@ -76,6 +76,11 @@ class Checker:
         fn("edge_detect", None, [_f32p, _f32p, C.c_int, C.c_int])
         fn("bloom", None, [_f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float])
         fn("rng_floats", None, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_int, _f32p])
+        fn("texture_sample", None, [C.c_int, C.c_float, vp, C.c_int, _f32p, _f32p])
+        if kind == "oracle":
+            fn("scene_set_texture_table", None, [vp, _u8p])
+        else:
+            fn("perlin_table", None, [_u8p])
         if kind == "oracle":
             fn("render_pt", None, [vp, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                    _f32p, C.c_int])
@@ -83,6 +88,20 @@ class Checker:
     # -- scene -------------------------------------------------------------
     def scene(self, sc):
         return CheckerScene(self, sc)
+
+    # -- procedural textures ------------------------------------------------
+    def texture_sample(self, kind, param, uv, perm=None):
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        out = np.zeros(len(uv), np.float32)
+        pp = None if perm is None else np.ascontiguousarray(perm, np.uint8)
+        self._fn["texture_sample"](int(kind), float(param), None if pp is None else pp.ctypes.data,
+                                   len(uv), uv, out)
+        return out
+
+    def perlin_table(self):
+        out = np.zeros(256, np.uint8)
+        self._fn["perlin_table"](out)
+        return out
 
     # -- BSDF --------------------------------------------------------------
     def bsdf_eval(self, mat, eta, N, V, L):
@@ -153,6 +172,9 @@ class CheckerScene:
             np.ascontiguousarray(sc.mesh_mat, np.int32), np.ascontiguousarray(sc.mesh_smooth, np.uint8),
             len(sc.mats), np.ascontiguousarray(sc.mats, np.float32),
             np.ascontiguousarray(sc.sky, np.float32), np.ascontiguousarray(sc.ground, np.float32))
+
+    def set_texture_table(self, perm):
+        self.chk._fn["scene_set_texture_table"](self.h, np.ascontiguousarray(perm, np.uint8))
 
     def close(self):
         if self.h:

@@ -447,6 +447,27 @@ void ref_bloom(const float* in, float* out, int W, int H, int size, float sigma,
   delete img;
 }
 
+// ProceduralTexture samplers (src/procedural.cpp:8-46) at n points;
+// PerlinNoise as constructed (its constructor never reseeds: siv's default
+// permutation) with `scale` = param
+void ref_texture_sample(int kind, float param, const uint8_t* perm, int n, const float* uv, float* out) {
+  (void)perm;
+  ProceduralTexture::CheckerBoard cb((int)param);
+  ProceduralTexture::Wave wv(param);
+  ProceduralTexture::PerlinNoise pn(0);
+  pn.scale = param;
+  for (int i = 0; i < n; ++i) {
+    Vector2f p(uv[2 * i], uv[2 * i + 1]);
+    out[i] = kind == 1 ? cb.Sample(p) : kind == 2 ? wv.Sample(p) : kind == 3 ? pn.Sample(p) : 1.0f;
+  }
+}
+
+// the permutation a default-constructed ProceduralTexture::PerlinNoise uses
+void ref_perlin_table(uint8_t* out) {
+  ProceduralTexture::PerlinNoise pn(0);
+  for (int i = 0; i < 256; ++i) out[i] = pn.perlin_noise_generator.m_permutation[i];
+}
+
 void ref_rng_floats(uint64_t seed, uint32_t pixel, uint32_t sample, int n,
                     float* out) {
   g_key.seed = seed;

@@ -515,6 +515,8 @@ struct Scene {
   std::vector<int> mesh_mat;
   std::vector<uint8_t> mesh_smooth;
   std::vector<Mat> mats;
+  std::vector<V3> mat_tex;  // per material: texture kind, parameter, scale (floats 21..23)
+  uint8_t perm[256];        // Perlin texture permutation
   std::vector<int> emitters;
   V3 sky, ground;
   std::vector<OctNode> nodes;
@@ -525,7 +527,101 @@ struct Scene {
   int intersect(V3 o, V3 d, int exclude, float& t, float& u, float& v,
                 V3* pos) const;                                 // bvh.cpp:266-341
   V3 normal_at(int tri, float u, float v) const;                // object.cpp:207-217
+  Mat shade_mat(int tri, V3 pos, V3 n) const;                   // textured material at a hit
 };
+
+// ----------------------------------------------------------------------------
+// Procedural textures, src/procedural.cpp:8-46 (bound to materials by floats
+// 21..23 of the record: an extension, see include/rtx.h).  The Perlin sampler
+// is improved gradient noise (K. Perlin, SIGGRAPH 2002) as siv::PerlinNoise
+// v3.0.0 (include/PerlinNoise/PerlinNoise.hpp:281-300, 365-400, 489-534,
+// 611-614) evaluates it in float.
+// ----------------------------------------------------------------------------
+float tex_checker(float x, float y, int scale) {
+  return (((int)(x * (float)scale) & 1) ^ ((int)(y * (float)scale) & 1)) == 1 ? 1.0f : 0.0f;
+}
+float tex_wave(float x, float period) { return (std::sin(2.0f * kPi * period * x) + 1.0f) / 2.0f; }
+float pfade(float t) { return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f); }
+float plerp(float a, float b, float t) { return a + (b - a) * t; }
+float pgrad(uint32_t hash, float x, float y, float z) {
+  uint32_t h = hash & 15u;
+  float u = h < 8u ? x : y;
+  float v = h < 4u ? y : (h == 12u || h == 14u ? x : z);
+  return ((h & 1u) == 0u ? u : -u) + ((h & 2u) == 0u ? v : -v);
+}
+float perlin_noise3(const uint8_t* perm, float x, float y, float z) {
+  float x0 = std::floor(x), y0 = std::floor(y), z0 = std::floor(z);
+  int ix = (int)x0 & 255, iy = (int)y0 & 255, iz = (int)z0 & 255;
+  float fx = x - x0, fy = y - y0, fz = z - z0;
+  float u = pfade(fx), v = pfade(fy), w = pfade(fz);
+  uint32_t A = (perm[ix & 255] + iy) & 255, B = (perm[(ix + 1) & 255] + iy) & 255;
+  uint32_t AA = (perm[A] + iz) & 255, AB = (perm[(A + 1) & 255] + iz) & 255;
+  uint32_t BA = (perm[B] + iz) & 255, BB = (perm[(B + 1) & 255] + iz) & 255;
+  float q0 = plerp(pgrad(perm[AA], fx, fy, fz), pgrad(perm[BA], fx - 1.0f, fy, fz), u);
+  float q1 = plerp(pgrad(perm[AB], fx, fy - 1.0f, fz), pgrad(perm[BB], fx - 1.0f, fy - 1.0f, fz), u);
+  float q2 = plerp(pgrad(perm[(AA + 1) & 255], fx, fy, fz - 1.0f), pgrad(perm[(BA + 1) & 255], fx - 1.0f, fy, fz - 1.0f), u);
+  float q3 = plerp(pgrad(perm[(AB + 1) & 255], fx, fy - 1.0f, fz - 1.0f),
+                   pgrad(perm[(BB + 1) & 255], fx - 1.0f, fy - 1.0f, fz - 1.0f), u);
+  return plerp(plerp(q0, q1, v), plerp(q2, q3, v), w);
+}
+float tex_perlin(const uint8_t* perm, float px, float py, float scale) {
+  float x = px * scale, y = py * scale, z = 0.0f, result = 0.0f, amplitude = 1.0f;
+  for (int i = 0; i < 4; ++i) {
+    result += perlin_noise3(perm, x, y, z) * amplitude;
+    x *= 2.0f;
+    y *= 2.0f;
+    z *= 2.0f;
+    amplitude *= 0.5f;
+  }
+  if (result <= -1.0f) return 0.0f;
+  if (1.0f <= result) return 1.0f;
+  return result * 0.5f + 0.5f;
+}
+float texture_sample(int kind, float param, const uint8_t* perm, float px, float py) {
+  if (kind == 1) return tex_checker(px, py, (int)param);
+  if (kind == 2) return tex_wave(px, param);
+  if (kind == 3) return tex_perlin(perm, px, py, param);
+  return 1.0f;
+}
+
+Mat Scene::shade_mat(int tri, V3 pos, V3 n) const {
+  int mi = mesh_mat[tris[tri].mesh];
+  Mat m = mats[mi];
+  V3 tx = mat_tex[mi];
+  if (tx.x != 0.0f) {
+    float ax = std::fabs(n.x), ay = std::fabs(n.y), az = std::fabs(n.z);
+    float px, py;
+    if (ax >= ay && ax >= az) {
+      px = pos.y;
+      py = pos.z;
+    } else if (ay >= az) {
+      px = pos.x;
+      py = pos.z;
+    } else {
+      px = pos.x;
+      py = pos.y;
+    }
+    float sm = texture_sample((int)tx.x, tx.y, perm, px * tx.z, py * tx.z);
+    m.base_color = scl(m.base_color, 0.25f + 0.75f * sm);
+  }
+  return m;
+}
+
+// the default texture permutation (include/rtx.h): Fisher-Yates over 0..255
+// driven by splitmix64 from 0
+void default_texture_table(uint8_t* p) {
+  for (int i = 0; i < 256; ++i) p[i] = (uint8_t)i;
+  uint64_t x = 0;
+  for (int i = 255; i > 0; --i) {
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    int j = (int)(z % (uint64_t)(i + 1));
+    std::swap(p[i], p[j]);
+  }
+}
 
 // object.cpp:107-167 — two-sided Moller-Trumbore variant
 bool tri_intersect(const Tri& tr, V3 o, V3 d, float& t, float& u, float& v) {
@@ -767,7 +863,7 @@ V3 emission_pdf(const Scene& s, int tri, V3 position, float u, float v, V3 to_po
 }
 
 V3 DirectLight(const Scene& s, const RayState& state, V3 orig_dir, int tri,
-               V3 pos, Rng& rng) {  // renderer.cpp:335-384
+               V3 pos, const Mat& m, Rng& rng) {  // renderer.cpp:335-384
   V3 ret = v3s(0.0f);
   if (s.emitters.empty()) return ret;  // world.cpp:7-16 (no draws)
   int e = s.emitters[rng.uniform_int(0, (int)s.emitters.size() - 1)];
@@ -787,7 +883,6 @@ V3 DirectLight(const Scene& s, const RayState& state, V3 orig_dir, int tri,
     float lightpdf;
     V3 em = emission_pdf(s, e, emit_pos, u, v, pos, neg(dir), lightpdf);
     float bsdfpdf;
-    const Mat& m = s.mats[s.mesh_mat[s.tris[tri].mesh]];
     V3 f = BsdfEval(m, state.eta, neg(orig_dir), state.ffnormal, dir, bsdfpdf);
     float weight = PowerHeuristic(lightpdf, bsdfpdf);
     if (bsdfpdf > 0.0f) {
@@ -809,8 +904,8 @@ V3 Radiance(const Scene& s, V3 o, V3 d, int last_hit, RayState& state, int depth
   int hit = s.intersect(o, d, last_hit, t, u, v, &hitpos);
   V3 radiance = v3s(0.0f);
   if (hit >= 0) {
-    const Mat& m = s.mats[s.mesh_mat[s.tris[hit].mesh]];
     state.ffnormal = s.normal_at(hit, u, v);
+    const Mat m = s.shade_mat(hit, hitpos, state.ffnormal);
     if (dot(d, state.ffnormal) > 0.0f) {
       state.ffnormal = neg(state.ffnormal);
       state.eta = m.ior;
@@ -827,7 +922,7 @@ V3 Radiance(const Scene& s, V3 o, V3 d, int last_hit, RayState& state, int depth
     float dist = length(sub(hitpos, o));
     V3 expo = scl(neg(state.absorption), dist);
     V3 bounce_ratio = v3(std::pow(kE, expo.x), std::pow(kE, expo.y), std::pow(kE, expo.z));
-    radiance = add(radiance, mul(DirectLight(s, state, d, hit, hitpos, rng), bounce_ratio));
+    radiance = add(radiance, mul(DirectLight(s, state, d, hit, hitpos, m, rng), bounce_ratio));
     V3 next_dir, color;
     float bsdfpdf;
     if (BsdfSample(m, state.eta, state.ffnormal, neg(d), rng, next_dir, color, bsdfpdf)) {
@@ -964,7 +1059,11 @@ void* orc_scene_create(int n_tris, const float* verts, const float* norms,
   }
   s->mesh_mat.assign(mesh_mat, mesh_mat + n_meshes);
   s->mesh_smooth.assign(mesh_smooth, mesh_smooth + n_meshes);
-  for (int i = 0; i < n_mat; ++i) s->mats.push_back(load_mat(mats + 24 * (size_t)i));
+  for (int i = 0; i < n_mat; ++i) {
+    s->mats.push_back(load_mat(mats + 24 * (size_t)i));
+    s->mat_tex.push_back(v3(mats[24 * (size_t)i + 21], mats[24 * (size_t)i + 22], mats[24 * (size_t)i + 23]));
+  }
+  default_texture_table(s->perm);
   s->sky = v3(sky[0], sky[1], sky[2]);
   s->ground = v3(ground[0], ground[1], ground[2]);
   // World::PrepareDirectLightSampling, world.cpp:24-37: meshes in order, their
@@ -986,6 +1085,19 @@ void* orc_scene_create(int n_tris, const float* verts, const float* norms,
 }
 
 void orc_scene_destroy(void* scene) { delete (Scene*)scene; }
+
+void orc_scene_set_texture_table(void* scene, const uint8_t* perm) {
+  std::memcpy(((Scene*)scene)->perm, perm, 256);
+}
+
+void orc_texture_sample(int kind, float param, const uint8_t* perm, int n, const float* uv, float* out) {
+  uint8_t def[256];
+  if (!perm) {
+    default_texture_table(def);
+    perm = def;
+  }
+  for (int i = 0; i < n; ++i) out[i] = texture_sample(kind, param, perm, uv[2 * i], uv[2 * i + 1]);
+}
 
 int orc_scene_emitters(void* scene, int32_t* out, int cap) {
   Scene* s = (Scene*)scene;
@@ -1050,7 +1162,7 @@ void orc_render_aov(void* scene, const float* cam, int W, int H, float near_,
         V3 n = s->normal_at(h, u, v);
         if (dot(s->tris[h].normal, neg(d)) < 0.0f) n = neg(n);
         nv = dvs(add(n, v3s(1.0f)), 2.0f);
-        av = s->mats[s->mesh_mat[s->tris[h].mesh]].base_color;
+        av = s->shade_mat(h, pos, n).base_color;
         dv = v3s(std::clamp((t - near_) * inv_range, 0.0f, 1.0f));
       }
       if (normal) { normal[p] = nv.x; normal[p + 1] = nv.y; normal[p + 2] = nv.z; }

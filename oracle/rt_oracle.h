@@ -37,6 +37,11 @@ void* orc_scene_create(int n_tris, const float* verts, const float* norms,
                        const float* ground);
 void orc_scene_destroy(void* scene);
 int orc_scene_emitters(void* scene, int32_t* out, int cap);
+/* the Perlin texture's permutation (default: include/rtx.h's seeded shuffle) */
+void orc_scene_set_texture_table(void* scene, const uint8_t* perm);
+/* procedural texture samplers at n points (perm NULL = the default table) */
+void orc_texture_sample(int kind, float param, const uint8_t* perm, int n,
+                        const float* uv, float* out);
 
 /* closest hit of n rays; exclude[i] = triangle id to skip (-1 none).
  * out_tri[i] = id or -1, out_tuv[3i..] = t,u,v (t = 1e7 and u=v=0 on miss). */

@@ -36,6 +36,8 @@ EXPORTS = [
     "rtx_nn_conv3x3_dgrad", "rtx_nn_conv3x3_wgrad", "rtx_dn_init", "rtx_dn_info", "rtx_dn_layer",
     "rtx_dn_get_params", "rtx_dn_set_params", "rtx_dn_get_grads", "rtx_dn_get_adam", "rtx_dn_set_adam",
     "rtx_dn_loss_grads", "rtx_dn_train_step", "rtx_dn_infer", "rtx_denoise",
+    "rtx_scene_set_texture_table", "rtx_texture_sample", "rtx_render_pt_resolved", "rtx_image_resolve",
+    "rtx_image_tonemap", "rtx_image_gamma", "rtx_encode_bmp", "rtx_encode_ppm",
 ]
 
 
@@ -108,6 +110,14 @@ def lib() -> C.CDLL:
         "rtx_dn_train_step": (i, [vp, vp, vp, i, i, i, f, C.POINTER(C.c_double)]),
         "rtx_dn_infer": (i, [vp, vp, vp, i, i, i]),
         "rtx_denoise": (i, [vp, vp, vp, vp, vp, vp, i, i]),
+        "rtx_scene_set_texture_table": (i, [vp, vp]),
+        "rtx_texture_sample": (i, [vp, i, f, i, vp, vp]),
+        "rtx_render_pt_resolved": (i, [vp, vp, i, i, i, i, u64, vp, f, f, vp, vp, i]),
+        "rtx_image_resolve": (i, [vp, vp, i, i, f, f, vp, vp, i]),
+        "rtx_image_tonemap": (i, [vp, vp, vp, i, i, f]),
+        "rtx_image_gamma": (i, [vp, vp, vp, i, i, f]),
+        "rtx_encode_bmp": (i, [vp, vp, i, i, vp, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rtx_encode_ppm": (i, [vp, vp, i, i, vp, C.c_size_t, C.POINTER(C.c_size_t)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -226,11 +236,13 @@ class Context:
                                            max_depth, seed, _ptr(o)))
         return o
 
-    def aov(self, W, H, near, far, camera=None):
+    def aov(self, W, H, near, far, camera=None, out=None):
+        """normal, albedo, depth passes (H x W x 3 each); out = three
+        preallocated buffers (host arrays or device tensors) or None."""
         cam = self._cam(camera)
-        n = np.zeros((H, W, 3), np.float32)
-        a = np.zeros((H, W, 3), np.float32)
-        d = np.zeros((H, W, 3), np.float32)
+        if out is None:
+            out = tuple(np.zeros((H, W, 3), np.float32) for _ in range(3))
+        n, a, d = out
         self._check(self.L.rtx_render_aov(self.h, _ptr(cam), W, H, near, far, _ptr(n), _ptr(a),
                                           _ptr(d)))
         return n, a, d
@@ -262,6 +274,71 @@ class Context:
         self._check(self.L.rtx_nn_gemm_bf16(self.h, M, N, K, _ptr(A), _ptr(B), _ptr(C_), int(a_mn),
                                             int(b_mn)))
         return C_
+
+    # -- display resolve and image files -------------------------------------------
+    BYTES_BMP, BYTES_RGB = 0, 1
+
+    @staticmethod
+    def _byte_buf(W, H, fmt):
+        n = ((3 * W + 3) & ~3) * H if fmt == 0 else 3 * W * H
+        return np.zeros(n, np.uint8)
+
+    def render_pt_resolved(self, W, H, spp, max_depth, seed=0, limit=1.5, gamma=2.2, fmt=1,
+                           want_display=True, want_bytes=True, camera=None):
+        cam = self._cam(camera)
+        o = np.zeros((H, W, 3), np.float32)
+        disp = np.zeros((H, W, 3), np.float32) if want_display else None
+        byt = self._byte_buf(W, H, fmt) if want_bytes else None
+        self._check(self.L.rtx_render_pt_resolved(self.h, _ptr(cam), W, H, spp, max_depth, seed, _ptr(o),
+                                                  limit, gamma, _ptr(disp), _ptr(byt), fmt))
+        return o, disp, byt
+
+    def resolve(self, img, limit=1.5, gamma=2.2, fmt=1, want_display=True, want_bytes=True):
+        img = img if hasattr(img, "data_ptr") else _f32(img)
+        H, W = int(img.shape[0]), int(img.shape[1])
+        disp = np.zeros((H, W, 3), np.float32) if want_display else None
+        byt = self._byte_buf(W, H, fmt) if want_bytes else None
+        self._check(self.L.rtx_image_resolve(self.h, _ptr(img), W, H, limit, gamma, _ptr(disp), _ptr(byt), fmt))
+        return disp, byt
+
+    def tonemap(self, img, limit=1.5, out=None):
+        img, out, W, H = self._img_io(img, out)
+        self._check(self.L.rtx_image_tonemap(self.h, _ptr(img), _ptr(out), W, H, limit))
+        return out
+
+    def gamma(self, img, gamma=2.2, out=None):
+        img, out, W, H = self._img_io(img, out)
+        self._check(self.L.rtx_image_gamma(self.h, _ptr(img), _ptr(out), W, H, gamma))
+        return out
+
+    def _encode(self, fn, img):
+        img = _f32(img)
+        H, W = img.shape[:2]
+        n = C.c_size_t()
+        self._check(fn(self.h, _ptr(img), W, H, None, 0, C.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        self._check(fn(self.h, _ptr(img), W, H, _ptr(buf), n.value, C.byref(n)))
+        return buf.tobytes()
+
+    def encode_bmp(self, img):
+        """BMPExporter output (bytes) of an H x W x 3 image."""
+        return self._encode(self.L.rtx_encode_bmp, img)
+
+    def encode_ppm(self, img):
+        """PPMExporter output (bytes) of an H x W x 3 image."""
+        return self._encode(self.L.rtx_encode_ppm, img)
+
+    # -- procedural textures ------------------------------------------------------
+    def set_texture_table(self, perm):
+        perm = np.ascontiguousarray(perm, np.uint8)
+        assert perm.size == 256
+        self._check(self.L.rtx_scene_set_texture_table(self.h, _ptr(perm)))
+
+    def texture_sample(self, kind, param, uv):
+        uv = _f32(uv).reshape(-1, 2)
+        out = np.zeros(len(uv), np.float32)
+        self._check(self.L.rtx_texture_sample(self.h, int(kind), float(param), len(uv), _ptr(uv), _ptr(out)))
+        return out
 
     # -- denoiser operators -------------------------------------------------------
     def conv3x3_fwd(self, x1, w, Cout, x2=None, up1=False, bias=None, relu=False, out=None):

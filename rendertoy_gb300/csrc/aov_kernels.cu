@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(64) k_primary(DeviceScene s, CamParams cam, in
       nv = (n + f3s(1.0f)) / 2.0f;
       const float* m = s.mats + 24 * (size_t)mat;
       av = f3(__ldg(m), __ldg(m + 1), __ldg(m + 2));
+      if (__ldg(m + 21) != 0.0f) av = textured_base(m, o + d * t, n, s.perm);
       dv = f3s(clamp01((t - near_) * inv_range));
     }
     if (normal) {
@@ -99,6 +100,20 @@ cudaError_t launch_intersect(const DeviceScene& s, int n, const float* rays, con
   if (n <= 0) return cudaSuccess;
   k_intersect<<<(n + 127) / 128, 128, 0, st>>>(s, n, rays, exclude, tri, tuv, err);
   ++*launches;
+  return cudaGetLastError();
+}
+
+// RenderToy's procedural textures sampled at points (the shading code's
+// samplers): out[i] = Sample(uv[2 i], uv[2 i + 1])
+__global__ void k_texture_sample(int kind, float param, const uint8_t* __restrict__ perm, int n,
+                                 const float* __restrict__ uv, float* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = texture_sample(kind, param, perm, uv[2 * i], uv[2 * i + 1]);
+}
+
+cudaError_t launch_texture_sample(int kind, float param, const uint8_t* perm, int n, const float* uv,
+                                  float* out, cudaStream_t st) {
+  if (n > 0) k_texture_sample<<<(n + 255) / 256, 256, 0, st>>>(kind, param, perm, n, uv, out);
   return cudaGetLastError();
 }
 

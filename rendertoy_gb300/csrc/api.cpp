@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -93,6 +94,7 @@ struct rtx_context {
   Counters* d_counters = nullptr;
   PtWorkspace* pt = nullptr;
   DevBuf stage[8];
+  DevBuf perm;  // Perlin texture permutation (256 bytes)
   rtx::nn::UNet* dn = nullptr;
   DevBuf weights;
   std::vector<float> host_weights;
@@ -239,6 +241,25 @@ int upload_weights(rtx_context* c, const float* w, size_t n) {
   return RTX_OK;
 }
 
+// The default permutation of the Perlin texture: a Fisher-Yates shuffle of
+// 0..255 driven by splitmix64 from 0 (siv::PerlinNoise's own default table is
+// not reproduced; rtx_scene_set_texture_table installs any table).
+void default_texture_table(uint8_t* p) {
+  for (int i = 0; i < 256; ++i) p[i] = (uint8_t)i;
+  uint64_t x = 0;
+  for (int i = 255; i > 0; --i) {
+    x += 0x9E3779B97F4A7C15ull;
+    uint64_t z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    int j = (int)(z % (uint64_t)(i + 1));
+    uint8_t t = p[i];
+    p[i] = p[j];
+    p[j] = t;
+  }
+}
+
 }  // namespace
 
 namespace rtx {
@@ -297,6 +318,13 @@ int rtx_create(rtx_context** out, int device) {
   if ((e = cudaMalloc(&c->d_err, sizeof(int))) != cudaSuccess) return bail(e);
   if ((e = cudaMalloc(&c->d_counters, sizeof(Counters))) != cudaSuccess) return bail(e);
   if ((e = cudaMemset(c->d_counters, 0, sizeof(Counters))) != cudaSuccess) return bail(e);
+  {
+    uint8_t tbl[256];
+    default_texture_table(tbl);
+    if ((e = c->perm.ensure(256)) != cudaSuccess) return bail(e);
+    if ((e = cudaMemcpy(c->perm.p, tbl, 256, cudaMemcpyHostToDevice)) != cudaSuccess) return bail(e);
+    c->ds.perm = (const uint8_t*)c->perm.p;
+  }
   c->pt = pt_workspace_create();
   *out = c;
   return RTX_OK;
@@ -314,6 +342,7 @@ void rtx_destroy(rtx_context* c) {
   c->mats.release();
   c->emit.release();
   for (auto& s : c->stage) s.release();
+  c->perm.release();
   delete c->dn;
   c->weights.release();
   if (c->pt) pt_workspace_destroy(c->pt);
@@ -440,6 +469,14 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   if (!sky || !ground) return fail(c, RTX_ERR_INVALID, "sky / ground is NULL");
   for (int m = 0; m < n_meshes; ++m)
     if (mesh_mat[m] < 0 || mesh_mat[m] >= n_mat) return fail(c, RTX_ERR_INVALID, "mesh material index out of range");
+  for (int m = 0; m < n_mat; ++m) {
+    float k = mats[RTX_MATERIAL_FLOATS * (size_t)m + 21];
+    if (!(k == 0.0f || k == 1.0f || k == 2.0f || k == 3.0f))
+      return fail(c, RTX_ERR_INVALID, "material texture kind must be 0, 1, 2 or 3");
+    float prm = mats[RTX_MATERIAL_FLOATS * (size_t)m + 22];
+    if (k == 1.0f && !(std::fabs(prm) < 1e6f))
+      return fail(c, RTX_ERR_INVALID, "checkerboard scale out of range");
+  }
   bool any_smooth = false;
   for (int m = 0; m < n_meshes; ++m) any_smooth |= mesh_smooth[m] != 0;
   if (any_smooth && !norms) return fail(c, RTX_ERR_INVALID, "a smooth mesh needs vertex normals");
@@ -509,6 +546,7 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   s.geo = (const float4*)c->geo.p;
   s.mats = (const float*)c->mats.p;
   s.emitters = (const int*)c->emit.p;
+  s.perm = (const uint8_t*)c->perm.p;
   s.root = b.root;
   s.n_tris = n;
   s.n_emitters = (int)c->emitters.size();
@@ -552,8 +590,72 @@ int rtx_scene_set_emitters(rtx_context* c, const int32_t* ids, int n) {
   return RTX_OK;
 }
 
+int rtx_scene_set_texture_table(rtx_context* c, const uint8_t* perm) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!perm) return fail(c, RTX_ERR_INVALID, "table is NULL");
+  int seen[256] = {0};
+  for (int i = 0; i < 256; ++i)
+    if (seen[perm[i]]++) return fail(c, RTX_ERR_INVALID, "the table is not a permutation of 0..255");
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  RTX_CUDA(cudaMemcpy(c->perm.p, perm, 256, cudaMemcpyHostToDevice), "table upload");
+  return RTX_OK;
+}
+
+int rtx_texture_sample(rtx_context* c, int kind, float param, int n, const float* uv, float* out) {
+  if (!c) return RTX_ERR_INVALID;
+  if (kind < 1 || kind > 3) return fail(c, RTX_ERR_INVALID, "kind must be 1, 2 or 3");
+  if (kind == 1 && !(std::fabs(param) < 1e6f)) return fail(c, RTX_ERR_INVALID, "checkerboard scale out of range");
+  if (n < 0 || (n > 0 && (!uv || !out))) return fail(c, RTX_ERR_INVALID, "bad point arrays");
+  int r;
+  if ((r = begin(c))) return r;
+  Arg ai, ao;
+  if ((r = bind_in(c, uv, (size_t)n * 8, 0, ai))) return r;
+  if ((r = bind_out(c, out, (size_t)n * 4, 1, ao))) return r;
+  cudaError_t e = launch_texture_sample(kind, param, (const uint8_t*)c->perm.p, n, (const float*)ai.dev,
+                                        (float*)ao.dev, c->stream);
+  c->stats.kernel_launches = n > 0 ? 1 : 0;
+  if (e != cudaSuccess) return cuda_fail(c, e, "texture kernel");
+  if ((r = copy_back(c, ao))) return r;
+  return finish(c, all_device({&ai, &ao}));
+}
+
+// A display resolve requested by the caller (see Resolve).
+struct ResolveReq {
+  float limit, gamma;
+  float* display;
+  uint8_t* bytes;
+  int format;
+};
+
+static int check_resolve(rtx_context* c, const ResolveReq& q) {
+  if (!(q.limit == q.limit) || !(q.gamma == q.gamma)) return fail(c, RTX_ERR_INVALID, "limit / gamma is NaN");
+  if (q.format != kResolveBmp && q.format != kResolveRgb) return fail(c, RTX_ERR_INVALID, "unknown byte format");
+  return RTX_OK;
+}
+
+static size_t resolve_bytes(int W, int H, int format) {
+  return format == kResolveBmp ? bmp_row_bytes(W) * (size_t)H : (size_t)W * H * 3;
+}
+
+// bind the resolve outputs to stage slots s, s + 1
+static int bind_resolve(rtx_context* c, const ResolveReq& q, int W, int H, int slot, Arg& ad, Arg& ab,
+                        Resolve& r) {
+  int e;
+  if ((e = bind_out(c, q.display, q.display ? (size_t)W * H * 12 : 0, slot, ad))) return e;
+  if ((e = bind_out(c, q.bytes, q.bytes ? resolve_bytes(W, H, q.format) : 0, slot + 1, ab))) return e;
+  r.limit = q.limit;
+  r.ratio = q.gamma > 0.0f ? 1.0f / q.gamma : 0.0f;  // GammaCorrection: ratio = 1.0f / gamma
+  r.display = (float*)ad.dev;
+  r.bytes = (uint8_t*)ab.dev;
+  r.format = q.format;
+  r.W = W;
+  return RTX_OK;
+}
+
 static int render_paths(rtx_context* c, const float* cam, int W, int H, int first, int n_samples,
-                        int spp, int max_depth, uint64_t seed, float* out, bool per_path) {
+                        int spp, int max_depth, uint64_t seed, float* out, bool per_path,
+                        const ResolveReq* rq = nullptr) {
   if (!c) return RTX_ERR_INVALID;
   int r;
   if ((r = check_cam(c, cam, W, H))) return r;
@@ -572,8 +674,15 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   } else if ((r = bind_out(c, out, out_elems * 3 * sizeof(float), 0, o))) {
     return r;
   }
+  Arg ad, ab;
+  Resolve rs{};
+  if (rq) {
+    if ((r = check_resolve(c, *rq))) return r;
+    if ((r = bind_resolve(c, *rq, W, H, 1, ad, ab, rs))) return r;
+  }
   CamParams cp = make_cam_params(cam, W, H);
   PtParams p;
+  p.resolve = rs;
   p.W = W;
   p.H = H;
   p.spp = spp;
@@ -602,13 +711,120 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
     return cuda_fail(c, e, "pt_render");
   }
   if ((r = copy_back(c, o))) return r;
-  return finish(c, all_device({&o}));
+  if ((r = copy_back(c, ad))) return r;
+  if ((r = copy_back(c, ab))) return r;
+  return finish(c, all_device({&o, &ad, &ab}));
 }
 
 int rtx_render_pt(rtx_context* c, const float* cam, int W, int H, int spp, int max_depth,
                   uint64_t seed, float* out) {
   if (c && spp <= 0) return fail(c, RTX_ERR_INVALID, "spp must be positive");
   return render_paths(c, cam, W, H, 0, spp, spp, max_depth, seed, out, false);
+}
+
+int rtx_render_pt_resolved(rtx_context* c, const float* cam, int W, int H, int spp, int max_depth,
+                           uint64_t seed, float* out, float limit, float gamma, float* display,
+                           uint8_t* bytes, int format) {
+  if (c && spp <= 0) return fail(c, RTX_ERR_INVALID, "spp must be positive");
+  ResolveReq q{limit, gamma, display, bytes, format};
+  return render_paths(c, cam, W, H, 0, spp, spp, max_depth, seed, out, false, &q);
+}
+
+// ---- display resolve and image files --------------------------------------------
+static int resolve_image(rtx_context* c, const float* in, int W, int H, const ResolveReq& q) {
+  if (!c) return RTX_ERR_INVALID;
+  int r;
+  if (!in) return fail(c, RTX_ERR_INVALID, "input is NULL");
+  if (W <= 0 || H <= 0 || (long long)W * H > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "bad image size");
+  if ((r = check_resolve(c, q))) return r;
+  if ((r = begin(c))) return r;
+  Arg ai, ad, ab;
+  Resolve rs{};
+  if ((r = bind_in(c, in, (size_t)W * H * 12, 0, ai))) return r;
+  if ((r = bind_resolve(c, q, W, H, 1, ad, ab, rs))) return r;
+  cudaError_t e = launch_resolve((const float*)ai.dev, W, H, rs, c->stream);
+  c->stats.kernel_launches = 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "resolve kernel");
+  if ((r = copy_back(c, ad))) return r;
+  if ((r = copy_back(c, ab))) return r;
+  return finish(c, all_device({&ai, &ad, &ab}));
+}
+
+int rtx_image_tonemap(rtx_context* c, const float* in, float* out, int W, int H, float limit) {
+  if (c && !(limit > 0.0f)) return fail(c, RTX_ERR_INVALID, "limit must be positive");
+  if (c && !out) return fail(c, RTX_ERR_INVALID, "output is NULL");
+  return resolve_image(c, in, W, H, ResolveReq{limit, 0.0f, out, nullptr, kResolveRgb});
+}
+
+int rtx_image_gamma(rtx_context* c, const float* in, float* out, int W, int H, float gamma) {
+  if (c && !(gamma > 0.0f)) return fail(c, RTX_ERR_INVALID, "gamma must be positive");
+  if (c && !out) return fail(c, RTX_ERR_INVALID, "output is NULL");
+  return resolve_image(c, in, W, H, ResolveReq{0.0f, gamma, out, nullptr, kResolveRgb});
+}
+
+int rtx_image_resolve(rtx_context* c, const float* in, int W, int H, float limit, float gamma,
+                      float* display, uint8_t* bytes, int format) {
+  return resolve_image(c, in, W, H, ResolveReq{limit, gamma, display, bytes, format});
+}
+
+namespace {
+void put32(uint8_t* p, uint32_t v) {
+  for (int k = 0; k < 4; ++k) p[k] = (uint8_t)(v >> (8 * k));
+}
+void put16(uint8_t* p, uint16_t v) {
+  p[0] = (uint8_t)v;
+  p[1] = (uint8_t)(v >> 8);
+}
+}  // namespace
+
+int rtx_encode_bmp(rtx_context* c, const float* in, int W, int H, uint8_t* file, size_t cap,
+                   size_t* size) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!size) return fail(c, RTX_ERR_INVALID, "size is NULL");
+  if (W <= 0 || H <= 0 || (long long)W * H > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "bad image size");
+  const size_t pixels = bmp_row_bytes(W) * (size_t)H;
+  *size = 54 + pixels;
+  if (!file) return RTX_OK;  // size query
+  if (cap < *size) return fail(c, RTX_ERR_INVALID, "file buffer too small");
+  // BITMAPFILEHEADER + BITMAPINFOHEADER as BMPExporter writes them
+  // (src/exporter.cpp:38-77), except that the file size counts the row padding
+  std::memset(file, 0, 54);
+  file[0] = 'B';
+  file[1] = 'M';
+  put32(file + 2, (uint32_t)*size);
+  put32(file + 10, 54);
+  put32(file + 14, 40);
+  put32(file + 18, (uint32_t)W);
+  put32(file + 22, (uint32_t)H);
+  put16(file + 26, 1);
+  put16(file + 28, 24);
+  put32(file + 38, 3780);
+  put32(file + 42, 3780);
+  return resolve_image(c, in, W, H, ResolveReq{0.0f, 0.0f, nullptr, file + 54, kResolveBmp});
+}
+
+int rtx_encode_ppm(rtx_context* c, const float* in, int W, int H, char* file, size_t cap,
+                   size_t* size) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!size) return fail(c, RTX_ERR_INVALID, "size is NULL");
+  if (W <= 0 || H <= 0 || (long long)W * H > (1LL << 28)) return fail(c, RTX_ERR_INVALID, "bad image size");
+  std::vector<uint8_t> rgb((size_t)W * H * 3);
+  int r = resolve_image(c, in, W, H, ResolveReq{0.0f, 0.0f, nullptr, rgb.data(), kResolveRgb});
+  if (r) return r;
+  // PPMExporter (src/exporter.cpp:8-29): "P3", "W H", "255", then one
+  // "r g b" line per pixel, buffer row 0 first
+  std::string txt = "P3\n" + std::to_string(W) + ' ' + std::to_string(H) + "\n255\n";
+  txt.reserve(txt.size() + rgb.size() * 4);
+  char line[16];
+  for (size_t i = 0; i < (size_t)W * H; ++i) {
+    int n = std::snprintf(line, sizeof line, "%d %d %d\n", rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+    txt.append(line, (size_t)n);
+  }
+  *size = txt.size();
+  if (!file) return RTX_OK;
+  if (cap < txt.size()) return fail(c, RTX_ERR_INVALID, "file buffer too small");
+  std::memcpy(file, txt.data(), txt.size());
+  return RTX_OK;
 }
 
 int rtx_trace_paths(rtx_context* c, const float* cam, int W, int H, int first_sample,
@@ -883,7 +1099,8 @@ int rtx_nn_conv3x3_wgrad(rtx_context* c, int N, int H, int W, const void* dout, 
   if (!c) return RTX_ERR_INVALID;
   int r;
   if ((r = check_conv_srcs(c, N, H, W, x1, C1, up1, x2, C2))) return r;
-  if (Cout <= 0 || Cout % 8) return fail(c, RTX_ERR_INVALID, "Cout must be a positive multiple of 8");
+  if (Cout <= 0 || Cout % 16 || Cout > 256)
+    return fail(c, RTX_ERR_INVALID, "Cout must be a multiple of 16, <= 256");
   if (!dout || !dw) return fail(c, RTX_ERR_INVALID, "NULL gradient or output");
   const int Cin = C1 + C2;
   const long long P = (long long)N * H * W;

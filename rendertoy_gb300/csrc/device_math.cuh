@@ -131,6 +131,104 @@ RTX_DEV Mat load_mat(const float* __restrict__ m) {
 }
 
 // ---------------------------------------------------------------------------
+// Procedural textures (RenderToy src/procedural.cpp:8-46).  The samplers take
+// the reference's 2D coordinate p; a surface point maps to p by its two world
+// coordinates across the dominant axis of the shading normal, times the
+// material's texture scale, and the sample scales base_color by
+// 0.25 + 0.75 s (the binding to materials is an extension: RenderToy only
+// rasterises textures to images).
+// ---------------------------------------------------------------------------
+
+// CheckerBoard::Sample (procedural.cpp:8-16): int() truncates toward zero
+RTX_DEV float tex_checker(float x, float y, int scale) {
+  return (((int)(x * (float)scale) & 1) ^ ((int)(y * (float)scale) & 1)) == 1 ? 1.0f : 0.0f;
+}
+
+// Wave::Sample (procedural.cpp:22-25)
+RTX_DEV float tex_wave(float x, float period) {
+  return (sinf(2.0f * kPi * period * x) + 1.0f) / 2.0f;
+}
+
+// Improved gradient noise (K. Perlin, "Improving Noise", SIGGRAPH 2002) as
+// siv::PerlinNoise v3.0.0 evaluates it in FP32: lattice indices masked to
+// 8 bits, hashes through a 256-entry permutation, quintic fade, gradient
+// selection by the low 4 bits of the hash.
+RTX_DEV float perlin_fade(float t) { return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f); }
+RTX_DEV float perlin_lerp(float a, float b, float t) { return a + (b - a) * t; }
+RTX_DEV float perlin_grad(uint32_t hash, float x, float y, float z) {
+  uint32_t h = hash & 15u;
+  float u = h < 8u ? x : y;
+  float v = h < 4u ? y : (h == 12u || h == 14u ? x : z);
+  return ((h & 1u) == 0u ? u : -u) + ((h & 2u) == 0u ? v : -v);
+}
+RTX_DEV float perlin_noise3(const uint8_t* __restrict__ perm, float x, float y, float z) {
+  float fx0 = floorf(x), fy0 = floorf(y), fz0 = floorf(z);
+  int ix = (int)fx0 & 255, iy = (int)fy0 & 255, iz = (int)fz0 & 255;
+  float fx = x - fx0, fy = y - fy0, fz = z - fz0;
+  float u = perlin_fade(fx), v = perlin_fade(fy), w = perlin_fade(fz);
+  uint32_t A = (__ldg(perm + (ix & 255)) + iy) & 255, B = (__ldg(perm + ((ix + 1) & 255)) + iy) & 255;
+  uint32_t AA = (__ldg(perm + A) + iz) & 255, AB = (__ldg(perm + ((A + 1) & 255)) + iz) & 255;
+  uint32_t BA = (__ldg(perm + B) + iz) & 255, BB = (__ldg(perm + ((B + 1) & 255)) + iz) & 255;
+  float p0 = perlin_grad(__ldg(perm + AA), fx, fy, fz);
+  float p1 = perlin_grad(__ldg(perm + BA), fx - 1.0f, fy, fz);
+  float p2 = perlin_grad(__ldg(perm + AB), fx, fy - 1.0f, fz);
+  float p3 = perlin_grad(__ldg(perm + BB), fx - 1.0f, fy - 1.0f, fz);
+  float p4 = perlin_grad(__ldg(perm + ((AA + 1) & 255)), fx, fy, fz - 1.0f);
+  float p5 = perlin_grad(__ldg(perm + ((BA + 1) & 255)), fx - 1.0f, fy, fz - 1.0f);
+  float p6 = perlin_grad(__ldg(perm + ((AB + 1) & 255)), fx, fy - 1.0f, fz - 1.0f);
+  float p7 = perlin_grad(__ldg(perm + ((BB + 1) & 255)), fx - 1.0f, fy - 1.0f, fz - 1.0f);
+  float q0 = perlin_lerp(p0, p1, u), q1 = perlin_lerp(p2, p3, u);
+  float q2 = perlin_lerp(p4, p5, u), q3 = perlin_lerp(p6, p7, u);
+  float r0 = perlin_lerp(q0, q1, v), r1 = perlin_lerp(q2, q3, v);
+  return perlin_lerp(r0, r1, w);
+}
+
+// PerlinNoise::Sample (procedural.cpp:43-46): octave3D_01(p.x * scale,
+// p.y * scale, time = 0, octaves = 4, persistence 0.5), clamped to [0, 1]
+RTX_DEV float tex_perlin(const uint8_t* __restrict__ perm, float px, float py, float scale) {
+  float x = px * scale, y = py * scale, z = 0.0f;
+  float result = 0.0f, amplitude = 1.0f;
+  for (int i = 0; i < 4; ++i) {
+    result += perlin_noise3(perm, x, y, z) * amplitude;
+    x *= 2.0f;
+    y *= 2.0f;
+    z *= 2.0f;
+    amplitude *= 0.5f;
+  }
+  if (result <= -1.0f) return 0.0f;
+  if (1.0f <= result) return 1.0f;
+  return result * 0.5f + 0.5f;
+}
+
+RTX_DEV float texture_sample(int kind, float param, const uint8_t* __restrict__ perm, float px, float py) {
+  if (kind == 1) return tex_checker(px, py, (int)param);
+  if (kind == 2) return tex_wave(px, param);
+  if (kind == 3) return tex_perlin(perm, px, py, param);
+  return 1.0f;
+}
+
+// base_color of the material record m (floats 21..23: kind, parameter,
+// texture scale; kind != 0) at surface point pos with normal n
+static __device__ __noinline__ F3 textured_base(const float* __restrict__ m, F3 pos, F3 n,
+                                                const uint8_t* __restrict__ perm) {
+  float4 a = __ldg(reinterpret_cast<const float4*>(m)), f = __ldg(reinterpret_cast<const float4*>(m) + 5);
+  float ax = fabsf(n.x), ay = fabsf(n.y), az = fabsf(n.z);
+  float px, py;
+  if (ax >= ay && ax >= az) {
+    px = pos.y;
+    py = pos.z;
+  } else if (ay >= az) {
+    px = pos.x;
+    py = pos.z;
+  } else {
+    px = pos.x;
+    py = pos.y;
+  }
+  float s = texture_sample((int)f.y, f.z, perm, px * f.w, py * f.w);
+  return f3(a.x, a.y, a.z) * (0.25f + 0.75f * s);
+}
+
+// ---------------------------------------------------------------------------
 // PBR helpers (src/rtmath.cpp:169-353)
 // ---------------------------------------------------------------------------
 // std::clamp(x, 0, 1): NaN passes through as in the reference

@@ -14,9 +14,10 @@
 //             the weights re-laid out as wt[c, t, o]; mask = (src > 0) when
 //             the source is a ReLU output
 //   wgrad   : dw[o, t, c] += sum_p dout[p, o] src[p + off(t), c]
-//             GEMM M = Cout (128 per CTA), N = 9 * Cin (128 per CTA), K = the
-//             CTA's range of pixels; both operands staged MN-major (16-byte
-//             chunks = 8 channels of one pixel); FP32 atomics combine ranges
+//             GEMM M = 9 * Cin (128 (t, c) rows per CTA), N = Cout (<= 256),
+//             K = the CTA's range of pixels; both operands staged MN-major
+//             (16-byte chunks = 8 channels of one pixel); FP32 atomics
+//             combine the ranges
 // off(t) = (t / 3 - 1, t % 3 - 1).  Out-of-image taps read zero ("same"
 // zero padding).
 #include <algorithm>
@@ -279,41 +280,49 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sa = smem;                     // 128 (o) x 64 (pixels) MN-major
-  uint8_t* sb = smem + 128 * kSlice * 2;  // 128 (t, c) x 64 (pixels) MN-major
+  uint8_t* sa = smem;                     // 128 (t, c) x 64 (pixels), MN-major
+  uint8_t* sb = smem + 128 * kSlice * 2;  // Cout x 64 (pixels), MN-major
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long P = (long long)a.N * a.H * a.W;
-  const int o0 = blockIdx.x * 128, j0 = blockIdx.y * 128;
-  const long long pb = (long long)blockIdx.z * a.pix_per_cta;
-  const long long pe = min(P, pb + a.pix_per_cta);
+  const int P = a.N * a.H * a.W;  // < 2^31 (checked by the host)
   const int J = 9 * a.Cin;
-  tc_begin(&tmem_slot, &bar, 128);
+  const int j0 = blockIdx.x * 128;
+  const int pb = blockIdx.y * a.pix_per_cta;
+  const int pe = min(P, pb + a.pix_per_cta);
+  const uint32_t ncols = a.Cout <= 32 ? 32 : (a.Cout <= 64 ? 64 : (a.Cout <= 128 ? 128 : 256));
+  tc_begin(&tmem_slot, &bar, ncols);
   const uint32_t tmem = tmem_slot;
-  const uint32_t idesc = tc::make_idesc_bf16(128, 128, true, true);
+  const uint32_t idesc = tc::make_idesc_bf16(128, a.Cout, true, true);
   uint32_t phase = 0;
-  // chunk c: row group c & 15 (8 rows), pixel c >> 4 of the slice
+  // this thread's 8 rows of the A tile: (tap, channel) j = j0 + 8 rg
   const int rg = tid & 15;
+  const int j = j0 + rg * 8;
+  const bool jv = j < J;
+  const int t = jv ? j / a.Cin : 0, c = jv ? j - t * a.Cin : 0;
+  const int dy = t / 3 - 1, dx = t % 3 - 1;
+  const int HW = a.H * a.W;
+  const int ng = a.Cout >> 3;
   bool ok = true;
-  for (long long q0 = pb; q0 < pe && ok; q0 += kSlice) {
+  for (int q0 = pb; q0 < pe && ok; q0 += kSlice) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       int kp = (tid >> 4) + 8 * i;  // pixel within the slice
-      long long p = q0 + kp;
-      uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
-      if (p < pe) {
-        int o = o0 + rg * 8;
-        if (o < a.Cout) va = *reinterpret_cast<const uint4*>(a.dout + (size_t)p * a.Cout + o);
-        int j = j0 + rg * 8;
-        if (j < J) {
-          int t = j / a.Cin, c = j - t * a.Cin;
-          Pix q = pix_of(p, a.H, a.W);
-          vb = src_chunk(a.s1, a.s2, a.N, a.H, a.W, q.n, q.y + t / 3 - 1, q.x + t % 3 - 1, c);
-        }
+      int p = q0 + kp;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (p < pe && jv) {
+        int n = p / HW, rem = p - n * HW;
+        int y = rem / a.W, x = rem - y * a.W;
+        v = src_chunk(a.s1, a.s2, a.N, a.H, a.W, n, y + dy, x + dx, c);
       }
-      *reinterpret_cast<uint4*>(sa + tc::tile_offset_mn(rg * 8, kp, 128)) = va;
-      *reinterpret_cast<uint4*>(sb + tc::tile_offset_mn(rg * 8, kp, 128)) = vb;
+      *reinterpret_cast<uint4*>(sa + tc::tile_offset_mn(rg * 8, kp, 128)) = v;
+    }
+    for (int ch = tid; ch < ng * kSlice; ch += 128) {
+      int og = ch % ng, kp = ch / ng;
+      int p = q0 + kp;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (p < pe) v = *reinterpret_cast<const uint4*>(a.dout + (size_t)p * a.Cout + og * 8);
+      *reinterpret_cast<uint4*>(sb + tc::tile_offset_mn(og * 8, kp, a.Cout)) = v;
     }
     tc::fence_proxy_async();
     __syncthreads();
@@ -323,7 +332,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
 #pragma unroll
       for (int s = 0; s < kSlice / 16; ++s)
         tc::mma_bf16(tmem, tc::make_desc(a0 + s * 2 * 16 * 128, 16 * 128, 128),
-                     tc::make_desc(b0 + s * 2 * 16 * 128, 16 * 128, 128), idesc, q0 > pb || s > 0);
+                     tc::make_desc(b0 + s * 2 * 16 * a.Cout, 16 * a.Cout, 128), idesc, q0 > pb || s > 0);
       tc::mma_commit(&bar);
     }
     ok = tc::mbar_wait(&bar, phase);
@@ -333,18 +342,17 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
   }
   tc::fence_after();
   if (ok && pe > pb) {
-    const int o = o0 + warp * 32 + lane;
+    const int jj = j0 + warp * 32 + lane;  // this thread's accumulator row
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c0 = 0; c0 < 128; c0 += 8) {
+    for (int c0 = 0; c0 < a.Cout; c0 += 8) {
       float v[8];
       tc::tmem_ld8(taddr + c0, v);
-      if (o < a.Cout)
+      if (jj < J)
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-          if (j0 + c0 + i < J) atomicAdd(a.dw + (size_t)o * J + j0 + c0 + i, v[i]);
+        for (int i = 0; i < 8; ++i) atomicAdd(a.dw + (size_t)(c0 + i) * J + jj, v[i]);
     }
   }
-  tc_end(tmem, 128);
+  tc_end(tmem, ncols);
 }
 
 // ---------------------------------------------------------------------------
@@ -368,7 +376,8 @@ cudaError_t conv_dgrad(const ConvDgrad& a, cudaStream_t st) {
 }
 
 int wgrad_pixels_per_cta(long long P, int Cout, int Cin) {
-  int tiles = ((Cout + 127) / 128) * ((9 * Cin + 127) / 128);
+  (void)Cout;
+  int tiles = (9 * Cin + 127) / 128;
   long long ranges = std::max(1, 8 * 152 / tiles);
   long long per = (P + ranges - 1) / ranges;
   per = (per + 63) / 64 * 64;
@@ -377,10 +386,11 @@ int wgrad_pixels_per_cta(long long P, int Cout, int Cin) {
 
 cudaError_t conv_wgrad(const ConvWgrad& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
-  size_t smem = 2 * 128 * kSlice * 2;
+  if (P >= (1LL << 31) || a.Cout % 16 || a.Cout > 256) return cudaErrorInvalidValue;
+  size_t smem = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
   cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
   if (e) return e;
-  dim3 grid((a.Cout + 127) / 128, (9 * a.Cin + 127) / 128, (unsigned)((P + a.pix_per_cta - 1) / a.pix_per_cta));
+  dim3 grid((9 * a.Cin + 127) / 128, (unsigned)((P + a.pix_per_cta - 1) / a.pix_per_cta));
   k_conv_wgrad<<<grid, 128, smem, st>>>(a);
   return cudaGetLastError();
 }

@@ -3,6 +3,8 @@
 // channel concatenation, the L1-on-log loss, bias gradients, Adam and the
 // BF16 weight layouts the convolutions read.  One thread per 8 channels of a
 // pixel (16-byte BF16 accesses) unless noted.
+#include <algorithm>
+
 #include "nn.h"
 #include "nn_ops.h"
 
@@ -154,17 +156,32 @@ __global__ void k_l1log_loss(const float* __restrict__ pred, const float* __rest
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)part);
 }
 
-// db[c] += sum_p dout[p, c]; a block sums 256 pixels of one 8-channel group
-__global__ void k_bias_grad(const bf16* __restrict__ dout, long long P, int C, float* __restrict__ db) {
-  int c = blockIdx.y * 8;
-  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (p < P) ld8(dout + p * C + c, v);
+// db[c] += sum_p dout[p, c].  Thread t of a 256-thread block owns the
+// 8-channel group t % (C / 8) and walks pixels t / (C / 8), + 256 / (C / 8),
+// ... of the block's range; the block then sums its partials in shared memory
+// and adds one value per channel (C <= 256).
+__global__ void __launch_bounds__(256) k_bias_grad(const bf16* __restrict__ dout, long long P, int C,
+                                                   long long per_block, float* __restrict__ db) {
+  __shared__ float part[256][9];
+  const int groups = C >> 3, lanes = 256 / groups, tid = threadIdx.x;
+  const int g = tid % groups, l = tid / groups;
+  float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
+  if (l < lanes) {
+    long long p0 = blockIdx.x * per_block, p1 = min(P, p0 + per_block);
+    for (long long p = p0 + l; p < p1; p += lanes) {
+      ld8(dout + p * C + 8 * g, v);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    float s = v[k];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(db + c + k, s);
+      for (int k = 0; k < 8; ++k) acc[k] += v[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) part[tid][k] = acc[k];
+  __syncthreads();
+  if (tid < C) {
+    int gg = tid >> 3, k = tid & 7;
+    float s = 0.0f;
+    for (int j = 0; j < lanes; ++j) s += part[j * groups + gg][k];
+    atomicAdd(db + tid, s);
   }
 }
 
@@ -267,8 +284,10 @@ cudaError_t l1log_loss(const float* pred, const float* target, bf16* dpred, long
   return cudaGetLastError();
 }
 cudaError_t bias_grad(const bf16* dout, long long P, int C, float* db, cudaStream_t st) {
-  dim3 g(blocks(P), C / 8);
-  k_bias_grad<<<g, 256, 0, st>>>(dout, P, C, db);
+  if (C % 8 || C > 256) return cudaErrorInvalidValue;
+  long long nb = std::min<long long>(2 * 152, (P + 255) / 256);
+  long long per = (P + nb - 1) / nb;
+  k_bias_grad<<<(unsigned)nb, 256, 0, st>>>(dout, P, C, per, db);
   return cudaGetLastError();
 }
 cudaError_t adam(float* p, const float* g, float* m, float* v, long long n, float lr, int step,

@@ -259,9 +259,11 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
     float t = h.y, u = h.z, v = h.w;
     float4 s0 = __ldg(s.shade + 4 * (size_t)tri), s1 = __ldg(s.shade + 4 * (size_t)tri + 1);
     int info = __float_as_int(s1.w);
-    Mat m = load_mat(s.mats + 24 * (size_t)(info & 0x7fffffff));
+    const float* mrec = s.mats + 24 * (size_t)(info & 0x7fffffff);
+    Mat m = load_mat(mrec);
     F3 pos = o + d * t;  // BVH::Intersect: src + t * direction
     F3 N = shading_normal(s, tri, u, v, s0, s1, info < 0);
+    if (__ldg(mrec + 21) != 0.0f) m.base_color = textured_base(mrec, pos, N, s.perm);
     F3 ff = N;
     float eta;
     if (dot(d, ff) > 0.0f) {  // renderer.cpp:288-298
@@ -469,8 +471,58 @@ RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec) {
   a.rad[p] = make_float4(acc.x + tb.x, acc.y + tb.y, acc.z + tb.z, 0.0f);
 }
 
+// One pixel of the display resolve (see Resolve).
+__device__ __forceinline__ uint8_t quantise(float x) {
+  // std::clamp keeps NaN; int(NaN) stores 0 in the exporters' 8-bit fields
+  if (!(x == x)) return 0;
+  float c = x < 0.0f ? 0.0f : (1.0f < x ? 1.0f : x);
+  return (uint8_t)(int)(255.99f * c);
+}
+
+__device__ void resolve_px(F3 c, int i, const Resolve& r) {
+  if (r.limit > 0.0f) {
+    float luma = 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z;
+    float s = 1.0f + luma / r.limit;
+    c = f3(c.x * 1.0f / s, c.y * 1.0f / s, c.z * 1.0f / s);
+  }
+  if (r.ratio > 0.0f) c = f3(powf(c.x, r.ratio), powf(c.y, r.ratio), powf(c.z, r.ratio));
+  if (r.display) {
+    r.display[3 * (size_t)i] = c.x;
+    r.display[3 * (size_t)i + 1] = c.y;
+    r.display[3 * (size_t)i + 2] = c.z;
+  }
+  if (r.bytes) {
+    int y = i / r.W, x = i - y * r.W;
+    if (r.format == kResolveBmp) {
+      size_t row = bmp_row_bytes(r.W);
+      uint8_t* px = r.bytes + (size_t)y * row + 3 * (size_t)x;
+      px[0] = quantise(c.z);
+      px[1] = quantise(c.y);
+      px[2] = quantise(c.x);
+      if (x == r.W - 1)
+        for (size_t k = 3 * (size_t)r.W; k < row; ++k) r.bytes[(size_t)y * row + k] = 0;
+    } else {
+      uint8_t* px = r.bytes + 3 * (size_t)i;
+      px[0] = quantise(c.x);
+      px[1] = quantise(c.y);
+      px[2] = quantise(c.z);
+    }
+  }
+}
+
+__global__ void k_resolve(const float* __restrict__ in, int n, Resolve r) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) resolve_px(f3(in[3 * (size_t)i], in[3 * (size_t)i + 1], in[3 * (size_t)i + 2]), i, r);
+}
+
+cudaError_t launch_resolve(const float* in, int W, int H, const Resolve& r, cudaStream_t st) {
+  int n = W * H;
+  if (n > 0) k_resolve<<<(n + 255) / 256, 256, 0, st>>>(in, n, r);
+  return cudaGetLastError();
+}
+
 __global__ void k_accumulate(const float4* rad, long long q0, int n_wave, int npix, float spp,
-                             float* out, int per_path) {
+                             float* out, int per_path, Resolve rs, int last) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (per_path) {
     if (i >= n_wave) return;
@@ -484,16 +536,19 @@ __global__ void k_accumulate(const float4* rad, long long q0, int n_wave, int np
   if (i >= npix) return;
   long long off = ((long long)i - q0 % npix + npix) % npix;
   long long qs = q0 + off;
-  if (qs >= q0 + n_wave) return;
   float* o = out + 3 * (size_t)i;
   F3 acc = f3(o[0], o[1], o[2]);
-  for (long long q = qs; q < q0 + n_wave; q += npix) {
-    float4 r = rad[q - q0];
-    acc = acc + f3(r.x, r.y, r.z) / spp;
+  if (qs < q0 + n_wave) {
+    for (long long q = qs; q < q0 + n_wave; q += npix) {
+      float4 r = rad[q - q0];
+      acc = acc + f3(r.x, r.y, r.z) / spp;
+    }
+    o[0] = acc.x;
+    o[1] = acc.y;
+    o[2] = acc.z;
   }
-  o[0] = acc.x;
-  o[1] = acc.y;
-  o[2] = acc.z;
+  // the last wave resolves every pixel for display in the same pass
+  if (last) resolve_px(acc, i, rs);
 }
 
 __global__ void k_tally(const int* counts, const int* shadow_counts, int max_depth, int first_traced,
@@ -683,8 +738,9 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
       *launches += 2;
     }
     int acc_n = p.per_path ? nw : (int)npix;
+    const bool last = !p.per_path && (p.resolve.display || p.resolve.bytes) && q0 + nw >= total;
     k_accumulate<<<(acc_n + 255) / 256, 256, 0, st>>>(ws->rad, q0, nw, (int)npix, spp, d_out,
-                                                     p.per_path ? 1 : 0);
+                                                     p.per_path ? 1 : 0, p.resolve, last ? 1 : 0);
     k_tally<<<1, 32, 0, st>>>(a.counts, a.shadow_counts, p.max_depth, prim ? 1 : 0, d_counters);
     *launches += 2;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

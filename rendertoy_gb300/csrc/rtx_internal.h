@@ -52,6 +52,7 @@ struct DeviceScene {
   const float4* __restrict__ geo;
   const float* __restrict__ mats;
   const int* __restrict__ emitters;
+  const uint8_t* __restrict__ perm;  // 256-entry permutation of the Perlin texture
   int root;  // node index (>= 0), leaf ref (< 0) or kEmptyRoot
   int n_tris, n_emitters, n_mats;
   float sky[3], ground[3];
@@ -121,6 +122,21 @@ cudaError_t launch_intersect(const DeviceScene& s, int n, const float* rays,
                              cudaStream_t st, int* launches);
 
 struct PtWorkspace;  // defined in pt_kernels.cu
+// Display resolve of a radiance image: Image::Tonemap<kITURBT709>(limit)
+// (include/RenderToy/compositor.h:220-226, rtmath.h:1142-1177), then
+// Image::GammaCorrection(gamma) (src/compositor.cpp:94-100), then the
+// exporters' quantisation int(255.99 * clamp(x, 0, 1)) (src/exporter.cpp).
+// limit <= 0 skips the tonemap, ratio <= 0 the gamma (ratio = 1 / gamma).
+struct Resolve {
+  float limit, ratio;
+  float* display;   // W x H RGB FP32 or nullptr
+  uint8_t* bytes;   // quantised pixels or nullptr
+  int format;       // 0: BMP pixel array (BGR rows of 4-byte multiples), 1: RGB in buffer order
+  int W;
+};
+constexpr int kResolveBmp = 0, kResolveRgb = 1;
+__host__ __device__ inline size_t bmp_row_bytes(int W) { return ((size_t)W * 3 + 3) & ~(size_t)3; }
+
 struct PtParams {
   int W, H, spp, first_sample, n_samples, max_depth;
   uint64_t seed;
@@ -132,6 +148,7 @@ struct PtParams {
   bool primary_cache;
   int traversal;  // RTX_OPT_TRAVERSAL
   int min_busy;   // RTX_OPT_MIN_BUSY
+  Resolve resolve;  // fused into the last accumulation when display or bytes is set
 };
 PtWorkspace* pt_workspace_create();
 void pt_workspace_destroy(PtWorkspace* ws);
@@ -140,6 +157,7 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
                       KernelTimer* timer, cudaStream_t st, int* launches, int* extend_launches,
                       std::string* why);
 
+cudaError_t launch_resolve(const float* in, int W, int H, const Resolve& r, cudaStream_t st);
 cudaError_t launch_convolve(const float* in, float* out, int W, int H, const float* d_k,
                             int kr, int kc, int flags, cudaStream_t st, int* launches);
 cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out, int W, int H,
@@ -147,6 +165,8 @@ cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out
                             cudaStream_t st, int* launches);
 cudaError_t launch_edge(const float* in, float* out, int W, int H, cudaStream_t st,
                         int* launches);
+cudaError_t launch_texture_sample(int kind, float param, const uint8_t* perm, int n, const float* uv,
+                                  float* out, cudaStream_t st);
 cudaError_t launch_gemm_bf16(const void* A, const void* B, float* C, int M, int N, int K, int a_mn,
                              int b_mn, int* err, cudaStream_t st);
 

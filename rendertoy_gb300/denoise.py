@@ -1,0 +1,207 @@
+"""The learned denoiser's data, training and evaluation (host side).
+
+Training pairs come from the renderer itself on procedural scenes
+(``scenes.procedural_scene``): the input is a low-spp radiance render plus the
+albedo, normal and depth passes of the same camera (10 channels), the target a
+high-spp render with an independent seed.  Minibatches are gathered on the
+device and stepped through ``Context.dn_train_step`` (forward, backward and
+Adam on the tensor cores).
+
+``study`` measures the denoised form against the plain one at equal accuracy
+on one scene: a high-spp FP32 reference, plain renders at growing spp, the
+denoised renders at a few input spp (render + passes + network + bloom), their
+relMSE against the reference and their frame times; a frame whose denoised
+relMSE exceeds that of the plain render of equal time falls back to the plain
+render.
+
+    python -m rendertoy_gb300.denoise train --scenes 256 --steps 2000 --out DIR
+    python -m rendertoy_gb300.denoise study --params DIR/params.npy --out DIR
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import scenes
+
+EPS = 1e-2  # relMSE = mean (x - ref)^2 / (ref^2 + EPS)
+
+
+def relmse(x, ref, eps=EPS):
+    """Mean over pixels and channels of (x - ref)^2 / (ref^2 + eps); NaN or
+    infinite pixels are masked and counted."""
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    ok = np.isfinite(x).all(-1) & np.isfinite(ref).all(-1)
+    e = ((x - ref) ** 2 / (ref ** 2 + eps))[ok]
+    return float(e.mean()), int((~ok).sum())
+
+
+def frame_passes(ctx, sc, W, H):
+    """albedo, normal, depth passes of the scene's camera (H x W x 3 each)."""
+    n, a, d = ctx.aov(W, H, float(sc.camera[19]), float(sc.camera[20]))
+    return a, n, d
+
+
+def network_input(rad, albedo, normal, depth):
+    return np.concatenate([rad, albedo, normal, depth[..., :1]], -1).astype(np.float32)
+
+
+def make_pairs(ctx, seeds, W=256, H=256, in_spp=4, target_spp=1024, max_depth=8,
+               tri_range=(1e3, 2e5), log=print):
+    """Render (input, target) pairs of the procedural scenes `seeds`:
+    X [n][H][W][10], Y [n][H][W][3]."""
+    X = np.zeros((len(seeds), H, W, 10), np.float32)
+    Y = np.zeros((len(seeds), H, W, 3), np.float32)
+    t0 = time.time()
+    for i, s in enumerate(seeds):
+        sc, _ = scenes.procedural_scene(int(s), tri_range=tri_range)
+        ctx.upload(sc)
+        rad = ctx.render_pt(W, H, in_spp, max_depth, seed=2 * int(s) + 1)
+        X[i] = network_input(rad, *frame_passes(ctx, sc, W, H))
+        Y[i] = ctx.render_pt(W, H, target_spp, max_depth, seed=2 * int(s) + 2)
+        if log and (i + 1) % max(1, len(seeds) // 8) == 0:
+            log(f"  pairs {i + 1}/{len(seeds)}  {time.time() - t0:.1f} s")
+    return X, Y
+
+
+def train(ctx, X, Y, steps, batch=32, crop=256, lr=3e-4, seed=0, log_every=200, log=print):
+    """Adam steps on random crops of random pairs (device-resident data).
+    Returns the per-step minibatch losses and the mean step time (ms)."""
+    import torch
+    n, H, W = X.shape[:3]
+    crop = min(crop, H, W) // 16 * 16
+    Xd = torch.from_numpy(X).cuda()
+    Yd = torch.from_numpy(Y).cuda()
+    g = torch.Generator().manual_seed(seed)
+    losses, ms = [], []
+    for it in range(steps):
+        idx = torch.randint(0, n, (batch,), generator=g).cuda()
+        y0 = int(torch.randint(0, H - crop + 1, (1,), generator=g))
+        x0 = int(torch.randint(0, W - crop + 1, (1,), generator=g))
+        xb = Xd[idx, y0:y0 + crop, x0:x0 + crop].contiguous()
+        yb = Yd[idx, y0:y0 + crop, x0:x0 + crop].contiguous()
+        losses.append(ctx.dn_train_step(xb, yb, lr=lr))
+        ms.append(ctx.stats()["last_gpu_ms"])
+        if log and (it + 1) % log_every == 0:
+            log(f"  step {it + 1}/{steps}  loss {np.mean(losses[-log_every:]):.4f}  "
+                f"{np.mean(ms[-log_every:]):.2f} ms/step")
+    return np.asarray(losses), float(np.mean(ms[min(5, len(ms) - 1):]))
+
+
+def _timed(ctx, fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, (time.perf_counter() - t0) * 1e3
+
+
+def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 2, 4),
+          plain_spp=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048), reps=20,
+          bloom=(49, 8.0, 1.0), target=1e-3, seed=1, log=print):
+    """Denoised vs plain at equal accuracy on one scene (see the module text).
+    Times are device-synchronised wall times of the whole frame, its buffers
+    resident on the device."""
+    ctx.upload(sc)
+    t0 = time.time()
+    ref = ctx.render_pt(W, H, ref_spp, max_depth, seed=10_000 + seed)
+    log(f"  reference {ref_spp} spp: {time.time() - t0:.1f} s")
+    out = {"scene": sc.name, "W": W, "H": H, "ref_spp": ref_spp, "max_depth": max_depth, "eps": EPS,
+           "target_relmse": target, "plain": [], "denoised": []}
+    import torch
+    dev = lambda: torch.empty((H, W, 3), dtype=torch.float32, device="cuda")  # noqa: E731
+    img, rad, alb, nrm, dep, den, fin = (dev() for _ in range(7))
+    near, far = float(sc.camera[19]), float(sc.camera[20])
+    # plain: relMSE and frame time per spp (device-resident frame)
+    for spp in plain_spp:
+        _, ms = _timed(ctx, lambda: ctx.render_pt(W, H, spp, max_depth, seed=seed, out=img))
+        e, bad = relmse(img.cpu().numpy(), ref)
+        out["plain"].append({"spp": spp, "ms": ms, "relmse": e, "nan_px": bad})
+        log(f"  plain {spp:5d} spp  {ms:9.2f} ms  relMSE {e:.3e}")
+    # plain relMSE ~ c / spp (Monte Carlo): spp and time to the target
+    p = out["plain"]
+    c = np.median([q["relmse"] * q["spp"] for q in p if q["spp"] >= 16] or [p[-1]["relmse"] * p[-1]["spp"]])
+    ms_per_spp = np.median([q["ms"] / q["spp"] for q in p if q["spp"] >= 16] or [p[-1]["ms"] / p[-1]["spp"]])
+    reached = [q for q in p if q["relmse"] <= target]
+    out["plain_time_to_target_ms"] = reached[0]["ms"] if reached else float(c / target * ms_per_spp)
+    out["plain_spp_to_target"] = reached[0]["spp"] if reached else float(c / target)
+    out["plain_fit"] = {"c": float(c), "ms_per_spp": float(ms_per_spp)}
+    # denoised: render + passes + network + bloom, per input spp
+    for spp in denoise_spp:
+        def frame():
+            ctx.render_pt(W, H, spp, max_depth, seed=seed, out=rad)
+            ctx.aov(W, H, near, far, out=(nrm, alb, dep))
+            ctx.denoise(rad, alb, nrm, dep, out=den)
+            if bloom:
+                ctx.bloom(den, *bloom, out=fin)
+        times = [_timed(ctx, frame)[1] for _ in range(reps)]
+        e_den, bad = relmse(den.cpu().numpy(), ref)
+        e_in, _ = relmse(rad.cpu().numpy(), ref)
+        t_med = float(np.median(times))
+        # the plain render of equal time (the fitted curve)
+        e_plain_equal = float(c / max(t_med / ms_per_spp, 1e-9))
+        fallback = e_den > e_plain_equal
+        out["denoised"].append({"spp": spp, "ms_p50": t_med, "ms_p99": float(np.percentile(times, 99)),
+                                "relmse": e_den, "relmse_input": e_in, "nan_px": bad,
+                                "relmse_plain_equal_time": e_plain_equal, "fallback": bool(fallback)})
+        log(f"  denoised {spp} spp  p50 {t_med:.2f} ms  relMSE {e_den:.3e} (input {e_in:.3e}, plain at equal "
+            f"time {e_plain_equal:.3e}){'  -> fallback' if fallback else ''}")
+    ok = [q for q in out["denoised"] if q["relmse"] <= target and not q["fallback"]]
+    out["denoised_time_to_target_ms"] = ok[0]["ms_p50"] if ok else None
+    best = min(out["denoised"], key=lambda q: q["relmse"])
+    out["denoised_best"] = best
+    if ok:
+        out["speedup_time_to_target"] = out["plain_time_to_target_ms"] / ok[0]["ms_p50"]
+    # equal-accuracy comparison at the best denoised frame: plain time to its relMSE
+    out["plain_time_to_best_denoised_ms"] = float(c / best["relmse"] * ms_per_spp)
+    out["speedup_at_best_denoised_accuracy"] = out["plain_time_to_best_denoised_ms"] / best["ms_p50"]
+    return out
+
+
+def _main():
+    import rendertoy_gb300 as rt
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["train", "study"])
+    ap.add_argument("--out", default="denoise_out")
+    ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--res", type=int, default=256)
+    ap.add_argument("--target-spp", type=int, default=1024)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--lr", type=float, default=3e-4)
+    ap.add_argument("--params", default="")
+    ap.add_argument("--study-res", default="1920x1080")
+    ap.add_argument("--ref-spp", type=int, default=16384)
+    a = ap.parse_args()
+    os.makedirs(a.out, exist_ok=True)
+    ctx = rt.Context(0)
+    ctx.dn_init(0)
+    if a.params:
+        ctx.dn_set_params(np.load(a.params))
+    if a.cmd == "train":
+        t0 = time.time()
+        X, Y = make_pairs(ctx, range(a.scenes), W=a.res, H=a.res, target_spp=a.target_spp)
+        t_data = time.time() - t0
+        losses, ms = train(ctx, X, Y, a.steps, batch=a.batch, lr=a.lr)
+        np.save(os.path.join(a.out, "params.npy"), ctx.dn_get_params())
+        res = {"scenes": a.scenes, "res": a.res, "target_spp": a.target_spp, "steps": a.steps,
+               "batch": a.batch, "lr": a.lr, "data_s": t_data, "ms_per_step": ms,
+               "loss_first100": float(losses[:100].mean()), "loss_last100": float(losses[-100:].mean())}
+        json.dump(res, open(os.path.join(a.out, "train.json"), "w"), indent=1)
+        print(json.dumps(res))
+    else:
+        W, H = (int(v) for v in a.study_res.split("x"))
+        res = study(ctx, scenes.displaced_icosphere(), W, H, ref_spp=a.ref_spp)
+        json.dump(res, open(os.path.join(a.out, "study.json"), "w"), indent=1)
+        print(json.dumps({k: v for k, v in res.items() if k not in ("plain", "denoised")}))
+
+
+if __name__ == "__main__":
+    _main()

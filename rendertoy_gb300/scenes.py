@@ -366,3 +366,135 @@ def cornell_mixed() -> Scene:
     _cornell_light(b, light)
     cam = fov_camera(CORNELL_EYE, vfov_deg=40.0, near=700.0, far=1500.0)
     return b.finish(cam, "cornell_mixed")
+
+
+# ---------------------------------------------------------------------------
+# Procedural scenes (batched-scene and denoiser-training workloads)
+# ---------------------------------------------------------------------------
+
+# Material texture slots (floats 21..23 of the record, padding in RenderToy's
+# PrincipledBSDF): [21] kind, [22] the texture's own parameter, [23] texture
+# units per world unit.  The texture is sampled at the hit point's two world
+# coordinates across the shading normal's dominant axis, times [23], and
+# scales base_color by 0.25 + 0.75 s.  RenderToy's textures (src/procedural.cpp)
+# only rasterise to an image: this binding is an extension.
+TEX_NONE, TEX_CHECKER, TEX_WAVE, TEX_PERLIN = 0, 1, 2, 3
+
+
+def blackbody_rgb(t_kelvin: float) -> np.ndarray:
+    """Convert::BlackBody (RenderToy src/rtmath.cpp:34-56): Krystek's
+    approximation of the Planckian locus in CIE 1960 UCS, to xyY (Y = 1), XYZ
+    and linear sRGB (Lindbloom's D65 matrix), normalised by the largest
+    channel.  Evaluated in float64 (scene construction only)."""
+    t = float(t_kelvin)
+    tt = t * t
+    u = (0.860117757 + 1.54118254e-4 * t + 1.28641212e-7 * tt) / (1.0 + 8.42420235e-4 * t + 7.08145163e-7 * tt)
+    v = (0.317398726 + 4.22806245e-5 * t + 4.20481691e-8 * tt) / (1.0 - 2.89741816e-5 * t + 1.61456053e-7 * tt)
+    d = 2.0 * u - 8.0 * v + 4.0
+    x, y = 3.0 * u / d, 2.0 * v / d
+    xyz = np.array([x / y, 1.0, (1.0 - x - y) / y])
+    m = np.array([[3.2404542, -1.5371385, -0.4985314],
+                  [-0.9692660, 1.8760108, 0.0415560],
+                  [0.0556434, -0.2040259, 1.0572252]])
+    rgb = m @ xyz
+    return rgb / rgb.max()
+
+
+def _grid_tris(n: int, size: float, amp: float, seed: int, center, rot_y_deg: float):
+    """A displaced n x n grid (2 n^2 triangles) of side `size`, heights
+    amp * perlin, lying on y = center.y, rotated about +y."""
+    g = np.linspace(-size / 2, size / 2, n + 1)
+    X, Z = np.meshgrid(g, g, indexing="ij")
+    pts = np.stack([X.ravel() / size * 6.0, Z.ravel() / size * 6.0, np.full(X.size, 0.5)], 1)
+    Y = amp * perlin3(pts, seed).reshape(X.shape)
+    a = math.radians(rot_y_deg)
+    ca, sa = math.cos(a), math.sin(a)
+    P = np.stack([center[0] + ca * X + sa * Z, center[1] + Y, center[2] - sa * X + ca * Z], -1)
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    i, j = i.ravel(), j.ravel()
+    p00, p10, p01, p11 = P[i, j], P[i + 1, j], P[i, j + 1], P[i + 1, j + 1]
+    t1 = np.stack([p00, p01, p11], 1)
+    t2 = np.stack([p00, p11, p10], 1)
+    return np.stack([t1, t2], 1).reshape(-1, 3, 3)
+
+
+def _sphere_tris(subdiv: int, radius: float, center, amp: float = 0.0, seed: int = 0):
+    v, f = icosphere(subdiv)
+    if amp:
+        v = v * (1.0 + amp * perlin3(v * 3.0, seed))[:, None]
+    v = v * radius + np.asarray(center, np.float64)
+    vn = _vertex_normals(v, f)
+    return v[f], vn[f]
+
+
+def procedural_scene(seed: int, n_tris=None, textures: bool = True, tri_range=(1e3, 2e6)):
+    """One seeded procedural scene and its render job.
+
+    Geometry: a 555-unit room (5 walls) holding 2-8 objects (boxes, smooth
+    icospheres, Perlin-displaced grids) whose sizes share a triangle budget
+    drawn log-uniformly from `tri_range` (or `n_tris`).  Materials: principled
+    parameters drawn as ``random_principled``, each object with a checkerboard,
+    wave or Perlin texture (or none) when `textures`.  Lights: 1-4 ceiling
+    quads with blackbody emission, 2500-9000 K.  Job: resolution drawn from
+    256^2, 512^2, 1280x720, 1920x1080 and spp uniform in [1, 64].
+    Returns (Scene, {"W", "H", "spp", "n_lights", "target_tris"})."""
+    rng = np.random.RandomState(1_000_003 + seed)
+    draw = math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))
+    target = int(n_tris if n_tris is not None else round(draw))
+    b = _Builder()
+
+    def tex(m):
+        if textures:
+            kind = rng.randint(0, 4)
+            m[21] = kind
+            m[22] = (rng.randint(2, 9) if kind == TEX_CHECKER else
+                     rng.uniform(1.0, 6.0) if kind == TEX_WAVE else 10.0 if kind == TEX_PERLIN else 0.0)
+            m[23] = rng.uniform(1.0 / 400.0, 1.0 / 100.0) if kind else 0.0
+        return m
+
+    walls = [b.add_material(tex(material(tuple(rng.uniform(0.3, 0.85, 3)), roughness=rng.uniform(0.5, 1.0))))
+             for _ in range(3)]
+    _cornell_room(b, walls[0], walls[1], walls[2], None)
+    budget = max(target - 10, 12)
+    n_obj = int(rng.randint(2, 9))
+    kinds = rng.choice(["box", "sphere", "grid"], size=n_obj, p=[0.3, 0.4, 0.3])
+    if not (kinds != "box").any():
+        kinds[0] = "sphere"
+    shares = rng.dirichlet(np.ones(int((kinds != "box").sum())))
+    si = 0
+    for k in kinds:
+        mat = b.add_material(tex(random_principled(rng)))
+        cx, cz = rng.uniform(110, 445), rng.uniform(140, 440)
+        if k == "box":
+            sx, sy, sz = rng.uniform(50, 160, 3)
+            b.add_mesh(_box_tris((cx, sy / 2 - 1.0, cz), (sx, sy, sz), rng.uniform(-45, 45)), mat)
+            continue
+        share = budget * shares[si]
+        si += 1
+        if k == "sphere":
+            s = int(np.clip(round(math.log(max(share, 80) / 20.0, 4)), 1, 8))
+            r = rng.uniform(40, 110)
+            tris, nrm = _sphere_tris(s, r, (cx, r + rng.uniform(-10, 60), cz), amp=rng.uniform(0, 0.08),
+                                     seed=int(rng.randint(1 << 30)))
+            b.add_mesh(tris, mat, smooth=True, norms=nrm)
+        else:
+            n = max(2, int(round(math.sqrt(max(share, 8) / 2.0))))
+            size = rng.uniform(150, 400)
+            tris = _grid_tris(n, size, rng.uniform(5, 60), int(rng.randint(1 << 30)),
+                              (cx, rng.uniform(20, 200), cz), rng.uniform(0, 90))
+            b.add_mesh(tris, mat)
+    n_lights = int(rng.randint(1, 5))
+    for _ in range(n_lights):
+        w, d = rng.uniform(60, 160, 2)
+        x0, z0 = rng.uniform(20, 535 - w), rng.uniform(20, 535 - d)
+        power = 17.0 * 130 * 105 / (w * d) / n_lights * rng.uniform(0.7, 1.4)
+        le = blackbody_rgb(rng.uniform(2500, 9000)) * power
+        light = b.add_material(material((0.78, 0.78, 0.78), emission=tuple(le), roughness=1.0))
+        y = 554.0  # 1 unit below the ceiling, as the Cornell light
+        b.add_quad((x0, y, z0), (x0 + w, y, z0), (x0 + w, y, z0 + d), (x0, y, z0 + d), light)
+    eye = (278.0 + rng.uniform(-60, 60), 273.0 + rng.uniform(-60, 60), -800.0 + rng.uniform(-100, 100))
+    cam = fov_camera(eye, vfov_deg=rng.uniform(35, 50), near=700.0, far=1500.0)
+    W, H = [(256, 256), (512, 512), (1280, 720), (1920, 1080)][rng.randint(4)]
+    spp = int(rng.randint(1, 65))
+    scene = b.finish(cam, f"procedural_{seed}")
+    return scene, {"W": W, "H": H, "spp": spp, "n_lights": n_lights, "target_tris": target}

@@ -230,12 +230,39 @@ def demo_case(ref_root):
     print(f"  demo_cornell (reference build): {out.shape[0]} buffers")
 
 
+TEXTURES = [(1, 4.0), (1, 7.0), (2, 2.5), (2, 0.75), (3, 10.0), (3, 3.0)]
+
+
+def texture_case(ref, orc):
+    """ProceduralTexture::{CheckerBoard, Wave, PerlinNoise}::Sample
+    (src/procedural.cpp:8-46) at seeded points, with the permutation a
+    default-constructed PerlinNoise uses."""
+    rng = np.random.RandomState(SEED)
+    uv = np.concatenate([rng.uniform(-3, 3, (4000, 2)), rng.uniform(-300, 300, (64, 2)),
+                         np.array([[0, 0], [-0.0, 0.5], [1, 1], [-1, -1], [0.25, -0.25], [2.5, 3.5]])])
+    uv = uv.astype(np.float32)
+    perm = ref.perlin_table()
+    out = {"uv": uv, "perm": perm, "kinds": np.array([k for k, _ in TEXTURES], np.int32),
+           "params": np.array([p for _, p in TEXTURES], np.float32)}
+    for i, (k, prm) in enumerate(TEXTURES):
+        a = ref.texture_sample(k, prm, uv)
+        check_equal(f"texture kind {k} param {prm}", orc.texture_sample(k, prm, uv, perm=perm), a)
+        out[f"out{i}"] = a
+    np.savez_compressed(os.path.join(OUT, "textures.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default="", help="regenerate one case: textures")
     args = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={args.ref}", "all", "ref"])
     ref, refo, orc = bind.load("ref"), bind.load("ref_orig"), bind.load("oracle")
+    if args.only == "textures":
+        texture_case(ref, orc)
+        return
+    print("textures:")
+    texture_case(ref, orc)
     print("scenes:")
     scene_case(ref, refo, orc, scenes.cornell_box(), 48, 40, "cornell")
     scene_case(ref, refo, orc, scenes.cornell_mixed(), 40, 32, "mixed")
