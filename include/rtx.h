@@ -169,6 +169,37 @@ int rtx_scene_set_texture_table(rtx_context* ctx, const uint8_t* perm);
 int rtx_texture_sample(rtx_context* ctx, int kind, float param, int n,
                        const float* uv, float* out);
 
+/* ---- OBJ / MTL import --------------------------------------------------------
+ * OBJModelImporter::Import and MTLImporter::Import (src/importer.cpp:29-229)
+ * straight into the arrays rtx_scene_upload takes, with RenderToy's token
+ * rules, fan triangulation (Polygon::ConvertToTriangle, src/object.cpp:
+ * 333-342) and triangle order: triangles in World::triangles order; each
+ * mesh's triangle list in Mesh::tris order (every face's block PREPENDED,
+ * importer.cpp:136), which is the order its emitters are sampled in -- pass
+ * it to rtx_scene_set_emitters.  Like the reference, an "s" value other than
+ * 0 / 1 or an unreadable number ends the import silently with what was read;
+ * "usemtl" is ignored (materials are assigned by the caller, by name).  Where
+ * the reference has undefined behaviour (face index out of range, more than
+ * three '/' fields, "s" / "f" before any "o", an MTL key before any
+ * "newmtl") the import fails with RTX_ERR_INVALID and a message in msg. */
+typedef struct rtx_obj rtx_obj;
+int rtx_obj_import(const char* obj_path, const char* mtl_path /* or NULL */,
+                   rtx_obj** out, char* msg, size_t msg_len);
+void rtx_obj_free(rtx_obj* obj);
+int rtx_obj_info(const rtx_obj* obj, int* n_tris, int* n_meshes,
+                 int* n_materials);
+/* verts / norms: n_tris x 9 floats (world space, v0 v1 v2), uvs n_tris x 6,
+ * tri_mesh n_tris; any pointer may be NULL */
+int rtx_obj_triangles(const rtx_obj* obj, float* verts, float* norms,
+                      float* uvs, int32_t* tri_mesh);
+/* mesh `mesh`: its name (valid until rtx_obj_free), smooth flag and its
+ * triangle ids in Mesh::tris order (tris may be NULL to query *n_tris) */
+int rtx_obj_mesh(const rtx_obj* obj, int mesh, const char** name,
+                 uint8_t* smooth, int32_t* tris, int* n_tris);
+/* material `mat` of the MTL file: its name and 24-float record */
+int rtx_obj_material(const rtx_obj* obj, int mat, const char** name,
+                     float* record);
+
 /* ---- renderers ------------------------------------------------------------
  * PathTracingRenderer::Render (src/renderer.cpp:236-270): out_rgb[p] =
  * sum over samples s = 0..spp-1 of L(p, s) / spp, summed in sample order;
@@ -210,7 +241,8 @@ int rtx_render_pt_resolved(rtx_context* ctx, const float* camera, int W, int H,
  * (include/RenderToy/compositor.h:220-226, rtmath.h:1142-1177), then
  * Image::GammaCorrection(gamma): p^(1 / gamma) per channel
  * (src/compositor.cpp:94-100), then the exporters' quantisation
- * int(255.99 * clamp(x, 0, 1)), NaN -> 0 (src/exporter.cpp:8-95).
+ * int(255.99 * clamp(x, 0, 1)), NaN -> 0 (src/exporter.cpp:8-95; there
+ * int(NaN) is undefined: on x86 the BMP gets 0 and the PPM -2147483648).
  * limit <= 0 skips the tonemap and gamma <= 0 the gamma correction. */
 #define RTX_BYTES_BMP 0 /* BMP pixel array: rows of B, G, R bytes, buffer row 0
                            first, each row zero-padded to a multiple of 4 */

@@ -77,10 +77,18 @@ class Checker:
         fn("bloom", None, [_f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float])
         fn("rng_floats", None, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_int, _f32p])
         fn("texture_sample", None, [C.c_int, C.c_float, vp, C.c_int, _f32p, _f32p])
+        fn("tonemap_gamma", None, [_f32p, C.c_int, C.c_int, C.c_float, C.c_float, _f32p])
+        fn("encode", C.c_long, [C.c_int, _f32p, C.c_int, C.c_int, _u8p, C.c_long])
         if kind == "oracle":
             fn("scene_set_texture_table", None, [vp, _u8p])
         else:
             fn("perlin_table", None, [_u8p])
+            fn("obj_import", vp, [C.c_char_p, C.c_char_p])
+            fn("obj_counts", None, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)])
+            fn("obj_arrays", None, [vp, _f32p, _f32p, _f32p, _i32p, _u8p, _i32p, _i32p, _f32p])
+            fn("obj_mesh_name", C.c_char_p, [vp, C.c_int])
+            fn("obj_mat_name", C.c_char_p, [vp, C.c_int])
+            fn("obj_free", None, [vp])
         if kind == "oracle":
             fn("render_pt", None, [vp, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                    _f32p, C.c_int])
@@ -97,6 +105,42 @@ class Checker:
         self._fn["texture_sample"](int(kind), float(param), None if pp is None else pp.ctypes.data,
                                    len(uv), uv, out)
         return out
+
+    def tonemap_gamma(self, img, limit, gamma):
+        img = np.ascontiguousarray(img, np.float32)
+        out = np.zeros_like(img)
+        self._fn["tonemap_gamma"](img, img.shape[1], img.shape[0], float(limit), float(gamma), out)
+        return out
+
+    def encode(self, img, bmp):
+        img = np.ascontiguousarray(img, np.float32)
+        H, W = img.shape[:2]
+        n = self._fn["encode"](int(bmp), img, W, H, np.zeros(1, np.uint8), 0)
+        assert n >= 0, "not encodable by this checker"
+        buf = np.zeros(n, np.uint8)
+        self._fn["encode"](int(bmp), img, W, H, buf, n)
+        return buf.tobytes()
+
+    def obj_import(self, obj_path, mtl_path=None):
+        """RenderToy's OBJModelImporter (+ MTLImporter) read back as arrays."""
+        h = self._fn["obj_import"](os.fsencode(obj_path), os.fsencode(mtl_path) if mtl_path else None)
+        try:
+            nt, nm, nmat = C.c_int(), C.c_int(), C.c_int()
+            self._fn["obj_counts"](h, C.byref(nt), C.byref(nm), C.byref(nmat))
+            n = nt.value
+            out = dict(verts=np.zeros((n, 9), np.float32), norms=np.zeros((n, 9), np.float32),
+                       uvs=np.zeros((n, 6), np.float32), tri_mesh=np.zeros(n, np.int32),
+                       mesh_smooth=np.zeros(nm.value, np.uint8), mesh_counts=np.zeros(nm.value, np.int32),
+                       mesh_tris=np.zeros(n + 1, np.int32), materials=np.zeros((max(nmat.value, 1), 24), np.float32))
+            self._fn["obj_arrays"](h, out["verts"], out["norms"], out["uvs"], out["tri_mesh"], out["mesh_smooth"],
+                                   out["mesh_counts"], out["mesh_tris"], out["materials"])
+            out["mesh_tris"] = out["mesh_tris"][:int(out["mesh_counts"].sum())]
+            out["materials"] = out["materials"][:nmat.value]
+            out["mesh_names"] = [self._fn["obj_mesh_name"](h, i).decode() for i in range(nm.value)]
+            out["material_names"] = [self._fn["obj_mat_name"](h, i).decode() for i in range(nmat.value)]
+            return out
+        finally:
+            self._fn["obj_free"](h)
 
     def perlin_table(self):
         out = np.zeros(256, np.uint8)

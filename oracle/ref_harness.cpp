@@ -28,6 +28,7 @@
 #include <optional>
 #include <queue>
 #include <random>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -445,6 +446,102 @@ void ref_bloom(const float* in, float* out, int W, int H, int size, float sigma,
   img->Bloom(size, sigma, threshold);
   read_image(img, W, H, out);
   delete img;
+}
+
+// OBJModelImporter::Import (+ MTLImporter::Import) into a World, read back
+// as flat arrays: triangles in World::triangles order (vert_w after
+// UpdateCache, normals, uvs, mesh index), meshes (name, smooth, Mesh::tris as
+// triangle indices), materials (24-float records).
+struct RefObj {
+  World w;
+  std::vector<int32_t> mesh_tris, mesh_counts;
+};
+
+void* ref_obj_import(const char* obj, const char* mtl) {
+  RefObj* o = new RefObj();
+  OBJModelImporter::Import(o->w, obj);
+  if (mtl) MTLImporter::Import(o->w, mtl);
+  std::map<const Triangle*, int> id;
+  for (size_t i = 0; i < o->w.triangles.size(); ++i) id[o->w.triangles[i]] = (int)i;
+  for (Mesh* m : o->w.meshes) {
+    o->mesh_counts.push_back((int32_t)m->tris.size());
+    for (const Triangle* t : m->tris) o->mesh_tris.push_back(id.at(t));
+  }
+  return o;
+}
+
+void ref_obj_counts(void* h, int* n_tris, int* n_meshes, int* n_mats) {
+  RefObj* o = (RefObj*)h;
+  *n_tris = (int)o->w.triangles.size();
+  *n_meshes = (int)o->w.meshes.size();
+  *n_mats = (int)o->w.materials.size();
+}
+
+void ref_obj_arrays(void* h, float* verts, float* norms, float* uvs, int32_t* tri_mesh, uint8_t* smooth,
+                    int32_t* mesh_counts, int32_t* mesh_tris, float* mats) {
+  RefObj* o = (RefObj*)h;
+  std::map<const Mesh*, int> mid;
+  for (size_t i = 0; i < o->w.meshes.size(); ++i) mid[o->w.meshes[i]] = (int)i;
+  for (size_t i = 0; i < o->w.triangles.size(); ++i) {
+    Triangle* t = o->w.triangles[i];
+    t->UpdateCache();
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) {
+        verts[9 * i + 3 * k + c] = t->vert_w[k][c];
+        norms[9 * i + 3 * k + c] = t->norm[k][c];
+      }
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 2; ++c) uvs[6 * i + 2 * k + c] = t->uv[k][c];
+    tri_mesh[i] = mid.at(t->parent);
+  }
+  for (size_t m = 0; m < o->w.meshes.size(); ++m) smooth[m] = o->w.meshes[m]->smooth ? 1 : 0;
+  std::memcpy(mesh_counts, o->mesh_counts.data(), o->mesh_counts.size() * 4);
+  std::memcpy(mesh_tris, o->mesh_tris.data(), o->mesh_tris.size() * 4);
+  for (size_t i = 0; i < o->w.materials.size(); ++i) {
+    const PrincipledBSDF* b = o->w.materials[i];
+    float* r = mats + 24 * i;
+    const float v[24] = {b->base_color[0], b->base_color[1], b->base_color[2], b->emission[0], b->emission[1],
+                         b->emission[2], b->roughness, b->metallic, b->anisotropic, b->subsurface,
+                         b->specular_tint, b->sheen, b->sheen_tint, b->clearcoat, b->clearcoat_roughness,
+                         b->spec_trans, b->ior, b->at_distance, b->extinction[0], b->extinction[1],
+                         b->extinction[2], 0, 0, 0};
+    std::memcpy(r, v, sizeof v);
+  }
+}
+
+const char* ref_obj_mesh_name(void* h, int i) { return ((RefObj*)h)->w.meshes[i]->name.c_str(); }
+const char* ref_obj_mat_name(void* h, int i) { return ((RefObj*)h)->w.materials[i]->name.c_str(); }
+void ref_obj_free(void* h) { delete (RefObj*)h; }
+
+// Image::Tonemap<kITURBT709>(limit) then Image::GammaCorrection(gamma) of a
+// W x H image (limit <= 0 / gamma <= 0 skip the step)
+void ref_tonemap_gamma(const float* in, int W, int H, float limit, float gamma, float* out) {
+  Image img(SizeN((std::size_t)W, (std::size_t)H));
+  Vector3f* b = img.GetBuffer();
+  for (size_t i = 0; i < (size_t)W * H; ++i) b[i] = Vector3f(in[3 * i], in[3 * i + 1], in[3 * i + 2]);
+  if (limit > 0.0f) img.Tonemap(limit);
+  if (gamma > 0.0f) img.GammaCorrection(gamma);
+  for (size_t i = 0; i < (size_t)W * H; ++i)
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = b[i][k];
+}
+
+// BMPExporter / PPMExporter output of a W x H image into out (cap bytes);
+// returns the size.  (BMP only for W % 4 == 0: the reference writes its row
+// padding from a null pointer.)
+long ref_encode(int bmp, const float* in, int W, int H, uint8_t* out, long cap) {
+  Image img(SizeN((std::size_t)W, (std::size_t)H));
+  Vector3f* b = img.GetBuffer();
+  for (size_t i = 0; i < (size_t)W * H; ++i) b[i] = Vector3f(in[3 * i], in[3 * i + 1], in[3 * i + 2]);
+  std::ostringstream os;
+  if (bmp) {
+    if (W % 4) return -1;
+    BMPExporter(img).Export(os);
+  } else {
+    PPMExporter(img).Export(os);
+  }
+  std::string s = os.str();
+  if ((long)s.size() <= cap) std::memcpy(out, s.data(), s.size());
+  return (long)s.size();
 }
 
 // ProceduralTexture samplers (src/procedural.cpp:8-46) at n points;

@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <string>
 #include <queue>
 #include <vector>
 
@@ -1085,6 +1086,69 @@ void* orc_scene_create(int n_tris, const float* verts, const float* norms,
 }
 
 void orc_scene_destroy(void* scene) { delete (Scene*)scene; }
+
+// Display resolve: Image::Tonemap<kITURBT709> (compositor.h:220-226,
+// rtmath.h:1142-1177), Image::GammaCorrection (compositor.cpp:94-100)
+void orc_tonemap_gamma(const float* in, int W, int H, float limit, float gamma, float* out) {
+  float ratio = gamma > 0.0f ? 1.0f / gamma : 0.0f;
+  for (size_t i = 0; i < (size_t)W * H; ++i) {
+    float c[3] = {in[3 * i], in[3 * i + 1], in[3 * i + 2]};
+    if (limit > 0.0f) {
+      float luma = 0.2126f * c[0] + 0.7152f * c[1] + 0.0722f * c[2];
+      float s = 1.0f + luma / limit;
+      for (float& x : c) x = x * 1.0f / s;
+    }
+    if (gamma > 0.0f)
+      for (float& x : c) x = std::pow(x, ratio);
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = c[k];
+  }
+}
+
+// the exporters' quantisation (exporter.cpp:20-25, 82-88): int(255.99 *
+// clamp(x, 0, 1)); std::clamp passes NaN through and int(NaN) is undefined
+// (x86: INT_MIN, which the BMP's 8-bit field truncates to 0 and the PPM
+// prints; Arm: 0) -- defined here as 0 for both files
+static uint8_t quantise(float x) {
+  if (!(x == x)) return 0;
+  return (uint8_t)(int)(255.99f * std::clamp(x, 0.0f, 1.0f));
+}
+
+// BMPExporter / PPMExporter (exporter.cpp:8-95) into out; returns the size.
+// BMP rows are zero-padded to 4 bytes and the header's size counts them.
+long orc_encode(int bmp, const float* in, int W, int H, uint8_t* out, long cap) {
+  std::string s;
+  if (bmp) {
+    size_t row = ((size_t)W * 3 + 3) & ~(size_t)3;
+    s.assign(54 + row * H, '\0');
+    auto p32 = [&](size_t o, uint32_t v) { for (int k = 0; k < 4; ++k) s[o + k] = (char)(v >> (8 * k)); };
+    s[0] = 'B';
+    s[1] = 'M';
+    p32(2, (uint32_t)s.size());
+    p32(10, 54);
+    p32(14, 40);
+    p32(18, (uint32_t)W);
+    p32(22, (uint32_t)H);
+    s[26] = 1;
+    s[28] = 24;
+    p32(38, 3780);
+    p32(42, 3780);
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const float* c = in + 3 * ((size_t)y * W + x);
+        size_t o = 54 + y * row + 3 * (size_t)x;
+        s[o] = (char)quantise(c[2]);
+        s[o + 1] = (char)quantise(c[1]);
+        s[o + 2] = (char)quantise(c[0]);
+      }
+  } else {
+    s = "P3\n" + std::to_string(W) + ' ' + std::to_string(H) + "\n255\n";
+    for (size_t i = 0; i < (size_t)W * H; ++i)
+      s += std::to_string(quantise(in[3 * i])) + ' ' + std::to_string(quantise(in[3 * i + 1])) + ' ' +
+           std::to_string(quantise(in[3 * i + 2])) + '\n';
+  }
+  if ((long)s.size() <= cap) std::memcpy(out, s.data(), s.size());
+  return (long)s.size();
+}
 
 void orc_scene_set_texture_table(void* scene, const uint8_t* perm) {
   std::memcpy(((Scene*)scene)->perm, perm, 256);

@@ -37,6 +37,10 @@ void* orc_scene_create(int n_tris, const float* verts, const float* norms,
                        const float* ground);
 void orc_scene_destroy(void* scene);
 int orc_scene_emitters(void* scene, int32_t* out, int cap);
+/* display resolve (limit / gamma <= 0 skip) and the exporters' files */
+void orc_tonemap_gamma(const float* in, int W, int H, float limit, float gamma,
+                       float* out);
+long orc_encode(int bmp, const float* in, int W, int H, uint8_t* out, long cap);
 /* the Perlin texture's permutation (default: include/rtx.h's seeded shuffle) */
 void orc_scene_set_texture_table(void* scene, const uint8_t* perm);
 /* procedural texture samplers at n points (perm NULL = the default table) */

@@ -38,6 +38,7 @@ EXPORTS = [
     "rtx_dn_loss_grads", "rtx_dn_train_step", "rtx_dn_infer", "rtx_denoise",
     "rtx_scene_set_texture_table", "rtx_texture_sample", "rtx_render_pt_resolved", "rtx_image_resolve",
     "rtx_image_tonemap", "rtx_image_gamma", "rtx_encode_bmp", "rtx_encode_ppm",
+    "rtx_obj_import", "rtx_obj_free", "rtx_obj_info", "rtx_obj_triangles", "rtx_obj_mesh", "rtx_obj_material",
 ]
 
 
@@ -118,6 +119,12 @@ def lib() -> C.CDLL:
         "rtx_image_gamma": (i, [vp, vp, vp, i, i, f]),
         "rtx_encode_bmp": (i, [vp, vp, i, i, vp, C.c_size_t, C.POINTER(C.c_size_t)]),
         "rtx_encode_ppm": (i, [vp, vp, i, i, vp, C.c_size_t, C.POINTER(C.c_size_t)]),
+        "rtx_obj_import": (i, [C.c_char_p, C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]),
+        "rtx_obj_free": (None, [vp]),
+        "rtx_obj_info": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
+        "rtx_obj_triangles": (i, [vp, vp, vp, vp, vp]),
+        "rtx_obj_mesh": (i, [vp, i, C.POINTER(C.c_char_p), C.POINTER(C.c_uint8), vp, C.POINTER(i)]),
+        "rtx_obj_material": (i, [vp, i, C.POINTER(C.c_char_p), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -138,6 +145,57 @@ def _ptr(a):
 
 def _f32(a):
     return np.ascontiguousarray(a, np.float32)
+
+
+class ObjModel:
+    """An OBJ (+ MTL) file imported by rtx_obj_import (no GPU needed): the
+    triangle arrays, the meshes (name, smooth flag, Mesh::tris order) and the
+    MTL materials."""
+
+    def __init__(self, obj_path, mtl_path=None):
+        L = lib()
+        h = C.c_void_p()
+        msg = C.create_string_buffer(512)
+        r = L.rtx_obj_import(os.fsencode(obj_path), os.fsencode(mtl_path) if mtl_path else None, C.byref(h),
+                             msg, 512)
+        if r != 0:
+            raise RtxError(r, msg.value.decode())
+        try:
+            nt, nm, nmat = C.c_int(), C.c_int(), C.c_int()
+            L.rtx_obj_info(h, C.byref(nt), C.byref(nm), C.byref(nmat))
+            n = nt.value
+            self.verts = np.zeros((n, 9), np.float32)
+            self.norms = np.zeros((n, 9), np.float32)
+            self.uvs = np.zeros((n, 6), np.float32)
+            self.tri_mesh = np.zeros(n, np.int32)
+            L.rtx_obj_triangles(h, _ptr(self.verts), _ptr(self.norms), _ptr(self.uvs), _ptr(self.tri_mesh))
+            self.mesh_names, self.mesh_smooth, self.mesh_tris = [], [], []
+            for m in range(nm.value):
+                name, sm, k = C.c_char_p(), C.c_uint8(), C.c_int()
+                L.rtx_obj_mesh(h, m, C.byref(name), C.byref(sm), None, C.byref(k))
+                t = np.zeros(k.value, np.int32)
+                L.rtx_obj_mesh(h, m, None, None, _ptr(t), C.byref(k))
+                self.mesh_names.append(name.value.decode())
+                self.mesh_smooth.append(sm.value)
+                self.mesh_tris.append(t)
+            self.material_names, recs = [], []
+            for m in range(nmat.value):
+                name = C.c_char_p()
+                rec = np.zeros(24, np.float32)
+                L.rtx_obj_material(h, m, C.byref(name), _ptr(rec))
+                self.material_names.append(name.value.decode())
+                recs.append(rec)
+            self.materials = np.stack(recs) if recs else np.zeros((0, 24), np.float32)
+        finally:
+            L.rtx_obj_free(h)
+
+    def emitter_order(self, mesh_mat, mats):
+        """Emitter triangle ids as World::PrepareDirectLightSampling collects
+        them (src/world.cpp:24-37): meshes in order, each emissive mesh's
+        Mesh::tris in order."""
+        out = [self.mesh_tris[m] for m in range(len(self.mesh_names))
+               if np.any(np.abs(np.asarray(mats)[mesh_mat[m], 3:6]) > np.float32(1e-7))]
+        return np.concatenate(out).astype(np.int32) if out else np.zeros(0, np.int32)
 
 
 class Context:

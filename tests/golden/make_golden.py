@@ -251,16 +251,174 @@ def texture_case(ref, orc):
     np.savez_compressed(os.path.join(OUT, "textures.npz"), **out)
 
 
+def resolve_case(ref, orc):
+    """Image::Tonemap / GammaCorrection (compositor.h:220-226,
+    compositor.cpp:94-100) and BMPExporter / PPMExporter (exporter.cpp) on a
+    seeded HDR image with negative, zero, large and NaN pixels."""
+    rng = np.random.RandomState(SEED)
+    W, H = 36, 20  # W % 4 == 0: the reference's BMP padding write needs no padding
+    img = (rng.exponential(0.8, (H, W, 3)) * rng.choice([0.1, 1.0, 10.0], (H, W, 1))).astype(np.float32)
+    img[0, 0] = (-0.5, 0.0, 2.0)
+    img[0, 1] = (np.nan, 0.25, 1.0)
+    img[1, 2] = (1.0, 1.0, 1.0)
+    out = {"img": img}
+    for tag, limit, gamma in (("tm", 1.5, 0.0), ("gm", 0.0, 2.2), ("tmgm", 1.5, 2.2), ("tmgm2", 4.0, 1.8)):
+        a = ref.tonemap_gamma(img, limit, gamma)
+        b = orc.tonemap_gamma(img, limit, gamma)
+        check_equal(f"resolve {tag}", np.nan_to_num(b, nan=-1), np.nan_to_num(a, nan=-1))
+        out[tag] = a
+    # int(NaN) in the exporters is undefined (x86 prints -2147483648 in the PPM,
+    # Arm 0); the files are pinned on NaN-free pixels
+    disp = np.where(np.isnan(out["tmgm"]), np.float32(0.5), out["tmgm"]).astype(np.float32)
+    out["enc_in"] = disp
+    for fmt in ("bmp", "ppm"):
+        a = ref.encode(disp, fmt == "bmp")
+        b = orc.encode(disp, fmt == "bmp")
+        ok = a == b
+        print(f"  {fmt}: {'byte-exact' if ok else 'MISMATCH'}")
+        if not ok:
+            raise SystemExit(f"oracle differs from the reference on {fmt}")
+        out[fmt] = np.frombuffer(a, np.uint8)
+    np.savez_compressed(os.path.join(OUT, "resolve.npz"), **out)
+
+
+OBJ_DIR = os.path.join(OUT, "obj")
+
+
+def _fmt(x, rng):
+    """A float written in one of the notations operator>> accepts."""
+    k = rng.randint(5)
+    if k == 0:
+        return f"{x:.6f}"
+    if k == 1:
+        return f"{x:.4e}"
+    if k == 2:
+        return f"{x:+.3E}"
+    if k == 3:
+        return repr(float(np.float32(x)))
+    return f"{x:.2f}".replace("0.", ".", 1) if 0 < x < 1 else f"{x:.1f}"
+
+
+def synthetic_obj_files():
+    """Seeded OBJ / MTL texts exercising the importer's token rules: faces of
+    3-6 vertices in v, v/vt, v//vn and v/vt/vn forms, runs of spaces, tabs,
+    CRLF line ends, comments, ignored keys, 4-component vertices, -0.0,
+    exponents; smoothing on and off; an 's off' that ends the import."""
+    rng = np.random.RandomState(SEED)
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    files = {}
+
+    def obj_text(n_obj, crlf=False, s_off_after=None):
+        L = ["# synthetic", "mtllib synthetic.mtl"]
+        nv = nt = nn = 0
+        for o in range(n_obj):
+            L.append(f"o Object_{o}")
+            L.append("g ignored_group")
+            k = rng.randint(4, 9)
+            for _ in range(k):
+                xyz = rng.uniform(-3, 3, 3)
+                if rng.rand() < 0.1:
+                    xyz[rng.randint(3)] = -0.0
+                extra = " 1.0" if rng.rand() < 0.1 else ""
+                L.append("v " + " ".join(_fmt(c, rng) for c in xyz) + extra)
+            nv += k
+            for _ in range(k):
+                L.append("vt " + " ".join(_fmt(c, rng) for c in rng.uniform(0, 1, 2)))
+            nt += k
+            for _ in range(k):
+                n = rng.normal(size=3)
+                n /= np.linalg.norm(n)
+                L.append("vn " + " ".join(_fmt(c, rng) for c in n))
+            nn += k
+            L.append("usemtl " + ("Light" if o == 0 else "Grey"))
+            L.append(f"s {int(rng.rand() < 0.5)}")
+            for f in range(rng.randint(2, 6)):
+                nvert = rng.randint(3, 7)
+                ids = rng.choice(np.arange(nv - k + 1, nv + 1), nvert, replace=nvert > k)
+                form = rng.randint(4)
+                parts = []
+                for i in ids:
+                    t = rng.randint(nt - k + 1, nt + 1)
+                    m = rng.randint(nn - k + 1, nn + 1)
+                    parts.append([f"{i}", f"{i}/{t}", f"{i}//{m}", f"{i}/{t}/{m}"][form])
+                sep = " " if rng.rand() < 0.7 else "   "
+                lead = "" if rng.rand() < 0.7 else "  "
+                trail = "" if rng.rand() < 0.7 else "  "
+                L.append("f " + lead + sep.join(parts) + trail)
+                if s_off_after is not None and o == s_off_after and f == 0:
+                    L.append("s off")
+            L.append("# end of object")
+        return ("\r\n" if crlf else "\n").join(L) + "\n"
+
+    files["basic.obj"] = obj_text(3)
+    files["crlf.obj"] = obj_text(2, crlf=True)
+    files["s_off.obj"] = obj_text(3, s_off_after=1)
+    files["synthetic.mtl"] = "\n".join([
+        "# materials", "newmtl Light", "Kd 0.780 0.780 0.780", "Ke 17 12 4", "Ns 10", "illum 2",
+        "newmtl Grey", "Kd .5 .5 .5", "Ni 1.5", "Pr 0.25", "Pm 0.75", "Ps 0.1", "Pc 0.3", "Pcr 0.05",
+        "aniso 0.2", "newmtl Default"]) + "\n"
+    for name, text in files.items():
+        with open(os.path.join(OBJ_DIR, name), "w", newline="") as f:
+            f.write(text)
+    return sorted(n for n in files if n.endswith(".obj"))
+
+
+def obj_case(ref, ref_root):
+    """RenderToy's OBJModelImporter / MTLImporter on the synthetic files
+    (fixtures), and the native importer against it on the reference's own
+    demo scenes (checked here only: those files are not copied)."""
+    import rendertoy_gb300 as rt
+    mtl = os.path.join(OBJ_DIR, "synthetic.mtl")
+    out = {}
+    for name in synthetic_obj_files():
+        r = ref.obj_import(os.path.join(OBJ_DIR, name), mtl)
+        tag = name[:-4]
+        for k in ("verts", "norms", "uvs", "tri_mesh", "mesh_smooth", "mesh_counts", "mesh_tris", "materials"):
+            out[f"{tag}_{k}"] = r[k]
+        out[f"{tag}_mesh_names"] = np.array(r["mesh_names"])
+        out[f"{tag}_material_names"] = np.array(r["material_names"])
+        _obj_equal(rt.ObjModel(os.path.join(OBJ_DIR, name), mtl), r, name)
+    np.savez_compressed(os.path.join(OUT, "obj.npz"), **out)
+    for d in ("CornellBox", "SmoothShading", "WithOIDN", "Emissive"):
+        dd = os.path.join(ref_root, "demo", d)
+        if not os.path.isdir(dd):
+            continue
+        for f in sorted(os.listdir(dd)):
+            if f.endswith(".obj"):
+                p = os.path.join(dd, f)
+                _obj_equal(rt.ObjModel(p), ref.obj_import(p), f"demo/{d}/{f}")
+
+
+def _obj_equal(m, r, name):
+    ok = (np.array_equal(bits(m.verts), bits(r["verts"] + np.float32(0.0)))
+          and np.array_equal(bits(m.norms), bits(r["norms"])) and np.array_equal(bits(m.uvs), bits(r["uvs"]))
+          and np.array_equal(m.tri_mesh, r["tri_mesh"]) and m.mesh_names == r["mesh_names"]
+          and np.array_equal(np.array(m.mesh_smooth, np.uint8), r["mesh_smooth"])
+          and np.array_equal(np.concatenate(m.mesh_tris) if m.mesh_tris else np.zeros(0, np.int32),
+                             r["mesh_tris"])
+          and m.material_names == r["material_names"] and np.array_equal(bits(m.materials), bits(r["materials"])))
+    print(f"  {name}: {len(m.verts)} triangles, {len(m.mesh_names)} meshes: {'equal' if ok else 'MISMATCH'}")
+    if not ok:
+        raise SystemExit(f"native importer differs from the reference on {name}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default="", help="regenerate one case: textures")
+    ap.add_argument("--only", default="", help="regenerate one case: textures, resolve, obj")
     args = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={args.ref}", "all", "ref"])
     ref, refo, orc = bind.load("ref"), bind.load("ref_orig"), bind.load("oracle")
-    if args.only == "textures":
-        texture_case(ref, orc)
+    if args.only == "obj":
+        obj_case(ref, args.ref)
         return
+    if args.only:
+        {"textures": texture_case, "resolve": resolve_case}[args.only](ref, orc)
+        return
+    print("obj import:")
+    obj_case(ref, args.ref)
+    print("resolve:")
+    resolve_case(ref, orc)
     print("textures:")
     texture_case(ref, orc)
     print("scenes:")

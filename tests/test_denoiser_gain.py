@@ -30,7 +30,10 @@ def test_trained_network_beats_its_input(ctx):
         den = ctx.denoise(rad, a, n, d)
         ref = ctx.render_pt(128, 128, 1024, 6, seed=8)
         e_in, _ = D.relmse(rad, ref)
-        e_dn, bad = D.relmse(den, ref)
-        assert bad == 0
+        # the renders may hold RenderToy's NaN paths (relmse masks them); the
+        # network's output may not
+        assert np.isfinite(den).all()
+        e_dn, _ = D.relmse(den, ref)
         gains.append(e_in / e_dn)
+    print("relMSE gain of the denoised 4-spp frame over its input:", gains)
     assert min(gains) >= 2.0, gains
