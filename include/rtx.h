@@ -183,8 +183,9 @@ int rtx_texture_sample(rtx_context* ctx, int kind, float param, int n,
  * three '/' fields, "s" / "f" before any "o", an MTL key before any
  * "newmtl") the import fails with RTX_ERR_INVALID and a message in msg. */
 typedef struct rtx_obj rtx_obj;
-int rtx_obj_import(const char* obj_path, const char* mtl_path /* or NULL */,
-                   rtx_obj** out, char* msg, size_t msg_len);
+int rtx_obj_import(const char* obj_path /* or NULL: MTL only */,
+                   const char* mtl_path /* or NULL */, rtx_obj** out,
+                   char* msg, size_t msg_len);
 void rtx_obj_free(rtx_obj* obj);
 int rtx_obj_info(const rtx_obj* obj, int* n_tris, int* n_meshes,
                  int* n_materials);

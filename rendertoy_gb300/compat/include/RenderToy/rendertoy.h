@@ -4,6 +4,8 @@
 #include "bvh.h"
 #include "compositor.h"
 #include "exception.h"
+#include "exporter.h"
+#include "importer.h"
 #include "material.h"
 #include "object.h"
 #include "ray.h"

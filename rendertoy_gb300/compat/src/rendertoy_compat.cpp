@@ -524,9 +524,109 @@ Image& Image::Bloom(const std::size_t size, const float sigma, const float thres
   return *this;
 }
 Image& Image::GammaCorrection(const float gamma) {
-  float ratio = 1.0f / gamma;
-  Transform([&ratio](Vector3f& p) { p = Vector3f::Pow(p, ratio); });
+  rtx_context* c = image_context();
+  check(rtx_image_gamma(c, (const float*)buffer, (float*)buffer, (int)resolution.width, (int)resolution.height,
+                        gamma),
+        c, "rtx_image_gamma");
   return *this;
+}
+
+// ---- files --------------------------------------------------------------------------
+void PPMExporter::Export(std::ostream& os) {
+  rtx_context* c = image_context();
+  int W = (int)image.resolution.width, H = (int)image.resolution.height;
+  const float* px = (const float*)&image(0, 0);
+  size_t n = 0;
+  check(rtx_encode_ppm(c, px, W, H, nullptr, 0, &n), c, "rtx_encode_ppm");
+  std::vector<char> buf(n);
+  check(rtx_encode_ppm(c, px, W, H, buf.data(), n, &n), c, "rtx_encode_ppm");
+  os.write(buf.data(), (std::streamsize)n);
+}
+
+void BMPExporter::Export(std::ostream& os) {
+  rtx_context* c = image_context();
+  int W = (int)image.resolution.width, H = (int)image.resolution.height;
+  const float* px = (const float*)&image(0, 0);
+  size_t n = 0;
+  check(rtx_encode_bmp(c, px, W, H, nullptr, 0, &n), c, "rtx_encode_bmp");
+  std::vector<uint8_t> buf(n);
+  check(rtx_encode_bmp(c, px, W, H, buf.data(), n, &n), c, "rtx_encode_bmp");
+  os.write((const char*)buf.data(), (std::streamsize)n);
+}
+
+// ---- import -------------------------------------------------------------------------
+void OBJModelImporter::Import(World& world, const std::string& path) {
+  rtx_obj* o = nullptr;
+  char msg[512] = {0};
+  int r = rtx_obj_import(path.c_str(), nullptr, &o, msg, sizeof msg);
+  if (r != RTX_OK) throw Exception::DeviceException(r, std::string("OBJ import: ") + msg);
+  int nt = 0, nm = 0;
+  rtx_obj_info(o, &nt, &nm, nullptr);
+  std::vector<float> v((size_t)nt * 9), n((size_t)nt * 9), t((size_t)nt * 6);
+  std::vector<int32_t> tm((size_t)nt);
+  rtx_obj_triangles(o, v.data(), n.data(), t.data(), tm.data());
+  std::vector<Mesh*> meshes;
+  for (int m = 0; m < nm; ++m) {
+    const char* name = nullptr;
+    uint8_t sm = 0;
+    rtx_obj_mesh(o, m, &name, &sm, nullptr, nullptr);
+    Mesh* mesh = new Mesh();
+    mesh->name = name;
+    mesh->smooth = sm != 0;
+    meshes.push_back(mesh);
+  }
+  size_t base = world.triangles.size();
+  for (int i = 0; i < nt; ++i) {
+    const float* p = &v[9 * (size_t)i];
+    const float* q = &n[9 * (size_t)i];
+    const float* w = &t[6 * (size_t)i];
+    Triangle* tri = new Triangle({Vector3f(p[0], p[1], p[2]), Vector3f(p[3], p[4], p[5]), Vector3f(p[6], p[7], p[8])},
+                                 {Vector3f(q[0], q[1], q[2]), Vector3f(q[3], q[4], q[5]), Vector3f(q[6], q[7], q[8])},
+                                 {Vector2f(w[0], w[1]), Vector2f(w[2], w[3]), Vector2f(w[4], w[5])}, meshes[tm[i]]);
+    world.triangles.push_back(tri);
+  }
+  for (int m = 0; m < nm; ++m) {
+    int k = 0;
+    rtx_obj_mesh(o, m, nullptr, nullptr, nullptr, &k);
+    std::vector<int32_t> ids((size_t)k);
+    rtx_obj_mesh(o, m, nullptr, nullptr, ids.data(), &k);
+    for (int32_t id : ids) meshes[m]->tris.push_back(world.triangles[base + id]);
+    world.meshes.push_back(meshes[m]);
+  }
+  rtx_obj_free(o);
+}
+
+void MTLImporter::Import(World& world, const std::string& path) {
+  rtx_obj* o = nullptr;
+  char msg[512] = {0};
+  int r = rtx_obj_import(nullptr, path.c_str(), &o, msg, sizeof msg);
+  if (r != RTX_OK) throw Exception::DeviceException(r, std::string("MTL import: ") + msg);
+  int nmat = 0;
+  rtx_obj_info(o, nullptr, nullptr, &nmat);
+  for (int i = 0; i < nmat; ++i) {
+    const char* name = nullptr;
+    float m[24];
+    rtx_obj_material(o, i, &name, m);
+    PrincipledBSDF* b = new PrincipledBSDF();
+    b->name = name;
+    b->base_color = Vector3f(m[0], m[1], m[2]);
+    b->emission = Vector3f(m[3], m[4], m[5]);
+    b->roughness = m[6];
+    b->metallic = m[7];
+    b->anisotropic = m[8];
+    b->subsurface = m[9];
+    b->specular_tint = m[10];
+    b->sheen = m[11];
+    b->sheen_tint = m[12];
+    b->clearcoat = m[13];
+    b->clearcoat_roughness = m[14];
+    b->spec_trans = m[15];
+    b->ior = m[16];
+    b->at_distance = m[17];
+    b->extinction = Vector3f(m[18], m[19], m[20]);
+    world.materials.push_back(b);
+  }
+  rtx_obj_free(o);
 }
 
 #define RTX_IMAGE_OP(op, name)                                                        \

@@ -361,7 +361,7 @@ int parse_mtl(const std::string& text, rtx_obj& o, std::string& err) {
 extern "C" {
 
 int rtx_obj_import(const char* obj_path, const char* mtl_path, rtx_obj** out, char* msg, size_t msg_len) {
-  if (!out || !obj_path) {
+  if (!out || (!obj_path && !mtl_path)) {
     set_msg(msg, msg_len, "NULL argument");
     return RTX_ERR_INVALID;
   }
@@ -369,12 +369,15 @@ int rtx_obj_import(const char* obj_path, const char* mtl_path, rtx_obj** out, ch
   rtx_obj* o = new (std::nothrow) rtx_obj();
   if (!o) return RTX_ERR_NOMEM;
   std::string text, err;
-  if (!read_file(obj_path, text)) {
-    set_msg(msg, msg_len, std::string("cannot read ") + obj_path);
-    delete o;
-    return RTX_ERR_INVALID;
+  int r = RTX_OK;
+  if (obj_path) {
+    if (!read_file(obj_path, text)) {
+      set_msg(msg, msg_len, std::string("cannot read ") + obj_path);
+      delete o;
+      return RTX_ERR_INVALID;
+    }
+    r = parse_obj(text, *o, err);
   }
-  int r = parse_obj(text, *o, err);
   if (r == RTX_OK && mtl_path) {
     if (!read_file(mtl_path, text)) {
       err = std::string("cannot read ") + mtl_path;

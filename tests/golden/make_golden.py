@@ -402,6 +402,63 @@ def _obj_equal(m, r, name):
         raise SystemExit(f"native importer differs from the reference on {name}")
 
 
+def write_obj_scene(sc, obj_path, mtl_path, cam_path):
+    """A scene as OBJ + MTL text (one object per mesh, named m<i> after its
+    material record; faces as triangles with v//vn) and its camera."""
+    L, M = ["# scene"], ["# materials"]
+    for k, m in enumerate(sc.mats):
+        M += [f"newmtl mat{k}", "Kd " + " ".join(repr(float(x)) for x in m[0:3]),
+              "Ke " + " ".join(repr(float(x)) for x in m[3:6]), f"Pr {float(m[6])!r}", f"Pm {float(m[7])!r}",
+              f"Ps {float(m[11])!r}", f"Pc {float(m[13])!r}", f"Pcr {float(m[14])!r}", f"Ni {float(m[16])!r}"]
+    nv = 0
+    for mi in range(len(sc.mesh_mat)):
+        ids = np.nonzero(sc.tri_mesh == mi)[0]
+        L.append(f"o mat{int(sc.mesh_mat[mi])}")
+        for t in ids:
+            for k in range(3):
+                L.append("v " + " ".join(repr(float(x)) for x in sc.verts[t, 3 * k:3 * k + 3]))
+                L.append("vn " + " ".join(repr(float(x)) for x in sc.norms[t, 3 * k:3 * k + 3]))
+        L.append(f"s {int(sc.mesh_smooth[mi])}")
+        # faces in reverse so that Mesh::tris (prepend order) lists them forwards
+        for j, t in reversed(list(enumerate(ids))):
+            a = nv + 3 * j + 1
+            L.append(f"f {a}//{a} {a + 1}//{a + 1} {a + 2}//{a + 2}")
+        nv += 3 * len(ids)
+    open(obj_path, "w").write("\n".join(L) + "\n")
+    open(mtl_path, "w").write("\n".join(M) + "\n")
+    np.asarray(sc.camera, np.float32).tofile(cam_path)
+
+
+DEMO_OBJ = (64, 48, 128)  # W, H, spp
+
+
+def demo_obj_case(ref_root):
+    """tests/compat/demo_obj.cpp built against RenderToy's sources: its
+    buffers and exported files on the mixed Cornell scene written as OBJ."""
+    rdir = os.path.join(ROOT, "oracle", "_ref")
+    exe = os.path.join(rdir, "demo_obj_ref")
+    srcs = [os.path.join(ref_root, "src", s + ".cpp") for s in (
+        "bvh", "object", "material", "rtmath", "surfacepoint", "world", "ray", "compositor",
+        "exception", "procedural", "importer", "exporter", "renderer")]
+    subprocess.check_call(["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-include", "functional",
+                           "-include", "vector", "-include", "cstdint", "-include", "optional",
+                           "-include", "algorithm", "-I" + os.path.join(ref_root, "include"),
+                           os.path.join(ROOT, "tests", "compat", "demo_obj.cpp"), *srcs, "-o", exe])
+    d = os.path.join(rdir, "demo_obj")
+    os.makedirs(d, exist_ok=True)
+    sc = scenes.cornell_mixed()
+    paths = [os.path.join(d, n) for n in ("scene.obj", "scene.mtl", "camera.bin")]
+    write_obj_scene(sc, *paths)
+    W, H, spp = DEMO_OBJ
+    prefix = os.path.join(d, "ref")
+    subprocess.check_call([exe, *paths, prefix, str(W), str(H), str(spp)])
+    out = read_demo_output(prefix + ".bin")
+    np.savez_compressed(os.path.join(OUT, "demo_obj.npz"), buffers=out, W=W, H=H, spp=spp,
+                        bmp=np.frombuffer(open(prefix + "_normal.bmp", "rb").read(), np.uint8),
+                        ppm=np.frombuffer(open(prefix + "_normal.ppm", "rb").read(), np.uint8))
+    print(f"  demo_obj (reference build): {out.shape[0]} buffers")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -411,12 +468,14 @@ def main():
     ref, refo, orc = bind.load("ref"), bind.load("ref_orig"), bind.load("oracle")
     if args.only == "obj":
         obj_case(ref, args.ref)
+        demo_obj_case(args.ref)
         return
     if args.only:
         {"textures": texture_case, "resolve": resolve_case}[args.only](ref, orc)
         return
     print("obj import:")
     obj_case(ref, args.ref)
+    demo_obj_case(args.ref)
     print("resolve:")
     resolve_case(ref, orc)
     print("textures:")

@@ -57,3 +57,39 @@ def test_demo_matches_reference_build(tmp_path, golden):
             # stream): the image means agree within Monte Carlo error
             ma, mb = a.reshape(-1, 3).mean(0), b.reshape(-1, 3).mean(0)
             assert np.all(np.abs(ma - mb) <= 0.03 * np.abs(mb) + 1e-3), (name, ma, mb)
+
+
+DEMO_OBJ = os.path.join(ROOT, "tests", "compat", "demo_obj.cpp")
+
+
+def test_obj_demo_compiles_against_compat_headers(tmp_path):
+    from rendertoy_gb300 import build
+    exe = str(tmp_path / "demo_obj")
+    build.compile_app(DEMO_OBJ, exe)
+    assert os.path.exists(exe)
+
+
+@pytest.mark.gpu
+def test_obj_demo_matches_reference_build(tmp_path, golden):
+    """An application that imports its scene with OBJModelImporter /
+    MTLImporter and exports with BMPExporter / PPMExporter, built unchanged
+    against the compatible API: passes and exported files equal RenderToy's,
+    path-traced image means within Monte Carlo error."""
+    import make_golden as mg
+    from rendertoy_gb300 import build, scenes
+    g = golden("demo_obj")
+    W, H, spp = int(g["W"]), int(g["H"]), int(g["spp"])
+    exe = str(tmp_path / "demo_obj")
+    build.compile_app(DEMO_OBJ, exe)
+    paths = [str(tmp_path / n) for n in ("scene.obj", "scene.mtl", "camera.bin")]
+    mg.write_obj_scene(scenes.cornell_mixed(), *paths)
+    prefix = str(tmp_path / "out")
+    subprocess.check_call([exe, *paths, prefix, str(W), str(H), str(spp)])
+    got, ref = mg.read_demo_output(prefix + ".bin"), g["buffers"]
+    for i in range(3):  # normal, albedo, depth
+        assert np.abs(got[i] - ref[i]).max() <= 1e-5, i
+    assert open(prefix + "_normal.bmp", "rb").read() == g["bmp"].tobytes()
+    assert open(prefix + "_normal.ppm", "rb").read() == g["ppm"].tobytes()
+    for i in (3, 4):  # path traced, tonemapped: RenderToy's mt19937 vs the counter-based stream
+        ma, mb = got[i].reshape(-1, 3).mean(0), ref[i].reshape(-1, 3).mean(0)
+        assert np.all(np.abs(ma - mb) <= 0.03 * np.abs(mb) + 1e-3), (i, ma, mb)
