@@ -17,6 +17,9 @@ result.  Metric: Msamples/s (pixel samples per second), with Mrays/s beside it.
           per ray, counted by an instrumented (untimed) run of the same step.
   cpu_baseline : the oracle's restatement of RenderToy's renderer (octree +
           priority-queue traversal) on the host cores, on a bounded sample.
+  denoiser : the learned denoiser outside the timed frames: one Adam step on a
+          32 x 256^2 minibatch and one 1920 x 1088 inference, device time and
+          tensor-core TFLOP/s against the measured BF16 peak.
 
 ``--impl reference`` times RenderToy's CPU path on the same workload (its
 compiled sources where they run here, otherwise the oracle restatement).
@@ -50,12 +53,54 @@ WORKLOAD = (f"displaced icosphere ({20 * 4 ** SUBDIV} tris, subdiv {SUBDIV}, Per
             f"Gaussian blur sigma {BLUR_SIGMA} size {BLUR_SIZE} + 5x5 edge convolution")
 
 
-def peaks():
+def peaks(key="hbm_gbs"):
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        return float(d[key]), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key], "fallback"
+
+
+def denoiser_block(ctx, rank):
+    """The learned denoiser on the tensor cores: one Adam step on a 32 x 256^2
+    minibatch (forward + backward + update; the training config's minibatch)
+    and inference on a 1920 x 1088 frame, each timed with the library's CUDA
+    events (median of 10 after 3 warm-up runs).  Tensor work = the padded
+    convolutions the kernels execute: 2 * 9 * Cin * Cout per pixel of each
+    layer's resolution, x 3 for a training step (forward, data and weight
+    gradients)."""
+    import torch
+    ctx.dn_init(rank)
+    fwd = sum(2 * 9 * L["cin_pad"] * L["cout_pad"] / 4 ** L["level"] for L in ctx.dn_layers())
+    g = torch.Generator(device="cuda").manual_seed(rank)
+    N, H, W = 32, 256, 256
+    raw = torch.rand(N, H, W, 10, device="cuda", generator=g)
+    raw[..., :3] *= 4.0
+    tgt = torch.rand(N, H, W, 3, device="cuda", generator=g)
+
+    def med(fn, n=10):
+        for _ in range(3):
+            fn()
+        t = []
+        for _ in range(n):
+            fn()
+            t.append(ctx.stats()["last_gpu_ms"])
+        return float(np.median(t))
+
+    train_ms = med(lambda: ctx.dn_train_step(raw, tgt, lr=3e-4))
+    train_launches = ctx.stats()["kernel_launches"]
+    fr = torch.rand(1, 1088, 1920, 10, device="cuda", generator=g)
+    out = torch.empty(1, 1088, 1920, 3, device="cuda")
+    infer_ms = med(lambda: ctx.dn_infer(fr, out))
+    peak, kind = peaks("bf16_tflops")
+    train_tf = 3 * fwd * N * H * W / (train_ms * 1e-3) / 1e12
+    infer_tf = fwd * 1088 * 1920 / (infer_ms * 1e-3) / 1e12
+    return {"train_step_ms": train_ms, "minibatch": [N, H, W], "train_tflops": train_tf,
+            "train_kernel_launches": train_launches, "infer_ms_1920x1088": infer_ms, "infer_tflops": infer_tf,
+            "gflop_per_mpixel_forward": fwd * 1e6 / 1e9,
+            "roofline": {"bound": "tensor", "achieved": train_tf, "peak": peak, "peak_kind": kind,
+                         "unit": "TFLOP/s", "frac": train_tf / peak,
+                         "note": "whole training step (all 88 launches) against the bf16 burst peak"}}
 
 
 class Clocks:
@@ -332,6 +377,8 @@ def main():
            "h2d_bytes_per_step": 2 * img_bytes + 84 + BLUR_SIZE * 4 + 25 * 4,
            "d2h_bytes_per_step": 3 * img_bytes, "steps": e2e_steps}
 
+    dn = denoiser_block(ctx, rank)
+
     cpu = None
     if rank == 0:
         v, ns, t, cores = cpu_sample_rate(sc, seconds=args.cpu_seconds)
@@ -364,6 +411,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": launches,
+            "denoiser": dn,
         }
         print(json.dumps(line))
     if ws > 1:

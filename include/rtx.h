@@ -79,7 +79,9 @@ enum rtx_option {
   RTX_OPT_WAVE_PATHS = 2,     /* max paths in flight per wavefront (0 = auto:
                                  the whole render up to 2^26 paths and a
                                  quarter of the free device memory) */
-  RTX_OPT_BLOCK = 3,          /* threads per block of the wavefront kernels */
+  RTX_OPT_BLOCK = 3,          /* threads per block of the persistent wavefront
+                                 kernels (extend, shade, connect): 64 or 128
+                                 (their register budgets cap blocks at 128) */
   RTX_OPT_SORT_MATERIAL = 4,  /* 0/1: sort hits by material before shading */
   RTX_OPT_COUNT_VISITS = 5,   /* 0/1: count node visits and triangle tests */
   RTX_OPT_LEAF_SIZE = 6,      /* max triangles per BVH leaf (1..8), next upload */
@@ -93,8 +95,11 @@ enum rtx_option {
                                  per lane until the warp's batch is done;
                                  1 = binary tree, lanes take new rays as theirs
                                  finish (while-while); 2 = 4-wide tree, batch */
-  RTX_OPT_MIN_BUSY = 11       /* with RTX_OPT_TRAVERSAL = 1: refill a warp once
+  RTX_OPT_MIN_BUSY = 11,      /* with RTX_OPT_TRAVERSAL = 1: refill a warp once
                                  fewer lanes than this are traversing (0..32) */
+  RTX_OPT_GRAPH = 12          /* 0/1: rtx_render_batch captures its launch
+                                 sequence as a CUDA graph and replays it for
+                                 later frames of the same shape */
 };
 
 typedef struct rtx_context rtx_context;
@@ -200,6 +205,60 @@ int rtx_obj_mesh(const rtx_obj* obj, int mesh, const char** name,
 /* material `mat` of the MTL file: its name and 24-float record */
 int rtx_obj_material(const rtx_obj* obj, int mat, const char** name,
                      float* record);
+
+/* ---- multi-scene batches ------------------------------------------------------
+ * No counterpart in RenderToy (one World per RenderContext).  Several scenes
+ * are merged into one set of device arrays (each with its own BVH, materials
+ * and emitter list); rtx_render_batch then traces frames over any of them --
+ * uneven sizes, resolutions and spp -- through one wavefront: every kernel
+ * launch of the frame serves the rays of all frames.  Each frame's random
+ * stream is the one rtx_render_pt uses for its scene, camera and seed, so a
+ * frame of a batch equals the frame rendered alone.  The batch is separate
+ * from the context's single scene (rtx_scene_upload). */
+typedef struct rtx_scene_desc {
+  int n_tris;
+  const float* verts;          /* as rtx_scene_upload */
+  const float* norms;
+  const int32_t* tri_mesh;
+  int n_meshes;
+  const int32_t* mesh_mat;
+  const uint8_t* mesh_smooth;
+  int n_materials;
+  const float* materials;
+  const float* sky;
+  const float* ground;
+  const int32_t* emitters;     /* sampling order, or NULL with n_emitters = -1
+                                  for World::PrepareDirectLightSampling's */
+  int n_emitters;
+} rtx_scene_desc;
+int rtx_batch_upload(rtx_context* ctx, int n_scenes, const rtx_scene_desc* scenes);
+
+typedef struct rtx_job {
+  int scene;                   /* index into the uploaded batch */
+  float camera[RTX_CAMERA_FLOATS];
+  int W, H, spp;
+  uint64_t seed;
+} rtx_job;
+/* out: the frames' images one after another (sum of W * H * 3 floats) */
+int rtx_render_batch(rtx_context* ctx, int n_jobs, const rtx_job* jobs,
+                     int max_depth, float* out);
+
+/* Autotuner: times the batch frame `jobs` (device time of rtx_render_batch,
+ * best of two) over BVH leaf sizes 2 / 4 / 8 -- rebuilding the batch from
+ * `scenes` for each; scenes = NULL keeps the uploaded batch and its leaf
+ * size -- then threads per block 64 / 128 x paths per wave 2^20, 2^22, 2^24,
+ * auto, coordinate-wise from the context's current options.  The fastest
+ * setting stays on the context (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK,
+ * RTX_OPT_WAVE_PATHS) and the batch is left built with it. */
+typedef struct rtx_tune_result {
+  int64_t block, wave_paths, leaf_size;
+  double ms, ms_default;       /* frame time chosen / at the starting options */
+  int trials;
+} rtx_tune_result;
+int rtx_batch_autotune(rtx_context* ctx, int n_scenes,
+                       const rtx_scene_desc* scenes, int n_jobs,
+                       const rtx_job* jobs, int max_depth,
+                       rtx_tune_result* out);
 
 /* ---- renderers ------------------------------------------------------------
  * PathTracingRenderer::Render (src/renderer.cpp:236-270): out_rgb[p] =

@@ -18,6 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "librtx.so")
 
+OPT_GRAPH = 12
 OPT_ASYNC, OPT_WAVE_PATHS, OPT_BLOCK, OPT_SORT_MATERIAL, OPT_COUNT_VISITS, OPT_LEAF_SIZE, \
     OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING, OPT_ACCUMULATE, OPT_TRAVERSAL, OPT_MIN_BUSY = \
     1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11
@@ -39,7 +40,25 @@ EXPORTS = [
     "rtx_scene_set_texture_table", "rtx_texture_sample", "rtx_render_pt_resolved", "rtx_image_resolve",
     "rtx_image_tonemap", "rtx_image_gamma", "rtx_encode_bmp", "rtx_encode_ppm",
     "rtx_obj_import", "rtx_obj_free", "rtx_obj_info", "rtx_obj_triangles", "rtx_obj_mesh", "rtx_obj_material",
+    "rtx_batch_upload", "rtx_render_batch", "rtx_batch_autotune",
 ]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("n_tris", C.c_int), ("verts", C.c_void_p), ("norms", C.c_void_p), ("tri_mesh", C.c_void_p),
+                ("n_meshes", C.c_int), ("mesh_mat", C.c_void_p), ("mesh_smooth", C.c_void_p),
+                ("n_materials", C.c_int), ("materials", C.c_void_p), ("sky", C.c_void_p), ("ground", C.c_void_p),
+                ("emitters", C.c_void_p), ("n_emitters", C.c_int)]
+
+
+class Job(C.Structure):
+    _fields_ = [("scene", C.c_int), ("camera", C.c_float * 21), ("W", C.c_int), ("H", C.c_int),
+                ("spp", C.c_int), ("seed", C.c_uint64)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("block", C.c_int64), ("wave_paths", C.c_int64), ("leaf_size", C.c_int64), ("ms", C.c_double),
+                ("ms_default", C.c_double), ("trials", C.c_int)]
 
 
 class RtxError(RuntimeError):
@@ -125,6 +144,9 @@ def lib() -> C.CDLL:
         "rtx_obj_triangles": (i, [vp, vp, vp, vp, vp]),
         "rtx_obj_mesh": (i, [vp, i, C.POINTER(C.c_char_p), C.POINTER(C.c_uint8), vp, C.POINTER(i)]),
         "rtx_obj_material": (i, [vp, i, C.POINTER(C.c_char_p), vp]),
+        "rtx_batch_upload": (i, [vp, i, C.POINTER(SceneDesc)]),
+        "rtx_render_batch": (i, [vp, i, C.POINTER(Job), i, vp]),
+        "rtx_batch_autotune": (i, [vp, i, C.POINTER(SceneDesc), i, C.POINTER(Job), i, C.POINTER(TuneResult)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -332,6 +354,65 @@ class Context:
         self._check(self.L.rtx_nn_gemm_bf16(self.h, M, N, K, _ptr(A), _ptr(B), _ptr(C_), int(a_mn),
                                             int(b_mn)))
         return C_
+
+    # -- multi-scene batches -------------------------------------------------------
+    def batch_upload(self, scene_list, emitters=None):
+        """Merge scenes (scenes.Scene) into the context's batch; emitters: per
+        scene an explicit emitter id list or None."""
+        descs, keep = self._scene_descs(scene_list, emitters)
+        self._check(self.L.rtx_batch_upload(self.h, len(scene_list), descs))
+        self.batch_scenes = list(scene_list)
+
+    def _scene_descs(self, scene_list, emitters=None):
+        keep, descs = [], (SceneDesc * len(scene_list))()
+        for k, sc in enumerate(scene_list):
+            arrs = [_f32(sc.verts), _f32(sc.norms), np.ascontiguousarray(sc.tri_mesh, np.int32),
+                    np.ascontiguousarray(sc.mesh_mat, np.int32), np.ascontiguousarray(sc.mesh_smooth, np.uint8),
+                    _f32(sc.mats), _f32(sc.sky), _f32(sc.ground)]
+            em = None if emitters is None or emitters[k] is None else np.ascontiguousarray(emitters[k], np.int32)
+            keep += arrs + [em]
+            v, n, tm, mm, ms, mats, sky, gr = arrs
+            descs[k] = SceneDesc(sc.n_tris, v.ctypes.data, n.ctypes.data, tm.ctypes.data, len(mm), mm.ctypes.data,
+                                 ms.ctypes.data, len(mats), mats.ctypes.data, sky.ctypes.data, gr.ctypes.data,
+                                 None if em is None else em.ctypes.data, -1 if em is None else len(em))
+        return descs, keep
+
+    def _jobs(self, jobs):
+        arr = (Job * len(jobs))()
+        for k, j in enumerate(jobs):
+            known = 0 <= j["scene"] < len(getattr(self, "batch_scenes", []))
+            cam = _f32(j["camera"] if "camera" in j else
+                       (self.batch_scenes[j["scene"]].camera if known else np.zeros(21)))  # rejected by the library
+            arr[k] = Job(j["scene"], (C.c_float * 21)(*cam.tolist()), j["W"], j["H"], j["spp"], j.get("seed", 0))
+        return arr
+
+    def batch_autotune(self, jobs, max_depth, scene_list=None):
+        """Tune leaf size (when scene_list is given: rebuilds), block and wave
+        size on the batch frame `jobs`; the best stays set.  Returns a dict."""
+        descs, keep = (None, None) if scene_list is None else self._scene_descs(scene_list)
+        res = TuneResult()
+        self._check(self.L.rtx_batch_autotune(self.h, 0 if scene_list is None else len(scene_list), descs,
+                                              len(jobs), self._jobs(jobs), max_depth, C.byref(res)))
+        if scene_list is not None:
+            self.batch_scenes = list(scene_list)
+        return {k: getattr(res, k) for k, _ in TuneResult._fields_}
+
+    def render_batch(self, jobs, max_depth, out=None):
+        """jobs: dicts with scene (index), W, H, spp, seed and optionally camera
+        (default: the scene's).  Returns the list of H x W x 3 images (views of
+        one buffer), or fills `out` (a flat device tensor or array)."""
+        arr = self._jobs(jobs)
+        total = sum(j["W"] * j["H"] for j in jobs)
+        buf = np.zeros(total * 3, np.float32) if out is None else out
+        self._check(self.L.rtx_render_batch(self.h, len(jobs), arr, max_depth, _ptr(buf)))
+        if out is not None:
+            return out
+        imgs, o = [], 0
+        for j in jobs:
+            n = j["W"] * j["H"] * 3
+            imgs.append(buf[o:o + n].reshape(j["H"], j["W"], 3))
+            o += n
+        return imgs
 
     # -- display resolve and image files -------------------------------------------
     BYTES_BMP, BYTES_RGB = 0, 1

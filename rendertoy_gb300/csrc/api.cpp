@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <thread>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -95,6 +97,22 @@ struct rtx_context {
   PtWorkspace* pt = nullptr;
   DevBuf stage[8];
   DevBuf perm;  // Perlin texture permutation (256 bytes)
+  // multi-scene batch (rtx_batch_upload / rtx_render_batch)
+  struct BatchScene {
+    int root, e_begin, n_emitters, n_tris;
+    float sky[3], ground[3];
+  };
+  bool has_batch = false;
+  DeviceScene bds{};
+  DevBuf b_nodes, b_tris, b_shade, b_geo, b_mats, b_emit, b_jobs, b_jobq;
+  std::vector<BatchScene> bscenes;
+  // CUDA graph of the last batch frame, keyed by its launch shape
+  bool use_graph = false;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<int64_t> graph_key;
+  PtJob* h_jobs_pinned = nullptr;
+  long long* h_jobq_pinned = nullptr;
+  int pinned_cap = 0;
   rtx::nn::UNet* dn = nullptr;
   DevBuf weights;
   std::vector<float> host_weights;
@@ -343,6 +361,11 @@ void rtx_destroy(rtx_context* c) {
   c->emit.release();
   for (auto& s : c->stage) s.release();
   c->perm.release();
+  DevBuf* bb[] = {&c->b_nodes, &c->b_tris, &c->b_shade, &c->b_geo, &c->b_mats, &c->b_emit, &c->b_jobs, &c->b_jobq};
+  for (DevBuf* b : bb) b->release();
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->h_jobs_pinned) cudaFreeHost(c->h_jobs_pinned);
+  if (c->h_jobq_pinned) cudaFreeHost(c->h_jobq_pinned);
   delete c->dn;
   c->weights.release();
   if (c->pt) pt_workspace_destroy(c->pt);
@@ -360,12 +383,13 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
   if (!c) return RTX_ERR_INVALID;
   switch (option) {
     case RTX_OPT_ASYNC: c->async = v != 0; return RTX_OK;
+    case RTX_OPT_GRAPH: c->use_graph = v != 0; return RTX_OK;
     case RTX_OPT_WAVE_PATHS:
       if (v < 0 || v > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "wave paths out of range");
       c->wave_paths = v;
       return RTX_OK;
     case RTX_OPT_BLOCK:
-      if (v < 32 || v > 1024 || v % 32) return fail(c, RTX_ERR_INVALID, "block must be a multiple of 32 in [32, 1024]");
+      if (v != 64 && v != 128) return fail(c, RTX_ERR_INVALID, "block must be 64 or 128");
       c->block = (int)v;
       return RTX_OK;
     case RTX_OPT_SORT_MATERIAL: c->sort_material = v != 0; return RTX_OK;
@@ -393,6 +417,7 @@ int rtx_get_option(rtx_context* c, int option, int64_t* v) {
   if (!c || !v) return RTX_ERR_INVALID;
   switch (option) {
     case RTX_OPT_ASYNC: *v = c->async; return RTX_OK;
+    case RTX_OPT_GRAPH: *v = c->use_graph; return RTX_OK;
     case RTX_OPT_WAVE_PATHS: *v = c->wave_paths; return RTX_OK;
     case RTX_OPT_BLOCK: *v = c->block; return RTX_OK;
     case RTX_OPT_SORT_MATERIAL: *v = c->sort_material; return RTX_OK;
@@ -456,11 +481,24 @@ int rtx_get_stats(rtx_context* c, rtx_stats* out) {
   return RTX_OK;
 }
 
-int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* norms,
-                     const int32_t* tri_mesh, int n_meshes, const int32_t* mesh_mat,
-                     const uint8_t* mesh_smooth, int n_mat, const float* mats, const float* sky,
-                     const float* ground) {
-  if (!c) return RTX_ERR_INVALID;
+}  // extern "C"
+
+namespace {
+
+// One scene prepared on the host: BVH, per-triangle shading and geometry
+// records, materials and the emitter list.
+struct HostScene {
+  BvhBuildResult b;
+  std::vector<float4> shade, geo;
+  std::vector<float> mats;
+  std::vector<int32_t> emitters;
+  int n_tris = 0, n_mats = 0;
+  float sky[3], ground[3];
+};
+
+int check_scene(rtx_context* c, int n, const float* verts, const float* norms, const int32_t* tri_mesh,
+                int n_meshes, const int32_t* mesh_mat, const uint8_t* mesh_smooth, int n_mat, const float* mats,
+                const float* sky, const float* ground) {
   if (n < 0 || n_meshes < 0 || n_mat < 0) return fail(c, RTX_ERR_INVALID, "negative count");
   if (n > (1 << 27)) return fail(c, RTX_ERR_INVALID, "more than 2^27 triangles");
   if (n > 0 && (!verts || !tri_mesh)) return fail(c, RTX_ERR_INVALID, "verts / tri_mesh is NULL");
@@ -482,60 +520,97 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   if (any_smooth && !norms) return fail(c, RTX_ERR_INVALID, "a smooth mesh needs vertex normals");
   for (int i = 0; i < n; ++i)
     if (tri_mesh[i] < 0 || tri_mesh[i] >= n_meshes) return fail(c, RTX_ERR_INVALID, "triangle mesh index out of range");
-  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
-  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return RTX_OK;
+}
 
+void build_host_scene(HostScene& h, int n, const float* verts, const float* norms, const int32_t* tri_mesh,
+                      int n_meshes, const int32_t* mesh_mat, const uint8_t* mesh_smooth, int n_mat,
+                      const float* mats, const float* sky, const float* ground, int leaf_size) {
   // Mesh's identity object-to-world turns -0.0 into +0.0 (object.cpp:42-48)
   std::vector<float> v((size_t)n * 9);
   for (size_t i = 0; i < v.size(); ++i) v[i] = verts[i] + 0.0f;
-
-  BvhBuildResult b = build_bvh(v.data(), n, c->leaf_size);
-
-  std::vector<float4> shade((size_t)n * 4), geo((size_t)n * 3);
+  h.b = build_bvh(v.data(), n, leaf_size);
+  h.shade.resize((size_t)n * 4);
+  h.geo.resize((size_t)n * 3);
   for (int i = 0; i < n; ++i) {
     const float* p = &v[9 * (size_t)i];
     V3 v0{p[0], p[1], p[2]}, v1{p[3], p[4], p[5]}, v2{p[6], p[7], p[8]};
     V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
     V3 cr = cross(e1, e2);
-    float area = std::sqrt(dot(cr, cr)) * 0.5f;        // Triangle::Area
+    float area = std::sqrt(dot(cr, cr)) * 0.5f;                 // Triangle::Area
     V3 nrm = normalized(cross(normalized(e1), sub(v2, v1)));  // Triangle::Normal
     int mesh = tri_mesh[i];
     uint32_t info = (uint32_t)mesh_mat[mesh] | (mesh_smooth[mesh] ? 0x80000000u : 0u);
     float infof;
     std::memcpy(&infof, &info, 4);
     const float* q = norms ? norms + 9 * (size_t)i : nullptr;
-    shade[4 * (size_t)i] = make_float4(nrm.x, nrm.y, nrm.z, area);
-    shade[4 * (size_t)i + 1] = make_float4(q ? q[0] : 0.f, q ? q[1] : 0.f, q ? q[2] : 0.f, infof);
-    shade[4 * (size_t)i + 2] = make_float4(q ? q[3] : 0.f, q ? q[4] : 0.f, q ? q[5] : 0.f, 0.f);
-    shade[4 * (size_t)i + 3] = make_float4(q ? q[6] : 0.f, q ? q[7] : 0.f, q ? q[8] : 0.f, 0.f);
-    geo[3 * (size_t)i] = make_float4(v0.x, v0.y, v0.z, 0.f);
-    geo[3 * (size_t)i + 1] = make_float4(e1.x, e1.y, e1.z, 0.f);
-    geo[3 * (size_t)i + 2] = make_float4(e2.x, e2.y, e2.z, 0.f);
+    h.shade[4 * (size_t)i] = make_float4(nrm.x, nrm.y, nrm.z, area);
+    h.shade[4 * (size_t)i + 1] = make_float4(q ? q[0] : 0.f, q ? q[1] : 0.f, q ? q[2] : 0.f, infof);
+    h.shade[4 * (size_t)i + 2] = make_float4(q ? q[3] : 0.f, q ? q[4] : 0.f, q ? q[5] : 0.f, 0.f);
+    h.shade[4 * (size_t)i + 3] = make_float4(q ? q[6] : 0.f, q ? q[7] : 0.f, q ? q[8] : 0.f, 0.f);
+    h.geo[3 * (size_t)i] = make_float4(v0.x, v0.y, v0.z, 0.f);
+    h.geo[3 * (size_t)i + 1] = make_float4(e1.x, e1.y, e1.z, 0.f);
+    h.geo[3 * (size_t)i + 2] = make_float4(e2.x, e2.y, e2.z, 0.f);
   }
   // World::PrepareDirectLightSampling (world.cpp:24-37)
   std::vector<std::vector<int>> per_mesh(n_meshes);
   for (int i = 0; i < n; ++i) per_mesh[tri_mesh[i]].push_back(i);
-  c->emitters.clear();
+  h.emitters.clear();
   for (int m = 0; m < n_meshes; ++m) {
     const float* em = mats + RTX_MATERIAL_FLOATS * (size_t)mesh_mat[m] + 3;
     bool emissive = std::fabs(em[0]) > 1e-7f || std::fabs(em[1]) > 1e-7f || std::fabs(em[2]) > 1e-7f;
     if (emissive)
-      for (int t : per_mesh[m]) c->emitters.push_back(t);
+      for (int t : per_mesh[m]) h.emitters.push_back(t);
   }
+  h.mats.assign(mats, mats + (size_t)n_mat * RTX_MATERIAL_FLOATS);
+  h.n_tris = n;
+  h.n_mats = n_mat;
+  for (int k = 0; k < 3; ++k) {
+    h.sky[k] = sky[k];
+    h.ground[k] = ground[k];
+  }
+}
 
-  auto up = [&](DevBuf& d, const void* src, size_t bytes, const char* what) -> int {
-    RTX_CUDA(d.ensure(bytes), what);
-    if (bytes) RTX_CUDA(cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice), what);
-    return RTX_OK;
-  };
+int upload_buf(rtx_context* c, DevBuf& d, const void* src, size_t bytes, const char* what) {
+  RTX_CUDA(d.ensure(bytes), what);
+  if (bytes) RTX_CUDA(cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice), what);
+  return RTX_OK;
+}
+
+// leaf reference of the binary tree, rebased by `tri_base` leaf-order records
+int rebase_leaf(int ref, int tri_base) {
+  int r = ~ref;
+  int first = r >> 3, cnt = r & 7;
+  return ~(((first + tri_base) << 3) | cnt);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* norms,
+                     const int32_t* tri_mesh, int n_meshes, const int32_t* mesh_mat,
+                     const uint8_t* mesh_smooth, int n_mat, const float* mats, const float* sky,
+                     const float* ground) {
+  if (!c) return RTX_ERR_INVALID;
   int r;
-  if ((r = up(c->nodes, b.nodes.data(), b.nodes.size() * sizeof(float4), "upload nodes"))) return r;
-  if ((r = up(c->nodes4, b.nodes4.data(), b.nodes4.size() * sizeof(float4), "upload nodes4"))) return r;
-  if ((r = up(c->tris, b.tris.data(), b.tris.size() * sizeof(float4), "upload tris"))) return r;
-  if ((r = up(c->shade, shade.data(), shade.size() * sizeof(float4), "upload shade"))) return r;
-  if ((r = up(c->geo, geo.data(), geo.size() * sizeof(float4), "upload geo"))) return r;
-  if ((r = up(c->mats, mats, (size_t)n_mat * RTX_MATERIAL_FLOATS * sizeof(float), "upload mats"))) return r;
-  if ((r = up(c->emit, c->emitters.data(), c->emitters.size() * sizeof(int32_t), "upload emitters"))) return r;
+  if ((r = check_scene(c, n, verts, norms, tri_mesh, n_meshes, mesh_mat, mesh_smooth, n_mat, mats, sky, ground)))
+    return r;
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  HostScene h;
+  build_host_scene(h, n, verts, norms, tri_mesh, n_meshes, mesh_mat, mesh_smooth, n_mat, mats, sky, ground,
+                   c->leaf_size);
+  const BvhBuildResult& b = h.b;
+  c->emitters = h.emitters;
+  if ((r = upload_buf(c, c->nodes, b.nodes.data(), b.nodes.size() * sizeof(float4), "upload nodes"))) return r;
+  if ((r = upload_buf(c, c->nodes4, b.nodes4.data(), b.nodes4.size() * sizeof(float4), "upload nodes4"))) return r;
+  if ((r = upload_buf(c, c->tris, b.tris.data(), b.tris.size() * sizeof(float4), "upload tris"))) return r;
+  if ((r = upload_buf(c, c->shade, h.shade.data(), h.shade.size() * sizeof(float4), "upload shade"))) return r;
+  if ((r = upload_buf(c, c->geo, h.geo.data(), h.geo.size() * sizeof(float4), "upload geo"))) return r;
+  if ((r = upload_buf(c, c->mats, h.mats.data(), h.mats.size() * sizeof(float), "upload mats"))) return r;
+  if ((r = upload_buf(c, c->emit, c->emitters.data(), c->emitters.size() * sizeof(int32_t), "upload emitters")))
+    return r;
 
   DeviceScene& s = c->ds;
   s.nodes = (const float4*)c->nodes.p;
@@ -560,6 +635,132 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   c->stats.bvh_nodes = b.n_nodes;
   c->stats.bvh_leaves = b.n_leaves;
   c->stats.bvh_depth = b.depth;
+  c->stats.node_bytes = 64;
+  c->stats.tri_bytes = 48;
+  return RTX_OK;
+}
+
+int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
+  if (!c) return RTX_ERR_INVALID;
+  if (n_scenes < 1 || !d) return fail(c, RTX_ERR_INVALID, "at least one scene is needed");
+  int r;
+  for (int i = 0; i < n_scenes; ++i) {
+    if ((r = check_scene(c, d[i].n_tris, d[i].verts, d[i].norms, d[i].tri_mesh, d[i].n_meshes, d[i].mesh_mat,
+                         d[i].mesh_smooth, d[i].n_materials, d[i].materials, d[i].sky, d[i].ground)))
+      return fail(c, r, "scene " + std::to_string(i) + ": " + c->err);
+    if (d[i].n_emitters >= 0 && d[i].n_emitters > 0 && !d[i].emitters)
+      return fail(c, RTX_ERR_INVALID, "scene " + std::to_string(i) + ": emitters is NULL");
+    for (int k = 0; k < std::max(d[i].n_emitters, 0); ++k)
+      if (d[i].emitters[k] < 0 || d[i].emitters[k] >= d[i].n_tris)
+        return fail(c, RTX_ERR_INVALID, "scene " + std::to_string(i) + ": emitter id out of range");
+  }
+  long long tot = 0;
+  for (int i = 0; i < n_scenes; ++i) tot += d[i].n_tris;
+  if (tot > (1 << 27)) return fail(c, RTX_ERR_INVALID, "more than 2^27 triangles in the batch");
+  RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  // host builds, several scenes at a time
+  std::vector<HostScene> hs(n_scenes);
+  auto t0 = std::chrono::steady_clock::now();
+  {
+    unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
+    std::atomic<int> next{0};
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t)
+      th.emplace_back([&] {
+        for (int i; (i = next++) < n_scenes;)
+          build_host_scene(hs[i], d[i].n_tris, d[i].verts, d[i].norms, d[i].tri_mesh, d[i].n_meshes,
+                           d[i].mesh_mat, d[i].mesh_smooth, d[i].n_materials, d[i].materials, d[i].sky,
+                           d[i].ground, c->leaf_size);
+      });
+    for (auto& t : th) t.join();
+  }
+  // merge: node, leaf-record, triangle-id, material and emitter indices rebased
+  std::vector<float4> nodes, tris, shade, geo;
+  std::vector<float> mats;
+  std::vector<int32_t> emit;
+  c->bscenes.assign(n_scenes, {});
+  int tri_base = 0, mat_base = 0;
+  for (int i = 0; i < n_scenes; ++i) {
+    const HostScene& h = hs[i];
+    int node_base = (int)(nodes.size() / 4);
+    for (size_t k = 0; k < h.b.nodes.size(); k += 4) {
+      float4 n0 = h.b.nodes[k], n1 = h.b.nodes[k + 1], n2 = h.b.nodes[k + 2], n3 = h.b.nodes[k + 3];
+      int ch[2];
+      std::memcpy(ch, &n3.x, 8);
+      for (int& x : ch) x = x >= 0 ? x + node_base : rebase_leaf(x, tri_base);
+      std::memcpy(&n3.x, ch, 8);
+      nodes.insert(nodes.end(), {n0, n1, n2, n3});
+    }
+    for (size_t k = 0; k < h.b.tris.size(); k += 3) {
+      float4 a = h.b.tris[k];
+      int id;
+      std::memcpy(&id, &a.w, 4);
+      id += tri_base;
+      std::memcpy(&a.w, &id, 4);
+      tris.insert(tris.end(), {a, h.b.tris[k + 1], h.b.tris[k + 2]});
+    }
+    for (size_t k = 0; k < h.shade.size(); ++k) {
+      float4 v = h.shade[k];
+      if (k % 4 == 1) {
+        uint32_t info;
+        std::memcpy(&info, &v.w, 4);
+        info = ((info & 0x7fffffffu) + (uint32_t)mat_base) | (info & 0x80000000u);
+        std::memcpy(&v.w, &info, 4);
+      }
+      shade.push_back(v);
+    }
+    geo.insert(geo.end(), h.geo.begin(), h.geo.end());
+    mats.insert(mats.end(), h.mats.begin(), h.mats.end());
+    rtx_context::BatchScene& bs = c->bscenes[i];
+    int root = h.b.root;
+    bs.root = root == kEmptyRoot ? kEmptyRoot : (root >= 0 ? root + node_base : rebase_leaf(root, tri_base));
+    bs.e_begin = (int)emit.size();
+    if (d[i].n_emitters >= 0) {
+      for (int k = 0; k < d[i].n_emitters; ++k) emit.push_back(d[i].emitters[k] + tri_base);
+      bs.n_emitters = d[i].n_emitters;
+    } else {
+      for (int e : h.emitters) emit.push_back(e + tri_base);
+      bs.n_emitters = (int)h.emitters.size();
+    }
+    bs.n_tris = h.n_tris;
+    for (int k = 0; k < 3; ++k) {
+      bs.sky[k] = h.sky[k];
+      bs.ground[k] = h.ground[k];
+    }
+    tri_base += h.n_tris;
+    mat_base += h.n_mats;
+  }
+  double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if ((r = upload_buf(c, c->b_nodes, nodes.data(), nodes.size() * sizeof(float4), "upload batch nodes"))) return r;
+  if ((r = upload_buf(c, c->b_tris, tris.data(), tris.size() * sizeof(float4), "upload batch tris"))) return r;
+  if ((r = upload_buf(c, c->b_shade, shade.data(), shade.size() * sizeof(float4), "upload batch shade"))) return r;
+  if ((r = upload_buf(c, c->b_geo, geo.data(), geo.size() * sizeof(float4), "upload batch geo"))) return r;
+  if ((r = upload_buf(c, c->b_mats, mats.data(), mats.size() * sizeof(float), "upload batch mats"))) return r;
+  if ((r = upload_buf(c, c->b_emit, emit.data(), emit.size() * sizeof(int32_t), "upload batch emitters"))) return r;
+  DeviceScene& s = c->bds;
+  s = DeviceScene{};
+  s.nodes = (const float4*)c->b_nodes.p;
+  s.nodes4 = nullptr;
+  s.root4 = kEmptyRoot;
+  s.tris = (const float4*)c->b_tris.p;
+  s.shade = (const float4*)c->b_shade.p;
+  s.geo = (const float4*)c->b_geo.p;
+  s.mats = (const float*)c->b_mats.p;
+  s.emitters = (const int*)c->b_emit.p;
+  s.perm = (const uint8_t*)c->perm.p;
+  s.root = kEmptyRoot;
+  s.n_tris = tri_base;
+  s.n_emitters = (int)emit.size();
+  s.n_mats = mat_base;
+  c->has_batch = true;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_key.clear();
+  }
+  c->stats.bvh_build_ms = ms;
+  c->stats.bvh_nodes = (int32_t)(nodes.size() / 4);
   c->stats.node_bytes = 64;
   c->stats.tri_bytes = 48;
   return RTX_OK;
@@ -696,6 +897,7 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   p.accumulate = acc;
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
+  p.sort_material = c->sort_material;
   p.traversal = c->traversal;
   p.min_busy = c->min_busy;
   RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
@@ -728,6 +930,217 @@ int rtx_render_pt_resolved(rtx_context* c, const float* cam, int W, int H, int s
   if (c && spp <= 0) return fail(c, RTX_ERR_INVALID, "spp must be positive");
   ResolveReq q{limit, gamma, display, bytes, format};
   return render_paths(c, cam, W, H, 0, spp, spp, max_depth, seed, out, false, &q);
+}
+
+// ---- multi-scene batch ------------------------------------------------------------
+int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_depth, float* out) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!c->has_batch) return fail(c, RTX_ERR_NO_SCENE, "no batch uploaded (rtx_batch_upload)");
+  if (n_jobs < 1 || !jobs || !out) return fail(c, RTX_ERR_INVALID, "no frames or NULL output");
+  if (max_depth < 1 || max_depth > 63) return fail(c, RTX_ERR_INVALID, "max_depth must be in [1, 63]");
+  if (c->traversal == 1) return fail(c, RTX_ERR_INVALID, "batches use the batch traversal (RTX_OPT_TRAVERSAL 0)");
+  std::vector<PtJob> hj((size_t)n_jobs);
+  long long q = 0, pix = 0;
+  for (int j = 0; j < n_jobs; ++j) {
+    const rtx_job& J = jobs[j];
+    if (J.scene < 0 || J.scene >= (int)c->bscenes.size())
+      return fail(c, RTX_ERR_INVALID, "frame " + std::to_string(j) + ": scene index out of range");
+    if (J.W <= 0 || J.H <= 0 || J.spp <= 0 || (long long)J.W * J.H > (1LL << 28))
+      return fail(c, RTX_ERR_INVALID, "frame " + std::to_string(j) + ": bad size or spp");
+    const rtx_context::BatchScene& bs = c->bscenes[J.scene];
+    PtJob& P = hj[j];
+    P.q_begin = q;
+    P.pix_begin = pix;
+    P.npix = J.W * J.H;
+    P.W = J.W;
+    P.spp = J.spp;
+    P.first_sample = 0;
+    P.root = bs.root;
+    P.root4 = kEmptyRoot;
+    P.e_begin = bs.e_begin;
+    P.n_emitters = bs.n_emitters;
+    P.k0 = (uint32_t)J.seed;
+    P.k1 = (uint32_t)(J.seed >> 32);
+    for (int k = 0; k < 3; ++k) {
+      P.sky[k] = bs.sky[k];
+      P.ground[k] = bs.ground[k];
+    }
+    P.cam = make_cam_params(J.camera, J.W, J.H);
+    q += (long long)P.npix * J.spp;
+    pix += P.npix;
+  }
+  if (pix > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "more than 2^30 pixels in one batch frame");
+  int r;
+  if ((r = begin(c))) return r;
+  // the job table through pinned staging (the copy a replayed graph needs)
+  if (c->pinned_cap < n_jobs) {
+    if (c->h_jobs_pinned) cudaFreeHost(c->h_jobs_pinned);
+    if (c->h_jobq_pinned) cudaFreeHost(c->h_jobq_pinned);
+    c->h_jobs_pinned = nullptr;
+    c->h_jobq_pinned = nullptr;
+    c->pinned_cap = 0;
+    RTX_CUDA(cudaMallocHost(&c->h_jobs_pinned, sizeof(PtJob) * n_jobs), "pinned jobs");
+    RTX_CUDA(cudaMallocHost(&c->h_jobq_pinned, sizeof(long long) * n_jobs), "pinned jobs");
+    c->pinned_cap = n_jobs;
+  }
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");  // staging reuse
+  std::memcpy(c->h_jobs_pinned, hj.data(), sizeof(PtJob) * n_jobs);
+  for (int j = 0; j < n_jobs; ++j) c->h_jobq_pinned[j] = hj[j].q_begin;
+  RTX_CUDA(c->b_jobs.ensure(sizeof(PtJob) * n_jobs), "job table");
+  RTX_CUDA(c->b_jobq.ensure(sizeof(long long) * n_jobs), "job table");
+  RTX_CUDA(cudaMemcpyAsync(c->b_jobs.p, c->h_jobs_pinned, sizeof(PtJob) * n_jobs, cudaMemcpyHostToDevice,
+                           c->stream),
+           "job table H2D");
+  RTX_CUDA(cudaMemcpyAsync(c->b_jobq.p, c->h_jobq_pinned, sizeof(long long) * n_jobs, cudaMemcpyHostToDevice,
+                           c->stream),
+           "job table H2D");
+  Arg o;
+  if ((r = bind_out(c, out, (size_t)pix * 12, 0, o))) return r;
+  PtParams p{};
+  p.max_depth = max_depth;
+  p.wave_paths = (int)c->wave_paths;
+  p.block = c->block;
+  p.count_visits = c->count_visits;
+  p.primary_cache = c->primary_cache;
+  p.sort_material = c->sort_material;
+  p.traversal = 0;
+  p.min_busy = c->min_busy;
+  p.accumulate = c->accumulate;
+  p.n_jobs = n_jobs;
+  p.d_jobs = (const PtJob*)c->b_jobs.p;
+  p.d_job_q = (const long long*)c->b_jobq.p;
+  p.h_jobs = hj.data();
+  RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
+  c->timer.reset();
+  // the launch shape: everything the captured kernels bake in
+  std::vector<int64_t> key = {n_jobs, max_depth, c->wave_paths, c->block, c->primary_cache, c->count_visits,
+                              c->accumulate, c->sort_material, (int64_t)(intptr_t)o.dev};
+  for (int j = 0; j < n_jobs; ++j) key.insert(key.end(), {jobs[j].scene, jobs[j].W, jobs[j].H, jobs[j].spp});
+  int launches = 0, ext_launches = 0;
+  std::string why;
+  cudaError_t e = cudaSuccess;
+  const bool graphable = c->use_graph && !c->timer.on;
+  if (graphable && c->graph && key == c->graph_key) {
+    e = cudaGraphLaunch(c->graph, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphLaunch");
+    c->stats.kernel_launches = 0;  // kernels are graph nodes
+  } else {
+    e = pt_render(c->pt, c->bds, CamParams{}, p, (float*)o.dev, c->d_err, c->d_counters, &c->timer, c->stream,
+                  &launches, &ext_launches, &why);
+    c->stats.kernel_launches = launches;
+    c->stats.extend_launches = ext_launches;
+    if (e != cudaSuccess) {
+      if (!why.empty()) return fail(c, RTX_ERR_INVALID, why);
+      return cuda_fail(c, e, "pt_render (batch)");
+    }
+    if (graphable) {
+      // capture the same launch sequence (the wave size this render used)
+      if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+      }
+      PtParams pc = p;
+      pc.wave_paths = (int)pt_last_wave(c->pt);
+      cudaGraph_t g = nullptr;
+      int l2 = 0, x2 = 0;
+      RTX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+      cudaError_t ec = pt_render(c->pt, c->bds, CamParams{}, pc, (float*)o.dev, c->d_err, c->d_counters,
+                                 &c->timer, c->stream, &l2, &x2, &why);
+      cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+      if (ec != cudaSuccess || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_fail(c, ec != cudaSuccess ? ec : ee, "graph capture");
+      }
+      ee = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ee != cudaSuccess) {
+        c->graph = nullptr;
+        return cuda_fail(c, ee, "cudaGraphInstantiate");
+      }
+      c->graph_key = key;
+    }
+  }
+  if ((r = copy_back(c, o))) return r;
+  return finish(c, all_device({&o}));
+}
+
+// Autotuner: frame time of a batch over BVH leaf sizes (each a rebuild of the
+// batch), then threads per block x paths per wave, coordinate-wise; each
+// candidate renders the frame twice and keeps the faster device time.
+static int time_frame(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_depth, float* d_out, double* ms) {
+  double best = 1e30;
+  for (int rep = 0; rep < 2; ++rep) {
+    int r = rtx_render_batch(c, n_jobs, jobs, max_depth, d_out);
+    if (r) return r;
+    best = std::min(best, c->stats.last_gpu_ms);
+  }
+  *ms = best;
+  return RTX_OK;
+}
+
+int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scenes, int n_jobs,
+                       const rtx_job* jobs, int max_depth, rtx_tune_result* out) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!out || !jobs || n_jobs < 1) return fail(c, RTX_ERR_INVALID, "NULL argument");
+  const bool saved_graph = c->use_graph, saved_timer = c->timer.on;
+  c->use_graph = false;
+  c->timer.on = false;
+  int r = RTX_OK;
+  long long pix = 0;
+  for (int j = 0; j < n_jobs; ++j) pix += (long long)std::max(jobs[j].W, 0) * std::max(jobs[j].H, 0);
+  float* d_out = nullptr;
+  rtx_tune_result res{};
+  res.trials = 0;
+  auto done = [&](int code) {
+    if (d_out) cudaFree(d_out);
+    c->use_graph = saved_graph;
+    c->timer.on = saved_timer;
+    return code;
+  };
+  cudaError_t e = cudaMalloc(&d_out, (size_t)std::max(pix, 1LL) * 12);
+  if (e != cudaSuccess) return done(cuda_fail(c, e, "autotune output"));
+  double ms = 0.0;
+  // the starting point: the context's current options
+  if (scenes && (r = rtx_batch_upload(c, n_scenes, scenes))) return done(r);
+  if ((r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms))) return done(r);
+  res.ms_default = ms;
+  res.block = c->block;
+  res.wave_paths = c->wave_paths;
+  res.leaf_size = c->leaf_size;
+  res.ms = ms;
+  ++res.trials;
+  if (scenes) {
+    for (int leaf : {2, 4, 8}) {
+      if (leaf == res.leaf_size) continue;
+      c->leaf_size = leaf;
+      if ((r = rtx_batch_upload(c, n_scenes, scenes)) || (r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms)))
+        return done(r);
+      ++res.trials;
+      if (ms < res.ms) {
+        res.ms = ms;
+        res.leaf_size = leaf;
+      }
+    }
+    c->leaf_size = (int)res.leaf_size;
+    if ((r = rtx_batch_upload(c, n_scenes, scenes))) return done(r);
+  }
+  for (int block : {64, 128})
+    for (long long wave : {1LL << 20, 1LL << 22, 1LL << 24, 0LL}) {
+      if (block == res.block && wave == res.wave_paths) continue;
+      c->block = block;
+      c->wave_paths = wave;
+      if ((r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms))) return done(r);
+      ++res.trials;
+      if (ms < res.ms) {
+        res.ms = ms;
+        res.block = block;
+        res.wave_paths = wave;
+      }
+    }
+  c->block = (int)res.block;
+  c->wave_paths = res.wave_paths;
+  *out = res;
+  return done(RTX_OK);
 }
 
 // ---- display resolve and image files --------------------------------------------

@@ -20,6 +20,14 @@
 //             combine the ranges
 // off(t) = (t / 3 - 1, t % 3 - 1).  Out-of-image taps read zero ("same"
 // zero padding).
+//
+// Pipeline (all three): the K (or pixel) range is cut into slices of 64;
+// every thread copies its 16-byte chunks of a slice straight into shared
+// memory with cp.async (zero-filled where the tap falls outside the image),
+// S - 1 slices ahead, into a ring of S stages.  Thread 0 issues the slice's
+// MMAs and commits them to the stage's mbarrier; a stage is refilled once the
+// MMAs that read it have completed.  The gathers of later slices therefore
+// overlap the MMAs of earlier ones, and no thread stalls on its own loads.
 #include <algorithm>
 
 #include "nn.h"
@@ -84,16 +92,30 @@ __device__ __forceinline__ uint4 f32_to_bf16x8(const float* f) {
   return u;
 }
 
-// Shared set-up of a tensor-core CTA: TMEM columns and the MMA barrier.
-struct TcCta {
-  uint32_t tmem;
-  uint32_t phase;
-};
+// Address of 8 channels [c, c + 8) of the (virtually concatenated,
+// upsampled) source at pixel (n, y, x), or nullptr outside the image.
+__device__ __forceinline__ const bf16* src_ptr(const Src& s1, const Src& s2, int H, int W, int n, int y, int x,
+                                               int c) {
+  if (y < 0 || y >= H || x < 0 || x >= W) return nullptr;
+  if (c < s1.C) {
+    if (s1.up) return s1.ptr + (((size_t)n * (H >> 1) + (y >> 1)) * (W >> 1) + (x >> 1)) * s1.C + c;
+    return s1.ptr + (((size_t)n * H + y) * W + x) * s1.C + c;
+  }
+  if (s2.ptr) return s2.ptr + (((size_t)n * H + y) * W + x) * s2.C + (c - s1.C);
+  return nullptr;
+}
 
-__device__ __forceinline__ void tc_begin(uint32_t* tmem_slot, uint64_t* bar, uint32_t ncols) {
+// 16 bytes from p into shared address dst, zeros when p is null (`base` is a
+// valid address the zero-fill form names but does not read)
+__device__ __forceinline__ void chunk_async(uint32_t dst, const void* p, const void* base) {
+  tc::cp_async16(dst, p ? p : base, p ? 16u : 0u);
+}
+
+// Shared set-up of a tensor-core CTA: TMEM columns and S MMA barriers.
+__device__ __forceinline__ void tc_begin(uint32_t* tmem_slot, uint64_t* bars, int nbar, uint32_t ncols) {
   if ((threadIdx.x >> 5) == 0) tc::tmem_alloc(tmem_slot, ncols);
   if (threadIdx.x == 0) {
-    tc::mbar_init(bar, 1);
+    for (int i = 0; i < nbar; ++i) tc::mbar_init(&bars[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_before();
@@ -107,24 +129,47 @@ __device__ __forceinline__ void tc_end(uint32_t tmem, uint32_t ncols) {
   if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
-// Issue the slice's MMAs (K-major A and B tiles of kSlice K) and wait.
-__device__ __forceinline__ bool tc_slice_kmajor(uint8_t* sa, uint8_t* sb, uint32_t tmem, uint32_t idesc,
-                                                bool first, uint64_t* bar, uint32_t& phase, int* err) {
-  tc::fence_proxy_async();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    tc::fence_after();
-    uint32_t a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
+// The S-stage ring over n slices (see the file comment).  load(slice, stage)
+// issues this thread's copies of a slice (nothing for slice >= n); mma(stage,
+// first) is run by thread 0.  Returns false, uniformly across the CTA, when
+// an MMA barrier wait ran out (error flag set); copies are drained either way.
+template <int S, class Load, class Mma>
+__device__ __forceinline__ bool conv_pipeline(int n, uint64_t* bars, Load&& load, Mma&& mma, int* err) {
+  uint32_t parity = 0;
 #pragma unroll
-    for (int s = 0; s < kSlice / 16; ++s)
-      tc::mma_bf16(tmem, tc::make_desc(a0 + s * 256, 128, kSlice * 16),
-                   tc::make_desc(b0 + s * 256, 128, kSlice * 16), idesc, !first || s > 0);
-    tc::mma_commit(bar);
+  for (int s = 0; s < S - 1; ++s) {
+    load(s, s);
+    tc::cp_async_commit();
   }
-  bool ok = tc::mbar_wait(bar, phase);
-  phase ^= 1;
+  bool wok = true, ok = true;
+  for (int it = 0; it < n; ++it) {
+    const int st = it % S;
+    tc::cp_async_wait<S - 2>();  // this thread's copies of slice `it` landed
+    tc::fence_proxy_async();
+    if (!__syncthreads_and(wok)) {
+      ok = false;
+      break;
+    }
+    if (threadIdx.x == 0) {
+      tc::fence_after();
+      mma(st, it == 0);
+      tc::mma_commit(&bars[st]);
+    }
+    if (it > 0) {  // the previous slice's MMAs free its stage for slice it + S - 1
+      const int ps = (it - 1) % S;
+      wok = tc::mbar_wait(&bars[ps], (parity >> ps) & 1u);
+      parity ^= 1u << ps;
+    }
+    load(it + S - 1, (it + S - 1) % S);
+    tc::cp_async_commit();
+  }
+  if (ok && n > 0) {
+    const int ls = (n - 1) % S;
+    const bool w = wok && tc::mbar_wait(&bars[ls], (parity >> ls) & 1u);
+    ok = __syncthreads_and(w);
+  }
   if (!ok && (threadIdx.x & 31) == 0) atomicOr(err, tc::kErrMbarTimeout);
-  __syncthreads();
+  tc::cp_async_wait_all();
   return ok;
 }
 
@@ -133,21 +178,22 @@ __device__ __forceinline__ bool tc_slice_kmajor(uint8_t* sa, uint8_t* sb, uint32
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
+template <int S>
 __global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sa = smem;                      // 128 x 64 K-major
-  uint8_t* sb = smem + 128 * kSlice * 2;   // Cout x 64 K-major
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bars[S];
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long P = (long long)a.N * a.H * a.W;
   const long long m0 = (long long)blockIdx.x * 128;
   const uint32_t ncols = a.Cout <= 32 ? 32 : (a.Cout <= 64 ? 64 : (a.Cout <= 128 ? 128 : 256));
-  tc_begin(&tmem_slot, &bar, ncols);
+  const uint32_t a_bytes = 128 * kSlice * 2, stage = a_bytes + (uint32_t)a.Cout * kSlice * 2;
+  tc_begin(&tmem_slot, bars, S, ncols);
   const uint32_t tmem = tmem_slot;
   const uint32_t idesc = tc::make_idesc_bf16(128, a.Cout);
-  uint32_t phase = 0;
+  const uint32_t s0 = tc::smem_u32(smem);
   const int K = 9 * a.Cin;
+  const int n_slices = (K + kSlice - 1) / kSlice;
   // this thread's 8 tile rows (tid >> 3) + 16 i and its chunk column tid & 7
   const int kc = tid & 7;
   Pix px[8];
@@ -158,26 +204,33 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
     pv[i] = p < P;
     px[i] = pix_of(pv[i] ? p : 0, a.H, a.W);
   }
-  bool ok = true;
-  for (int k0 = 0; k0 < K && ok; k0 += kSlice) {
-    int k = k0 + kc * 8;
-    int t = k / a.Cin, c = k - t * a.Cin;
-    int dy = t / 3 - 1, dx = t % 3 - 1;
+  auto load = [&](int slice, int st) {
+    if (slice >= n_slices) return;
+    const uint32_t sa = s0 + st * stage, sb = sa + a_bytes;
+    const int k0 = slice * kSlice, k = k0 + kc * 8;
+    const bool kv = k < K;
+    const int t = kv ? k / a.Cin : 0, c = k - t * a.Cin;
+    const int dy = t / 3 - 1, dx = t % 3 - 1;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      int row = (tid >> 3) + 16 * i;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (pv[i] && k < K) v = src_chunk(a.s1, a.s2, a.N, a.H, a.W, px[i].n, px[i].y + dy, px[i].x + dx, c);
-      *reinterpret_cast<uint4*>(sa + tc::tile_offset(row, kc * 8, kSlice)) = v;
+      const int row = (tid >> 3) + 16 * i;
+      const bf16* p = (pv[i] && kv) ? src_ptr(a.s1, a.s2, a.H, a.W, px[i].n, px[i].y + dy, px[i].x + dx, c) : nullptr;
+      chunk_async(sa + tc::tile_offset(row, kc * 8, kSlice), p, a.s1.ptr);
     }
     for (int ch = tid; ch < a.Cout * 8; ch += 128) {
-      int row = ch >> 3, kk = (ch & 7) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (k0 + kk < K) v = *reinterpret_cast<const uint4*>(a.w + (size_t)row * K + k0 + kk);
-      *reinterpret_cast<uint4*>(sb + tc::tile_offset(row, kk, kSlice)) = v;
+      const int row = ch >> 3, kk = (ch & 7) * 8;
+      const bf16* p = k0 + kk < K ? a.w + (size_t)row * K + k0 + kk : nullptr;
+      chunk_async(sb + tc::tile_offset(row, kk, kSlice), p, a.w);
     }
-    ok = tc_slice_kmajor(sa, sb, tmem, idesc, k0 == 0, &bar, phase, a.err);
-  }
+  };
+  auto mma = [&](int st, bool first) {
+    const uint32_t a0 = s0 + st * stage, b0 = a0 + a_bytes;
+#pragma unroll
+    for (int s = 0; s < kSlice / 16; ++s)
+      tc::mma_bf16(tmem, tc::make_desc(a0 + s * 256, 128, kSlice * 16), tc::make_desc(b0 + s * 256, 128, kSlice * 16),
+                   idesc, !first || s > 0);
+  };
+  const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
   if (ok) {
     const long long p = m0 + warp * 32 + lane;
@@ -204,11 +257,10 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
 // ---------------------------------------------------------------------------
 // data gradient
 // ---------------------------------------------------------------------------
+template <int S>
 __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sa = smem;
-  uint8_t* sb = smem + 128 * kSlice * 2;
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bars[S];
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long P = (long long)a.N * a.H * a.W;
@@ -216,11 +268,13 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
   const int n0 = blockIdx.y * 256;
   const int NT = min(256, a.Cin - n0);  // output channels of this CTA
   const uint32_t ncols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
-  tc_begin(&tmem_slot, &bar, ncols);
+  const uint32_t a_bytes = 128 * kSlice * 2, stage = a_bytes + (uint32_t)min(256, a.Cin) * kSlice * 2;
+  tc_begin(&tmem_slot, bars, S, ncols);
   const uint32_t tmem = tmem_slot;
   const uint32_t idesc = tc::make_idesc_bf16(128, NT);
-  uint32_t phase = 0;
+  const uint32_t s0 = tc::smem_u32(smem);
   const int K = 9 * a.Cout;
+  const int n_slices = (K + kSlice - 1) / kSlice;
   const int kc = tid & 7;
   Pix px[8];
   bool pv[8];
@@ -230,28 +284,36 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
     pv[i] = p < P;
     px[i] = pix_of(pv[i] ? p : 0, a.H, a.W);
   }
-  bool ok = true;
-  for (int k0 = 0; k0 < K && ok; k0 += kSlice) {
-    int k = k0 + kc * 8;
-    int t = k / a.Cout, o = k - t * a.Cout;
-    int dy = t / 3 - 1, dx = t % 3 - 1;
+  auto load = [&](int slice, int st) {
+    if (slice >= n_slices) return;
+    const uint32_t sa = s0 + st * stage, sb = sa + a_bytes;
+    const int k0 = slice * kSlice, k = k0 + kc * 8;
+    const bool kv = k < K;
+    const int t = kv ? k / a.Cout : 0, o = k - t * a.Cout;
+    const int dy = t / 3 - 1, dx = t % 3 - 1;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      int row = (tid >> 3) + 16 * i;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      int yy = px[i].y - dy, xx = px[i].x - dx;
-      if (pv[i] && k < K && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
-        v = *reinterpret_cast<const uint4*>(a.dout + (((size_t)px[i].n * a.H + yy) * a.W + xx) * a.Cout + o);
-      *reinterpret_cast<uint4*>(sa + tc::tile_offset(row, kc * 8, kSlice)) = v;
+      const int row = (tid >> 3) + 16 * i;
+      const int yy = px[i].y - dy, xx = px[i].x - dx;
+      const bf16* p = (pv[i] && kv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
+                          ? a.dout + (((size_t)px[i].n * a.H + yy) * a.W + xx) * a.Cout + o
+                          : nullptr;
+      chunk_async(sa + tc::tile_offset(row, kc * 8, kSlice), p, a.dout);
     }
     for (int ch = tid; ch < NT * 8; ch += 128) {
-      int row = ch >> 3, kk = (ch & 7) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (k0 + kk < K) v = *reinterpret_cast<const uint4*>(a.wt + (size_t)(n0 + row) * K + k0 + kk);
-      *reinterpret_cast<uint4*>(sb + tc::tile_offset(row, kk, kSlice)) = v;
+      const int row = ch >> 3, kk = (ch & 7) * 8;
+      const bf16* p = k0 + kk < K ? a.wt + (size_t)(n0 + row) * K + k0 + kk : nullptr;
+      chunk_async(sb + tc::tile_offset(row, kk, kSlice), p, a.wt);
     }
-    ok = tc_slice_kmajor(sa, sb, tmem, idesc, k0 == 0, &bar, phase, a.err);
-  }
+  };
+  auto mma = [&](int st, bool first) {
+    const uint32_t a0 = s0 + st * stage, b0 = a0 + a_bytes;
+#pragma unroll
+    for (int s = 0; s < kSlice / 16; ++s)
+      tc::mma_bf16(tmem, tc::make_desc(a0 + s * 256, 128, kSlice * 16), tc::make_desc(b0 + s * 256, 128, kSlice * 16),
+                   idesc, !first || s > 0);
+  };
+  const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
   if (ok) {
     const long long p = m0 + warp * 32 + lane;
@@ -262,11 +324,11 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
       tc::tmem_ld8(taddr + c0, v);
       if (p < P) {
         if (a.mask_relu) {
-          float s[8];
-          bf16x8_to_f32(src_chunk(a.s1, a.s2, a.N, a.H, a.W, q.n, q.y, q.x, n0 + c0), s);
+          float sv[8];
+          bf16x8_to_f32(src_chunk(a.s1, a.s2, a.N, a.H, a.W, q.n, q.y, q.x, n0 + c0), sv);
 #pragma unroll
           for (int i = 0; i < 8; ++i)
-            if (!(s[i] > 0.0f)) v[i] = 0.0f;
+            if (!(sv[i] > 0.0f)) v[i] = 0.0f;
         }
         *reinterpret_cast<uint4*>(a.din + (size_t)p * a.Cin + n0 + c0) = f32_to_bf16x8(v);
       }
@@ -278,11 +340,10 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
 // ---------------------------------------------------------------------------
 // weight gradient
 // ---------------------------------------------------------------------------
+template <int S>
 __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sa = smem;                     // 128 (t, c) x 64 (pixels), MN-major
-  uint8_t* sb = smem + 128 * kSlice * 2;  // Cout x 64 (pixels), MN-major
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(8) uint64_t bars[S];
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int P = a.N * a.H * a.W;  // < 2^31 (checked by the host)
@@ -291,10 +352,12 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
   const int pb = blockIdx.y * a.pix_per_cta;
   const int pe = min(P, pb + a.pix_per_cta);
   const uint32_t ncols = a.Cout <= 32 ? 32 : (a.Cout <= 64 ? 64 : (a.Cout <= 128 ? 128 : 256));
-  tc_begin(&tmem_slot, &bar, ncols);
+  const uint32_t a_bytes = 128 * kSlice * 2, stage = a_bytes + (uint32_t)a.Cout * kSlice * 2;
+  tc_begin(&tmem_slot, bars, S, ncols);
   const uint32_t tmem = tmem_slot;
   const uint32_t idesc = tc::make_idesc_bf16(128, a.Cout, true, true);
-  uint32_t phase = 0;
+  const uint32_t s0 = tc::smem_u32(smem);
+  const int n_slices = pe > pb ? (pe - pb + kSlice - 1) / kSlice : 0;
   // this thread's 8 rows of the A tile: (tap, channel) j = j0 + 8 rg
   const int rg = tid & 15;
   const int j = j0 + rg * 8;
@@ -303,45 +366,39 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
   const int dy = t / 3 - 1, dx = t % 3 - 1;
   const int HW = a.H * a.W;
   const int ng = a.Cout >> 3;
-  bool ok = true;
-  for (int q0 = pb; q0 < pe && ok; q0 += kSlice) {
+  auto load = [&](int slice, int st) {
+    if (slice >= n_slices) return;
+    const uint32_t sa = s0 + st * stage, sb = sa + a_bytes;
+    const int q0 = pb + slice * kSlice;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      int kp = (tid >> 4) + 8 * i;  // pixel within the slice
-      int p = q0 + kp;
-      uint4 v = make_uint4(0, 0, 0, 0);
+      const int kp = (tid >> 4) + 8 * i;  // pixel within the slice
+      const int p = q0 + kp;
+      const bf16* src = nullptr;
       if (p < pe && jv) {
-        int n = p / HW, rem = p - n * HW;
-        int y = rem / a.W, x = rem - y * a.W;
-        v = src_chunk(a.s1, a.s2, a.N, a.H, a.W, n, y + dy, x + dx, c);
+        const int n = p / HW, rem = p - n * HW;
+        const int y = rem / a.W, x = rem - y * a.W;
+        src = src_ptr(a.s1, a.s2, a.H, a.W, n, y + dy, x + dx, c);
       }
-      *reinterpret_cast<uint4*>(sa + tc::tile_offset_mn(rg * 8, kp, 128)) = v;
+      chunk_async(sa + tc::tile_offset_mn(rg * 8, kp, 128), src, a.s1.ptr);
     }
     for (int ch = tid; ch < ng * kSlice; ch += 128) {
-      int og = ch % ng, kp = ch / ng;
-      int p = q0 + kp;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (p < pe) v = *reinterpret_cast<const uint4*>(a.dout + (size_t)p * a.Cout + og * 8);
-      *reinterpret_cast<uint4*>(sb + tc::tile_offset_mn(og * 8, kp, a.Cout)) = v;
+      const int og = ch % ng, kp = ch / ng;
+      const int p = q0 + kp;
+      const bf16* src = p < pe ? a.dout + (size_t)p * a.Cout + og * 8 : nullptr;
+      chunk_async(sb + tc::tile_offset_mn(og * 8, kp, a.Cout), src, a.dout);
     }
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      uint32_t a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
+  };
+  auto mma = [&](int st, bool first) {
+    const uint32_t a0 = s0 + st * stage, b0 = a0 + a_bytes;
 #pragma unroll
-      for (int s = 0; s < kSlice / 16; ++s)
-        tc::mma_bf16(tmem, tc::make_desc(a0 + s * 2 * 16 * 128, 16 * 128, 128),
-                     tc::make_desc(b0 + s * 2 * 16 * a.Cout, 16 * a.Cout, 128), idesc, q0 > pb || s > 0);
-      tc::mma_commit(&bar);
-    }
-    ok = tc::mbar_wait(&bar, phase);
-    phase ^= 1;
-    if (!ok && lane == 0) atomicOr(a.err, tc::kErrMbarTimeout);
-    __syncthreads();
-  }
+    for (int s = 0; s < kSlice / 16; ++s)
+      tc::mma_bf16(tmem, tc::make_desc(a0 + s * 2 * 16 * 128, 16 * 128, 128),
+                   tc::make_desc(b0 + s * 2 * 16 * a.Cout, 16 * a.Cout, 128), idesc, !first || s > 0);
+  };
+  const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
-  if (ok && pe > pb) {
+  if (ok && n_slices > 0) {
     const int jj = j0 + warp * 32 + lane;  // this thread's accumulator row
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
     for (int c0 = 0; c0 < a.Cout; c0 += 8) {
@@ -356,23 +413,43 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
 }
 
 // ---------------------------------------------------------------------------
+// Stages of the ring for a B tile of nb rows: 4 / 3 / 2 stages keep a CTA's
+// shared memory at or below 96 KB (two CTAs per SM).
+static int stages_for(int nb) { return nb <= 64 ? 4 : (nb <= 128 ? 3 : 2); }
+
+template <class K4, class K3, class K2, class Args>
+static cudaError_t launch_staged(K4 k4, K3 k3, K2 k2, int stages, dim3 grid, size_t stage_bytes, const Args& a,
+                                 cudaStream_t st) {
+  size_t smem = stage_bytes * stages;
+  cudaError_t e;
+  if (stages == 4) {
+    if ((e = cudaFuncSetAttribute(k4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    k4<<<grid, 128, smem, st>>>(a);
+  } else if (stages == 3) {
+    if ((e = cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    k3<<<grid, 128, smem, st>>>(a);
+  } else {
+    if ((e = cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    k2<<<grid, 128, smem, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
-  size_t smem = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-  if (e) return e;
-  k_conv_fwd<<<(unsigned)((P + 127) / 128), 128, smem, st>>>(a);
-  return cudaGetLastError();
+  if (a.Cout % 16 || a.Cout > 256 || a.Cin % 8) return cudaErrorInvalidValue;
+  size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
+  return launch_staged(k_conv_fwd<4>, k_conv_fwd<3>, k_conv_fwd<2>, stages_for(a.Cout),
+                       dim3((unsigned)((P + 127) / 128)), stage, a, st);
 }
 
 cudaError_t conv_dgrad(const ConvDgrad& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
-  size_t smem = 128 * kSlice * 2 + 256 * kSlice * 2;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_dgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-  if (e) return e;
-  dim3 grid((unsigned)((P + 127) / 128), (a.Cin + 255) / 256);
-  k_conv_dgrad<<<grid, 128, smem, st>>>(a);
-  return cudaGetLastError();
+  if (a.Cin % 16 || a.Cout % 8) return cudaErrorInvalidValue;
+  int nb = std::min(256, a.Cin);
+  size_t stage = 128 * kSlice * 2 + (size_t)nb * kSlice * 2;
+  return launch_staged(k_conv_dgrad<4>, k_conv_dgrad<3>, k_conv_dgrad<2>, stages_for(nb),
+                       dim3((unsigned)((P + 127) / 128), (a.Cin + 255) / 256), stage, a, st);
 }
 
 int wgrad_pixels_per_cta(long long P, int Cout, int Cin) {
@@ -387,12 +464,9 @@ int wgrad_pixels_per_cta(long long P, int Cout, int Cin) {
 cudaError_t conv_wgrad(const ConvWgrad& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
   if (P >= (1LL << 31) || a.Cout % 16 || a.Cout > 256) return cudaErrorInvalidValue;
-  size_t smem = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
-  cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-  if (e) return e;
+  size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
   dim3 grid((9 * a.Cin + 127) / 128, (unsigned)((P + a.pix_per_cta - 1) / a.pix_per_cta));
-  k_conv_wgrad<<<grid, 128, smem, st>>>(a);
-  return cudaGetLastError();
+  return launch_staged(k_conv_wgrad<4>, k_conv_wgrad<3>, k_conv_wgrad<2>, stages_for(a.Cout), grid, stage, a, st);
 }
 
 }  // namespace nn

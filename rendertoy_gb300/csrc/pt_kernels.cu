@@ -27,6 +27,8 @@
 namespace rtx {
 
 constexpr int kMaxDepthSlots = 64;
+// material sort: at most this many materials (+1 bin for misses)
+constexpr int kMaxSortBins = 4096;
 // minimum resident blocks of 128 threads per SM (register budget)
 #ifndef RTX_SHADE_MINB
 #define RTX_SHADE_MINB 8
@@ -34,8 +36,8 @@ constexpr int kMaxDepthSlots = 64;
 #ifndef RTX_TRACE_MINB
 #define RTX_TRACE_MINB 1
 #endif
-// path state 6 x 16 B + shadow record 4 x 16 B + two queue entries
-constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 2 * 4;
+// path state 6 x 16 B + shadow record 4 x 16 B + three queue entries
+constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 3 * 4;
 
 struct PtWorkspace {
   size_t cap = 0;
@@ -44,11 +46,16 @@ struct PtWorkspace {
   float4 *ray_o = nullptr, *ray_d = nullptr, *thr = nullptr, *rad = nullptr, *absb = nullptr,
          *hit = nullptr;
   int* queue[2] = {nullptr, nullptr};
+  int* sorted = nullptr;    // the shading queue ordered by material
+  int* mat_hist = nullptr;  // kMaxSortBins + 1 bins: counts, then write offsets
   float4* shadow = nullptr;
   int* counters = nullptr;  // counts[64] | shadow_counts[64] | work[2 * 64]
   int num_sms = 0;
   int occ_extend = 0, occ_connect = 0, occ_shade = 0, block_cached = 0;
+  long long last_wave = 0;  // paths per wave of the last render
 };
+
+long long pt_last_wave(const PtWorkspace* ws) { return ws->last_wave; }
 
 PtWorkspace* pt_workspace_create() { return new PtWorkspace(); }
 
@@ -58,6 +65,9 @@ static void ws_free(PtWorkspace* w) {
     if (p) cudaFree(p);
   if (w->queue[0]) cudaFree(w->queue[0]);
   if (w->queue[1]) cudaFree(w->queue[1]);
+  if (w->sorted) cudaFree(w->sorted);
+  if (w->mat_hist) cudaFree(w->mat_hist);
+  w->sorted = w->mat_hist = nullptr;
   if (w->counters) cudaFree(w->counters);
   w->ray_o = w->ray_d = w->thr = w->rad = w->absb = w->hit = w->shadow = nullptr;
   w->queue[0] = w->queue[1] = nullptr;
@@ -82,6 +92,8 @@ static cudaError_t ws_reserve(PtWorkspace* w, size_t cap) {
   if ((e = cudaMalloc(&w->shadow, cap * 4 * sizeof(float4))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->queue[0], cap * sizeof(int))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->queue[1], cap * sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->sorted, cap * sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->mat_hist, 2 * (kMaxSortBins + 1) * sizeof(int))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->counters, 4 * kMaxDepthSlots * sizeof(int))) != cudaSuccess) return e;
   w->cap = cap;
   return cudaSuccess;
@@ -96,7 +108,84 @@ struct PtArgs {
   long long q0;
   int n_wave, npix, W, first_sample, max_depth, depth, min_busy;
   uint32_t k0, k1;
+  // multi-scene batch: frames and their first paths (ascending)
+  const PtJob* jobs;
+  const long long* job_q;
+  int n_jobs;
 };
+
+// The per-frame quantities of global path q: for a single render the scene's
+// and the render's own; in a batch those of q's frame (binary search on the
+// frames' first paths).
+struct JobView {
+  int root, root4, n_emitters;
+  const int* emitters;
+  float sky[3], ground[3];
+  uint32_t k0, k1;
+  long long q;  // path index within the frame
+  int npix, first_sample;
+};
+
+template <bool kJobs>
+RTX_DEV int job_index(const PtArgs& a, long long q) {
+  if (!kJobs) return 0;
+  int lo = 0, hi = a.n_jobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(a.job_q + mid) <= q)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+template <bool kJobs>
+RTX_DEV JobView job_of(const PtArgs& a, const DeviceScene& s, long long q) {
+  JobView v;
+  if (!kJobs) {
+    v.root = s.root;
+    v.root4 = s.root4;
+    v.n_emitters = s.n_emitters;
+    v.emitters = s.emitters;
+    for (int k = 0; k < 3; ++k) {
+      v.sky[k] = s.sky[k];
+      v.ground[k] = s.ground[k];
+    }
+    v.k0 = a.k0;
+    v.k1 = a.k1;
+    v.q = q;
+    v.npix = a.npix;
+    v.first_sample = a.first_sample;
+  } else {
+    const PtJob& J = a.jobs[job_index<true>(a, q)];
+    v.root = J.root;
+    v.root4 = J.root4;
+    v.n_emitters = J.n_emitters;
+    v.emitters = s.emitters + J.e_begin;
+    for (int k = 0; k < 3; ++k) {
+      v.sky[k] = J.sky[k];
+      v.ground[k] = J.ground[k];
+    }
+    v.k0 = J.k0;
+    v.k1 = J.k1;
+    v.q = q - J.q_begin;
+    v.npix = J.npix;
+    v.first_sample = J.first_sample;
+  }
+  return v;
+}
+
+// the scene as one frame's traversal sees it (its own tree roots)
+template <bool kJobs>
+RTX_DEV DeviceScene scene_of(const DeviceScene& s, const PtArgs& a, long long q) {
+  if (!kJobs) return s;
+  DeviceScene r = s;
+  const PtJob& J = a.jobs[job_index<true>(a, q)];
+  r.root = J.root;
+  r.root4 = J.root4;
+  return r;
+}
 
 // Append with one atomic per warp; returns this thread's slot.
 RTX_DEV int warp_append(int* counter) {
@@ -117,15 +206,27 @@ RTX_DEV int warp_fetch(int* work) {
   return __shfl_sync(0xffffffffu, base, 0);
 }
 
+template <bool kJobs>
 __global__ void k_raygen(PtArgs a, CamParams cam, const float4* __restrict__ prim) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) a.counts[0] = a.n_wave;
   if (i >= a.n_wave) return;
   long long q = a.q0 + i;
-  int pix = (int)(q % a.npix);
-  if (prim) a.hit[i] = prim[pix];
+  int pix, W;
+  long long pix_base = 0;
+  if (kJobs) {
+    const PtJob& J = a.jobs[job_index<true>(a, q)];
+    pix = (int)((q - J.q_begin) % J.npix);
+    W = J.W;
+    pix_base = J.pix_begin;
+    cam = J.cam;
+  } else {
+    pix = (int)(q % a.npix);
+    W = a.W;
+  }
+  if (prim) a.hit[i] = prim[pix_base + pix];
   F3 o, d;
-  camera_ray(cam, pix % a.W, pix / a.W, o, d);
+  camera_ray(cam, pix % W, pix / W, o, d);
   a.ray_o[i] = make_float4(o.x, o.y, o.z, 0.0f);
   a.ray_d[i] = make_float4(d.x, d.y, d.z, __int_as_float(-1));
   a.thr[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
@@ -189,8 +290,8 @@ __global__ void __launch_bounds__(128) k_extend(PtArgs a, DeviceScene s) {
 
 // Variant: a warp takes 32 rays at a time and each lane traces its ray to the
 // end before the warp takes the next batch.
-template <bool kCount, bool kWide>
-__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_extend_batch(PtArgs a, DeviceScene s) {
+template <bool kCount, bool kWide, bool kJobs>
+__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_extend_batch(PtArgs a, DeviceScene s0) {
   const int n = a.counts[a.depth];
   VisitCount vc;
   int lane = threadIdx.x & 31;
@@ -200,6 +301,7 @@ __global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_extend_batch(PtArgs a, 
     int i = base + lane;
     if (i < n) {
       int p = a.queue_in[i];
+      const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + p);
       float4 ro = a.ray_o[p], rd = a.ray_d[p];
       float t, u, v;
       int h = kWide ? trace4<false, kCount>(s, f3(ro.x, ro.y, ro.z), f3(rd.x, rd.y, rd.z),
@@ -217,8 +319,7 @@ __global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_extend_batch(PtArgs a, 
 
 // Primary hits of every pixel, traced once per render: all samples of a pixel
 // share its primary ray (renderer.cpp:255-259 has no per-sample jitter).
-__global__ void __launch_bounds__(64) k_primary_cache(DeviceScene s, CamParams cam, float4* out,
-                                                      int* err, Counters* ctr) {
+RTX_DEV void primary_px(const DeviceScene& s, const CamParams& cam, float4* out, int* err, Counters* ctr) {
   int tiles_x = (cam.W + 7) >> 3;
   int x = (blockIdx.x % tiles_x) * 8 + (threadIdx.x & 7);
   int y = (blockIdx.x / tiles_x) * 8 + (threadIdx.x >> 3);
@@ -235,11 +336,28 @@ __global__ void __launch_bounds__(64) k_primary_cache(DeviceScene s, CamParams c
   out[(size_t)y * cam.W + x] = make_float4(__int_as_float(h), t, u, v);
 }
 
+__global__ void __launch_bounds__(64) k_primary_cache(DeviceScene s, CamParams cam, float4* out, int* err,
+                                                      Counters* ctr) {
+  primary_px(s, cam, out, err, ctr);
+}
+
+// A frame of a batch: camera and tree root from the device job table, so that
+// a replayed graph picks up new cameras.
+__global__ void __launch_bounds__(64) k_primary_cache_job(DeviceScene s, const PtJob* jobs, int j, float4* prim,
+                                                          int* err, Counters* ctr) {
+  const PtJob& J = jobs[j];
+  DeviceScene sj = s;
+  sj.root = J.root;
+  primary_px(sj, J.cam, prim + J.pix_begin, err, ctr);
+}
+
+template <bool kJobs>
 __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceScene s) {
   int n = a.counts[a.depth];
   const int depth = a.depth;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int p = a.queue_in[i];
+    const JobView J = job_of<kJobs>(a, s, a.q0 + p);
     float4 ro = a.ray_o[p], rd = a.ray_d[p], h = a.hit[p], th = a.thr[p], rr = a.rad[p];
     F3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z);
     float last_pdf = ro.w;
@@ -248,8 +366,8 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
     F3 acc = f3(rr.x, rr.y, rr.z);
     if (tri < 0) {
       // World::GetDefaultEmission (world.cpp:39-42) of -direction
-      F3 env = (-d.z < 0.0f) ? f3(s.sky[0], s.sky[1], s.sky[2])
-                             : f3(s.ground[0], s.ground[1], s.ground[2]);
+      F3 env = (-d.z < 0.0f) ? f3(J.sky[0], J.sky[1], J.sky[2])
+                             : f3(J.ground[0], J.ground[1], J.ground[2]);
       acc = acc + T * env;
       a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
       continue;
@@ -288,12 +406,12 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
                expo.z == 0.0f ? 1.0f : powf(kE, expo.z));
     ShadingFrame fr = make_frame(m, eta, ff, -d);
 
-    long long q = a.q0 + p;
-    Rng rng{a.k0, a.k1, (uint32_t)(q % a.npix), (uint32_t)(a.first_sample + q / a.npix),
+    long long q = J.q;
+    Rng rng{J.k0, J.k1, (uint32_t)(q % J.npix), (uint32_t)(J.first_sample + q / J.npix),
             __float_as_uint(th.w)};
-    if (s.n_emitters > 0) {
+    if (J.n_emitters > 0) {
       // World::SampleEmitter + Triangle::GetSamplePoint (world.cpp:5-17, object.cpp:169-178)
-      int e = __ldg(s.emitters + rng.uniform_int(0, s.n_emitters - 1));
+      int e = __ldg(J.emitters + rng.uniform_int(0, J.n_emitters - 1));
       float sqr1 = sqrtf(rng.uniform());
       float r2 = rng.uniform();
       float aa = 1.0f - sqr1;
@@ -374,10 +492,10 @@ RTX_DEV bool emitter_hit(const DeviceScene& s, F3 pos, F3 dir, int e, int ex, fl
 // Visibility of each light sample (renderer.cpp:352-354: the light is seen
 // when the closest hit is the sampled emitter or nothing) as an occlusion
 // query, then the MIS-weighted contribution (renderer.cpp:356-379).
-RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec);
+RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec, int n_emitters);
 
-template <bool kCount, bool kWide>
-__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_connect_batch(PtArgs a, DeviceScene s) {
+template <bool kCount, bool kWide, bool kJobs>
+__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_connect_batch(PtArgs a, DeviceScene s0) {
   const int n = a.shadow_counts[a.depth];
   VisitCount vc;
   int lane = threadIdx.x & 31;
@@ -388,6 +506,7 @@ __global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_connect_batch(PtArgs a,
     if (i >= n) continue;
     const float4* q = a.shadow + 4 * (size_t)i;
     float4 q0 = q[0], q1 = q[1], q3 = q[3];
+    const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + __float_as_int(q0.w));
     F3 pos = f3(q0.x, q0.y, q0.z);
     F3 dir = normalized(f3(q1.x, q1.y, q1.z) - pos);
     int e = __float_as_int(q1.w), ex = __float_as_int(q3.w);
@@ -400,7 +519,7 @@ __global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_connect_batch(PtArgs a,
     } else {
       occ = occluded<kCount>(s, pos, dir, ex, he ? e : -1, te, a.err, vc);
     }
-    if (!occ) add_light(a, s, i);
+    if (!occ) add_light(a, s, i, job_of<kJobs>(a, s, a.q0 + __float_as_int(q0.w)).n_emitters);
   }
   if (kCount) {
     atomicAdd(&a.ctr->sh_node_visits, (unsigned long long)vc.nodes);
@@ -432,7 +551,7 @@ __global__ void __launch_bounds__(128) k_connect(PtArgs a, DeviceScene s) {
     }
     if (__all_sync(0xffffffffu, rec < 0)) break;
     if (rec >= 0 && trav_run<true, kCount>(r, stack, s, a.err, vc, a.min_busy)) {
-      if (r.best != 1) add_light(a, s, rec);
+      if (r.best != 1) add_light(a, s, rec, s.n_emitters);
       rec = -1;
     }
   }
@@ -444,7 +563,7 @@ __global__ void __launch_bounds__(128) k_connect(PtArgs a, DeviceScene s) {
 
 // MIS-weighted light contribution of a visible light sample
 // (renderer.cpp:356-379), added to its path's radiance.
-RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec) {
+RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec, int n_emitters) {
   const float4* q = a.shadow + 4 * (size_t)rec;
   float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
   F3 pos = f3(q0.x, q0.y, q0.z), emit_pos = f3(q1.x, q1.y, q1.z);
@@ -464,7 +583,7 @@ RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec) {
   float w = PowerHeuristic(lpdf, q2.w);
   F3 c = f3(q2.x, q2.y, q2.z) * w;
   c = c * Le;
-  c = c * (float)s.n_emitters;
+  c = c * (float)n_emitters;
   c = c / lpdf;
   float4 acc = a.rad[p];
   F3 tb = f3(q3.x, q3.y, q3.z) * c;
@@ -519,6 +638,39 @@ cudaError_t launch_resolve(const float* in, int W, int H, const Resolve& r, cuda
   int n = W * H;
   if (n > 0) k_resolve<<<(n + 255) / 256, 256, 0, st>>>(in, n, r);
   return cudaGetLastError();
+}
+
+// Batch: pixel i of the concatenated output belongs to the frame whose
+// pixels begin at or before it; its paths are q_begin + s * npix + pixel.
+__global__ void k_accumulate_jobs(const float4* rad, long long q0, int n_wave, const PtJob* jobs,
+                                  int n_jobs, long long total_pix, float* out) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= total_pix) return;
+  int lo = 0, hi = n_jobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].pix_begin <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const PtJob& J = jobs[lo];
+  long long pix = i - J.pix_begin;
+  long long first = J.q_begin + pix;                 // sample 0 of this pixel
+  long long last = first + (long long)(J.spp - 1) * J.npix;
+  if (last < q0 || first >= q0 + n_wave) return;
+  long long qs = first;
+  if (qs < q0) qs = first + (q0 - first + J.npix - 1) / J.npix * J.npix;
+  float* o = out + 3 * (size_t)i;
+  F3 acc = f3(o[0], o[1], o[2]);
+  const float spp = (float)J.spp;
+  for (long long q = qs; q <= last && q < q0 + n_wave; q += J.npix) {
+    float4 r = rad[q - q0];
+    acc = acc + f3(r.x, r.y, r.z) / spp;
+  }
+  o[0] = acc.x;
+  o[1] = acc.y;
+  o[2] = acc.z;
 }
 
 __global__ void k_accumulate(const float4* rad, long long q0, int n_wave, int npix, float spp,
@@ -593,6 +745,152 @@ cudaError_t KernelTimer::collect() {
   return cudaSuccess;
 }
 
+// ---------------------------------------------------------------------------
+// Material sort of the shading queue (RTX_OPT_SORT_MATERIAL): a counting sort
+// of the live paths by the material of their hit (misses last), so that the
+// warps of the shading kernel meet fewer materials.  Paths keep their state
+// slots; only the order the shading kernel visits them changes.
+// ---------------------------------------------------------------------------
+RTX_DEV int mat_key(const DeviceScene& s, const float4* hit, int p) {
+  int tri = __float_as_int(hit[p].x);
+  if (tri < 0) return s.n_mats;
+  return __float_as_int(__ldg(s.shade + 4 * (size_t)tri + 1).w) & 0x7fffffff;
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(PtArgs a, DeviceScene s, int* hist) {
+  extern __shared__ int sh[];
+  const int bins = s.n_mats + 1;
+  for (int b = threadIdx.x; b < bins; b += blockDim.x) sh[b] = 0;
+  __syncthreads();
+  const int n = a.counts[a.depth];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    atomicAdd(&sh[mat_key(s, a.hit, a.queue_in[i])], 1);
+  __syncthreads();
+  for (int b = threadIdx.x; b < bins; b += blockDim.x)
+    if (sh[b]) atomicAdd(&hist[b], sh[b]);
+}
+
+// exclusive prefix sum of the bins into hist[kMaxSortBins + 1 + b]; one block
+__global__ void __launch_bounds__(1024) k_sort_scan(DeviceScene s, int* hist) {
+  __shared__ int part[1024];
+  const int bins = s.n_mats + 1;
+  const int per = (bins + 1023) / 1024;
+  const int b0 = threadIdx.x * per;
+  int sum = 0;
+  for (int b = b0; b < b0 + per && b < bins; ++b) sum += hist[b];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    int v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = part[threadIdx.x] - sum;  // exclusive
+  int* offs = hist + kMaxSortBins + 1;
+  for (int b = b0; b < b0 + per && b < bins; ++b) {
+    offs[b] = run;
+    run += hist[b];
+  }
+}
+
+// lanes with equal keys take consecutive slots with one atomic per key
+__global__ void __launch_bounds__(256) k_sort_scatter(PtArgs a, DeviceScene s, int* hist, int* sorted) {
+  int* offs = hist + kMaxSortBins + 1;
+  const int n = a.counts[a.depth];
+  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    int i = base + threadIdx.x;
+    bool live = i < n;
+    int p = live ? a.queue_in[i] : 0;
+    int key = live ? mat_key(s, a.hit, p) : -1;
+    unsigned act = __ballot_sync(0xffffffffu, live);
+    if (!live) continue;
+    unsigned peers = __match_any_sync(act, key);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(peers) - 1;
+    int slot0 = 0;
+    if (lane == leader) slot0 = atomicAdd(&offs[key], __popc(peers));
+    slot0 = __shfl_sync(peers, slot0, leader);
+    sorted[slot0 + __popc(peers & ((1u << lane) - 1u))] = p;
+  }
+}
+
+// The launch sequence of one wave: raygen, then per vertex extend (skipped at
+// depth 0 when the primary hits are cached), shade and connect.
+template <bool kJobs>
+static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene& s, const CamParams& cam,
+                                 const float4* prim, PtWorkspace* ws, KernelTimer* timer, cudaStream_t st,
+                                 int grid_ext, int grid_con, int grid_sh, int block, int nw, int* launches,
+                                 int* extend_launches) {
+  cudaError_t e;
+  a.queue_in = ws->queue[0];
+  a.queue_out = ws->queue[1];
+  a.depth = 0;
+  k_raygen<kJobs><<<(nw + 255) / 256, 256, 0, st>>>(a, cam, prim);
+  ++*launches;
+  for (int depth = 0; depth < p.max_depth; ++depth) {
+    a.depth = depth;
+    a.queue_in = ws->queue[depth & 1];
+    a.queue_out = ws->queue[(depth + 1) & 1];
+    if (!(prim && depth == 0)) {
+      if ((e = timer->mark(0, st, true))) return e;
+      if (p.traversal == 2) {
+        if (p.count_visits)
+          k_extend_batch<true, true, kJobs><<<grid_ext, block, 0, st>>>(a, s);
+        else
+          k_extend_batch<false, true, kJobs><<<grid_ext, block, 0, st>>>(a, s);
+      } else if (p.traversal == 0 || kJobs) {
+        if (p.count_visits)
+          k_extend_batch<true, false, kJobs><<<grid_ext, block, 0, st>>>(a, s);
+        else
+          k_extend_batch<false, false, kJobs><<<grid_ext, block, 0, st>>>(a, s);
+      } else if (p.count_visits) {
+        k_extend<true><<<grid_ext, block, 0, st>>>(a, s);
+      } else {
+        k_extend<false><<<grid_ext, block, 0, st>>>(a, s);
+      }
+      if ((e = timer->mark(0, st, false))) return e;
+      ++*extend_launches;
+      ++*launches;
+    }
+    if ((e = timer->mark(1, st, true))) return e;
+    if (p.sort_material && s.n_mats + 1 <= kMaxSortBins) {
+      // the shading kernel reads the sorted queue; its output queue is unchanged
+      if ((e = cudaMemsetAsync(ws->mat_hist, 0, (kMaxSortBins + 1) * sizeof(int), st))) return e;
+      size_t shm = (size_t)(s.n_mats + 1) * sizeof(int);
+      k_sort_hist<<<grid_sh, 256, shm, st>>>(a, s, ws->mat_hist);
+      k_sort_scan<<<1, 1024, 0, st>>>(s, ws->mat_hist);
+      k_sort_scatter<<<grid_sh, 256, 0, st>>>(a, s, ws->mat_hist, ws->sorted);
+      *launches += 3;
+      PtArgs as = a;
+      as.queue_in = ws->sorted;
+      k_shade<kJobs><<<grid_sh, block, 0, st>>>(as, s);
+    } else {
+      k_shade<kJobs><<<grid_sh, block, 0, st>>>(a, s);
+    }
+    if ((e = timer->mark(1, st, false))) return e;
+    if ((e = timer->mark(2, st, true))) return e;
+    if (p.traversal == 2) {
+      if (p.count_visits)
+        k_connect_batch<true, true, kJobs><<<grid_con, block, 0, st>>>(a, s);
+      else
+        k_connect_batch<false, true, kJobs><<<grid_con, block, 0, st>>>(a, s);
+    } else if (p.traversal == 0 || kJobs) {
+      if (p.count_visits)
+        k_connect_batch<true, false, kJobs><<<grid_con, block, 0, st>>>(a, s);
+      else
+        k_connect_batch<false, false, kJobs><<<grid_con, block, 0, st>>>(a, s);
+    } else if (p.count_visits) {
+      k_connect<true><<<grid_con, block, 0, st>>>(a, s);
+    } else {
+      k_connect<false><<<grid_con, block, 0, st>>>(a, s);
+    }
+    if ((e = timer->mark(2, st, false))) return e;
+    *launches += 2;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& cam,
                       const PtParams& p, float* d_out, int* err, Counters* d_counters,
                       KernelTimer* timer, cudaStream_t st, int* launches, int* extend_launches,
@@ -602,8 +900,18 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     *why = "max_depth must be in [1, 63]";
     return cudaErrorInvalidValue;
   }
+  const bool jobs = p.n_jobs > 0;
+  if (jobs && (p.per_path || p.traversal == 1)) {
+    *why = "a batch renders images with the binary or 4-wide batch traversal";
+    return cudaErrorInvalidValue;
+  }
   long long npix = (long long)p.W * p.H;
   long long total = npix * p.n_samples;
+  if (jobs) {
+    const PtJob& L = p.h_jobs[p.n_jobs - 1];
+    npix = L.pix_begin + L.npix;
+    total = L.q_begin + (long long)L.npix * L.spp;
+  }
   if (!p.per_path && !p.accumulate &&
       (e = cudaMemsetAsync(d_out, 0, (size_t)npix * 3 * sizeof(float), st)))
     return e;
@@ -619,6 +927,7 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     wave = std::max(1LL << 20, std::min(1LL << 26, fit));
   }
   wave = std::min(wave, total);
+  ws->last_wave = wave;
   if ((e = ws_reserve(ws, (size_t)wave)) != cudaSuccess) return e;
   int block = p.block > 0 ? p.block : 128;
   if (ws->num_sms == 0 || ws->block_cached != block) {
@@ -626,17 +935,23 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, dev);
     int o1 = 0, o2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_extend, k_extend<false>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_extend, k_extend<false>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, false, false>, block, 0);
     ws->occ_extend = std::min(ws->occ_extend, o1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, true>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, true, false>, block, 0);
     ws->occ_extend = std::min(ws->occ_extend, o1);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_connect, k_connect<false>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, false>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, false, true>, block, 0);
+    ws->occ_extend = std::min(ws->occ_extend, o1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_connect, k_connect<false>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, false, false>, block, 0);
     ws->occ_connect = std::min(ws->occ_connect, o2);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, true>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, true, false>, block, 0);
     ws->occ_connect = std::min(ws->occ_connect, o2);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, false, true>, block, 0);
+    ws->occ_connect = std::min(ws->occ_connect, o2);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade<false>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_shade<true>, block, 0);
+    ws->occ_shade = std::min(ws->occ_shade, o1);
     ws->block_cached = block;
   }
   int grid_ext = ws->num_sms * std::max(ws->occ_extend, 1);
@@ -663,6 +978,9 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
   a.k0 = (uint32_t)p.seed;
   a.k1 = (uint32_t)(p.seed >> 32);
   a.min_busy = p.min_busy;
+  a.jobs = p.d_jobs;
+  a.job_q = p.d_job_q;
+  a.n_jobs = p.n_jobs;
   float spp = (float)p.spp;
 
   const float4* prim = nullptr;
@@ -674,9 +992,18 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
       if ((e = cudaMalloc(&ws->prim, (size_t)npix * sizeof(float4))) != cudaSuccess) return e;
       ws->prim_cap = (size_t)npix;
     }
-    int tiles = ((p.W + 7) >> 3) * ((p.H + 7) >> 3);
-    k_primary_cache<<<tiles, 64, 0, st>>>(s, cam, ws->prim, err, d_counters);
-    ++*launches;
+    if (jobs) {
+      for (int j = 0; j < p.n_jobs; ++j) {
+        const PtJob& J = p.h_jobs[j];  // the launch shape only (W, H)
+        int tiles = ((J.cam.W + 7) >> 3) * ((J.cam.H + 7) >> 3);
+        k_primary_cache_job<<<tiles, 64, 0, st>>>(s, p.d_jobs, j, ws->prim, err, d_counters);
+        ++*launches;
+      }
+    } else {
+      int tiles = ((p.W + 7) >> 3) * ((p.H + 7) >> 3);
+      k_primary_cache<<<tiles, 64, 0, st>>>(s, cam, ws->prim, err, d_counters);
+      ++*launches;
+    }
     prim = ws->prim;
   }
 
@@ -685,62 +1012,20 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     a.q0 = q0;
     a.n_wave = nw;
     if ((e = cudaMemsetAsync(ws->counters, 0, 4 * kMaxDepthSlots * sizeof(int), st))) return e;
-    a.queue_in = ws->queue[0];
-    a.queue_out = ws->queue[1];
-    a.depth = 0;
-    k_raygen<<<(nw + 255) / 256, 256, 0, st>>>(a, cam, prim);
-    ++*launches;
-    for (int depth = 0; depth < p.max_depth; ++depth) {
-      a.depth = depth;
-      a.queue_in = ws->queue[depth & 1];
-      a.queue_out = ws->queue[(depth + 1) & 1];
-      if (!(prim && depth == 0)) {
-        if ((e = timer->mark(0, st, true))) return e;
-        if (p.traversal == 2) {
-          if (p.count_visits)
-            k_extend_batch<true, true><<<grid_ext, 128, 0, st>>>(a, s);
-          else
-            k_extend_batch<false, true><<<grid_ext, 128, 0, st>>>(a, s);
-        } else if (p.traversal == 0) {
-          if (p.count_visits)
-            k_extend_batch<true, false><<<grid_ext, 128, 0, st>>>(a, s);
-          else
-            k_extend_batch<false, false><<<grid_ext, 128, 0, st>>>(a, s);
-        } else if (p.count_visits) {
-          k_extend<true><<<grid_ext, 128, 0, st>>>(a, s);
-        } else {
-          k_extend<false><<<grid_ext, 128, 0, st>>>(a, s);
-        }
-        if ((e = timer->mark(0, st, false))) return e;
-        ++*extend_launches;
-        ++*launches;
-      }
-      if ((e = timer->mark(1, st, true))) return e;
-      k_shade<<<grid_sh, 128, 0, st>>>(a, s);
-      if ((e = timer->mark(1, st, false))) return e;
-      if ((e = timer->mark(2, st, true))) return e;
-      if (p.traversal == 2) {
-        if (p.count_visits)
-          k_connect_batch<true, true><<<grid_con, 128, 0, st>>>(a, s);
-        else
-          k_connect_batch<false, true><<<grid_con, 128, 0, st>>>(a, s);
-      } else if (p.traversal == 0) {
-        if (p.count_visits)
-          k_connect_batch<true, false><<<grid_con, 128, 0, st>>>(a, s);
-        else
-          k_connect_batch<false, false><<<grid_con, 128, 0, st>>>(a, s);
-      } else if (p.count_visits) {
-        k_connect<true><<<grid_con, 128, 0, st>>>(a, s);
-      } else {
-        k_connect<false><<<grid_con, 128, 0, st>>>(a, s);
-      }
-      if ((e = timer->mark(2, st, false))) return e;
-      *launches += 2;
+    e = jobs ? wave_launches<true>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,
+                                   extend_launches)
+             : wave_launches<false>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,
+                                    extend_launches);
+    if (e) return e;
+    if (jobs) {
+      k_accumulate_jobs<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(ws->rad, q0, nw, p.d_jobs, p.n_jobs,
+                                                                        npix, d_out);
+    } else {
+      int acc_n = p.per_path ? nw : (int)npix;
+      const bool last = !p.per_path && (p.resolve.display || p.resolve.bytes) && q0 + nw >= total;
+      k_accumulate<<<(acc_n + 255) / 256, 256, 0, st>>>(ws->rad, q0, nw, (int)npix, spp, d_out,
+                                                       p.per_path ? 1 : 0, p.resolve, last ? 1 : 0);
     }
-    int acc_n = p.per_path ? nw : (int)npix;
-    const bool last = !p.per_path && (p.resolve.display || p.resolve.bytes) && q0 + nw >= total;
-    k_accumulate<<<(acc_n + 255) / 256, 256, 0, st>>>(ws->rad, q0, nw, (int)npix, spp, d_out,
-                                                     p.per_path ? 1 : 0, p.resolve, last ? 1 : 0);
     k_tally<<<1, 32, 0, st>>>(a.counts, a.shadow_counts, p.max_depth, prim ? 1 : 0, d_counters);
     *launches += 2;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -137,6 +137,21 @@ struct Resolve {
 constexpr int kResolveBmp = 0, kResolveRgb = 1;
 __host__ __device__ inline size_t bmp_row_bytes(int W) { return ((size_t)W * 3 + 3) & ~(size_t)3; }
 
+// One frame of a multi-scene batch: a camera over one of the merged scenes.
+// Paths of all frames share one index space: frame j owns
+// [q_begin, q_begin + W * H * spp), sample-major like a single render, and
+// pixels [pix_begin, pix_begin + W * H) of the concatenated output.  The
+// random stream of each frame is the one rtx_render_pt would use for its
+// scene, seed and camera, so a batched frame equals the frame rendered alone.
+struct PtJob {
+  long long q_begin, pix_begin;
+  int npix, W, spp, first_sample;
+  int root, root4, e_begin, n_emitters;
+  uint32_t k0, k1;
+  float sky[3], ground[3];
+  CamParams cam;
+};
+
 struct PtParams {
   int W, H, spp, first_sample, n_samples, max_depth;
   uint64_t seed;
@@ -146,11 +161,19 @@ struct PtParams {
   bool accumulate; // add the mean to the output instead of overwriting it
   bool count_visits;
   bool primary_cache;
+  bool sort_material = false;  // counting-sort the shading queue by material
   int traversal;  // RTX_OPT_TRAVERSAL
   int min_busy;   // RTX_OPT_MIN_BUSY
   Resolve resolve;  // fused into the last accumulation when display or bytes is set
+  // multi-scene batch (n_jobs > 0): device job table and its q_begin column,
+  // the host copy for launch sizing; W, H, spp, n_samples, seed are unused
+  int n_jobs = 0;
+  const PtJob* d_jobs = nullptr;
+  const long long* d_job_q = nullptr;
+  const PtJob* h_jobs = nullptr;
 };
 PtWorkspace* pt_workspace_create();
+long long pt_last_wave(const PtWorkspace* ws);
 void pt_workspace_destroy(PtWorkspace* ws);
 cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& cam,
                       const PtParams& p, float* d_out, int* err, Counters* d_counters,
