@@ -352,12 +352,15 @@ def main():
     bytes_per_launch = ext_bytes_frame / ext_launch_per_frame
     achieved = bytes_per_launch / (avg_launch_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
+    # DRAM bytes per launch from the ncu capture in profiles/ (fixed + per-ray
+    # fit, cold L2 per launch), scaled to this run's rays per launch
     traffic = None
     tf = os.path.join(ROOT, "profiles", "k_extend_traffic.txt")
     if os.path.exists(tf):
-        for ln in open(tf):
-            if ln.startswith("dram_bytes_per_extension_ray"):
-                traffic = float(ln.split()[1]) * cs["extension_rays"] / ext_launch_per_frame
+        fit = {ln.split()[0]: float(ln.split()[1]) for ln in open(tf) if ln.startswith("dram_bytes")}
+        if "dram_bytes_per_extension_ray" in fit:
+            traffic = (fit.get("dram_bytes_per_launch_fixed", 0.0) +
+                       fit["dram_bytes_per_extension_ray"] * cs["extension_rays"] / ext_launch_per_frame)
 
     # end to end through the C ABI with pinned host buffers
     ctx.set_option(rt.OPT_ASYNC, 0)

@@ -626,6 +626,8 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   s.n_tris = n;
   s.n_emitters = (int)c->emitters.size();
   s.n_mats = n_mat;
+  s.textured = 0;
+  for (int m = 0; m < n_mat; ++m) s.textured |= mats[RTX_MATERIAL_FLOATS * (size_t)m + 21] != 0.0f;
   for (int k = 0; k < 3; ++k) {
     s.sky[k] = sky[k];
     s.ground[k] = ground[k];
@@ -753,6 +755,9 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   s.n_tris = tri_base;
   s.n_emitters = (int)emit.size();
   s.n_mats = mat_base;
+  s.textured = 0;
+  for (size_t m = 0; m < mats.size() / RTX_MATERIAL_FLOATS; ++m)
+    s.textured |= mats[RTX_MATERIAL_FLOATS * m + 21] != 0.0f;
   c->has_batch = true;
   if (c->graph) {
     cudaGraphExecDestroy(c->graph);

@@ -38,7 +38,8 @@ namespace nn {
 
 namespace {
 
-constexpr int kSlice = 64;  // K per shared-memory slice
+constexpr int kSlice = 64;    // K per shared-memory slice
+constexpr int kThreads = 256;  // 8 warps: all gather, warps w and w + 4 share accumulator lanes
 
 struct Pix {
   int n, y, x;
@@ -179,7 +180,7 @@ __device__ __forceinline__ bool conv_pipeline(int n, uint64_t* bars, Load&& load
 // forward
 // ---------------------------------------------------------------------------
 template <int S>
-__global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
+__global__ void __launch_bounds__(kThreads, 2) k_conv_fwd(ConvFwd a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t bars[S];
   __shared__ uint32_t tmem_slot;
@@ -194,13 +195,13 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
   const uint32_t s0 = tc::smem_u32(smem);
   const int K = 9 * a.Cin;
   const int n_slices = (K + kSlice - 1) / kSlice;
-  // this thread's 8 tile rows (tid >> 3) + 16 i and its chunk column tid & 7
+  // this thread's 4 tile rows (tid >> 3) + 32 i and its chunk column tid & 7
   const int kc = tid & 7;
-  Pix px[8];
-  bool pv[8];
+  Pix px[4];
+  bool pv[4];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    long long p = m0 + (tid >> 3) + 16 * i;
+  for (int i = 0; i < 4; ++i) {
+    long long p = m0 + (tid >> 3) + 32 * i;
     pv[i] = p < P;
     px[i] = pix_of(pv[i] ? p : 0, a.H, a.W);
   }
@@ -212,12 +213,12 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
     const int t = kv ? k / a.Cin : 0, c = k - t * a.Cin;
     const int dy = t / 3 - 1, dx = t % 3 - 1;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int row = (tid >> 3) + 16 * i;
+    for (int i = 0; i < 4; ++i) {
+      const int row = (tid >> 3) + 32 * i;
       const bf16* p = (pv[i] && kv) ? src_ptr(a.s1, a.s2, a.H, a.W, px[i].n, px[i].y + dy, px[i].x + dx, c) : nullptr;
       chunk_async(sa + tc::tile_offset(row, kc * 8, kSlice), p, a.s1.ptr);
     }
-    for (int ch = tid; ch < a.Cout * 8; ch += 128) {
+    for (int ch = tid; ch < a.Cout * 8; ch += kThreads) {
       const int row = ch >> 3, kk = (ch & 7) * 8;
       const bf16* p = k0 + kk < K ? a.w + (size_t)row * K + k0 + kk : nullptr;
       chunk_async(sb + tc::tile_offset(row, kk, kSlice), p, a.w);
@@ -233,9 +234,11 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
   const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
   if (ok) {
-    const long long p = m0 + warp * 32 + lane;
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c0 = 0; c0 < a.Cout; c0 += 8) {
+    // warp w reads accumulator lanes 32 (w % 4) .. + 31, half w / 4 of the columns
+    const int lw = warp & 3, half = a.Cout >> 1;
+    const long long p = m0 + lw * 32 + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
+    for (int c0 = (warp >> 2) * half; c0 < (warp >> 2) * half + half; c0 += 8) {
       float v[8];
       tc::tmem_ld8(taddr + c0, v);
       if (p < P) {
@@ -258,7 +261,7 @@ __global__ void __launch_bounds__(128) k_conv_fwd(ConvFwd a) {
 // data gradient
 // ---------------------------------------------------------------------------
 template <int S>
-__global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
+__global__ void __launch_bounds__(kThreads, 2) k_conv_dgrad(ConvDgrad a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t bars[S];
   __shared__ uint32_t tmem_slot;
@@ -276,11 +279,11 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
   const int K = 9 * a.Cout;
   const int n_slices = (K + kSlice - 1) / kSlice;
   const int kc = tid & 7;
-  Pix px[8];
-  bool pv[8];
+  Pix px[4];
+  bool pv[4];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    long long p = m0 + (tid >> 3) + 16 * i;
+  for (int i = 0; i < 4; ++i) {
+    long long p = m0 + (tid >> 3) + 32 * i;
     pv[i] = p < P;
     px[i] = pix_of(pv[i] ? p : 0, a.H, a.W);
   }
@@ -292,15 +295,15 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
     const int t = kv ? k / a.Cout : 0, o = k - t * a.Cout;
     const int dy = t / 3 - 1, dx = t % 3 - 1;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int row = (tid >> 3) + 16 * i;
+    for (int i = 0; i < 4; ++i) {
+      const int row = (tid >> 3) + 32 * i;
       const int yy = px[i].y - dy, xx = px[i].x - dx;
       const bf16* p = (pv[i] && kv && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
                           ? a.dout + (((size_t)px[i].n * a.H + yy) * a.W + xx) * a.Cout + o
                           : nullptr;
       chunk_async(sa + tc::tile_offset(row, kc * 8, kSlice), p, a.dout);
     }
-    for (int ch = tid; ch < NT * 8; ch += 128) {
+    for (int ch = tid; ch < NT * 8; ch += kThreads) {
       const int row = ch >> 3, kk = (ch & 7) * 8;
       const bf16* p = k0 + kk < K ? a.wt + (size_t)(n0 + row) * K + k0 + kk : nullptr;
       chunk_async(sb + tc::tile_offset(row, kk, kSlice), p, a.wt);
@@ -316,10 +319,11 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
   const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
   if (ok) {
-    const long long p = m0 + warp * 32 + lane;
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    const int lw = warp & 3, half = NT >> 1;
+    const long long p = m0 + lw * 32 + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
     Pix q = pix_of(p < P ? p : 0, a.H, a.W);
-    for (int c0 = 0; c0 < NT; c0 += 8) {
+    for (int c0 = (warp >> 2) * half; c0 < (warp >> 2) * half + half; c0 += 8) {
       float v[8];
       tc::tmem_ld8(taddr + c0, v);
       if (p < P) {
@@ -341,7 +345,7 @@ __global__ void __launch_bounds__(128) k_conv_dgrad(ConvDgrad a) {
 // weight gradient
 // ---------------------------------------------------------------------------
 template <int S>
-__global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
+__global__ void __launch_bounds__(kThreads, 2) k_conv_wgrad(ConvWgrad a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t bars[S];
   __shared__ uint32_t tmem_slot;
@@ -371,8 +375,8 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
     const uint32_t sa = s0 + st * stage, sb = sa + a_bytes;
     const int q0 = pb + slice * kSlice;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int kp = (tid >> 4) + 8 * i;  // pixel within the slice
+    for (int i = 0; i < 4; ++i) {
+      const int kp = (tid >> 4) + 16 * i;  // pixel within the slice
       const int p = q0 + kp;
       const bf16* src = nullptr;
       if (p < pe && jv) {
@@ -382,7 +386,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
       }
       chunk_async(sa + tc::tile_offset_mn(rg * 8, kp, 128), src, a.s1.ptr);
     }
-    for (int ch = tid; ch < ng * kSlice; ch += 128) {
+    for (int ch = tid; ch < ng * kSlice; ch += kThreads) {
       const int og = ch % ng, kp = ch / ng;
       const int p = q0 + kp;
       const bf16* src = p < pe ? a.dout + (size_t)p * a.Cout + og * 8 : nullptr;
@@ -399,9 +403,10 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
   const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
   if (ok && n_slices > 0) {
-    const int jj = j0 + warp * 32 + lane;  // this thread's accumulator row
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c0 = 0; c0 < a.Cout; c0 += 8) {
+    const int lw = warp & 3, half = a.Cout >> 1;
+    const int jj = j0 + lw * 32 + lane;  // this thread's accumulator row
+    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
+    for (int c0 = (warp >> 2) * half; c0 < (warp >> 2) * half + half; c0 += 8) {
       float v[8];
       tc::tmem_ld8(taddr + c0, v);
       if (jj < J)
@@ -413,9 +418,9 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(ConvWgrad a) {
 }
 
 // ---------------------------------------------------------------------------
-// Stages of the ring for a B tile of nb rows: 4 / 3 / 2 stages keep a CTA's
-// shared memory at or below 96 KB (two CTAs per SM).
-static int stages_for(int nb) { return nb <= 64 ? 4 : (nb <= 128 ? 3 : 2); }
+// Stages of the ring for a B tile of nb rows: 3 stages up to 128 rows, 2
+// beyond (72 KB per CTA for nb <= 64, at most 96 KB otherwise).
+static int stages_for(int nb) { return nb <= 128 ? 3 : 2; }
 
 template <class K4, class K3, class K2, class Args>
 static cudaError_t launch_staged(K4 k4, K3 k3, K2 k2, int stages, dim3 grid, size_t stage_bytes, const Args& a,
@@ -424,13 +429,13 @@ static cudaError_t launch_staged(K4 k4, K3 k3, K2 k2, int stages, dim3 grid, siz
   cudaError_t e;
   if (stages == 4) {
     if ((e = cudaFuncSetAttribute(k4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
-    k4<<<grid, 128, smem, st>>>(a);
+    k4<<<grid, kThreads, smem, st>>>(a);
   } else if (stages == 3) {
     if ((e = cudaFuncSetAttribute(k3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
-    k3<<<grid, 128, smem, st>>>(a);
+    k3<<<grid, kThreads, smem, st>>>(a);
   } else {
     if ((e = cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
-    k2<<<grid, 128, smem, st>>>(a);
+    k2<<<grid, kThreads, smem, st>>>(a);
   }
   return cudaGetLastError();
 }

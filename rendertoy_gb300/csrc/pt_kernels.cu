@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(64) k_primary_cache_job(DeviceScene s, const P
   primary_px(sj, J.cam, prim + J.pix_begin, err, ctr);
 }
 
-template <bool kJobs>
+template <bool kJobs, bool kTex>
 __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceScene s) {
   int n = a.counts[a.depth];
   const int depth = a.depth;
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
     Mat m = load_mat(mrec);
     F3 pos = o + d * t;  // BVH::Intersect: src + t * direction
     F3 N = shading_normal(s, tri, u, v, s0, s1, info < 0);
-    if (__ldg(mrec + 21) != 0.0f) m.base_color = textured_base(mrec, pos, N, s.perm);
+    if (kTex && __ldg(mrec + 21) != 0.0f) m.base_color = textured_base(mrec, pos, N, s.perm);
     F3 ff = N;
     float eta;
     if (dot(d, ff) > 0.0f) {  // renderer.cpp:288-298
@@ -864,9 +864,14 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
       *launches += 3;
       PtArgs as = a;
       as.queue_in = ws->sorted;
-      k_shade<kJobs><<<grid_sh, block, 0, st>>>(as, s);
+      if (s.textured)
+        k_shade<kJobs, true><<<grid_sh, block, 0, st>>>(as, s);
+      else
+        k_shade<kJobs, false><<<grid_sh, block, 0, st>>>(as, s);
+    } else if (s.textured) {
+      k_shade<kJobs, true><<<grid_sh, block, 0, st>>>(a, s);
     } else {
-      k_shade<kJobs><<<grid_sh, block, 0, st>>>(a, s);
+      k_shade<kJobs, false><<<grid_sh, block, 0, st>>>(a, s);
     }
     if ((e = timer->mark(1, st, false))) return e;
     if ((e = timer->mark(2, st, true))) return e;
@@ -949,9 +954,11 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     ws->occ_connect = std::min(ws->occ_connect, o2);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, false, true>, block, 0);
     ws->occ_connect = std::min(ws->occ_connect, o2);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade<false>, block, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_shade<true>, block, 0);
-    ws->occ_shade = std::min(ws->occ_shade, o1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade<false, false>, block, 0);
+    for (auto k : {k_shade<true, false>, k_shade<false, true>, k_shade<true, true>}) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k, block, 0);
+      ws->occ_shade = std::min(ws->occ_shade, o1);
+    }
     ws->block_cached = block;
   }
   int grid_ext = ws->num_sms * std::max(ws->occ_extend, 1);

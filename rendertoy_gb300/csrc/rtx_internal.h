@@ -55,6 +55,7 @@ struct DeviceScene {
   const uint8_t* __restrict__ perm;  // 256-entry permutation of the Perlin texture
   int root;  // node index (>= 0), leaf ref (< 0) or kEmptyRoot
   int n_tris, n_emitters, n_mats;
+  int textured;  // some material has a procedural texture
   float sky[3], ground[3];
 };
 
