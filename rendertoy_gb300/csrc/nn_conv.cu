@@ -258,6 +258,159 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_fwd(ConvFwd a) {
 }
 
 // ---------------------------------------------------------------------------
+// forward, row tiles: a CTA takes 128 consecutive pixels of one image row.
+// Per slice of 16 input channels it copies the 3-row halo (pixels x0 - 1 ..
+// x0 + 128, 2 chunks of 8 channels each) once; the nine taps are the same
+// halo read through descriptors shifted by whole pixels (rows of the
+// K-major layout are 16 B apart and the two channel chunks one halo row
+// apart, so every shift is a legal start address).  One third of the gather
+// traffic of k_conv_fwd, with one address per copied pixel chunk.
+// ---------------------------------------------------------------------------
+constexpr int kHalo = 130;                                  // pixels x0 - 1 .. x0 + 128
+constexpr uint32_t kHaloBytes = 3 * 2 * kHalo * 16;          // rows x chunks x pixels x 16 B
+
+template <int S>
+__global__ void __launch_bounds__(kThreads, 2) k_conv_fwd_row(ConvFwd a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bars[S];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int x0 = blockIdx.x * 128, y = blockIdx.y, n = blockIdx.z;
+  const uint32_t ncols = a.Cout <= 32 ? 32 : (a.Cout <= 64 ? 64 : (a.Cout <= 128 ? 128 : 256));
+  const uint32_t tap_bytes = (uint32_t)a.Cout * 32, stage = kHaloBytes + 9 * tap_bytes;
+  tc_begin(&tmem_slot, bars, S, ncols);
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = tc::make_idesc_bf16(128, a.Cout);
+  const uint32_t s0 = tc::smem_u32(smem);
+  const int n_slices = a.Cin / 16;
+  auto load = [&](int slice, int st) {
+    if (slice >= n_slices) return;
+    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
+    const int c0 = slice * 16;
+    // chunk c of pixel h of halo row r: neighbouring threads take the two
+    // chunks of one pixel (32 contiguous bytes)
+    for (int i = tid; i < 3 * kHalo * 2; i += kThreads) {
+      const int c = i & 1, h = (i >> 1) % kHalo, r = (i >> 1) / kHalo;
+      const bf16* p = src_ptr(a.s1, a.s2, a.H, a.W, n, y + r - 1, x0 + h - 1, c0 + 8 * c);
+      chunk_async(sh + ((r * 2 + c) * kHalo + h) * 16, p, a.s1.ptr);
+    }
+    // tap t: Cout x 16 K-major tile of w[o][t][c0 .. c0 + 15]
+    for (int i = tid; i < 9 * a.Cout * 2; i += kThreads) {
+      const int kc = i & 1, o = (i >> 1) % a.Cout, t = (i >> 1) / a.Cout;
+      chunk_async(sb + t * tap_bytes + tc::tile_offset(o, 8 * kc, 16), a.w + ((size_t)o * 9 + t) * a.Cin + c0 + 8 * kc,
+                  a.w);
+    }
+  };
+  auto mma = [&](int st, bool first) {
+    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const int dy = t / 3 - 1, dx = t % 3 - 1;
+      // A: pixel groups 128 B apart (SBO), channel chunks one halo row apart (LBO)
+      const uint64_t ad = tc::make_desc(sh + ((dy + 1) * 2 * kHalo + 1 + dx) * 16, kHalo * 16, 128);
+      const uint64_t bd = tc::make_desc(sb + t * tap_bytes, 128, 256);
+      tc::mma_bf16(tmem, ad, bd, idesc, !first || t > 0);
+    }
+  };
+  const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
+  tc::fence_after();
+  if (ok) {
+    const int lw = warp & 3, half = a.Cout >> 1;
+    const int x = x0 + lw * 32 + lane;
+    const size_t p = ((size_t)n * a.H + y) * a.W + x;
+    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
+    for (int c0 = (warp >> 2) * half; c0 < (warp >> 2) * half + half; c0 += 8) {
+      float v[8];
+      tc::tmem_ld8(taddr + c0, v);
+      if (x < a.W) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          if (a.bias) v[i] += a.bias[c0 + i];
+          if (a.relu) v[i] = fmaxf(v[i], 0.0f);
+        }
+        if (a.out) *reinterpret_cast<uint4*>(a.out + p * a.Cout + c0) = f32_to_bf16x8(v);
+        if (a.out_f32)
+#pragma unroll
+          for (int i = 0; i < 8; ++i) a.out_f32[p * a.Cout + c0 + i] = v[i];
+      }
+    }
+  }
+  tc_end(tmem, ncols);
+}
+
+// data gradient, row tiles: din[p] = sum_t dout[p - off(t)] wt_t, the same
+// halo scheme over dout (slices of 16 of its channels, shifts negated)
+template <int S>
+__global__ void __launch_bounds__(kThreads, 2) k_conv_dgrad_row(ConvDgrad a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bars[S];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int x0 = blockIdx.x * 128, y = blockIdx.y;
+  const int n = blockIdx.z / ((a.Cin + 255) / 256);
+  const int n0 = (blockIdx.z % ((a.Cin + 255) / 256)) * 256;
+  const int NT = min(256, a.Cin - n0);
+  const uint32_t ncols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
+  const uint32_t tap_bytes = (uint32_t)min(256, a.Cin) * 32, stage = kHaloBytes + 9 * tap_bytes;
+  tc_begin(&tmem_slot, bars, S, ncols);
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = tc::make_idesc_bf16(128, NT);
+  const uint32_t s0 = tc::smem_u32(smem);
+  const int n_slices = a.Cout / 16;
+  auto load = [&](int slice, int st) {
+    if (slice >= n_slices) return;
+    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
+    const int o0 = slice * 16;
+    for (int i = tid; i < 3 * kHalo * 2; i += kThreads) {
+      const int c = i & 1, h = (i >> 1) % kHalo, r = (i >> 1) / kHalo;
+      const int yy = y + r - 1, xx = x0 + h - 1;
+      const bf16* p = (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
+                          ? a.dout + (((size_t)n * a.H + yy) * a.W + xx) * a.Cout + o0 + 8 * c
+                          : nullptr;
+      chunk_async(sh + ((r * 2 + c) * kHalo + h) * 16, p, a.dout);
+    }
+    for (int i = tid; i < 9 * NT * 2; i += kThreads) {
+      const int kc = i & 1, row = (i >> 1) % NT, t = (i >> 1) / NT;
+      chunk_async(sb + t * tap_bytes + tc::tile_offset(row, 8 * kc, 16),
+                  a.wt + ((size_t)(n0 + row) * 9 + t) * a.Cout + o0 + 8 * kc, a.wt);
+    }
+  };
+  auto mma = [&](int st, bool first) {
+    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const int dy = t / 3 - 1, dx = t % 3 - 1;
+      const uint64_t ad = tc::make_desc(sh + ((1 - dy) * 2 * kHalo + 1 - dx) * 16, kHalo * 16, 128);
+      const uint64_t bd = tc::make_desc(sb + t * tap_bytes, 128, 256);
+      tc::mma_bf16(tmem, ad, bd, idesc, !first || t > 0);
+    }
+  };
+  const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
+  tc::fence_after();
+  if (ok) {
+    const int lw = warp & 3, half = NT >> 1;
+    const int x = x0 + lw * 32 + lane;
+    const size_t p = ((size_t)n * a.H + y) * a.W + x;
+    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
+    for (int c0 = (warp >> 2) * half; c0 < (warp >> 2) * half + half; c0 += 8) {
+      float v[8];
+      tc::tmem_ld8(taddr + c0, v);
+      if (x < a.W) {
+        if (a.mask_relu) {
+          float sv[8];
+          bf16x8_to_f32(src_chunk(a.s1, a.s2, a.N, a.H, a.W, n, y, x, n0 + c0), sv);
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            if (!(sv[i] > 0.0f)) v[i] = 0.0f;
+        }
+        *reinterpret_cast<uint4*>(a.din + p * a.Cin + n0 + c0) = f32_to_bf16x8(v);
+      }
+    }
+  }
+  tc_end(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
 // data gradient
 // ---------------------------------------------------------------------------
 template <int S>
@@ -440,9 +593,21 @@ static cudaError_t launch_staged(K4 k4, K3 k3, K2 k2, int stages, dim3 grid, siz
   return cudaGetLastError();
 }
 
+// Row tiles pay off once a row holds at least half a tile; they need input
+// slices of 16 channels and a grid that fits the y / z limits.
+static bool use_rows(int N, int H, int W, int Ck, int nz = 1) {
+  return W >= 64 && Ck % 16 == 0 && H <= 65535 && (long long)N * nz <= 65535;
+}
+
 cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
   if (a.Cout % 16 || a.Cout > 256 || a.Cin % 8) return cudaErrorInvalidValue;
+  if (use_rows(a.N, a.H, a.W, a.Cin)) {
+    size_t stage = kHaloBytes + (size_t)9 * a.Cout * 32;
+    dim3 grid((a.W + 127) / 128, a.H, a.N);
+    return launch_staged(k_conv_fwd_row<3>, k_conv_fwd_row<3>, k_conv_fwd_row<2>, stage <= 34 * 1024 ? 3 : 2,
+                         grid, stage, a, st);
+  }
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
   return launch_staged(k_conv_fwd<4>, k_conv_fwd<3>, k_conv_fwd<2>, stages_for(a.Cout),
                        dim3((unsigned)((P + 127) / 128)), stage, a, st);
@@ -451,6 +616,13 @@ cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st) {
 cudaError_t conv_dgrad(const ConvDgrad& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
   if (a.Cin % 16 || a.Cout % 8) return cudaErrorInvalidValue;
+  const int nt = (a.Cin + 255) / 256;
+  if (use_rows(a.N, a.H, a.W, a.Cout, nt)) {
+    size_t stage = kHaloBytes + (size_t)9 * std::min(256, a.Cin) * 32;
+    dim3 grid((a.W + 127) / 128, a.H, a.N * nt);
+    return launch_staged(k_conv_dgrad_row<3>, k_conv_dgrad_row<3>, k_conv_dgrad_row<2>,
+                         stage <= 34 * 1024 ? 3 : 2, grid, stage, a, st);
+  }
   int nb = std::min(256, a.Cin);
   size_t stage = 128 * kSlice * 2 + (size_t)nb * kSlice * 2;
   return launch_staged(k_conv_dgrad<4>, k_conv_dgrad<3>, k_conv_dgrad<2>, stages_for(nb),

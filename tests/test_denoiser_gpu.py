@@ -36,6 +36,11 @@ CASES = [  # N, H, W, C1, up1, C2, Cout, relu
     (1, 16, 16, 160, 1, 128, 128, 1),  # decoder: upsampled 160 + skip 128 = 288
     (2, 8, 12, 64, 0, 0, 160, 1),      # Cout 160: two weight-gradient row tiles
     (1, 32, 32, 64, 1, 32, 32, 1),     # decoder at full resolution: 96 inputs
+    # rows of 64 pixels or more take the row-tile kernels
+    (1, 3, 200, 32, 0, 0, 32, 1),      # two row tiles, the second partial
+    (2, 2, 128, 64, 1, 32, 64, 1),     # upsampled source + skip in row tiles
+    (1, 2, 64, 160, 1, 128, 128, 1),   # 288 inputs: two data-gradient tiles
+    (1, 2, 96, 16, 0, 0, 16, 0),       # the output layer's shape
 ]
 
 
