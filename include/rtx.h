@@ -247,13 +247,15 @@ int rtx_render_batch(rtx_context* ctx, int n_jobs, const rtx_job* jobs,
  * best of two) over BVH leaf sizes 2 / 4 / 8 -- rebuilding the batch from
  * `scenes` for each; scenes = NULL keeps the uploaded batch and its leaf
  * size -- then threads per block 64 / 128 x paths per wave 2^20, 2^22, 2^24,
- * auto, coordinate-wise from the context's current options.  The fastest
- * setting stays on the context (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK,
- * RTX_OPT_WAVE_PATHS) and the batch is left built with it. */
+ * auto, then material-sorted shading on / off, coordinate-wise from the
+ * context's current options.  The fastest setting stays on the context
+ * (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK, RTX_OPT_WAVE_PATHS,
+ * RTX_OPT_SORT_MATERIAL) and the batch is left built with it. */
 typedef struct rtx_tune_result {
   int64_t block, wave_paths, leaf_size;
   double ms, ms_default;       /* frame time chosen / at the starting options */
   int trials;
+  int sort_material;           /* RTX_OPT_SORT_MATERIAL chosen */
 } rtx_tune_result;
 int rtx_batch_autotune(rtx_context* ctx, int n_scenes,
                        const rtx_scene_desc* scenes, int n_jobs,

@@ -1144,6 +1144,17 @@ int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scene
     }
   c->block = (int)res.block;
   c->wave_paths = res.wave_paths;
+  // material-sorted shading helps scenes with many materials and costs a
+  // little where there are few: keep whichever is faster
+  res.sort_material = c->sort_material ? 1 : 0;
+  c->sort_material = !c->sort_material;
+  if ((r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms))) return done(r);
+  ++res.trials;
+  if (ms < res.ms) {
+    res.ms = ms;
+    res.sort_material = c->sort_material ? 1 : 0;
+  }
+  c->sort_material = res.sort_material != 0;
   *out = res;
   return done(RTX_OK);
 }

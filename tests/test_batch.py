@@ -115,7 +115,8 @@ def test_autotune(ctx):
     jobs = [dict(j, spp=j["spp"] * 4) for j in JOBS]
     try:
         res = ctx.batch_autotune(jobs, 6, scene_list=sc)
-        assert res["trials"] >= 8 and res["ms"] <= res["ms_default"]
+        assert res["trials"] >= 9 and res["ms"] <= res["ms_default"]
+        assert ctx.get_option(rt.OPT_SORT_MATERIAL) == res["sort_material"]
         assert res["leaf_size"] in (2, 4, 8) and res["block"] in (64, 128)
         assert ctx.get_option(rt.OPT_BLOCK) == res["block"]
         assert ctx.get_option(rt.OPT_LEAF_SIZE) == res["leaf_size"]
@@ -127,3 +128,4 @@ def test_autotune(ctx):
         ctx.set_option(rt.OPT_BLOCK, 128)
         ctx.set_option(rt.OPT_WAVE_PATHS, 0)
         ctx.set_option(rt.OPT_LEAF_SIZE, 4)
+        ctx.set_option(rt.OPT_SORT_MATERIAL, 0)
