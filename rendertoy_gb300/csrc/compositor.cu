@@ -60,6 +60,49 @@ __global__ void k_convolve(const float* __restrict__ in, float* __restrict__ out
   o[2] = acc.z;
 }
 
+// The same convolution from a shared-memory tile: a block fills its 32 x 8
+// pixels plus the kernel's halo once (every element through reflect_index,
+// so RenderToy's reflection, including its row wrap, is kept), then each
+// thread sums its taps in the same order as k_convolve.
+constexpr int kConvTX = 32, kConvTY = 8;
+
+__global__ void __launch_bounds__(kConvTX * kConvTY) k_convolve_tiled(const float* __restrict__ in,
+                                                                     float* __restrict__ out, int W, int H,
+                                                                     const float* __restrict__ k, int kr,
+                                                                     int kc, int flags) {
+  extern __shared__ float sm[];
+  float* wsm = sm;            // kr * kc weights
+  float* tile = sm + kr * kc; // (kConvTY + kr - 1) x (kConvTX + kc - 1) pixels
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * kConvTX, y0 = blockIdx.y * kConvTY;
+  const int r2 = kr >> 1, c2 = kc >> 1, tw = kConvTX + kc - 1, th = kConvTY + kr - 1;
+  for (int i = tid; i < kr * kc; i += blockDim.x) wsm[i] = k[i];
+  for (int i = tid; i < tw * th; i += blockDim.x) {
+    const int ty = i / tw, tx = i - ty * tw;
+    F3 p = load_px(in, reflect_index((long long)y0 - r2 + ty, (long long)x0 - c2 + tx, W, H));
+    tile[3 * i] = p.x;
+    tile[3 * i + 1] = p.y;
+    tile[3 * i + 2] = p.z;
+  }
+  __syncthreads();
+  const int lx = tid % kConvTX, ly = tid / kConvTX;
+  const int x = x0 + lx, y = y0 + ly;
+  if (x >= W || y >= H) return;
+  F3 acc = f3s(0.0f);
+  for (int ii = 0; ii < kr; ++ii)
+    for (int jj = 0; jj < kc; ++jj) {
+      const float* q = tile + 3 * ((ly + ii) * tw + lx + jj);
+      acc = acc + f3(q[0], q[1], q[2]) * wsm[ii * kc + jj];
+    }
+  if (flags & kAbs) acc = f3(fabsf(acc.x), fabsf(acc.y), fabsf(acc.z));
+  if (flags & kLength) acc = f3s(length(acc));
+  if (flags & kNormalize) acc = normalized(acc);
+  float* o = out + 3 * ((size_t)y * W + x);
+  o[0] = acc.x;
+  o[1] = acc.y;
+  o[2] = acc.z;
+}
+
 // Horizontal pass (1 x size kernel): a block computes kTileX pixels of one row
 // from a shared-memory copy of the row segment plus its halo.
 constexpr int kTileX = 256;
@@ -185,8 +228,14 @@ __global__ void k_add(const float* __restrict__ a, const float* __restrict__ b,
 
 cudaError_t launch_convolve(const float* in, float* out, int W, int H, const float* d_k, int kr,
                             int kc, int flags, cudaStream_t st, int* launches) {
-  dim3 grid((W + 127) / 128, H);
-  k_convolve<<<grid, 128, 0, st>>>(in, out, W, H, d_k, kr, kc, flags);
+  const size_t smem = sizeof(float) * ((size_t)kr * kc + 3 * (size_t)(kConvTY + kr - 1) * (kConvTX + kc - 1));
+  if (smem <= 48 * 1024) {
+    dim3 grid((W + kConvTX - 1) / kConvTX, (H + kConvTY - 1) / kConvTY);
+    k_convolve_tiled<<<grid, kConvTX * kConvTY, smem, st>>>(in, out, W, H, d_k, kr, kc, flags);
+  } else {
+    dim3 grid((W + 127) / 128, H);
+    k_convolve<<<grid, 128, 0, st>>>(in, out, W, H, d_k, kr, kc, flags);
+  }
   ++*launches;
   return cudaGetLastError();
 }
