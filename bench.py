@@ -13,13 +13,16 @@ result.  Metric: Msamples/s (pixel samples per second), with Mrays/s beside it.
           is copied back after the render and each filter copies its image in
           and out, as RenderToy's Image does; host wall clock.
   roofline : the closest-hit traversal kernel (k_extend), algorithmic bytes =
-          BVH nodes visited x 64 B + triangles tested x 48 B + 52 B of ray I/O
-          per ray, counted by an instrumented (untimed) run of the same step.
+          BVH nodes visited x node size (112 B for the default 4-wide tree,
+          64 B binary) + triangles tested x 48 B + 52 B of ray I/O per ray,
+          counted by an instrumented (untimed) run of the same step.
   cpu_baseline : the oracle's restatement of RenderToy's renderer (octree +
           priority-queue traversal) on the host cores, on a bounded sample.
   denoiser : the learned denoiser outside the timed frames: one Adam step on a
           32 x 256^2 minibatch and one 1920 x 1088 inference, device time and
           tensor-core TFLOP/s against the measured BF16 peak.
+  compositor : each filter timed alone on the resident image, achieved GB/s of
+          its algorithmic bytes as a fraction of the measured HBM bandwidth.
 
 ``--impl reference`` times RenderToy's CPU path on the same workload (its
 compiled sources where they run here, otherwise the oracle restatement).
@@ -101,6 +104,37 @@ def denoiser_block(ctx, rank):
             "roofline": {"bound": "tensor", "achieved": train_tf, "peak": peak, "peak_kind": kind,
                          "unit": "TFLOP/s", "frac": train_tf / peak,
                          "note": "whole training step (all 88 launches) against the bf16 burst peak"}}
+
+
+def compositor_block(ctx, img, tmp, out, flush):
+    """The Compositor filters timed alone on the resident 1024^2 image (the
+    library's CUDA events, median of 10; L2 flushed before each run):
+    algorithmic bytes per pixel = 12 B read + 12 B written per pass (blur: two
+    passes; 5 x 5 convolution: one; bloom: extract + blur x, then blur y + add
+    = 12 + 12 + 24 + 12)."""
+    import torch
+    peak, kind = peaks()
+
+    def med(fn):
+        t = []
+        for _ in range(12):
+            flush.zero_()
+            torch.cuda.synchronize()
+            fn()
+            t.append(ctx.stats()["last_gpu_ms"])
+        return float(np.median(t[2:]))
+
+    px = RES * RES
+    res = {}
+    for name, fn, bpp in (("gaussian_blur_49", lambda: ctx.gaussian_blur(img, BLUR_SIZE, BLUR_SIGMA, out=tmp), 48),
+                          ("convolve_5x5", lambda: ctx.convolve(tmp, EDGE5, absval=True, out=out), 24),
+                          ("bloom_49", lambda: ctx.bloom(img, BLUR_SIZE, BLUR_SIGMA, 1.0, out=tmp), 60)):
+        ms = med(fn)
+        gbs = bpp * px / (ms * 1e-3) / 1e9
+        res[name] = {"ms": ms, "bytes_per_pixel": bpp, "achieved_gbs": gbs, "frac_hbm": gbs / peak}
+    res["peak_gbs"] = peak
+    res["peak_kind"] = kind
+    return res
 
 
 class Clocks:
@@ -409,7 +443,8 @@ def main():
     ctx.set_option(rt.OPT_COUNT_VISITS, 0)
     # kernels per step: the render's launches + blur (2) + convolution (1)
     launches = (cs["kernel_launches"] + 3) * args.steps
-    ext_bytes_frame = cs["ext_node_visits"] * 64 + cs["ext_tri_tests"] * 48 + cs["extension_rays"] * 52
+    ext_bytes_frame = (cs["ext_node_visits"] * cs["node_bytes"] + cs["ext_tri_tests"] * 48 +
+                       cs["extension_rays"] * 52)
     frames = args.steps
     ext_launch_per_frame = ext_launch / frames
     avg_launch_ms = ext_ms / ext_launch
@@ -444,6 +479,7 @@ def main():
            "h2d_bytes_per_step": 2 * img_bytes + 84 + BLUR_SIZE * 4 + 25 * 4,
            "d2h_bytes_per_step": 3 * img_bytes, "steps": e2e_steps}
 
+    comp = compositor_block(ctx, img, blur, edge, flush)
     dn = denoiser_block(ctx, rank)
 
     cpu = None
@@ -479,6 +515,7 @@ def main():
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "denoiser": dn,
+            "compositor": comp,
         }
         print(json.dumps(line))
     if ws > 1:

@@ -91,10 +91,11 @@ enum rtx_option {
   RTX_OPT_ACCUMULATE = 9,     /* 0/1: rtx_render_pt adds its mean to out_rgb
                                  (RenderToy's buffer +=, renderer.cpp:261)
                                  instead of overwriting it */
-  RTX_OPT_TRAVERSAL = 10,     /* traversal kernels: 0 (default) = binary tree, one ray
-                                 per lane until the warp's batch is done;
-                                 1 = binary tree, lanes take new rays as theirs
-                                 finish (while-while); 2 = 4-wide tree, batch */
+  RTX_OPT_TRAVERSAL = 10,     /* traversal kernels: 0 = binary tree, one ray per
+                                 lane until the warp's batch is done; 1 = binary
+                                 tree, lanes take new rays as theirs finish
+                                 (while-while; single scenes only); 2 (default) =
+                                 4-wide tree, batch */
   RTX_OPT_MIN_BUSY = 11,      /* with RTX_OPT_TRAVERSAL = 1: refill a warp once
                                  fewer lanes than this are traversing (0..32) */
   RTX_OPT_GRAPH = 12          /* 0/1: rtx_render_batch captures its launch
@@ -121,7 +122,8 @@ typedef struct rtx_stats {
   int32_t bvh_nodes;         /* inner nodes of the current BVH */
   int32_t bvh_leaves;
   int32_t bvh_depth;
-  int32_t node_bytes;        /* bytes per BVH node record */
+  int32_t node_bytes;        /* bytes per BVH node record of the tree in use
+                                (64 binary, 112 4-wide) */
   int32_t tri_bytes;         /* bytes per triangle record */
   int32_t reserved;
   uint64_t ext_rays_by_depth[16]; /* closest-hit rays per path vertex 0..15 */
@@ -247,15 +249,17 @@ int rtx_render_batch(rtx_context* ctx, int n_jobs, const rtx_job* jobs,
  * best of two) over BVH leaf sizes 2 / 4 / 8 -- rebuilding the batch from
  * `scenes` for each; scenes = NULL keeps the uploaded batch and its leaf
  * size -- then threads per block 64 / 128 x paths per wave 2^20, 2^22, 2^24,
- * auto, then material-sorted shading on / off, coordinate-wise from the
- * context's current options.  The fastest setting stays on the context
- * (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK, RTX_OPT_WAVE_PATHS,
- * RTX_OPT_SORT_MATERIAL) and the batch is left built with it. */
+ * auto, then the binary or 4-wide tree, then material-sorted shading on /
+ * off, coordinate-wise from the context's current options.  The fastest
+ * setting stays on the context (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK,
+ * RTX_OPT_WAVE_PATHS, RTX_OPT_TRAVERSAL, RTX_OPT_SORT_MATERIAL) and the batch
+ * is left built with it. */
 typedef struct rtx_tune_result {
   int64_t block, wave_paths, leaf_size;
   double ms, ms_default;       /* frame time chosen / at the starting options */
   int trials;
   int sort_material;           /* RTX_OPT_SORT_MATERIAL chosen */
+  int traversal;               /* RTX_OPT_TRAVERSAL chosen (0 or 2) */
 } rtx_tune_result;
 int rtx_batch_autotune(rtx_context* ctx, int n_scenes,
                        const rtx_scene_desc* scenes, int n_jobs,

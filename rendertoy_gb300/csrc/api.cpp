@@ -83,7 +83,7 @@ struct rtx_context {
   int leaf_size = 4;
   bool primary_cache = true;
   bool accumulate = false;
-  int traversal = 0;
+  int traversal = 2;
   int min_busy = 20;
   KernelTimer timer;
   // scene
@@ -99,12 +99,12 @@ struct rtx_context {
   DevBuf perm;  // Perlin texture permutation (256 bytes)
   // multi-scene batch (rtx_batch_upload / rtx_render_batch)
   struct BatchScene {
-    int root, e_begin, n_emitters, n_tris;
+    int root, root4, e_begin, n_emitters, n_tris;
     float sky[3], ground[3];
   };
   bool has_batch = false;
   DeviceScene bds{};
-  DevBuf b_nodes, b_tris, b_shade, b_geo, b_mats, b_emit, b_jobs, b_jobq;
+  DevBuf b_nodes, b_nodes4, b_tris, b_shade, b_geo, b_mats, b_emit, b_jobs, b_jobq;
   std::vector<BatchScene> bscenes;
   // CUDA graph of the last batch frame, keyed by its launch shape
   bool use_graph = false;
@@ -361,7 +361,8 @@ void rtx_destroy(rtx_context* c) {
   c->emit.release();
   for (auto& s : c->stage) s.release();
   c->perm.release();
-  DevBuf* bb[] = {&c->b_nodes, &c->b_tris, &c->b_shade, &c->b_geo, &c->b_mats, &c->b_emit, &c->b_jobs, &c->b_jobq};
+  DevBuf* bb[] = {&c->b_nodes, &c->b_nodes4, &c->b_tris, &c->b_shade, &c->b_geo, &c->b_mats, &c->b_emit,
+                  &c->b_jobs, &c->b_jobq};
   for (DevBuf* b : bb) b->release();
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->h_jobs_pinned) cudaFreeHost(c->h_jobs_pinned);
@@ -473,6 +474,8 @@ int rtx_get_stats(rtx_context* c, rtx_stats* out) {
   c->stats.shadow_node_visits = h.sh_node_visits;
   c->stats.shadow_tri_tests = h.sh_tri_tests;
   for (int d = 0; d < 16; ++d) c->stats.ext_rays_by_depth[d] = h.ext_rays_by_depth[d];
+  // node visits count records of the tree in use: 4 x 16 B binary, 7 x 16 B 4-wide
+  c->stats.node_bytes = c->traversal == 2 ? 112 : 64;
   RTX_CUDA(c->timer.collect(), "kernel timing");
   c->stats.extend_ms = c->timer.ms[0];
   c->stats.shade_ms = c->timer.ms[1];
@@ -678,7 +681,7 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
     for (auto& t : th) t.join();
   }
   // merge: node, leaf-record, triangle-id, material and emitter indices rebased
-  std::vector<float4> nodes, tris, shade, geo;
+  std::vector<float4> nodes, nodes4, tris, shade, geo;
   std::vector<float> mats;
   std::vector<int32_t> emit;
   c->bscenes.assign(n_scenes, {});
@@ -693,6 +696,18 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
       for (int& x : ch) x = x >= 0 ? x + node_base : rebase_leaf(x, tri_base);
       std::memcpy(&n3.x, ch, 8);
       nodes.insert(nodes.end(), {n0, n1, n2, n3});
+    }
+    // 4-wide nodes: seven float4, child references in the last one (empty
+    // slots hold 0 behind a box that is never hit)
+    int node4_base = (int)(nodes4.size() / 7);
+    for (size_t k = 0; k < h.b.nodes4.size(); k += 7) {
+      for (int r = 0; r < 6; ++r) nodes4.push_back(h.b.nodes4[k + r]);
+      float4 m = h.b.nodes4[k + 6];
+      int ch[4];
+      std::memcpy(ch, &m, 16);
+      for (int& x : ch) x = x >= 0 ? x + node4_base : rebase_leaf(x, tri_base);
+      std::memcpy(&m, ch, 16);
+      nodes4.push_back(m);
     }
     for (size_t k = 0; k < h.b.tris.size(); k += 3) {
       float4 a = h.b.tris[k];
@@ -717,6 +732,8 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
     rtx_context::BatchScene& bs = c->bscenes[i];
     int root = h.b.root;
     bs.root = root == kEmptyRoot ? kEmptyRoot : (root >= 0 ? root + node_base : rebase_leaf(root, tri_base));
+    int root4 = h.b.root4;
+    bs.root4 = root4 == kEmptyRoot ? kEmptyRoot : (root4 >= 0 ? root4 + node4_base : rebase_leaf(root4, tri_base));
     bs.e_begin = (int)emit.size();
     if (d[i].n_emitters >= 0) {
       for (int k = 0; k < d[i].n_emitters; ++k) emit.push_back(d[i].emitters[k] + tri_base);
@@ -735,6 +752,8 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   }
   double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if ((r = upload_buf(c, c->b_nodes, nodes.data(), nodes.size() * sizeof(float4), "upload batch nodes"))) return r;
+  if ((r = upload_buf(c, c->b_nodes4, nodes4.data(), nodes4.size() * sizeof(float4), "upload batch nodes4")))
+    return r;
   if ((r = upload_buf(c, c->b_tris, tris.data(), tris.size() * sizeof(float4), "upload batch tris"))) return r;
   if ((r = upload_buf(c, c->b_shade, shade.data(), shade.size() * sizeof(float4), "upload batch shade"))) return r;
   if ((r = upload_buf(c, c->b_geo, geo.data(), geo.size() * sizeof(float4), "upload batch geo"))) return r;
@@ -743,7 +762,7 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   DeviceScene& s = c->bds;
   s = DeviceScene{};
   s.nodes = (const float4*)c->b_nodes.p;
-  s.nodes4 = nullptr;
+  s.nodes4 = (const float4*)c->b_nodes4.p;
   s.root4 = kEmptyRoot;
   s.tris = (const float4*)c->b_tris.p;
   s.shade = (const float4*)c->b_shade.p;
@@ -943,7 +962,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   if (!c->has_batch) return fail(c, RTX_ERR_NO_SCENE, "no batch uploaded (rtx_batch_upload)");
   if (n_jobs < 1 || !jobs || !out) return fail(c, RTX_ERR_INVALID, "no frames or NULL output");
   if (max_depth < 1 || max_depth > 63) return fail(c, RTX_ERR_INVALID, "max_depth must be in [1, 63]");
-  if (c->traversal == 1) return fail(c, RTX_ERR_INVALID, "batches use the batch traversal (RTX_OPT_TRAVERSAL 0)");
+  if (c->traversal == 1) return fail(c, RTX_ERR_INVALID, "batches use the batch traversals (RTX_OPT_TRAVERSAL 0 or 2)");
   std::vector<PtJob> hj((size_t)n_jobs);
   long long q = 0, pix = 0;
   for (int j = 0; j < n_jobs; ++j) {
@@ -961,7 +980,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
     P.spp = J.spp;
     P.first_sample = 0;
     P.root = bs.root;
-    P.root4 = kEmptyRoot;
+    P.root4 = bs.root4;
     P.e_begin = bs.e_begin;
     P.n_emitters = bs.n_emitters;
     P.k0 = (uint32_t)J.seed;
@@ -1008,7 +1027,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
   p.sort_material = c->sort_material;
-  p.traversal = 0;
+  p.traversal = c->traversal;
   p.min_busy = c->min_busy;
   p.accumulate = c->accumulate;
   p.n_jobs = n_jobs;
@@ -1019,7 +1038,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   c->timer.reset();
   // the launch shape: everything the captured kernels bake in
   std::vector<int64_t> key = {n_jobs, max_depth, c->wave_paths, c->block, c->primary_cache, c->count_visits,
-                              c->accumulate, c->sort_material, (int64_t)(intptr_t)o.dev};
+                              c->accumulate, c->sort_material, c->traversal, (int64_t)(intptr_t)o.dev};
   for (int j = 0; j < n_jobs; ++j) key.insert(key.end(), {jobs[j].scene, jobs[j].W, jobs[j].H, jobs[j].spp});
   int launches = 0, ext_launches = 0;
   std::string why;
@@ -1096,6 +1115,7 @@ int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scene
   float* d_out = nullptr;
   rtx_tune_result res{};
   res.trials = 0;
+  if (c->traversal == 1) c->traversal = 2;  // batches take the batch traversals
   auto done = [&](int code) {
     if (d_out) cudaFree(d_out);
     c->use_graph = saved_graph;
@@ -1144,6 +1164,16 @@ int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scene
     }
   c->block = (int)res.block;
   c->wave_paths = res.wave_paths;
+  // binary or 4-wide tree
+  res.traversal = c->traversal;
+  c->traversal = c->traversal == 2 ? 0 : 2;
+  if ((r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms))) return done(r);
+  ++res.trials;
+  if (ms < res.ms) {
+    res.ms = ms;
+    res.traversal = c->traversal;
+  }
+  c->traversal = res.traversal;
   // material-sorted shading helps scenes with many materials and costs a
   // little where there are few: keep whichever is faster
   res.sort_material = c->sort_material ? 1 : 0;

@@ -947,12 +947,16 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     ws->occ_extend = std::min(ws->occ_extend, o1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, false, true>, block, 0);
     ws->occ_extend = std::min(ws->occ_extend, o1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_extend_batch<false, true, true>, block, 0);
+    ws->occ_extend = std::min(ws->occ_extend, o1);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_connect, k_connect<false>, block, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, false, false>, block, 0);
     ws->occ_connect = std::min(ws->occ_connect, o2);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, true, false>, block, 0);
     ws->occ_connect = std::min(ws->occ_connect, o2);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, false, true>, block, 0);
+    ws->occ_connect = std::min(ws->occ_connect, o2);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, true, true>, block, 0);
     ws->occ_connect = std::min(ws->occ_connect, o2);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade<false, false>, block, 0);
     for (auto k : {k_shade<true, false>, k_shade<false, true>, k_shade<true, true>}) {

@@ -43,6 +43,21 @@ def test_batch_frames_equal_single_renders(ctx):
         assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), j
 
 
+def test_batch_binary_and_wide_trees(ctx):
+    """Frames equal single renders with the binary (0) and 4-wide (2) trees."""
+    sc = _scenes()
+    for trav in (0, 2):
+        ctx.set_option(rt.OPT_TRAVERSAL, trav)
+        try:
+            ctx.batch_upload(sc)
+            imgs = ctx.render_batch(JOBS[:3], 5)
+            for j, img in zip(JOBS[:3], imgs):
+                ref = _alone(ctx, sc[j["scene"]], j, 5)
+                assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (trav, j)
+        finally:
+            ctx.set_option(rt.OPT_TRAVERSAL, 2)
+
+
 def test_batch_with_small_waves(ctx):
     """Waves that split frames and samples (64k paths) give the same images."""
     sc = _scenes()
@@ -104,6 +119,7 @@ def test_material_sort_keeps_images(ctx):
         bb = ctx.render_batch(JOBS, 6)
     finally:
         ctx.set_option(rt.OPT_SORT_MATERIAL, 0)
+        ctx.set_option(rt.OPT_TRAVERSAL, 2)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
     for x, y in zip(ba, bb):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
@@ -115,8 +131,9 @@ def test_autotune(ctx):
     jobs = [dict(j, spp=j["spp"] * 4) for j in JOBS]
     try:
         res = ctx.batch_autotune(jobs, 6, scene_list=sc)
-        assert res["trials"] >= 9 and res["ms"] <= res["ms_default"]
+        assert res["trials"] >= 10 and res["ms"] <= res["ms_default"]
         assert ctx.get_option(rt.OPT_SORT_MATERIAL) == res["sort_material"]
+        assert ctx.get_option(rt.OPT_TRAVERSAL) == res["traversal"] and res["traversal"] in (0, 2)
         assert res["leaf_size"] in (2, 4, 8) and res["block"] in (64, 128)
         assert ctx.get_option(rt.OPT_BLOCK) == res["block"]
         assert ctx.get_option(rt.OPT_LEAF_SIZE) == res["leaf_size"]
@@ -129,3 +146,4 @@ def test_autotune(ctx):
         ctx.set_option(rt.OPT_WAVE_PATHS, 0)
         ctx.set_option(rt.OPT_LEAF_SIZE, 4)
         ctx.set_option(rt.OPT_SORT_MATERIAL, 0)
+        ctx.set_option(rt.OPT_TRAVERSAL, 2)

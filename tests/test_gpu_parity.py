@@ -221,3 +221,23 @@ def test_full_size_icosphere(ctx, oracle, icosphere_scene):
     ok = rel_close(got, ref, 1e-4, 1e-6).all(-1)
     print(f"icosphere depth 12: {ok.mean() * 100:.2f} % of paths within 1e-4")
     assert ok.mean() >= 0.97
+
+
+@pytest.mark.gpu
+def test_traversal_variants_agree(ctx):
+    """The binary batch walk (0), the binary while-while walk with ray refill
+    (1) and the 4-wide tree (2, the default) find the same closest hits and
+    occluders (nearest triangle, lower-id ties): per-path radiance is
+    bit-identical."""
+    import rendertoy_gb300 as rt
+    ctx.upload(scenes.cornell_mixed())
+    out = {}
+    try:
+        for trav in (0, 1, 2):
+            ctx.set_option(rt.OPT_TRAVERSAL, trav)
+            out[trav] = ctx.trace_paths(40, 32, 0, 2, 8, seed=3)
+    finally:
+        ctx.set_option(rt.OPT_TRAVERSAL, 2)
+    for trav in (1, 2):
+        assert np.array_equal(np.nan_to_num(out[trav], nan=-7).view(np.uint32),
+                              np.nan_to_num(out[0], nan=-7).view(np.uint32)), trav
