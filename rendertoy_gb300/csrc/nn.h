@@ -51,6 +51,9 @@ struct ConvWgrad {
   int pix_per_cta;   // pixels each CTA sums (multiple of 64)
   float* dw;         // [Cout][9][Cin], accumulated
   int* err;
+  // set by conv_wgrad for the row-tile kernel: channels per CTA, tile width
+  // in pixels, row tiles per CTA
+  int cr, tw, tiles_per_cta;
 };
 
 cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st);

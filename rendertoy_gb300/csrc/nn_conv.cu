@@ -134,8 +134,12 @@ __device__ __forceinline__ void tc_end(uint32_t tmem, uint32_t ncols) {
 // issues this thread's copies of a slice (nothing for slice >= n); mma(stage,
 // first) is run by thread 0.  Returns false, uniformly across the CTA, when
 // an MMA barrier wait ran out (error flag set); copies are drained either way.
-template <int S, class Load, class Mma>
-__device__ __forceinline__ bool conv_pipeline(int n, uint64_t* bars, Load&& load, Mma&& mma, int* err) {
+// `done(it)` runs on every thread once slice it's MMAs (and all earlier
+// ones) have completed, after the copies of slice it + S - 1 were issued and
+// while slice it + 1's MMAs run: the persistent kernels read a finished
+// accumulator there.
+template <int S, class Load, class Mma, class Done>
+__device__ __forceinline__ bool conv_ring(int n, uint64_t* bars, Load&& load, Mma&& mma, Done&& done, int* err) {
   uint32_t parity = 0;
 #pragma unroll
   for (int s = 0; s < S - 1; ++s) {
@@ -147,13 +151,14 @@ __device__ __forceinline__ bool conv_pipeline(int n, uint64_t* bars, Load&& load
     const int st = it % S;
     tc::cp_async_wait<S - 2>();  // this thread's copies of slice `it` landed
     tc::fence_proxy_async();
+    tc::fence_before();  // order the previous done()'s TMEM reads before the barrier
     if (!__syncthreads_and(wok)) {
       ok = false;
       break;
     }
     if (threadIdx.x == 0) {
       tc::fence_after();
-      mma(st, it == 0);
+      mma(it, st, it == 0);
       tc::mma_commit(&bars[st]);
     }
     if (it > 0) {  // the previous slice's MMAs free its stage for slice it + S - 1
@@ -163,15 +168,175 @@ __device__ __forceinline__ bool conv_pipeline(int n, uint64_t* bars, Load&& load
     }
     load(it + S - 1, (it + S - 1) % S);
     tc::cp_async_commit();
+    if (it > 0 && wok) {
+      tc::fence_after();
+      done(it - 1);
+    }
   }
   if (ok && n > 0) {
     const int ls = (n - 1) % S;
     const bool w = wok && tc::mbar_wait(&bars[ls], (parity >> ls) & 1u);
     ok = __syncthreads_and(w);
+    if (ok) {
+      tc::fence_after();
+      done(n - 1);
+    }
   }
   if (!ok && (threadIdx.x & 31) == 0) atomicOr(err, tc::kErrMbarTimeout);
   tc::cp_async_wait_all();
   return ok;
+}
+
+// Warp-specialised rings (no CTA-wide barrier per slice).  Thread 0 issues
+// the MMAs; producer warp 1 + p (p < S <= 7) owns ring stage p and copies
+// units p, p + S, p + 2S, ...: it waits for the stage to be free (empty: the
+// MMA commit of the unit S before), issues its 32 lanes' cp.async copies,
+// waits for them, fences them to the async proxy and arrives on full (32
+// arrivals).  Up to S units are in flight, each warp blocking only on its own
+// copies; the MMA thread consumes units in order.  Because a warp's units on
+// its stage are exactly one lap apart, every parity wait targets the
+// barrier's current or next phase, never one two laps away.
+// load(unit, stage, lane) copies with item stride kLoadStride.
+constexpr int kProducerWarps = 7;
+constexpr int kLoadStride = 32;
+
+// pre(pw, lane) issues copies every MMA needs (resident weights, split over
+// the producer warps); the warp waits for them and its 32 lanes arrive on
+// wbar (kProducerWarps * 32 arrivals; null: none) before its first unit, so
+// that arrival never waits on MMA progress.
+template <int S, class Pre, class Load>
+__device__ __forceinline__ bool produce(int n, uint64_t* full, uint64_t* empty, uint64_t* wbar, Pre&& pre,
+                                        Load&& load) {
+  static_assert(S >= 1 && S <= kProducerWarps, "one producer warp per stage");
+  const int pw = (threadIdx.x >> 5) - 1, lane = threadIdx.x & 31;
+  if (wbar) {
+    pre(pw, lane);
+    tc::cp_async_commit();
+    tc::cp_async_wait<0>();
+    tc::fence_proxy_async();
+    tc::mbar_arrive(wbar);
+  }
+  if (pw >= S) return true;
+  for (int u = pw; u < n; u += S) {
+    if (u >= S && !tc::mbar_wait(&empty[pw], (uint32_t)(u / S - 1) & 1u)) return false;
+    load(u, pw, lane);
+    tc::cp_async_commit();
+    tc::cp_async_wait<0>();
+    tc::fence_proxy_async();
+    tc::mbar_arrive(&full[pw]);
+  }
+  return true;
+}
+
+// One accumulation over n slices (the weight gradient).  Returns true,
+// uniformly, once every MMA has completed; false (error flag set) when a
+// bounded wait ran out.
+template <int S, class Load, class Mma>
+__device__ __forceinline__ bool ws_ring(int n, uint64_t* full, uint64_t* empty, Load&& load, Mma&& mma, int* err) {
+  const int tid = threadIdx.x;
+  bool ok = true;
+  if (tid < 32) {
+    if (tid == 0) {
+      for (int it = 0; it < n; ++it) {
+        const int st = it % S;
+        if (!tc::mbar_wait(&full[st], (uint32_t)(it / S) & 1u)) {
+          ok = false;
+          break;
+        }
+        tc::fence_after();
+        mma(it, st);
+        tc::mma_commit(&empty[st]);
+      }
+    }
+  } else {
+    ok = produce<S>(n, full, empty, nullptr, [](int, int) {}, load);
+  }
+  // the last commit covers every MMA (waited after a plain barrier, so the
+  // producers do not spin while the MMAs drain)
+  bool fin = __syncthreads_and(ok);
+  if (fin && n > 0) fin = tc::mbar_wait(&empty[(n - 1) % S], (uint32_t)((n - 1) / S) & 1u);
+  fin = __syncthreads_and(fin);
+  if (!fin && (tid & 31) == 0) atomicOr(err, tc::kErrMbarTimeout);
+  tc::fence_after();
+  return fin;
+}
+
+// Persistent tiles (kTileThreads = 12 warps): thread 0 issues MMAs, warps
+// 1 .. 7 produce, warps 8 .. 11 run the epilogue, warp 8 + q reading
+// accumulator lanes 32 q .. 32 q + 31.  A CTA walks n_tiles output tiles of
+// nsl slices each; tile i accumulates in TMEM buffer i & 1, so tile i's
+// epilogue overlaps tile i + 1's copies and MMAs.  accf[b]: MMA commit after
+// a tile's last slice (buffer b complete); acce[b]: the 128 epilogue threads'
+// arrivals once they have read buffer b.  mma(unit, stage, buffer, slice)
+// and epi(tile, buffer) are the kernel's.
+constexpr int kTileThreads = 384;
+constexpr int kEpilogue = 128;
+constexpr int kMaxStages = 8;
+
+struct TileBars {
+  uint64_t full[kMaxStages], empty[kMaxStages], accf[2], acce[2], wbar;
+};
+
+template <int S>
+__device__ __forceinline__ void tile_bars_init(TileBars& b) {
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < S; ++i) {
+      tc::mbar_init(&b.full[i], kLoadStride);
+      tc::mbar_init(&b.empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&b.accf[i], 1);
+      tc::mbar_init(&b.acce[i], kEpilogue);
+    }
+    tc::mbar_init(&b.wbar, kProducerWarps * 32);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+}
+
+template <int S, class Pre, class Load, class Mma, class Epi>
+__device__ __forceinline__ bool ws_tiles(int n_tiles, int nsl, TileBars& b, Pre&& pre, Load&& load, Mma&& mma,
+                                         Epi&& epi, int* err) {
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int n = n_tiles * nsl;
+  bool ok = true;
+  if (warp == 0) {
+    if (tid == 0) {
+      if (n > 0) ok = tc::mbar_wait(&b.wbar, 0u);
+      for (int u = 0; u < n && ok; ++u) {
+        const int i = u / nsl, s = u - i * nsl, st = u % S, buf = i & 1;
+        if (s == 0 && i >= 2) ok = tc::mbar_wait(&b.acce[buf], (uint32_t)((i >> 1) - 1) & 1u);
+        if (ok) ok = tc::mbar_wait(&b.full[st], (uint32_t)(u / S) & 1u);
+        if (!ok) break;
+        tc::fence_after();
+        mma(u, st, buf, s);
+        tc::mma_commit(&b.empty[st]);
+        if (s == nsl - 1) tc::mma_commit(&b.accf[buf]);
+      }
+    }
+  } else if (warp <= kProducerWarps) {
+    ok = produce<S>(n, b.full, b.empty, &b.wbar, pre, load);
+  } else {
+    for (int i = 0; i < n_tiles; ++i) {
+      const int buf = i & 1;
+      if (!tc::mbar_wait(&b.accf[buf], (uint32_t)(i >> 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+      epi(i, buf);
+      tc::fence_before();
+      tc::mbar_arrive(&b.acce[buf]);
+    }
+  }
+  ok = __syncthreads_and(ok);
+  if (!ok && (tid & 31) == 0) atomicOr(err, tc::kErrMbarTimeout);
+  return ok;
+}
+
+template <int S, class Load, class Mma>
+__device__ __forceinline__ bool conv_pipeline(int n, uint64_t* bars, Load&& load, Mma&& mma, int* err) {
+  return conv_ring<S>(
+      n, bars, load, [&](int, int st, bool first) { mma(st, first); }, [](int) {}, err);
 }
 
 }  // namespace
@@ -226,10 +391,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_fwd(ConvFwd a) {
   };
   auto mma = [&](int st, bool first) {
     const uint32_t a0 = s0 + st * stage, b0 = a0 + a_bytes;
+    // consecutive K steps are 256 B apart: +16 in the descriptors' address field
+    const uint64_t ad = tc::make_desc(a0, 128, kSlice * 16), bd = tc::make_desc(b0, 128, kSlice * 16);
 #pragma unroll
-    for (int s = 0; s < kSlice / 16; ++s)
-      tc::mma_bf16(tmem, tc::make_desc(a0 + s * 256, 128, kSlice * 16), tc::make_desc(b0 + s * 256, 128, kSlice * 16),
-                   idesc, !first || s > 0);
+    for (int s = 0; s < kSlice / 16; ++s) tc::mma_bf16(tmem, ad + 16 * s, bd + 16 * s, idesc, !first || s > 0);
   };
   const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
@@ -258,141 +423,213 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_fwd(ConvFwd a) {
 }
 
 // ---------------------------------------------------------------------------
-// forward, row tiles: a CTA takes 128 consecutive pixels of one image row.
-// Per slice of 16 input channels it copies the 3-row halo (pixels x0 - 1 ..
-// x0 + 128, 2 chunks of 8 channels each) once; the nine taps are the same
-// halo read through descriptors shifted by whole pixels (rows of the
+// forward, row tiles: a tile is 128 consecutive pixels of one image row.  Per
+// slice of 16 input channels the producers copy the tile's 3-row halo (pixels
+// x0 - 1 .. x0 + 128, 2 chunks of 8 channels each) once; the nine taps are
+// the same halo read through descriptors shifted by whole pixels (rows of the
 // K-major layout are 16 B apart and the two channel chunks one halo row
-// apart, so every shift is a legal start address).  One third of the gather
-// traffic of k_conv_fwd, with one address per copied pixel chunk.
+// apart, so every shift is a legal start address): one third of the gather
+// traffic of k_conv_fwd, one address per copied pixel chunk.  Persistent and
+// warp-specialised (ws_tiles): a CTA walks tiles blockIdx.x, + gridDim.x, ...;
+// with kRes the whole weight tensor stays in shared memory ([slice][tap]
+// tiles of Cout x 16, K-major), otherwise each stage carries its slice's nine
+// weight tiles.
 // ---------------------------------------------------------------------------
 constexpr int kHalo = 130;                                  // pixels x0 - 1 .. x0 + 128
 constexpr uint32_t kHaloBytes = 3 * 2 * kHalo * 16;          // rows x chunks x pixels x 16 B
 
-template <int S>
-__global__ void __launch_bounds__(kThreads, 2) k_conv_fwd_row(ConvFwd a) {
+// smem byte offset of chunk c (of 2) of halo pixel h in halo row r
+__device__ __forceinline__ uint32_t halo_off(int r, int c, int h) { return ((r * 2 + c) * kHalo + h) * 16; }
+
+template <int S, bool kRes>
+__global__ void __launch_bounds__(kTileThreads, 1) k_conv_fwd_rows(ConvFwd a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t bars[S];
+  __shared__ __align__(8) TileBars bars;
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int x0 = blockIdx.x * 128, y = blockIdx.y, n = blockIdx.z;
+  const int TR = (a.W + 127) / 128;  // tiles per image row
+  const int T = a.N * a.H * TR;
+  const int n_tiles = (int)blockIdx.x < T ? (T - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int nsl = a.Cin / 16;
   const uint32_t ncols = a.Cout <= 32 ? 32 : (a.Cout <= 64 ? 64 : (a.Cout <= 128 ? 128 : 256));
-  const uint32_t tap_bytes = (uint32_t)a.Cout * 32, stage = kHaloBytes + 9 * tap_bytes;
-  tc_begin(&tmem_slot, bars, S, ncols);
+  const uint32_t tap_bytes = (uint32_t)a.Cout * 32;
+  const uint32_t stage = kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes;
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
+  tile_bars_init<S>(bars);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
   const uint32_t tmem = tmem_slot;
   const uint32_t idesc = tc::make_idesc_bf16(128, a.Cout);
-  const uint32_t s0 = tc::smem_u32(smem);
-  const int n_slices = a.Cin / 16;
-  auto load = [&](int slice, int st) {
-    if (slice >= n_slices) return;
-    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
-    const int c0 = slice * 16;
-    // chunk c of pixel h of halo row r: neighbouring threads take the two
-    // chunks of one pixel (32 contiguous bytes)
-    for (int i = tid; i < 3 * kHalo * 2; i += kThreads) {
-      const int c = i & 1, h = (i >> 1) % kHalo, r = (i >> 1) / kHalo;
-      const bf16* p = src_ptr(a.s1, a.s2, a.H, a.W, n, y + r - 1, x0 + h - 1, c0 + 8 * c);
-      chunk_async(sh + ((r * 2 + c) * kHalo + h) * 16, p, a.s1.ptr);
-    }
-    // tap t: Cout x 16 K-major tile of w[o][t][c0 .. c0 + 15]
-    for (int i = tid; i < 9 * a.Cout * 2; i += kThreads) {
-      const int kc = i & 1, o = (i >> 1) % a.Cout, t = (i >> 1) / a.Cout;
-      chunk_async(sb + t * tap_bytes + tc::tile_offset(o, 8 * kc, 16), a.w + ((size_t)o * 9 + t) * a.Cin + c0 + 8 * kc,
-                  a.w);
-    }
+  const uint32_t s0 = tc::smem_u32(smem), sw = s0 + S * stage;  // sw: resident weights
+  auto tile_of = [&](int i, int& n, int& y, int& x0) {
+    const int j = (int)blockIdx.x + i * (int)gridDim.x;
+    const int row = j / TR;
+    x0 = (j - row * TR) * 128;
+    n = row / a.H;
+    y = row - n * a.H;
   };
-  auto mma = [&](int st, bool first) {
-    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
+  auto weight_tile = [&](uint32_t dst, int q) {  // chunk q of one [slice][tap] tile set
+    const int kc = q & 1, o = (q >> 1) % a.Cout, st = (q >> 1) / a.Cout, sl = st / 9, t = st - sl * 9;
+    chunk_async(dst + st * tap_bytes + tc::tile_offset(o, 8 * kc, 16),
+                a.w + ((size_t)o * 9 + t) * a.Cin + sl * 16 + 8 * kc, a.w);
+  };
+  auto pre = [&](int pw, int lane) {
+    if (kRes)
+      for (int q = pw * 32 + lane; q < nsl * 9 * a.Cout * 2; q += kProducerWarps * 32) weight_tile(sw, q);
+  };
+  auto load = [&](int u, int st, int lane) {
+    const int i = u / nsl, s = u - i * nsl;
+    int n, y, x0;
+    tile_of(i, n, y, x0);
+    const uint32_t sh = s0 + st * stage;
+    const int c0 = s * 16;
+    // neighbouring lanes take the two chunks of one pixel (32 B)
+    for (int q = lane; q < 3 * kHalo * 2; q += kLoadStride) {
+      const int c = q & 1, h = (q >> 1) % kHalo, r = (q >> 1) / kHalo;
+      chunk_async(sh + halo_off(r, c, h), src_ptr(a.s1, a.s2, a.H, a.W, n, y + r - 1, x0 + h - 1, c0 + 8 * c),
+                  a.s1.ptr);
+    }
+    if (!kRes)  // slice s's nine tiles: q -> (tap, row, chunk) with the slice fixed
+      for (int q = lane; q < 9 * a.Cout * 2; q += kLoadStride) {
+        const int kc = q & 1, o = (q >> 1) % a.Cout, t = (q >> 1) / a.Cout;
+        chunk_async(sh + kHaloBytes + t * tap_bytes + tc::tile_offset(o, 8 * kc, 16),
+                    a.w + ((size_t)o * 9 + t) * a.Cin + c0 + 8 * kc, a.w);
+      }
+  };
+  auto mma = [&](int, int st, int buf, int s) {
+    const uint32_t sh = s0 + st * stage;
+    const uint32_t sb = kRes ? sw + (uint32_t)s * 9 * tap_bytes : sh + kHaloBytes;
+    // A: pixel groups 128 B apart (SBO), channel chunks one halo row apart
+    // (LBO); tap t starts (dy + 1) halo rows and 1 + dx pixels in (offsets in
+    // the descriptors' 16-byte address units)
+    const uint64_t ah = tc::make_desc(sh, kHalo * 16, 128), bw = tc::make_desc(sb, 128, 256);
+    const uint32_t d = tmem + buf * ncols;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
       const int dy = t / 3 - 1, dx = t % 3 - 1;
-      // A: pixel groups 128 B apart (SBO), channel chunks one halo row apart (LBO)
-      const uint64_t ad = tc::make_desc(sh + ((dy + 1) * 2 * kHalo + 1 + dx) * 16, kHalo * 16, 128);
-      const uint64_t bd = tc::make_desc(sb + t * tap_bytes, 128, 256);
-      tc::mma_bf16(tmem, ad, bd, idesc, !first || t > 0);
+      tc::mma_bf16(d, ah + ((dy + 1) * 2 * kHalo + 1 + dx), bw + t * (tap_bytes >> 4), idesc, s > 0 || t > 0);
     }
   };
-  const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
-  tc::fence_after();
-  if (ok) {
-    const int lw = warp & 3, half = a.Cout >> 1;
-    const int x = x0 + lw * 32 + lane;
+  auto epi = [&](int i, int buf) {
+    const int q = warp & 3;  // accumulator lanes 32 q .. 32 q + 31 = pixels
+    int n, y, x0;
+    tile_of(i, n, y, x0);
+    const int x = x0 + q * 32 + lane;
     const size_t p = ((size_t)n * a.H + y) * a.W + x;
-    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
-    for (int c0 = (warp >> 2) * half; c0 < (warp >> 2) * half + half; c0 += 8) {
+    const uint32_t taddr = tmem + buf * ncols + ((uint32_t)(q * 32) << 16);
+    for (int c0 = 0; c0 < a.Cout; c0 += 8) {
       float v[8];
       tc::tmem_ld8(taddr + c0, v);
       if (x < a.W) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          if (a.bias) v[i] += a.bias[c0 + i];
-          if (a.relu) v[i] = fmaxf(v[i], 0.0f);
+        for (int k = 0; k < 8; ++k) {
+          if (a.bias) v[k] += a.bias[c0 + k];
+          if (a.relu) v[k] = fmaxf(v[k], 0.0f);
         }
         if (a.out) *reinterpret_cast<uint4*>(a.out + p * a.Cout + c0) = f32_to_bf16x8(v);
         if (a.out_f32)
 #pragma unroll
-          for (int i = 0; i < 8; ++i) a.out_f32[p * a.Cout + c0 + i] = v[i];
+          for (int k = 0; k < 8; ++k) a.out_f32[p * a.Cout + c0 + k] = v[k];
       }
     }
-  }
-  tc_end(tmem, ncols);
+  };
+  ws_tiles<S>(n_tiles, nsl, bars, pre, load, mma, epi, a.err);
+  tc_end(tmem, 2 * ncols);
 }
 
 // data gradient, row tiles: din[p] = sum_t dout[p - off(t)] wt_t, the same
-// halo scheme over dout (slices of 16 of its channels, shifts negated)
-template <int S>
-__global__ void __launch_bounds__(kThreads, 2) k_conv_dgrad_row(ConvDgrad a) {
+// halo scheme over dout (slices of 16 of its channels, shifts negated).  A
+// tile is (image row, 128 pixels, 256 input channels); the channel tile
+// varies fastest, so neighbouring CTAs read the same dout halo.  Resident
+// weights: [channel tile][slice][tap] tiles of NTmax x 16.
+template <int S, bool kRes>
+__global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ __align__(8) uint64_t bars[S];
+  __shared__ __align__(8) TileBars bars;
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int x0 = blockIdx.x * 128, y = blockIdx.y;
-  const int n = blockIdx.z / ((a.Cin + 255) / 256);
-  const int n0 = (blockIdx.z % ((a.Cin + 255) / 256)) * 256;
-  const int NT = min(256, a.Cin - n0);
-  const uint32_t ncols = NT <= 32 ? 32 : (NT <= 64 ? 64 : (NT <= 128 ? 128 : 256));
-  const uint32_t tap_bytes = (uint32_t)min(256, a.Cin) * 32, stage = kHaloBytes + 9 * tap_bytes;
-  tc_begin(&tmem_slot, bars, S, ncols);
+  const int TR = (a.W + 127) / 128, nt = (a.Cin + 255) / 256;
+  const int T = a.N * a.H * TR * nt;
+  const int n_tiles = (int)blockIdx.x < T ? (T - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int nsl = a.Cout / 16;
+  const int ntm = min(256, a.Cin);  // widest channel tile
+  const uint32_t ncols = ntm <= 32 ? 32 : (ntm <= 64 ? 64 : (ntm <= 128 ? 128 : 256));
+  const uint32_t tap_bytes = (uint32_t)ntm * 32;
+  const uint32_t stage = kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes;
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
+  tile_bars_init<S>(bars);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
   const uint32_t tmem = tmem_slot;
-  const uint32_t idesc = tc::make_idesc_bf16(128, NT);
-  const uint32_t s0 = tc::smem_u32(smem);
-  const int n_slices = a.Cout / 16;
-  auto load = [&](int slice, int st) {
-    if (slice >= n_slices) return;
-    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
-    const int o0 = slice * 16;
-    for (int i = tid; i < 3 * kHalo * 2; i += kThreads) {
-      const int c = i & 1, h = (i >> 1) % kHalo, r = (i >> 1) / kHalo;
+  const uint32_t s0 = tc::smem_u32(smem), sw = s0 + S * stage;
+  auto tile_of = [&](int i, int& n, int& y, int& x0, int& ct) {
+    const int j = (int)blockIdx.x + i * (int)gridDim.x;
+    const int rx = j / nt;
+    ct = j - rx * nt;
+    const int row = rx / TR;
+    x0 = (rx - row * TR) * 128;
+    n = row / a.H;
+    y = row - n * a.H;
+  };
+  auto pre = [&](int pw, int lane) {
+    if (kRes)  // q -> (channel tile, slice, tap, row, chunk)
+      for (int q = pw * 32 + lane; q < nt * nsl * 9 * ntm * 2; q += kProducerWarps * 32) {
+        const int kc = q & 1, row = (q >> 1) % ntm, set = (q >> 1) / ntm;  // set = (ct * nsl + sl) * 9 + t
+        const int t = set % 9, cs = set / 9, sl = cs % nsl, c = cs / nsl;
+        const int ch = c * 256 + row;
+        chunk_async(sw + set * tap_bytes + tc::tile_offset(row, 8 * kc, 16),
+                    ch < a.Cin ? a.wt + ((size_t)ch * 9 + t) * a.Cout + sl * 16 + 8 * kc : nullptr, a.wt);
+      }
+  };
+  auto load = [&](int u, int st, int lane) {
+    const int i = u / nsl, s = u - i * nsl;
+    int n, y, x0, ct;
+    tile_of(i, n, y, x0, ct);
+    const uint32_t sh = s0 + st * stage;
+    const int o0 = s * 16;
+    for (int q = lane; q < 3 * kHalo * 2; q += kLoadStride) {
+      const int c = q & 1, h = (q >> 1) % kHalo, r = (q >> 1) / kHalo;
       const int yy = y + r - 1, xx = x0 + h - 1;
       const bf16* p = (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
                           ? a.dout + (((size_t)n * a.H + yy) * a.W + xx) * a.Cout + o0 + 8 * c
                           : nullptr;
-      chunk_async(sh + ((r * 2 + c) * kHalo + h) * 16, p, a.dout);
+      chunk_async(sh + halo_off(r, c, h), p, a.dout);
     }
-    for (int i = tid; i < 9 * NT * 2; i += kThreads) {
-      const int kc = i & 1, row = (i >> 1) % NT, t = (i >> 1) / NT;
-      chunk_async(sb + t * tap_bytes + tc::tile_offset(row, 8 * kc, 16),
-                  a.wt + ((size_t)(n0 + row) * 9 + t) * a.Cout + o0 + 8 * kc, a.wt);
+    if (!kRes) {
+      const int n0 = ct * 256, NT = min(256, a.Cin - n0);
+      for (int q = lane; q < 9 * NT * 2; q += kLoadStride) {
+        const int kc = q & 1, row = (q >> 1) % NT, t = (q >> 1) / NT;
+        chunk_async(sh + kHaloBytes + t * tap_bytes + tc::tile_offset(row, 8 * kc, 16),
+                    a.wt + ((size_t)(n0 + row) * 9 + t) * a.Cout + o0 + 8 * kc, a.wt);
+      }
     }
   };
-  auto mma = [&](int st, bool first) {
-    const uint32_t sh = s0 + st * stage, sb = sh + kHaloBytes;
+  auto mma = [&](int u, int st, int buf, int s) {
+    int n, y, x0, ct;
+    tile_of(u / nsl, n, y, x0, ct);
+    const int NT = min(256, a.Cin - ct * 256);
+    const uint32_t idesc = tc::make_idesc_bf16(128, NT);
+    const uint32_t sh = s0 + st * stage;
+    const uint32_t sb = kRes ? sw + (uint32_t)(ct * nsl + s) * 9 * tap_bytes : sh + kHaloBytes;
+    const uint64_t ah = tc::make_desc(sh, kHalo * 16, 128), bw = tc::make_desc(sb, 128, 256);
+    const uint32_t d = tmem + buf * ncols;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
       const int dy = t / 3 - 1, dx = t % 3 - 1;
-      const uint64_t ad = tc::make_desc(sh + ((1 - dy) * 2 * kHalo + 1 - dx) * 16, kHalo * 16, 128);
-      const uint64_t bd = tc::make_desc(sb + t * tap_bytes, 128, 256);
-      tc::mma_bf16(tmem, ad, bd, idesc, !first || t > 0);
+      tc::mma_bf16(d, ah + ((1 - dy) * 2 * kHalo + 1 - dx), bw + t * (tap_bytes >> 4), idesc, s > 0 || t > 0);
     }
   };
-  const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
-  tc::fence_after();
-  if (ok) {
-    const int lw = warp & 3, half = NT >> 1;
-    const int x = x0 + lw * 32 + lane;
+  auto epi = [&](int i, int buf) {
+    const int q = warp & 3;
+    int n, y, x0, ct;
+    tile_of(i, n, y, x0, ct);
+    const int n0 = ct * 256, NT = min(256, a.Cin - n0);
+    const int x = x0 + q * 32 + lane;
     const size_t p = ((size_t)n * a.H + y) * a.W + x;
-    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
-    for (int c0 = (warp >> 2) * half; c0 < (warp >> 2) * half + half; c0 += 8) {
+    const uint32_t taddr = tmem + buf * ncols + ((uint32_t)(q * 32) << 16);
+    for (int c0 = 0; c0 < NT; c0 += 8) {
       float v[8];
       tc::tmem_ld8(taddr + c0, v);
       if (x < a.W) {
@@ -400,14 +637,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_dgrad_row(ConvDgrad a) {
           float sv[8];
           bf16x8_to_f32(src_chunk(a.s1, a.s2, a.N, a.H, a.W, n, y, x, n0 + c0), sv);
 #pragma unroll
-          for (int i = 0; i < 8; ++i)
-            if (!(sv[i] > 0.0f)) v[i] = 0.0f;
+          for (int k = 0; k < 8; ++k)
+            if (!(sv[k] > 0.0f)) v[k] = 0.0f;
         }
         *reinterpret_cast<uint4*>(a.din + p * a.Cin + n0 + c0) = f32_to_bf16x8(v);
       }
     }
-  }
-  tc_end(tmem, ncols);
+  };
+  ws_tiles<S>(n_tiles, nsl, bars, pre, load, mma, epi, a.err);
+  tc_end(tmem, 2 * ncols);
 }
 
 // ---------------------------------------------------------------------------
@@ -464,10 +702,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_dgrad(ConvDgrad a) {
   };
   auto mma = [&](int st, bool first) {
     const uint32_t a0 = s0 + st * stage, b0 = a0 + a_bytes;
+    // consecutive K steps are 256 B apart: +16 in the descriptors' address field
+    const uint64_t ad = tc::make_desc(a0, 128, kSlice * 16), bd = tc::make_desc(b0, 128, kSlice * 16);
 #pragma unroll
-    for (int s = 0; s < kSlice / 16; ++s)
-      tc::mma_bf16(tmem, tc::make_desc(a0 + s * 256, 128, kSlice * 16), tc::make_desc(b0 + s * 256, 128, kSlice * 16),
-                   idesc, !first || s > 0);
+    for (int s = 0; s < kSlice / 16; ++s) tc::mma_bf16(tmem, ad + 16 * s, bd + 16 * s, idesc, !first || s > 0);
   };
   const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
@@ -548,10 +786,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_wgrad(ConvWgrad a) {
   };
   auto mma = [&](int st, bool first) {
     const uint32_t a0 = s0 + st * stage, b0 = a0 + a_bytes;
+    const uint64_t ad = tc::make_desc(a0, 16 * 128, 128), bd = tc::make_desc(b0, 16 * a.Cout, 128);
 #pragma unroll
     for (int s = 0; s < kSlice / 16; ++s)
-      tc::mma_bf16(tmem, tc::make_desc(a0 + s * 2 * 16 * 128, 16 * 128, 128),
-                   tc::make_desc(b0 + s * 2 * 16 * a.Cout, 16 * a.Cout, 128), idesc, !first || s > 0);
+      tc::mma_bf16(tmem, ad + s * 2 * 128, bd + s * 2 * a.Cout, idesc, !first || s > 0);
   };
   const bool ok = conv_pipeline<S>(n_slices, bars, load, mma, a.err);
   tc::fence_after();
@@ -571,14 +809,149 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_wgrad(ConvWgrad a) {
 }
 
 // ---------------------------------------------------------------------------
+// weight gradient, row tiles: a CTA owns source channels [c0, c0 + CR)
+// (CR <= 48) for all nine taps and sums over a run of row tiles (TW pixels
+// of one image row, TW = 64 or 128).  GEMM M = output channels (the 128
+// accumulator lanes; lanes >= Cout are never read), N = CR per tap, K = the
+// tile's pixels, both operands MN-major:
+//   A = the dout tile, chunk g of pixel k at (g * TW + k) * 16
+//   B = the 3-row source halo, chunk ch of pixel h of row r at
+//       ((r * CR / 8 + ch) * (TW + 2) + h) * 16
+// Tap t = (dy, dx) reads halo row dy + 1 shifted by dx pixels (any 16-byte
+// shift of an MN-major operand whose K neighbours are 16 B apart is a legal
+// start address) into accumulator columns [t * CR, t * CR + CR).  Per tile a
+// CTA copies the dout tile and the halo once, so the source is read about
+// three times and dout Cin / CR times, against nine and 9 Cin / 128 times in
+// k_conv_wgrad.  The accumulator lives in TMEM across all of the CTA's tiles;
+// one set of FP32 atomics per CTA combines the runs.
+// ---------------------------------------------------------------------------
+template <int S>
+__global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t full[S], empty[S];
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int TW = a.tw, TW2 = a.tw + 2;
+  const int c0 = blockIdx.x * a.cr;
+  const int CR = min(a.cr, a.Cin - c0);  // this CTA's channels (multiple of 16)
+  const int nch = CR >> 3, nco = a.Cout >> 3;
+  const int TR = (a.W + TW - 1) / TW;  // tiles per image row
+  const int T = a.N * a.H * TR;
+  const int tb = blockIdx.y * a.tiles_per_cta;
+  const int n_tiles = max(0, min(a.tiles_per_cta, T - tb));
+  const uint32_t ncols = 9 * a.cr <= 256 ? 256 : 512;
+  const uint32_t dout_bytes = (uint32_t)a.Cout * TW * 2;
+  const uint32_t stage = dout_bytes + 3u * (a.cr >> 3) * TW2 * 16;
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) {
+      tc::mbar_init(&full[i], kLoadStride);
+      tc::mbar_init(&empty[i], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = tc::make_idesc_bf16(128, CR, true, true);
+  const uint32_t s0 = tc::smem_u32(smem);
+  // a producer's starting item and the per-iteration step of the two copy
+  // loops (items: dout = (pixel k, chunk g), g fastest; halo = (row r, pixel
+  // h, chunk ch), ch fastest, so neighbouring threads read contiguous bytes)
+  const int pt = lane;
+  const int d_g0 = pt % nco, d_k0 = pt / nco, d_dg = kLoadStride % nco, d_dk = kLoadStride / nco;
+  const int h_c0 = pt % nch, h_p0 = pt / nch, h_dc = kLoadStride % nch, h_dp = kLoadStride / nch;
+  auto load = [&](int slice, int st, int ptid) {
+    const uint32_t sd = s0 + st * stage, sh = sd + dout_bytes;
+    const int j = tb + slice;
+    const int row = j / TR, x0 = (j - row * TR) * TW;  // row = n * H + y
+    const int n = row / a.H, y = row - n * a.H;
+    const bf16* drow = a.dout + (size_t)row * a.W * a.Cout;
+    for (int i = ptid, g = d_g0, k = d_k0; i < TW * nco; i += kLoadStride) {
+      const bf16* p = x0 + k < a.W ? drow + (size_t)(x0 + k) * a.Cout + g * 8 : nullptr;
+      chunk_async(sd + (g * TW + k) * 16, p, a.dout);
+      g += d_dg;
+      k += d_dk;
+      if (g >= nco) {
+        g -= nco;
+        ++k;
+      }
+    }
+    int r = 0, h = h_p0;
+    while (h >= TW2) {
+      h -= TW2;
+      ++r;
+    }
+    for (int i = ptid, ch = h_c0; i < 3 * TW2 * nch; i += kLoadStride) {
+      const bf16* p = src_ptr(a.s1, a.s2, a.H, a.W, n, y + r - 1, x0 + h - 1, c0 + 8 * ch);
+      chunk_async(sh + ((r * nch + ch) * TW2 + h) * 16, p, a.s1.ptr);
+      ch += h_dc;
+      h += h_dp;
+      if (ch >= nch) {
+        ch -= nch;
+        ++h;
+      }
+      while (h >= TW2) {
+        h -= TW2;
+        ++r;
+      }
+    }
+  };
+  auto mma = [&](int it, int st) {
+    const bool first = it == 0;
+    const uint32_t sd = s0 + st * stage, sh = sd + dout_bytes;
+    // descriptors built once; a K step (16 pixels) is +256 B = +16 in the
+    // address field, tap t's B starts (dy + 1) halo rows and 1 + dx pixels in
+    const uint64_t ad0 = tc::make_desc(sd, 128, TW * 16), bh = tc::make_desc(sh, 128, TW2 * 16);
+    const int nks = TW / 16;
+#pragma unroll 1
+    for (int t = 0; t < 9; ++t) {
+      const int dy = t / 3 - 1, dx = t % 3 - 1;
+      const uint64_t bd = bh + ((dy + 1) * nch * TW2 + 1 + dx);
+      const uint32_t d = tmem + t * CR;
+      tc::mma_bf16(d, ad0, bd, idesc, !first);
+#pragma unroll 8
+      for (int ks = 1; ks < nks; ++ks) tc::mma_bf16(d, ad0 + 16 * ks, bd + 16 * ks, idesc, true);
+    }
+  };
+  const bool ok = ws_ring<S>(n_tiles, full, empty, load, mma, a.err);
+  const int lw = warp & 3;
+  if (ok && n_tiles > 0 && lw * 32 < a.Cout) {
+    // warp w reads lanes 32 (w % 4) .. + 31 (output channel o), half w / 4 of
+    // the 9 CR / 8 column chunks
+    const int o = lw * 32 + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
+    const int nq = 9 * nch, q0 = (warp >> 2) * (nq >> 1), q1 = (warp >> 2) ? nq : (nq >> 1);
+    const bool vec = ((reinterpret_cast<uintptr_t>(a.dw) & 15) == 0);
+    for (int q = q0; q < q1; ++q) {
+      float v[8];
+      tc::tmem_ld8(taddr + q * 8, v);
+      if (o < a.Cout) {
+        const int t = q / nch, cl = (q - t * nch) * 8;
+        float* d = a.dw + ((size_t)o * 9 + t) * a.Cin + c0 + cl;
+        if (vec) {
+          atomicAdd(reinterpret_cast<float4*>(d), make_float4(v[0], v[1], v[2], v[3]));
+          atomicAdd(reinterpret_cast<float4*>(d + 4), make_float4(v[4], v[5], v[6], v[7]));
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) atomicAdd(d + i, v[i]);
+        }
+      }
+    }
+  }
+  tc_end(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
 // Stages of the ring for a B tile of nb rows: 3 stages up to 128 rows, 2
 // beyond (72 KB per CTA for nb <= 64, at most 96 KB otherwise).
 static int stages_for(int nb) { return nb <= 128 ? 3 : 2; }
 
 template <class K4, class K3, class K2, class Args>
 static cudaError_t launch_staged(K4 k4, K3 k3, K2 k2, int stages, dim3 grid, size_t stage_bytes, const Args& a,
-                                 cudaStream_t st) {
-  size_t smem = stage_bytes * stages;
+                                 cudaStream_t st, size_t extra = 0) {
+  size_t smem = stage_bytes * stages + extra;
   cudaError_t e;
   if (stages == 4) {
     if ((e = cudaFuncSetAttribute(k4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
@@ -593,20 +966,67 @@ static cudaError_t launch_staged(K4 k4, K3 k3, K2 k2, int stages, dim3 grid, siz
   return cudaGetLastError();
 }
 
-// Row tiles pay off once a row holds at least half a tile; they need input
-// slices of 16 channels and a grid that fits the y / z limits.
-static bool use_rows(int N, int H, int W, int Ck, int nz = 1) {
-  return W >= 64 && Ck % 16 == 0 && H <= 65535 && (long long)N * nz <= 65535;
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 148;
+  }
+  return n;
 }
+
+// Row tiles pay off once a row holds at least half a tile; they need input
+// slices of 16 channels.
+static bool use_rows(int W, int Ck) { return W >= 64 && Ck % 16 == 0; }
+
+// Persistent tile kernels (ws_tiles): one CTA per SM, shared memory padded
+// past half the SM so that a second CTA never waits on the first one's TMEM
+// columns.  Resident weights take a 7-stage halo ring; streamed weights the
+// deepest ring (6, 4 or 2 stages) that fits 200 KB.
+template <class KR, class K6, class K4, class K2, class Args>
+static cudaError_t launch_tiles(KR kr, K6 k6, K4 k4, K2 k2, bool res, size_t stage, size_t res_bytes, long long T,
+                                const Args& a, cudaStream_t st) {
+  if (T <= 0) return cudaSuccess;
+  int S = 7;
+  size_t smem = 7 * stage + res_bytes;
+  if (!res) {
+    S = 6 * stage <= 200 * 1024 ? 6 : (4 * stage <= 200 * 1024 ? 4 : 2);
+    smem = S * stage;
+  }
+  smem = std::max(smem, (size_t)116 * 1024);
+  const unsigned grid = (unsigned)std::min<long long>(T, sm_count());
+  cudaError_t e;
+#define RTX_LAUNCH_TILES(K)                                                                          \
+  if ((e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e; \
+  K<<<grid, kTileThreads, smem, st>>>(a);
+  if (res) {
+    RTX_LAUNCH_TILES(kr)
+  } else if (S == 6) {
+    RTX_LAUNCH_TILES(k6)
+  } else if (S == 4) {
+    RTX_LAUNCH_TILES(k4)
+  } else {
+    RTX_LAUNCH_TILES(k2)
+  }
+#undef RTX_LAUNCH_TILES
+  return cudaGetLastError();
+}
+
+// weights kept in shared memory by the persistent kernels up to this size
+constexpr size_t kResidentWeights = 96 * 1024;
 
 cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
   if (a.Cout % 16 || a.Cout > 256 || a.Cin % 8) return cudaErrorInvalidValue;
-  if (use_rows(a.N, a.H, a.W, a.Cin)) {
-    size_t stage = kHaloBytes + (size_t)9 * a.Cout * 32;
-    dim3 grid((a.W + 127) / 128, a.H, a.N);
-    return launch_staged(k_conv_fwd_row<3>, k_conv_fwd_row<3>, k_conv_fwd_row<2>, stage <= 34 * 1024 ? 3 : 2,
-                         grid, stage, a, st);
+  if (use_rows(a.W, a.Cin)) {
+    const size_t wbytes = (size_t)9 * a.Cin * a.Cout * 2;
+    const bool res = wbytes <= kResidentWeights;
+    const size_t stage = res ? kHaloBytes : kHaloBytes + (size_t)9 * a.Cout * 32;
+    const long long T = (long long)a.N * a.H * ((a.W + 127) / 128);
+    return launch_tiles(k_conv_fwd_rows<7, true>, k_conv_fwd_rows<6, false>, k_conv_fwd_rows<4, false>,
+                        k_conv_fwd_rows<2, false>, res, stage, res ? wbytes : 0, T, a, st);
   }
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
   return launch_staged(k_conv_fwd<4>, k_conv_fwd<3>, k_conv_fwd<2>, stages_for(a.Cout),
@@ -617,11 +1037,14 @@ cudaError_t conv_dgrad(const ConvDgrad& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
   if (a.Cin % 16 || a.Cout % 8) return cudaErrorInvalidValue;
   const int nt = (a.Cin + 255) / 256;
-  if (use_rows(a.N, a.H, a.W, a.Cout, nt)) {
-    size_t stage = kHaloBytes + (size_t)9 * std::min(256, a.Cin) * 32;
-    dim3 grid((a.W + 127) / 128, a.H, a.N * nt);
-    return launch_staged(k_conv_dgrad_row<3>, k_conv_dgrad_row<3>, k_conv_dgrad_row<2>,
-                         stage <= 34 * 1024 ? 3 : 2, grid, stage, a, st);
+  if (use_rows(a.W, a.Cout)) {
+    const int ntm = std::min(256, a.Cin);
+    const size_t wbytes = (size_t)nt * ntm * 9 * a.Cout * 2;
+    const bool res = wbytes <= kResidentWeights;
+    const size_t stage = res ? kHaloBytes : kHaloBytes + (size_t)9 * ntm * 32;
+    const long long T = (long long)a.N * a.H * ((a.W + 127) / 128) * nt;
+    return launch_tiles(k_conv_dgrad_rows<7, true>, k_conv_dgrad_rows<6, false>, k_conv_dgrad_rows<4, false>,
+                        k_conv_dgrad_rows<2, false>, res, stage, res ? wbytes : 0, T, a, st);
   }
   int nb = std::min(256, a.Cin);
   size_t stage = 128 * kSlice * 2 + (size_t)nb * kSlice * 2;
@@ -638,9 +1061,48 @@ int wgrad_pixels_per_cta(long long P, int Cout, int Cin) {
   return (int)std::max(64LL, std::min(per, 1LL << 30));
 }
 
-cudaError_t conv_wgrad(const ConvWgrad& a, cudaStream_t st) {
-  long long P = (long long)a.N * a.H * a.W;
-  if (P >= (1LL << 31) || a.Cout % 16 || a.Cout > 256) return cudaErrorInvalidValue;
+// Channels per CTA of the row-tile weight gradient (16, 32 or 48; the last
+// range may be narrower): fewest ranges, weighing each range's fixed dout
+// copy against its width.
+static int wgrad_row_channels(int Cin, int Cout) {
+  int best = 16;
+  long long best_cost = -1;
+  for (int cr : {48, 32, 16}) {
+    if (cr > Cin) continue;
+    long long cost = (long long)((Cin + cr - 1) / cr) * (cr + Cout / 4 + 8);
+    if (best_cost < 0 || cost < best_cost) best = cr, best_cost = cost;
+  }
+  return best;
+}
+
+cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
+  long long P = (long long)a0.N * a0.H * a0.W;
+  if (P >= (1LL << 31) || a0.Cout % 16 || a0.Cout > 256) return cudaErrorInvalidValue;
+  if (use_rows(a0.W, a0.Cin) && a0.Cout <= 128) {
+    ConvWgrad a = a0;
+    a.tw = a.W >= 128 ? 128 : 64;
+    a.cr = wgrad_row_channels(a.Cin, a.Cout);
+    const int nr = (a.Cin + a.cr - 1) / a.cr;
+    const long long T = (long long)a.N * a.H * ((a.W + a.tw - 1) / a.tw);
+    const size_t stage = (size_t)a.Cout * a.tw * 2 + (size_t)3 * (a.cr / 8) * (a.tw + 2) * 16;
+    const int S = 4 * stage <= 190 * 1024 ? 4 : (3 * stage <= 190 * 1024 ? 3 : 2);
+    // the MMA's A operand spans 128 rows of TW pixels; rows past Cout are
+    // read (and their accumulator lanes ignored), so they must lie inside the
+    // allocation
+    const size_t a_span = (size_t)256 * a.tw;
+    size_t extra = a_span > stage ? a_span - stage : 0;
+    const int per_sm = (9 * a.cr <= 256 && S * stage + extra <= 110 * 1024) ? 2 : 1;
+    // one CTA per SM when it takes all 512 TMEM columns: a second CTA on the
+    // SM would wait in its allocation for the first to finish
+    if (per_sm == 1 && S * stage + extra < 116 * 1024) extra = 116 * 1024 - S * stage;
+    const long long ctas = (long long)sm_count() * per_sm;
+    const long long npg = std::max(1LL, ctas / nr);
+    a.tiles_per_cta = (int)((T + npg - 1) / npg);
+    const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
+    return launch_staged(k_conv_wgrad_row<4>, k_conv_wgrad_row<3>, k_conv_wgrad_row<2>, S, dim3(nr, gy), stage, a,
+                         st, extra);
+  }
+  const ConvWgrad& a = a0;
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
   dim3 grid((9 * a.Cin + 127) / 128, (unsigned)((P + a.pix_per_cta - 1) / a.pix_per_cta));
   return launch_staged(k_conv_wgrad<4>, k_conv_wgrad<3>, k_conv_wgrad<2>, stages_for(a.Cout), grid, stage, a, st);

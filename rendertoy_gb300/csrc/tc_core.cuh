@@ -16,7 +16,7 @@
 namespace rtx {
 namespace tc {
 
-constexpr int kWaitLimit = 1 << 26;  // bounded spin on an mbarrier
+constexpr int kWaitLimit = 1 << 22;  // bounded spin on an mbarrier (far above any legitimate wait)
 enum TcError : int { kErrMbarTimeout = 8 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -79,6 +79,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// One arrival on the barrier (release: this thread's earlier writes are
+// visible to a thread that observes the phase complete).
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // Wait for phase `parity` of the barrier; false after kWaitLimit polls.

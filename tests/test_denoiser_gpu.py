@@ -41,6 +41,8 @@ CASES = [  # N, H, W, C1, up1, C2, Cout, relu
     (2, 2, 128, 64, 1, 32, 64, 1),     # upsampled source + skip in row tiles
     (1, 2, 64, 160, 1, 128, 128, 1),   # 288 inputs: two data-gradient tiles
     (1, 2, 96, 16, 0, 0, 16, 0),       # the output layer's shape
+    (1, 2, 128, 96, 1, 64, 64, 1),     # 160 inputs: five weight-gradient channel ranges
+    (8, 64, 256, 32, 0, 0, 32, 1),     # several row tiles per weight-gradient CTA (ring wraps)
 ]
 
 
