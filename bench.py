@@ -96,14 +96,44 @@ def denoiser_block(ctx, rank):
     out = torch.empty(1, 1088, 1920, 3, device="cuda")
     infer_ms = med(lambda: ctx.dn_infer(fr, out))
     peak, kind = peaks("bf16_tflops")
+    hbm, _ = peaks()
     train_tf = 3 * fwd * N * H * W / (train_ms * 1e-3) / 1e12
     infer_tf = fwd * 1088 * 1920 / (infer_ms * 1e-3) / 1e12
+    bound_train = layer_bound_ms(ctx.dn_layers(), N * H * W, peak, hbm, train=True)
+    bound_infer = layer_bound_ms(ctx.dn_layers(), 1088 * 1920, peak, hbm, train=False)
     return {"train_step_ms": train_ms, "minibatch": [N, H, W], "train_tflops": train_tf,
             "train_kernel_launches": train_launches, "infer_ms_1920x1088": infer_ms, "infer_tflops": infer_tf,
             "gflop_per_mpixel_forward": fwd * 1e6 / 1e9,
             "roofline": {"bound": "tensor", "achieved": train_tf, "peak": peak, "peak_kind": kind,
                          "unit": "TFLOP/s", "frac": train_tf / peak,
-                         "note": "whole training step (all 88 launches) against the bf16 burst peak"}}
+                         "note": "whole training step (all 88 launches) against the bf16 burst peak"},
+            "layer_roofline": {"train_bound_ms": bound_train, "train_frac": bound_train / train_ms,
+                               "infer_bound_ms": bound_infer, "infer_frac": bound_infer / infer_ms,
+                               "note": "sum over layers and passes of max(FLOPs / bf16 peak, "
+                                       "compulsory bytes / HBM peak) against the measured time"}}
+
+
+def layer_bound_ms(layers, px0, tflops, gbs, train):
+    """Lower bound on the network's time from each convolution's own
+    roofline: per layer and pass, max(tensor FLOPs / peak, compulsory HBM
+    bytes / peak), summed.  Compulsory bytes per output pixel of a layer
+    (BF16 activations): forward reads its sources once (an upsampled source
+    at a quarter of the pixels) and writes Cout; the data gradient reads dout
+    and the source (ReLU mask) and writes the source's gradient; the weight
+    gradient reads dout and the source.  The small elementwise kernels
+    (pooling, loss, Adam) are left out, so the bound is optimistic."""
+    t = 0.0
+    for L in layers:
+        px = px0 / 4 ** L["level"]
+        ci, co = L["cin_pad"], L["cout_pad"]
+        c1 = L["c1_pad"]
+        src = (c1 / 4 if L["up1"] else c1) + (ci - c1)
+        flops = 2 * 9 * ci * co * px
+        passes = [(flops, (src + co) * 2 * px)]
+        if train:
+            passes += [(flops, (co + src + ci) * 2 * px), (flops, (co + src) * 2 * px)]
+        t += sum(max(f / (tflops * 1e12), b / (gbs * 1e9)) for f, b in passes)
+    return t * 1e3
 
 
 def compositor_block(ctx, img, tmp, out, flush):

@@ -16,6 +16,11 @@ render.
 
     python -m rendertoy_gb300.denoise train --scenes 256 --steps 2000 --out DIR
     python -m rendertoy_gb300.denoise study --params DIR/params.npy --out DIR
+    python -m rendertoy_gb300.denoise step --batch 8 --steps 2   # profiling
+
+``step`` runs Adam steps of the network on one seeded random minibatch
+already on the device (no rendering), the unit the convolution profiles
+capture.
 """
 from __future__ import annotations
 
@@ -168,7 +173,7 @@ def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 2, 4),
 def _main():
     import rendertoy_gb300 as rt
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train", "study"])
+    ap.add_argument("cmd", choices=["train", "study", "step"])
     ap.add_argument("--out", default="denoise_out")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--res", type=int, default=256)
@@ -180,11 +185,22 @@ def _main():
     ap.add_argument("--study-res", default="1920x1080")
     ap.add_argument("--ref-spp", type=int, default=16384)
     a = ap.parse_args()
-    os.makedirs(a.out, exist_ok=True)
     ctx = rt.Context(0)
     ctx.dn_init(0)
     if a.params:
         ctx.dn_set_params(np.load(a.params))
+    if a.cmd == "step":
+        import torch
+        g = torch.Generator(device="cuda").manual_seed(0)
+        xb = torch.rand(a.batch, a.res, a.res, 10, device="cuda", generator=g)
+        yb = 2 * torch.rand(a.batch, a.res, a.res, 3, device="cuda", generator=g)
+        ms = []
+        for _ in range(a.steps):
+            loss = ctx.dn_train_step(xb, yb, lr=a.lr)
+            ms.append(ctx.stats()["last_gpu_ms"])
+        print(json.dumps({"batch": a.batch, "res": a.res, "steps": a.steps, "loss": loss, "ms": ms}))
+        return
+    os.makedirs(a.out, exist_ok=True)
     if a.cmd == "train":
         t0 = time.time()
         X, Y = make_pairs(ctx, range(a.scenes), W=a.res, H=a.res, target_spp=a.target_spp)
