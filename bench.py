@@ -138,10 +138,14 @@ def layer_bound_ms(layers, px0, tflops, gbs, train):
 
 def compositor_block(ctx, img, tmp, out, flush):
     """The Compositor filters timed alone on the resident 1024^2 image (the
-    library's CUDA events, median of 10; L2 flushed before each run):
-    algorithmic bytes per pixel = 12 B read + 12 B written per pass (blur: two
-    passes; 5 x 5 convolution: one; bloom: extract + blur x, then blur y + add
-    = 12 + 12 + 24 + 12)."""
+    library's CUDA events around the whole call, median of 10; L2 flushed
+    before each run): algorithmic bytes per pixel = 12 B read + 12 B written
+    per pass (blur: two passes; 5 x 5 convolution: one; bloom: extract + blur
+    x, then blur y + add = 12 + 12 + 24 + 12).  The filters keep the
+    reference's unfused multiply-then-add per tap, so FP32 issue bounds them
+    before HBM does: `bound_us` = max(bytes / HBM peak, FP32 operations /
+    the FP32 rate of 152 SMs x 128 lanes at 2.07 GHz), `frac_bound` = that
+    bound / the measured time."""
     import torch
     peak, kind = peaks()
 
@@ -155,13 +159,18 @@ def compositor_block(ctx, img, tmp, out, flush):
         return float(np.median(t[2:]))
 
     px = RES * RES
+    fp32_ops = 152 * 128 * 2.07e9  # FP32 operations per second, nominal
+    blur_ops = 2 * BLUR_SIZE * 3 * 2  # two passes, a multiply and an add per tap and channel
     res = {}
-    for name, fn, bpp in (("gaussian_blur_49", lambda: ctx.gaussian_blur(img, BLUR_SIZE, BLUR_SIGMA, out=tmp), 48),
-                          ("convolve_5x5", lambda: ctx.convolve(tmp, EDGE5, absval=True, out=out), 24),
-                          ("bloom_49", lambda: ctx.bloom(img, BLUR_SIZE, BLUR_SIGMA, 1.0, out=tmp), 60)):
+    for name, fn, bpp, ops in (
+            ("gaussian_blur_49", lambda: ctx.gaussian_blur(img, BLUR_SIZE, BLUR_SIGMA, out=tmp), 48, blur_ops),
+            ("convolve_5x5", lambda: ctx.convolve(tmp, EDGE5, absval=True, out=out), 24, 25 * 3 * 2 + 3),
+            ("bloom_49", lambda: ctx.bloom(img, BLUR_SIZE, BLUR_SIGMA, 1.0, out=tmp), 60, blur_ops + 8)):
         ms = med(fn)
         gbs = bpp * px / (ms * 1e-3) / 1e9
-        res[name] = {"ms": ms, "bytes_per_pixel": bpp, "achieved_gbs": gbs, "frac_hbm": gbs / peak}
+        bound_us = max(bpp * px / (peak * 1e9), ops * px / fp32_ops) * 1e6
+        res[name] = {"ms": ms, "bytes_per_pixel": bpp, "achieved_gbs": gbs, "frac_hbm": gbs / peak,
+                     "fp32_ops_per_pixel": ops, "bound_us": bound_us, "frac_bound": bound_us / (ms * 1e3)}
     res["peak_gbs"] = peak
     res["peak_kind"] = kind
     return res

@@ -115,7 +115,8 @@ struct rtx_context {
   int pinned_cap = 0;
   rtx::nn::UNet* dn = nullptr;
   DevBuf weights;
-  std::vector<float> host_weights;
+  std::vector<float> host_weights;  // what `weights` holds when weights_valid
+  bool weights_valid = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   rtx_stats stats{};
   bool pending_timing = false;
@@ -250,12 +251,19 @@ void gaussian_weights(int size, float sigma, float* w) {
   for (int j = 0; j < size; ++j) w[j] /= sum;
 }
 
+// Filter weights to the device.  The device copy is kept while the weights
+// do not change: a frame loop applies the same filters every frame.
 int upload_weights(rtx_context* c, const float* w, size_t n) {
+  if (c->weights_valid && c->host_weights.size() == n &&
+      std::memcmp(c->host_weights.data(), w, n * sizeof(float)) == 0)
+    return RTX_OK;
+  c->weights_valid = false;
   c->host_weights.assign(w, w + n);
   RTX_CUDA(c->weights.ensure(n * sizeof(float)), "weights alloc");
   RTX_CUDA(cudaMemcpyAsync(c->weights.p, c->host_weights.data(), n * sizeof(float),
                            cudaMemcpyHostToDevice, c->stream),
            "weights H2D");
+  c->weights_valid = true;
   return RTX_OK;
 }
 
@@ -369,6 +377,7 @@ void rtx_destroy(rtx_context* c) {
   if (c->h_jobq_pinned) cudaFreeHost(c->h_jobq_pinned);
   delete c->dn;
   c->weights.release();
+  c->weights_valid = false;
   if (c->pt) pt_workspace_destroy(c->pt);
   if (c->d_err) cudaFree(c->d_err);
   if (c->d_counters) cudaFree(c->d_counters);

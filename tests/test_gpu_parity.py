@@ -105,6 +105,40 @@ def test_compositor_bit_exact(ctx, golden, oracle):
             assert np.array_equal(bits(gpu[rows]), bits(g[f"{name}_{tag}"][rows])), (tag, name)
 
 
+@pytest.mark.parametrize("shape", [(131, 2061), (1, 1030), (70, 9), (200, 1024)])
+def test_compositor_tiles_nan_inf(ctx, oracle, shape):
+    """Images that cross the kernels' tiles (rows of more than 1,024 pixels,
+    columns of more than 64 rows, ragged edges, single rows) and carry the NaN
+    and infinite pixels renders can hold: every filter still bit-exact, and a
+    NaN spreads exactly as far as the reference's taps reach."""
+    H, W = shape
+    rng = np.random.RandomState(H * 7919 + W)
+    img = rng.exponential(0.7, (H, W, 3)).astype(np.float32)
+    flat = img.reshape(-1, 3)
+    bad = rng.choice(H * W, size=max(1, H * W // 997), replace=False)
+    flat[bad[::2], 0] = np.nan
+    flat[bad[1::2], 2] = np.inf
+    k5 = rng.normal(0, 1, (5, 5)).astype(np.float32)
+    k3 = rng.normal(0, 1, (3, 3)).astype(np.float32)
+    cases = {
+        "blur49": lambda c: c.gaussian_blur(img, 49, 8.0),
+        "blur7": lambda c: c.gaussian_blur(img, 7, 1.5),
+        "blur2": lambda c: c.gaussian_blur(img, 2, 0.7),
+        "bloom17": lambda c: c.bloom(img, 17, 3.0, 1.0),
+        "conv5_abs": lambda c: c.convolve(img, k5, absval=True),
+        "conv3_len": lambda c: c.convolve(img, k3, length=True),
+        "conv3_norm": lambda c: c.convolve(img, k3, normalize=True),
+    }
+    for name, fn in cases.items():
+        gpu, orc = fn(ctx), fn(oracle)
+        # NaN payloads are not portable (the host propagates the input's, the
+        # GPU writes its canonical NaN): NaN positions must agree, every other
+        # value bit for bit
+        nan = np.isnan(orc)
+        assert np.array_equal(np.isnan(gpu), nan), (shape, name)
+        assert np.array_equal(bits(gpu)[~nan], bits(orc)[~nan]), (shape, name)
+
+
 def test_compositor_large_kernel(ctx, oracle):
     """Bloom(500, 50, 1) as RenderToy's Cornell demo applies it: a kernel wider
     than the image takes the direct path; still bit-exact."""
