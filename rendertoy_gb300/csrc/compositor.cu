@@ -127,28 +127,13 @@ __global__ void __launch_bounds__(kConvTX * kConvTY) k_convolve_tiled(const floa
   o[2] = acc.z;
 }
 
-// Two FP32 lanes in one 64-bit register: Blackwell's packed FP32
-// instructions (.f32x2) round each lane exactly as the scalar instruction
-// does, at twice the issue rate.  ptxas contracts a packed multiply followed
-// by a packed add into one fused operation even under --fmad=false, so the
-// product is formed as fma(p, w, z) with z = -0.0 passed in at run time:
-// that rounds p * w once, exactly as a multiply does (x + -0 == x, also for
-// x = +0 and -0), and leaves nothing for ptxas to contract with the add.
-typedef unsigned long long f2_t;
-RTX_DEV f2_t f2_pack(float lo, float hi) {
-  f2_t r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-RTX_DEV void f2_unpack(f2_t v, float& lo, float& hi) { asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v)); }
-// acc + p * w with the product rounded before the addition; nz holds -0.0 in
-// both lanes and must not be known to the compiler
-RTX_DEV f2_t f2_mul_add(f2_t acc, f2_t p, f2_t w, f2_t nz) {
-  f2_t m, r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(m) : "l"(p), "l"(w), "l"(nz));
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(acc), "l"(m));
-  return r;
-}
+// acc + p * w with the product rounded before the addition, exactly as the
+// scalar multiply and add.  ptxas contracts a packed multiply followed by a
+// packed add into one fused operation even under --fmad=false, so the
+// product is formed as fma(p, w, nz) with nz = -0.0 passed in at run time
+// (unknown to the compiler): that rounds p * w once, as a multiply does
+// (x + -0 == x, also for x = +0 and -0), and leaves nothing to contract.
+RTX_DEV f2_t f2_mul_add(f2_t acc, f2_t p, f2_t w, f2_t nz) { return f2_add(acc, f2_fma(p, w, nz)); }
 RTX_DEV float f3c(F3 p, int c) { return c == 0 ? p.x : (c == 1 ? p.y : p.z); }
 
 // Small 2-D kernels (3 x 3, 5 x 5), register-blocked: a thread computes

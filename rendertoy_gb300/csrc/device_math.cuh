@@ -25,6 +25,40 @@ namespace rtx {
 #define RTX_LOBE RTX_DEV
 #endif
 
+// Two FP32 lanes in one 64-bit register: Blackwell's packed FP32
+// instructions (.f32x2) round each lane exactly as the scalar instruction
+// does.  They occupy the FMA pipe for two cycles, so they save issue slots,
+// not FMA throughput.
+typedef unsigned long long f2_t;
+RTX_DEV f2_t f2_pack(float lo, float hi) {
+  f2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+RTX_DEV void f2_unpack(f2_t v, float& lo, float& hi) { asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v)); }
+// a * b + c, one rounding per lane
+RTX_DEV f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+  f2_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+RTX_DEV f2_t f2_add(f2_t a, f2_t b) {
+  f2_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// three-input minimum / maximum (one instruction on sm_100 and later)
+RTX_DEV float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+RTX_DEV float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 struct F3 {
   float x, y, z;
 };

@@ -29,12 +29,18 @@ namespace rtx {
 constexpr int kMaxDepthSlots = 64;
 // material sort: at most this many materials (+1 bin for misses)
 constexpr int kMaxSortBins = 4096;
-// minimum resident blocks of 128 threads per SM (register budget)
+// Minimum resident blocks of 128 threads per SM, i.e. the register budget
+// (measured on the 1.3M-triangle frame: the traversal kernels are latency
+// bound and gain from more warps until spills begin; shading at 8 blocks
+// spills ~170 B yet beats 6 and 5 blocks by 3-7 %).
 #ifndef RTX_SHADE_MINB
 #define RTX_SHADE_MINB 8
 #endif
-#ifndef RTX_TRACE_MINB
-#define RTX_TRACE_MINB 1
+#ifndef RTX_EXTEND_MINB
+#define RTX_EXTEND_MINB 10
+#endif
+#ifndef RTX_CONNECT_MINB
+#define RTX_CONNECT_MINB 8
 #endif
 // path state 6 x 16 B + shadow record 4 x 16 B + three queue entries
 constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 3 * 4;
@@ -291,7 +297,7 @@ __global__ void __launch_bounds__(128) k_extend(PtArgs a, DeviceScene s) {
 // Variant: a warp takes 32 rays at a time and each lane traces its ray to the
 // end before the warp takes the next batch.
 template <bool kCount, bool kWide, bool kJobs>
-__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_extend_batch(PtArgs a, DeviceScene s0) {
+__global__ void __launch_bounds__(128, RTX_EXTEND_MINB) k_extend_batch(PtArgs a, DeviceScene s0) {
   const int n = a.counts[a.depth];
   VisitCount vc;
   int lane = threadIdx.x & 31;
@@ -495,7 +501,7 @@ RTX_DEV bool emitter_hit(const DeviceScene& s, F3 pos, F3 dir, int e, int ex, fl
 RTX_DEV void add_light(const PtArgs& a, const DeviceScene& s, int rec, int n_emitters);
 
 template <bool kCount, bool kWide, bool kJobs>
-__global__ void __launch_bounds__(128, RTX_TRACE_MINB) k_connect_batch(PtArgs a, DeviceScene s0) {
+__global__ void __launch_bounds__(128, RTX_CONNECT_MINB) k_connect_batch(PtArgs a, DeviceScene s0) {
   const int n = a.shadow_counts[a.depth];
   VisitCount vc;
   int lane = threadIdx.x & 31;
