@@ -358,6 +358,8 @@ def main():
     ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batched"],
                     help="batched: 64 procedural scenes in one wavefront per frame (not the default)")
     ap.add_argument("--scenes", type=int, default=64, help="with --workload batched")
+    ap.add_argument("--opt", action="append", default=[],
+                    help="library option NAME=VALUE for the run (e.g. sort_rays=1), recorded in config")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     from rendertoy_gb300 import scenes
@@ -415,6 +417,11 @@ def main():
     sc = scenes.displaced_icosphere(subdiv=args.subdiv)
     gen_s = time.perf_counter() - t0
     ctx = rt.Context(local)
+    opts = {}
+    for o in args.opt:
+        k, v = o.split("=")
+        ctx.set_option(getattr(rt, "OPT_" + k.upper()), int(v))
+        opts[k] = int(v)
     ctx.upload(sc)
     st0 = ctx.stats()
     if args.profile:
@@ -538,7 +545,7 @@ def main():
                        "max_depth": DEPTH, "triangles": sc.n_tris,
                        "l2": "flushed between steps (256 MiB write, outside the timed events)",
                        "bvh_build_ms": st0["bvh_build_ms"], "bvh_nodes": st0["bvh_nodes"],
-                       "scene_gen_s": round(gen_s, 2)},
+                       "scene_gen_s": round(gen_s, 2), "options": opts},
             "mrays_per_s": mrays,
             "rays_per_step": {"extension": rays_e / args.steps, "shadow": rays_s / args.steps},
             "e2e": e2e,

@@ -98,9 +98,14 @@ enum rtx_option {
                                  4-wide tree, batch */
   RTX_OPT_MIN_BUSY = 11,      /* with RTX_OPT_TRAVERSAL = 1: refill a warp once
                                  fewer lanes than this are traversing (0..32) */
-  RTX_OPT_GRAPH = 12          /* 0/1: rtx_render_batch captures its launch
+  RTX_OPT_GRAPH = 12,         /* 0/1: rtx_render_batch captures its launch
                                  sequence as a CUDA graph and replays it for
                                  later frames of the same shape */
+  RTX_OPT_SORT_RAYS = 13      /* 0/1 (default 1): counting-sort the extension
+                                 rays after the primary ones and the shadow
+                                 rays by origin cell and direction octant
+                                 before they are traced (results unchanged;
+                                 only the visiting order) */
 };
 
 typedef struct rtx_context rtx_context;
@@ -250,16 +255,18 @@ int rtx_render_batch(rtx_context* ctx, int n_jobs, const rtx_job* jobs,
  * `scenes` for each; scenes = NULL keeps the uploaded batch and its leaf
  * size -- then threads per block 64 / 128 x paths per wave 2^20, 2^22, 2^24,
  * auto, then the binary or 4-wide tree, then material-sorted shading on /
- * off, coordinate-wise from the context's current options.  The fastest
- * setting stays on the context (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK,
- * RTX_OPT_WAVE_PATHS, RTX_OPT_TRAVERSAL, RTX_OPT_SORT_MATERIAL) and the batch
- * is left built with it. */
+ * off, then ray-sorted traversal on / off, coordinate-wise from the
+ * context's current options.  The fastest setting stays on the context
+ * (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK, RTX_OPT_WAVE_PATHS, RTX_OPT_TRAVERSAL,
+ * RTX_OPT_SORT_MATERIAL, RTX_OPT_SORT_RAYS) and the batch is left built with
+ * it. */
 typedef struct rtx_tune_result {
   int64_t block, wave_paths, leaf_size;
   double ms, ms_default;       /* frame time chosen / at the starting options */
   int trials;
   int sort_material;           /* RTX_OPT_SORT_MATERIAL chosen */
   int traversal;               /* RTX_OPT_TRAVERSAL chosen (0 or 2) */
+  int sort_rays;               /* RTX_OPT_SORT_RAYS chosen */
 } rtx_tune_result;
 int rtx_batch_autotune(rtx_context* ctx, int n_scenes,
                        const rtx_scene_desc* scenes, int n_jobs,

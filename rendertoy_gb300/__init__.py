@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "librtx.so")
 
 OPT_GRAPH = 12
+OPT_SORT_RAYS = 13
 OPT_ASYNC, OPT_WAVE_PATHS, OPT_BLOCK, OPT_SORT_MATERIAL, OPT_COUNT_VISITS, OPT_LEAF_SIZE, \
     OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING, OPT_ACCUMULATE, OPT_TRAVERSAL, OPT_MIN_BUSY = \
     1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11
@@ -59,7 +60,7 @@ class Job(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("block", C.c_int64), ("wave_paths", C.c_int64), ("leaf_size", C.c_int64), ("ms", C.c_double),
                 ("ms_default", C.c_double), ("trials", C.c_int), ("sort_material", C.c_int),
-                ("traversal", C.c_int)]
+                ("traversal", C.c_int), ("sort_rays", C.c_int)]
 
 
 class RtxError(RuntimeError):

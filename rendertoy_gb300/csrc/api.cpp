@@ -79,6 +79,7 @@ struct rtx_context {
   int64_t wave_paths = 0;
   int block = 128;
   bool sort_material = false;
+  bool sort_rays = true;
   bool count_visits = false;
   int leaf_size = 4;
   bool primary_cache = true;
@@ -403,6 +404,7 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
       c->block = (int)v;
       return RTX_OK;
     case RTX_OPT_SORT_MATERIAL: c->sort_material = v != 0; return RTX_OK;
+    case RTX_OPT_SORT_RAYS: c->sort_rays = v != 0; return RTX_OK;
     case RTX_OPT_COUNT_VISITS: c->count_visits = v != 0; return RTX_OK;
     case RTX_OPT_LEAF_SIZE:
       if (v < 1 || v > kMaxLeaf) return fail(c, RTX_ERR_INVALID, "leaf size must be in [1, 8]");
@@ -431,6 +433,7 @@ int rtx_get_option(rtx_context* c, int option, int64_t* v) {
     case RTX_OPT_WAVE_PATHS: *v = c->wave_paths; return RTX_OK;
     case RTX_OPT_BLOCK: *v = c->block; return RTX_OK;
     case RTX_OPT_SORT_MATERIAL: *v = c->sort_material; return RTX_OK;
+    case RTX_OPT_SORT_RAYS: *v = c->sort_rays; return RTX_OK;
     case RTX_OPT_COUNT_VISITS: *v = c->count_visits; return RTX_OK;
     case RTX_OPT_LEAF_SIZE: *v = c->leaf_size; return RTX_OK;
     case RTX_OPT_PRIMARY_CACHE: *v = c->primary_cache; return RTX_OK;
@@ -931,6 +934,7 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
   p.sort_material = c->sort_material;
+  p.sort_rays = c->sort_rays;
   p.traversal = c->traversal;
   p.min_busy = c->min_busy;
   RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
@@ -1036,6 +1040,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
   p.sort_material = c->sort_material;
+  p.sort_rays = c->sort_rays;
   p.traversal = c->traversal;
   p.min_busy = c->min_busy;
   p.accumulate = c->accumulate;
@@ -1047,7 +1052,8 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   c->timer.reset();
   // the launch shape: everything the captured kernels bake in
   std::vector<int64_t> key = {n_jobs, max_depth, c->wave_paths, c->block, c->primary_cache, c->count_visits,
-                              c->accumulate, c->sort_material, c->traversal, (int64_t)(intptr_t)o.dev};
+                              c->accumulate, c->sort_material, c->sort_rays, c->traversal,
+                              (int64_t)(intptr_t)o.dev};
   for (int j = 0; j < n_jobs; ++j) key.insert(key.end(), {jobs[j].scene, jobs[j].W, jobs[j].H, jobs[j].spp});
   int launches = 0, ext_launches = 0;
   std::string why;
@@ -1194,6 +1200,16 @@ int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scene
     res.sort_material = c->sort_material ? 1 : 0;
   }
   c->sort_material = res.sort_material != 0;
+  // ray-sorted traversal: its sorts cost a fixed few launches per vertex
+  res.sort_rays = c->sort_rays ? 1 : 0;
+  c->sort_rays = !c->sort_rays;
+  if ((r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms))) return done(r);
+  ++res.trials;
+  if (ms < res.ms) {
+    res.ms = ms;
+    res.sort_rays = c->sort_rays ? 1 : 0;
+  }
+  c->sort_rays = res.sort_rays != 0;
   *out = res;
   return done(RTX_OK);
 }

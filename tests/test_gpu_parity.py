@@ -191,6 +191,28 @@ def test_waves_do_not_change_results(ctx):
     assert np.array_equal(bits(c), bits(d))
 
 
+def test_ray_sort_does_not_change_results(ctx):
+    """Sorting the extension queue by ray key (and the shading queue by
+    material) only changes the order in which paths are visited: per-path
+    radiance and the accumulated image stay bit-identical."""
+    import rendertoy_gb300 as rt
+    sc = scenes.displaced_icosphere(subdiv=3)
+    ctx.upload(sc)
+    a = ctx.trace_paths(40, 30, 0, 3, 12, seed=5)
+    c = ctx.render_pt(64, 48, 6, 12, seed=5)
+    for opts in ((rt.OPT_SORT_RAYS,), (rt.OPT_SORT_RAYS, rt.OPT_SORT_MATERIAL)):
+        for o in opts:
+            ctx.set_option(o, 1)
+        try:
+            b = ctx.trace_paths(40, 30, 0, 3, 12, seed=5)
+            d = ctx.render_pt(64, 48, 6, 12, seed=5)
+        finally:
+            for o in opts:
+                ctx.set_option(o, 0)
+        assert np.array_equal(bits(a), bits(b)), opts
+        assert np.array_equal(bits(c), bits(d)), opts
+
+
 def test_edge_cases(ctx, oracle):
     import rendertoy_gb300 as rt
     # no emitters: no light samples are drawn; only the environment lights
