@@ -106,7 +106,7 @@ def denoiser_block(ctx, rank):
             "gflop_per_mpixel_forward": fwd * 1e6 / 1e9,
             "roofline": {"bound": "tensor", "achieved": train_tf, "peak": peak, "peak_kind": kind,
                          "unit": "TFLOP/s", "frac": train_tf / peak,
-                         "note": "whole training step (all 88 launches) against the bf16 burst peak"},
+                         "note": "whole training step (all its launches) against the bf16 burst peak"},
             "layer_roofline": {"train_bound_ms": bound_train, "train_frac": bound_train / train_ms,
                                "infer_bound_ms": bound_infer, "infer_frac": bound_infer / infer_ms,
                                "note": "sum over layers and passes of max(FLOPs / bf16 peak, "

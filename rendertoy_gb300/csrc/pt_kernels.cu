@@ -890,30 +890,59 @@ RTX_DEV int warp_count(int* counter, int key, unsigned act, int& base) {
 // Keys of the items to sort: kShadow = false, the extension queue (item i is
 // path queue_in[i]); kShadow = true, the shadow records (item i is record i,
 // its ray from the shading point towards the light sample).
+// Each thread takes kHistPer items per step and issues all their loads
+// before computing a key, so the queue -> ray loads of several items are in
+// flight at once.
+constexpr int kHistPer = 4;
+
 template <bool kJobs, bool kShadow>
 __global__ void __launch_bounds__(256) k_raykey_hist(PtArgs a, DeviceScene s0, int* hist, int* keys) {
   __shared__ int sh[kRayKeyBins];
   for (int b = threadIdx.x; b < kRayKeyBins; b += blockDim.x) sh[b] = 0;
   __syncthreads();
   const int n = kShadow ? a.shadow_counts[a.depth] : a.counts[a.depth];
-  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-    const int i = base + threadIdx.x;
-    const bool live = i < n;
-    const unsigned act = __ballot_sync(0xffffffffu, live);
-    if (!live) continue;
-    int k;
-    if (kShadow) {
-      const float4 q0 = a.shadow[4 * (size_t)i], q1 = a.shadow[4 * (size_t)i + 1];
-      const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + __float_as_int(q0.w));
-      k = ray_key(s, q0, make_float4(q1.x - q0.x, q1.y - q0.y, q1.z - q0.z, 0.0f));
-    } else {
-      const int p = a.queue_in[i];
-      const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + p);
-      k = ray_key(s, a.ray_o[p], a.ray_d[p]);
+  const int step = gridDim.x * blockDim.x * kHistPer;
+  for (int base = blockIdx.x * blockDim.x * kHistPer; base < n; base += step) {
+    int idx[kHistPer], path[kHistPer];
+    float4 o[kHistPer], d[kHistPer];
+#pragma unroll
+    for (int j = 0; j < kHistPer; ++j) {
+      idx[j] = base + j * blockDim.x + threadIdx.x;
+      path[j] = 0;
+      if (idx[j] < n) {
+        if (kShadow) {
+          o[j] = a.shadow[4 * (size_t)idx[j]];
+          d[j] = a.shadow[4 * (size_t)idx[j] + 1];
+        } else {
+          path[j] = a.queue_in[idx[j]];
+        }
+      }
     }
-    keys[i] = k;
-    int b0;
-    warp_count(sh, k, act, b0);
+    if (!kShadow) {
+#pragma unroll
+      for (int j = 0; j < kHistPer; ++j)
+        if (idx[j] < n) {
+          o[j] = a.ray_o[path[j]];
+          d[j] = a.ray_d[path[j]];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kHistPer; ++j) {
+      const bool live = idx[j] < n;
+      const unsigned act = __ballot_sync(0xffffffffu, live);
+      if (!live) continue;
+      int k;
+      if (kShadow) {
+        const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + __float_as_int(o[j].w));
+        k = ray_key(s, o[j], make_float4(d[j].x - o[j].x, d[j].y - o[j].y, d[j].z - o[j].z, 0.0f));
+      } else {
+        const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + path[j]);
+        k = ray_key(s, o[j], d[j]);
+      }
+      keys[idx[j]] = k;
+      int b0;
+      warp_count(sh, k, act, b0);
+    }
   }
   __syncthreads();
   for (int b = threadIdx.x; b < kRayKeyBins; b += blockDim.x)

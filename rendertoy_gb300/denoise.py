@@ -8,13 +8,14 @@ device and stepped through ``Context.dn_train_step`` (forward, backward and
 Adam on the tensor cores).
 
 ``study`` measures the denoised form against the plain one at equal accuracy
-on one scene: a high-spp FP32 reference, plain renders at growing spp, the
-denoised renders at a few input spp (render + passes + network + bloom), their
-relMSE against the reference and their frame times; a frame whose denoised
-relMSE exceeds that of the plain render of equal time falls back to the plain
-render.
+on one scene: a high-spp FP32 reference rendered as two independent halves
+(so that its own noise can be taken out of every error), plain renders at
+growing spp, the denoised renders at growing input spp (render + passes +
+network + bloom), their relMSE against the reference and their frame times;
+a frame whose denoised relMSE exceeds that of the plain render of equal time
+falls back to the plain render.
 
-    python -m rendertoy_gb300.denoise train --scenes 256 --steps 2000 --out DIR
+    python -m rendertoy_gb300.denoise train --scenes 256 --steps 2000 --in-spp 1,1024 --out DIR
     python -m rendertoy_gb300.denoise study --params DIR/params.npy --out DIR
     python -m rendertoy_gb300.denoise step --batch 8 --steps 2   # profiling
 
@@ -47,6 +48,26 @@ def relmse(x, ref, eps=EPS):
     return float(e.mean()), int((~ok).sum())
 
 
+def relmse_corrected(x, ref_a, ref_b, eps=EPS):
+    """relMSE of x against ref = (ref_a + ref_b) / 2, two renders of the
+    same frame with independent random streams, with the reference's own
+    noise taken out: for x independent of the reference,
+    E[(x - ref)^2] = E[(x - mean)^2] + Var(ref), and (ref_a - ref_b)^2 / 4 is
+    an unbiased per-pixel estimate of Var(ref).  Returns (raw relMSE,
+    corrected relMSE, the reference's own relMSE estimate, masked pixels);
+    NaN or infinite pixels of any of the three are masked."""
+    x = np.asarray(x, np.float64)
+    a = np.asarray(ref_a, np.float64)
+    b = np.asarray(ref_b, np.float64)
+    ok = np.isfinite(x).all(-1) & np.isfinite(a).all(-1) & np.isfinite(b).all(-1)
+    x, a, b = x[ok], a[ok], b[ok]
+    ref = 0.5 * (a + b)
+    den = ref ** 2 + eps
+    raw = ((x - ref) ** 2 / den).mean()
+    noise = ((a - b) ** 2 / 4.0 / den).mean()
+    return float(raw), float(raw - noise), float(noise), int((~ok).sum())
+
+
 def frame_passes(ctx, sc, W, H):
     """albedo, normal, depth passes of the scene's camera (H x W x 3 each)."""
     n, a, d = ctx.aov(W, H, float(sc.camera[19]), float(sc.camera[20]))
@@ -60,14 +81,20 @@ def network_input(rad, albedo, normal, depth):
 def make_pairs(ctx, seeds, W=256, H=256, in_spp=4, target_spp=1024, max_depth=8,
                tri_range=(1e3, 2e5), log=print):
     """Render (input, target) pairs of the procedural scenes `seeds`:
-    X [n][H][W][10], Y [n][H][W][3]."""
+    X [n][H][W][10], Y [n][H][W][3].  in_spp: the input's samples per pixel,
+    or a range (lo, hi) from which each pair draws its own, log-uniformly
+    (seeded by the scene), so that one network serves many noise levels."""
     X = np.zeros((len(seeds), H, W, 10), np.float32)
     Y = np.zeros((len(seeds), H, W, 3), np.float32)
     t0 = time.time()
     for i, s in enumerate(seeds):
         sc, _ = scenes.procedural_scene(int(s), tri_range=tri_range)
         ctx.upload(sc)
-        rad = ctx.render_pt(W, H, in_spp, max_depth, seed=2 * int(s) + 1)
+        spp = in_spp
+        if isinstance(in_spp, (tuple, list)):
+            lo, hi = np.log(in_spp[0]), np.log(in_spp[1])
+            spp = int(round(np.exp(np.random.RandomState(int(s)).uniform(lo, hi))))
+        rad = ctx.render_pt(W, H, spp, max_depth, seed=2 * int(s) + 1)
         X[i] = network_input(rad, *frame_passes(ctx, sc, W, H))
         Y[i] = ctx.render_pt(W, H, target_spp, max_depth, seed=2 * int(s) + 2)
         if log and (i + 1) % max(1, len(seeds) // 8) == 0:
@@ -108,36 +135,65 @@ def _timed(ctx, fn):
     return out, (time.perf_counter() - t0) * 1e3
 
 
-def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 2, 4),
-          plain_spp=(1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048), reps=20,
+def _time_to(points, target):
+    """Frame time at which a (ms, relMSE) curve, measured at increasing time,
+    first reaches `target`: log-log interpolation between the two measured
+    points around it; None when no measured point reaches it."""
+    for (t0, e0), (t1, e1) in zip(points, points[1:]):
+        if e0 > target >= e1 and e1 > 0 and e0 > 0:
+            f = (math.log(e0) - math.log(target)) / (math.log(e0) - math.log(e1))
+            return float(math.exp(math.log(t0) + f * (math.log(t1) - math.log(t0))))
+    if points and 0 < points[0][1] <= target:
+        return float(points[0][0])
+    return None
+
+
+def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 4, 16, 64, 256, 1024, 4096),
+          plain_spp=(1, 4, 16, 64, 256, 1024, 4096), reps=20,
           bloom=(49, 8.0, 1.0), target=1e-3, seed=1, log=print):
     """Denoised vs plain at equal accuracy on one scene (see the module text).
-    Times are device-synchronised wall times of the whole frame, its buffers
-    resident on the device."""
+    The reference is two renders of ref_spp / 2 samples with independent
+    random streams; errors are reported raw and with the reference's own
+    noise removed (relmse_corrected), and times to the target use the
+    corrected errors.  Times are device-synchronised wall times of the whole
+    frame, its buffers resident on the device (median of `reps` runs for
+    frames under a second, of 3 above)."""
     ctx.upload(sc)
     t0 = time.time()
-    ref = ctx.render_pt(W, H, ref_spp, max_depth, seed=10_000 + seed)
-    log(f"  reference {ref_spp} spp: {time.time() - t0:.1f} s")
-    out = {"scene": sc.name, "W": W, "H": H, "ref_spp": ref_spp, "max_depth": max_depth, "eps": EPS,
+    half = ref_spp // 2
+    ref_a = ctx.render_pt(W, H, half, max_depth, seed=10_000 + seed)
+    ref_b = ctx.render_pt(W, H, half, max_depth, seed=20_000 + seed)
+    log(f"  reference 2 x {half} spp: {time.time() - t0:.1f} s")
+    out = {"scene": sc.name, "W": W, "H": H, "ref_spp": 2 * half, "max_depth": max_depth, "eps": EPS,
            "target_relmse": target, "plain": [], "denoised": []}
     import torch
     dev = lambda: torch.empty((H, W, 3), dtype=torch.float32, device="cuda")  # noqa: E731
     img, rad, alb, nrm, dep, den, fin = (dev() for _ in range(7))
     near, far = float(sc.camera[19]), float(sc.camera[20])
+
+    def timed_reps(fn):
+        first = _timed(ctx, fn)[1]
+        n = reps if first < 1000.0 else 3
+        times = [first] + [_timed(ctx, fn)[1] for _ in range(n - 1)]
+        return float(np.median(times)), float(np.percentile(times, 99))
+
     # plain: relMSE and frame time per spp (device-resident frame)
     for spp in plain_spp:
-        _, ms = _timed(ctx, lambda: ctx.render_pt(W, H, spp, max_depth, seed=seed, out=img))
-        e, bad = relmse(img.cpu().numpy(), ref)
-        out["plain"].append({"spp": spp, "ms": ms, "relmse": e, "nan_px": bad})
-        log(f"  plain {spp:5d} spp  {ms:9.2f} ms  relMSE {e:.3e}")
-    # plain relMSE ~ c / spp (Monte Carlo): spp and time to the target
+        ms, _ = timed_reps(lambda: ctx.render_pt(W, H, spp, max_depth, seed=seed, out=img))
+        raw, corr, noise, bad = relmse_corrected(img.cpu().numpy(), ref_a, ref_b)
+        out["plain"].append({"spp": spp, "ms": ms, "relmse_raw": raw, "relmse": corr, "nan_px": bad})
+        log(f"  plain {spp:5d} spp  {ms:9.2f} ms  relMSE {corr:.3e} (raw {raw:.3e})")
+    out["ref_noise_relmse"] = noise
+    # plain relMSE ~ c / spp (Monte Carlo): fitted on the corrected errors
     p = out["plain"]
-    c = np.median([q["relmse"] * q["spp"] for q in p if q["spp"] >= 16] or [p[-1]["relmse"] * p[-1]["spp"]])
-    ms_per_spp = np.median([q["ms"] / q["spp"] for q in p if q["spp"] >= 16] or [p[-1]["ms"] / p[-1]["spp"]])
-    reached = [q for q in p if q["relmse"] <= target]
-    out["plain_time_to_target_ms"] = reached[0]["ms"] if reached else float(c / target * ms_per_spp)
-    out["plain_spp_to_target"] = reached[0]["spp"] if reached else float(c / target)
-    out["plain_fit"] = {"c": float(c), "ms_per_spp": float(ms_per_spp)}
+    fit = [q for q in p if q["spp"] >= 16 and q["relmse"] > 0]
+    c = float(np.median([q["relmse"] * q["spp"] for q in fit]))
+    ms_per_spp = float(np.median([q["ms"] / q["spp"] for q in fit]))
+    out["plain_fit"] = {"c": c, "ms_per_spp": ms_per_spp}
+    measured = _time_to([(q["ms"], q["relmse"]) for q in p], target)
+    out["plain_time_to_target_ms"] = measured if measured is not None else c / target * ms_per_spp
+    out["plain_time_to_target_from"] = "measured" if measured is not None else "fit c / spp"
+    out["plain_spp_to_target"] = c / target
     # denoised: render + passes + network + bloom, per input spp
     for spp in denoise_spp:
         def frame():
@@ -146,27 +202,29 @@ def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 2, 4),
             ctx.denoise(rad, alb, nrm, dep, out=den)
             if bloom:
                 ctx.bloom(den, *bloom, out=fin)
-        times = [_timed(ctx, frame)[1] for _ in range(reps)]
-        e_den, bad = relmse(den.cpu().numpy(), ref)
-        e_in, _ = relmse(rad.cpu().numpy(), ref)
-        t_med = float(np.median(times))
+        t_med, t_99 = timed_reps(frame)
+        raw, e_den, _, bad = relmse_corrected(den.cpu().numpy(), ref_a, ref_b)
+        _, e_in, _, _ = relmse_corrected(rad.cpu().numpy(), ref_a, ref_b)
         # the plain render of equal time (the fitted curve)
         e_plain_equal = float(c / max(t_med / ms_per_spp, 1e-9))
         fallback = e_den > e_plain_equal
-        out["denoised"].append({"spp": spp, "ms_p50": t_med, "ms_p99": float(np.percentile(times, 99)),
-                                "relmse": e_den, "relmse_input": e_in, "nan_px": bad,
+        out["denoised"].append({"spp": spp, "ms_p50": t_med, "ms_p99": t_99, "relmse": e_den,
+                                "relmse_raw": raw, "relmse_input": e_in, "nan_px": bad,
                                 "relmse_plain_equal_time": e_plain_equal, "fallback": bool(fallback)})
         log(f"  denoised {spp} spp  p50 {t_med:.2f} ms  relMSE {e_den:.3e} (input {e_in:.3e}, plain at equal "
             f"time {e_plain_equal:.3e}){'  -> fallback' if fallback else ''}")
-    ok = [q for q in out["denoised"] if q["relmse"] <= target and not q["fallback"]]
-    out["denoised_time_to_target_ms"] = ok[0]["ms_p50"] if ok else None
-    best = min(out["denoised"], key=lambda q: q["relmse"])
+    # the denoised form with its fallback: each frame is the better of the
+    # denoised and the plain render of equal time
+    d = out["denoised"]
+    curve = [(q["ms_p50"], min(q["relmse"], q["relmse_plain_equal_time"])) for q in d]
+    out["denoised_time_to_target_ms"] = _time_to(curve, target)
+    if out["denoised_time_to_target_ms"]:
+        out["speedup_time_to_target"] = out["plain_time_to_target_ms"] / out["denoised_time_to_target_ms"]
+    best = min(d, key=lambda q: q["relmse"])
     out["denoised_best"] = best
-    if ok:
-        out["speedup_time_to_target"] = out["plain_time_to_target_ms"] / ok[0]["ms_p50"]
-    # equal-accuracy comparison at the best denoised frame: plain time to its relMSE
-    out["plain_time_to_best_denoised_ms"] = float(c / best["relmse"] * ms_per_spp)
-    out["speedup_at_best_denoised_accuracy"] = out["plain_time_to_best_denoised_ms"] / best["ms_p50"]
+    out["plain_time_to_best_denoised_ms"] = float(c / best["relmse"] * ms_per_spp) if best["relmse"] > 0 else None
+    if out["plain_time_to_best_denoised_ms"]:
+        out["speedup_at_best_denoised_accuracy"] = out["plain_time_to_best_denoised_ms"] / best["ms_p50"]
     return out
 
 
@@ -178,6 +236,8 @@ def _main():
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--res", type=int, default=256)
     ap.add_argument("--target-spp", type=int, default=1024)
+    ap.add_argument("--in-spp", default="4",
+                    help="input samples per pixel of the training pairs: N, or LO,HI (log-uniform per pair)")
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--lr", type=float, default=3e-4)
@@ -203,11 +263,13 @@ def _main():
     os.makedirs(a.out, exist_ok=True)
     if a.cmd == "train":
         t0 = time.time()
-        X, Y = make_pairs(ctx, range(a.scenes), W=a.res, H=a.res, target_spp=a.target_spp)
+        in_spp = tuple(int(v) for v in a.in_spp.split(","))
+        in_spp = in_spp[0] if len(in_spp) == 1 else in_spp
+        X, Y = make_pairs(ctx, range(a.scenes), W=a.res, H=a.res, in_spp=in_spp, target_spp=a.target_spp)
         t_data = time.time() - t0
         losses, ms = train(ctx, X, Y, a.steps, batch=a.batch, lr=a.lr)
         np.save(os.path.join(a.out, "params.npy"), ctx.dn_get_params())
-        res = {"scenes": a.scenes, "res": a.res, "target_spp": a.target_spp, "steps": a.steps,
+        res = {"scenes": a.scenes, "res": a.res, "in_spp": a.in_spp, "target_spp": a.target_spp, "steps": a.steps,
                "batch": a.batch, "lr": a.lr, "data_s": t_data, "ms_per_step": ms,
                "loss_first100": float(losses[:100].mean()), "loss_last100": float(losses[-100:].mean())}
         json.dump(res, open(os.path.join(a.out, "train.json"), "w"), indent=1)
