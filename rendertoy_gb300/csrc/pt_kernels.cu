@@ -216,6 +216,8 @@ RTX_DEV int warp_append(int* counter) {
 }
 
 // Persistent-warp work fetch: returns the first item of this warp's batch.
+// (32 rays per fetch: 64, each lane tracing two rays in turn, measured 17 %
+// slower per frame)
 RTX_DEV int warp_fetch(int* work) {
   int lane = threadIdx.x & 31;
   int base = 0;
@@ -878,14 +880,11 @@ RTX_DEV int ray_key(const DeviceScene& s, float4 o, float4 d) {
 // warp-aggregated add of 1 per lane to counter[key] (shared or global);
 // returns this lane's rank among the lanes that share its key and the
 // counter's value before the warp's add (in `base`)
-RTX_DEV int warp_count(int* counter, int key, unsigned act, int& base) {
-  const unsigned peers = __match_any_sync(act, key);
-  const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
-  int b = 0;
-  if (lane == leader) b = atomicAdd(counter + key, __popc(peers));
-  base = __shfl_sync(peers, b, leader);
-  return __popc(peers & ((1u << lane) - 1u));
-}
+// Count `key` in a shared-memory histogram; returns the counter's value
+// before this lane's add (a rank unique among the lanes and warps that add to
+// the same key).  Plain shared atomics measured 3.3 % faster per frame than
+// aggregating equal keys per warp with __match_any_sync.
+RTX_DEV int count_key(int* counter, int key) { return atomicAdd(counter + key, 1); }
 
 // Keys of the items to sort: kShadow = false, the extension queue (item i is
 // path queue_in[i]); kShadow = true, the shadow records (item i is record i,
@@ -928,9 +927,7 @@ __global__ void __launch_bounds__(256) k_raykey_hist(PtArgs a, DeviceScene s0, i
     }
 #pragma unroll
     for (int j = 0; j < kHistPer; ++j) {
-      const bool live = idx[j] < n;
-      const unsigned act = __ballot_sync(0xffffffffu, live);
-      if (!live) continue;
+      if (idx[j] >= n) continue;
       int k;
       if (kShadow) {
         const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + __float_as_int(o[j].w));
@@ -940,8 +937,7 @@ __global__ void __launch_bounds__(256) k_raykey_hist(PtArgs a, DeviceScene s0, i
         k = ray_key(s, o[j], d[j]);
       }
       keys[idx[j]] = k;
-      int b0;
-      warp_count(sh, k, act, b0);
+      count_key(sh, k);
     }
   }
   __syncthreads();
@@ -967,15 +963,11 @@ __global__ void __launch_bounds__(256) k_raykey_scatter(PtArgs a, const int* key
 #pragma unroll
     for (int j = 0; j < kScatterPer; ++j) {
       const int i = c0 + j * 256 + tid;
-      const bool live = i < n;
-      const unsigned act = __ballot_sync(0xffffffffu, live);
       key[j] = -1;
-      if (live) {
+      if (i < n) {
         key[j] = keys[i];
         path[j] = kShadow ? i : a.queue_in[i];
-        int b0;
-        rank[j] = warp_count(cnt, key[j], act, b0);
-        rank[j] += b0;
+        rank[j] = count_key(cnt, key[j]);
       }
     }
     __syncthreads();
