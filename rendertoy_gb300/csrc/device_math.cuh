@@ -125,10 +125,31 @@ struct Rng {
     ++draw;
     return s == 0 ? r.x : (s == 1 ? r.y : (s == 2 ? r.z : r.w));
   }
-  RTX_DEV float uniform() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
-  RTX_DEV int uniform_int(int a, int b) {
+  RTX_DEV float uniform() { return to_uniform(next_u32()); }
+  RTX_DEV int uniform_int(int a, int b) { return to_int(next_u32(), a, b); }
+  static RTX_DEV float to_uniform(uint32_t u) { return (float)(u >> 8) * (1.0f / 16777216.0f); }
+  static RTX_DEV int to_int(uint32_t u, int a, int b) {
     uint32_t n = (uint32_t)(b - a + 1);
-    return a + (int)(((uint64_t)next_u32() * (uint64_t)n) >> 32);
+    return a + (int)(((uint64_t)u * (uint64_t)n) >> 32);
+  }
+  // The next five draws (a shading vertex makes at most five): they lie in
+  // the two consecutive Philox blocks from draw >> 2, computed here by one
+  // copy of the rounds; draw advances by `used` afterwards.
+  RTX_DEV void draw5(uint32_t (&v)[5]) {
+    const uint32_t c = draw >> 2, s = draw & 3u;
+    uint4 w0 = make_uint4(0u, 0u, 0u, 0u), w1 = w0;
+#pragma unroll 1
+    for (uint32_t b = 0; b < 2; ++b) {
+      const uint4 r = philox4x32_10(make_uint4(c + b, sample, pixel, 0u), k0, k1);
+      if (b == 0)
+        w0 = r;
+      else
+        w1 = r;
+    }
+    const uint32_t w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+      v[k] = s == 0 ? w[k] : (s == 1 ? w[k + 1] : (s == 2 ? w[k + 2] : w[k + 3]));
   }
 };
 

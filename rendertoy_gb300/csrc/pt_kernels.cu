@@ -428,11 +428,17 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
     long long q = J.q;
     Rng rng{J.k0, J.k1, (uint32_t)(q % J.npix), (uint32_t)(J.first_sample + q / J.npix),
             __float_as_uint(th.w)};
-    if (J.n_emitters > 0) {
+    // the vertex's draws, in the reference's order: Int (emitter), Float,
+    // Float (point on it) when there are emitters, then Float, Float (BSDF)
+    uint32_t dv[5];
+    rng.draw5(dv);
+    const bool nee = J.n_emitters > 0;
+    rng.draw += nee ? 5u : 2u;
+    if (nee) {
       // World::SampleEmitter + Triangle::GetSamplePoint (world.cpp:5-17, object.cpp:169-178)
-      int e = __ldg(J.emitters + rng.uniform_int(0, J.n_emitters - 1));
-      float sqr1 = sqrtf(rng.uniform());
-      float r2 = rng.uniform();
+      int e = __ldg(J.emitters + Rng::to_int(dv[0], 0, J.n_emitters - 1));
+      float sqr1 = sqrtf(Rng::to_uniform(dv[1]));
+      float r2 = Rng::to_uniform(dv[2]);
       float aa = 1.0f - sqr1;
       float bb = (1.0f - r2) * sqr1;
       const float4* g = s.geo + 3 * (size_t)e;
@@ -451,8 +457,8 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
         r[3] = make_float4(tb.x, tb.y, tb.z, __int_as_float(tri));
       }
     }
-    float r1 = rng.uniform();
-    float r2 = rng.uniform();
+    float r1 = Rng::to_uniform(nee ? dv[3] : dv[0]);
+    float r2 = Rng::to_uniform(nee ? dv[4] : dv[1]);
     F3 nd, color;
     float pdf;
     bool cont = false;
