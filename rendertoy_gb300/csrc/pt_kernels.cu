@@ -841,11 +841,10 @@ __global__ void __launch_bounds__(256) k_sort_scatter(PtArgs a, DeviceScene s, i
 }
 
 // ---------------------------------------------------------------------------
-// Ray sort (RTX_OPT_SORT_RAYS): counting sorts by a 12-bit key, the Morton
-// code of the ray origin's cell in an 8 x 8 x 8 grid over the scene's bounds,
-// then the direction octant, so that a warp of a traversal kernel takes rays
-// that start close together and head the same way: fewer divergent node
-// visits and more cache hits.  Two sorts per path vertex: the extension
+// Ray sort (RTX_OPT_SORT_RAYS): counting sorts by a 12-bit key of the ray's
+// origin cell and direction (ray_key), so that a warp of a traversal kernel
+// takes rays that start close together and head the same way: fewer
+// divergent node visits and more cache hits.  Two sorts per path vertex: the extension
 // queue before the closest-hit kernel, and the shadow records before the
 // occlusion kernel.  The shading kernel keeps visiting paths in the order
 // the previous vertex wrote them, which keeps its path-state reads
@@ -856,11 +855,19 @@ __global__ void __launch_bounds__(256) k_sort_scatter(PtArgs a, DeviceScene s, i
 // ---------------------------------------------------------------------------
 constexpr int kRayKeyBins = 4096;
 
-RTX_DEV uint32_t spread3(uint32_t v) { return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4); }
 
+
+// Sort keys (12 bits, 4,096 bins).  kShadow = false, extension rays: the
+// Morton code of the origin's cell in a 4^3 grid over the scene bounds, then
+// the direction's cube face (major axis and sign) and its 3 x 3 cell on that
+// face.  kShadow = true, shadow rays (which all head for the lights, so the
+// origin says most about the path): the origin's cell in a 16^3 grid.
+// Measured on the 1.3M-triangle frame against 8^3 origin cells + octant for
+// both: 552.7 -> 567.6 Msamples/s; 8^3 cells + cube face only for extension
+// rays: 545.
+template <bool kShadow>
 RTX_DEV int ray_key(const DeviceScene& s, float4 o, float4 d) {
-  const int oct = (d.x < 0.0f) | ((d.y < 0.0f) << 1) | ((d.z < 0.0f) << 2);
-  if (s.root4 < 0) return oct;
+  if (s.root4 < 0) return 0;
   // scene bounds: the union of the 4-wide root's children (empty slots hold
   // planes at 1e30 and are skipped)
   const float4* n = s.nodes4 + 7 * (size_t)s.root4;
@@ -874,13 +881,41 @@ RTX_DEV int ray_key(const DeviceScene& s, float4 o, float4 d) {
   };
   const float x0 = lo4(lx), y0 = lo4(ly), z0 = lo4(lz);
   const float x1 = hi4(hx), y1 = hi4(hy), z1 = hi4(hz);
+  constexpr int G = kShadow ? 16 : 4;
   auto cell = [](float v, float a, float b) {
-    const float f = (v - a) * (8.0f / fmaxf(b - a, 1e-20f));
-    return (uint32_t)min(max((int)f, 0), 7);
+    const float f = (v - a) * ((float)G / fmaxf(b - a, 1e-20f));
+    return (uint32_t)min(max((int)f, 0), G - 1);
   };
-  const uint32_t m = spread3(cell(o.x, x0, x1)) | (spread3(cell(o.y, y0, y1)) << 1) |
-                     (spread3(cell(o.z, z0, z1)) << 2);
-  return (int)((m << 3) | (uint32_t)oct);
+  auto spread = [](uint32_t v) {  // bit k of v to bit 3k
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+  };
+  const uint32_t m = spread(cell(o.x, x0, x1)) | (spread(cell(o.y, y0, y1)) << 1) |
+                     (spread(cell(o.z, z0, z1)) << 2);
+  if (kShadow) return (int)m;
+  // direction: cube face (major axis and sign), then a 3 x 3 cell on the face
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int face;
+  float u, v, mj;
+  if (ax >= ay && ax >= az) {
+    face = d.x < 0.0f;
+    u = d.y;
+    v = d.z;
+    mj = ax;
+  } else if (ay >= az) {
+    face = 2 + (d.y < 0.0f);
+    u = d.x;
+    v = d.z;
+    mj = ay;
+  } else {
+    face = 4 + (d.z < 0.0f);
+    u = d.x;
+    v = d.y;
+    mj = az;
+  }
+  const float inv = 1.0f / fmaxf(mj, 1e-30f);
+  const int cu = min(max((int)((u * inv + 1.0f) * 1.5f), 0), 2);
+  const int cv = min(max((int)((v * inv + 1.0f) * 1.5f), 0), 2);
+  return (int)((m << 6) | (uint32_t)(face * 9 + cu * 3 + cv));
 }
 
 // warp-aggregated add of 1 per lane to counter[key] (shared or global);
@@ -937,10 +972,10 @@ __global__ void __launch_bounds__(256) k_raykey_hist(PtArgs a, DeviceScene s0, i
       int k;
       if (kShadow) {
         const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + __float_as_int(o[j].w));
-        k = ray_key(s, o[j], make_float4(d[j].x - o[j].x, d[j].y - o[j].y, d[j].z - o[j].z, 0.0f));
+        k = ray_key<true>(s, o[j], make_float4(d[j].x - o[j].x, d[j].y - o[j].y, d[j].z - o[j].z, 0.0f));
       } else {
         const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + path[j]);
-        k = ray_key(s, o[j], d[j]);
+        k = ray_key<false>(s, o[j], d[j]);
       }
       keys[idx[j]] = k;
       count_key(sh, k);
