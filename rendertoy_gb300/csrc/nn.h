@@ -41,6 +41,7 @@ struct ConvDgrad {
   int mask_relu;
   bf16* din;         // [P][Cin] (s1's channels upsampled when s1.up)
   int* err;
+  int ctw = 256;     // row-tile kernel: input channels per tile (multiple of 16, <= 256)
 };
 
 struct ConvWgrad {

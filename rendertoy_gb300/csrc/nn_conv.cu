@@ -549,11 +549,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a
   __shared__ __align__(8) TileBars bars;
   __shared__ uint32_t tmem_slot;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int TR = (a.W + 127) / 128, nt = (a.Cin + 255) / 256;
+  const int TR = (a.W + 127) / 128, nt = (a.Cin + a.ctw - 1) / a.ctw;
   const int T = a.N * a.H * TR * nt;
   const int n_tiles = (int)blockIdx.x < T ? (T - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   const int nsl = a.Cout / 16;
-  const int ntm = min(256, a.Cin);  // widest channel tile
+  const int ntm = min(a.ctw, a.Cin);  // widest channel tile
   const uint32_t ncols = ntm <= 32 ? 32 : (ntm <= 64 ? 64 : (ntm <= 128 ? 128 : 256));
   const uint32_t tap_bytes = (uint32_t)ntm * 32;
   const uint32_t stage = kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes;
@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a
       for (int q = pw * 32 + lane; q < nt * nsl * 9 * ntm * 2; q += kProducerWarps * 32) {
         const int kc = q & 1, row = (q >> 1) % ntm, set = (q >> 1) / ntm;  // set = (ct * nsl + sl) * 9 + t
         const int t = set % 9, cs = set / 9, sl = cs % nsl, c = cs / nsl;
-        const int ch = c * 256 + row;
+        const int ch = c * a.ctw + row;
         chunk_async(sw + set * tap_bytes + tc::tile_offset(row, 8 * kc, 16),
                     ch < a.Cin ? a.wt + ((size_t)ch * 9 + t) * a.Cout + sl * 16 + 8 * kc : nullptr, a.wt);
       }
@@ -598,7 +598,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a
       chunk_async(sh + halo_off(r, c, h), p, a.dout);
     }
     if (!kRes) {
-      const int n0 = ct * 256, NT = min(256, a.Cin - n0);
+      const int n0 = ct * a.ctw, NT = min(a.ctw, a.Cin - n0);
       for (int q = lane; q < 9 * NT * 2; q += kLoadStride) {
         const int kc = q & 1, row = (q >> 1) % NT, t = (q >> 1) / NT;
         chunk_async(sh + kHaloBytes + t * tap_bytes + tc::tile_offset(row, 8 * kc, 16),
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a
   auto mma = [&](int u, int st, int buf, int s) {
     int n, y, x0, ct;
     tile_of(u / nsl, n, y, x0, ct);
-    const int NT = min(256, a.Cin - ct * 256);
+    const int NT = min(a.ctw, a.Cin - ct * a.ctw);
     const uint32_t idesc = tc::make_idesc_bf16(128, NT);
     const uint32_t sh = s0 + st * stage;
     const uint32_t sb = kRes ? sw + (uint32_t)(ct * nsl + s) * 9 * tap_bytes : sh + kHaloBytes;
@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a
     const int q = warp & 3;
     int n, y, x0, ct;
     tile_of(i, n, y, x0, ct);
-    const int n0 = ct * 256, NT = min(256, a.Cin - n0);
+    const int n0 = ct * a.ctw, NT = min(a.ctw, a.Cin - n0);
     const int x = x0 + q * 32 + lane;
     const size_t p = ((size_t)n * a.H + y) * a.W + x;
     const uint32_t taddr = tmem + buf * ncols + ((uint32_t)(q * 32) << 16);
@@ -1038,13 +1038,25 @@ cudaError_t conv_dgrad(const ConvDgrad& a, cudaStream_t st) {
   if (a.Cin % 16 || a.Cout % 8) return cudaErrorInvalidValue;
   const int nt = (a.Cin + 255) / 256;
   if (use_rows(a.W, a.Cout)) {
-    const int ntm = std::min(256, a.Cin);
-    const size_t wbytes = (size_t)nt * ntm * 9 * a.Cout * 2;
+    ConvDgrad b = a;
+    b.ctw = std::min(256, a.Cin);
+    const size_t wbytes = (size_t)nt * b.ctw * 9 * a.Cout * 2;
     const bool res = wbytes <= kResidentWeights;
-    const size_t stage = res ? kHaloBytes : kHaloBytes + (size_t)9 * ntm * 32;
-    const long long T = (long long)a.N * a.H * ((a.W + 127) / 128) * nt;
+    if (!res) {
+      // streamed weights: split the channels into the fewest equal tiles
+      // (multiples of 16) whose stage lets at least four stages fit
+      for (int k = 1; k <= 16; ++k) {
+        const int w = ((a.Cin + k - 1) / k + 15) / 16 * 16;
+        if (w > 256) continue;
+        b.ctw = w;
+        if (4 * (kHaloBytes + (size_t)9 * w * 32) <= 200 * 1024) break;
+      }
+    }
+    const int ntb = (a.Cin + b.ctw - 1) / b.ctw;
+    const size_t stage = res ? kHaloBytes : kHaloBytes + (size_t)9 * b.ctw * 32;
+    const long long T = (long long)a.N * a.H * ((a.W + 127) / 128) * ntb;
     return launch_tiles(k_conv_dgrad_rows<7, true>, k_conv_dgrad_rows<6, false>, k_conv_dgrad_rows<4, false>,
-                        k_conv_dgrad_rows<2, false>, res, stage, res ? wbytes : 0, T, a, st);
+                        k_conv_dgrad_rows<2, false>, res, stage, res ? wbytes : 0, T, b, st);
   }
   int nb = std::min(256, a.Cin);
   size_t stage = 128 * kSlice * 2 + (size_t)nb * kSlice * 2;
