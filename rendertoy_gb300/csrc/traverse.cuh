@@ -1,4 +1,5 @@
-// traverse.cuh — closest-hit and occlusion traversal of the binary BVH.
+// traverse.cuh — closest-hit and occlusion traversal of the binary and the
+// 4-wide BVH.
 //
 // Closest hit restates the result of BVH::Intersect (RenderToy
 // src/bvh.cpp:266-341): the nearest triangle whose two-sided Moller-Trumbore
@@ -8,10 +9,10 @@
 // depth-first walk with a per-thread stack; equal distances resolve to the
 // lower triangle id, so the result does not depend on the walk order.
 //
-// Loads: a node is four 16-byte __ldg loads (both children), a triangle three.
+// Loads: a binary node is four 16-byte __ldg loads (both children), a 4-wide
+// node seven, a triangle three.
 #pragma once
 #include "device_math.cuh"
-
 #include "rtx_internal.h"
 
 namespace rtx {
