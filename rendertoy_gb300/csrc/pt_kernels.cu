@@ -42,8 +42,9 @@ constexpr int kMaxSortBins = 4096;
 #ifndef RTX_CONNECT_MINB
 #define RTX_CONNECT_MINB 8
 #endif
-// path state 6 x 16 B + shadow record 4 x 16 B + three queue entries
-constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 3 * 4;
+// path state 6 x 16 B + shadow record 4 x 16 B + six 4-byte entries (two
+// queues, the material order, the ray order, the ray keys, the shadow order)
+constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 6 * 4;
 
 struct PtWorkspace {
   size_t cap = 0;
