@@ -1151,7 +1151,7 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
   if (total == 0) return cudaSuccess;
   // Paths in flight: the whole render when it fits (every vertex launch has an
   // idle tail, so fewer, larger waves are faster), at most 2^26 paths and a
-  // quarter of the free device memory (176 B of path state per path).
+  // quarter of the free device memory (kPathBytes = 184 B per path).
   long long wave = p.wave_paths;
   if (wave <= 0) {
     size_t free_b = 0, total_b = 0;
