@@ -19,7 +19,10 @@
 // (96 B per path); live paths and shadow records are compacted into queues with
 // warp-aggregated atomics, and queue lengths stay on the device, so the host
 // issues a fixed launch sequence per wave with no synchronisation.
-// Traversal kernels run persistent warps that fetch 32 rays at a time.
+// Traversal kernels run persistent warps that fetch 32 rays at a time; with
+// RTX_OPT_SORT_RAYS (the default) they visit the extension rays and the
+// shadow records in ray-key order (origin cell, direction cell), while the
+// shading kernel keeps the path order (see the ray-sort section below).
 #include <algorithm>
 
 #include "traverse.cuh"
