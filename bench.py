@@ -15,9 +15,27 @@ result.  Metric: Msamples/s (pixel samples per second), with Mrays/s beside it.
   roofline : the closest-hit traversal kernel (k_extend), algorithmic bytes =
           BVH nodes visited x node size (112 B for the default 4-wide tree,
           64 B binary) + triangles tested x 48 B + 52 B of ray I/O per ray,
-          counted by an instrumented (untimed) run of the same step.
+          counted by an instrumented (untimed) run of the same step, against
+          the measured HBM copy bandwidth and (roofline.l2) against the L2
+          read bandwidth this run measures (the tree and triangles, 112 MB,
+          stay L2-resident).  roofline_connect: the same for the occlusion
+          kernel (80 B of shadow-record I/O per ray).  roofline_shade: the
+          shading kernel, the largest of the frame, against SM instruction
+          issue (4 warp instructions per SM per clock at the sampled SM clock)
+          and FP32 (128 lanes per SM per clock); its executed instructions per
+          sample come from an ncu capture (profiles/k_shade_issue.txt).
+  c1     : the 36-triangle Cornell box (256^2, 16 spp, depth 8), which is
+          cache-resident and so reported as SM issue utilisation and active
+          lanes per warp (instructions per frame from an ncu capture,
+          profiles/cornell_c1_issue.txt), not as a memory fraction.
+  batched : 16 procedural scenes traced through one wavefront per frame,
+          autotuned and replayed as a CUDA graph (the batched workload on
+          fewer scenes, so that the run stays within minutes).
   cpu_baseline : the oracle's restatement of RenderToy's renderer (octree +
-          priority-queue traversal) on the host cores, on a bounded sample.
+          priority-queue traversal) on the host cores, on a bounded sample, at
+          the workload's depth 12 and at RenderToy's native depth 5, with the
+          restatement's measured speed relative to RenderToy's own build
+          (oracle/cpu_calibration.json, made where RenderToy's sources are).
   denoiser : the learned denoiser outside the timed frames: one Adam step on a
           32 x 256^2 minibatch and one 1920 x 1088 inference, device time and
           tensor-core TFLOP/s against the measured BF16 peak.
@@ -136,7 +154,7 @@ def layer_bound_ms(layers, px0, tflops, gbs, train):
     return t * 1e3
 
 
-def compositor_block(ctx, img, tmp, out, flush):
+def compositor_block(ctx, img, tmp, out, flush, sms, clk_mhz):
     """The Compositor filters timed alone on the resident 1024^2 image (the
     library's CUDA events around the whole call, median of 10; L2 flushed
     before each run): algorithmic bytes per pixel = 12 B read + 12 B written
@@ -144,8 +162,11 @@ def compositor_block(ctx, img, tmp, out, flush):
     x, then blur y + add = 12 + 12 + 24 + 12).  The filters keep the
     reference's unfused multiply-then-add per tap, so FP32 issue bounds them
     before HBM does: `bound_us` = max(bytes / HBM peak, FP32 operations /
-    the FP32 rate of 152 SMs x 128 lanes at 2.07 GHz), `frac_bound` = that
-    bound / the measured time."""
+    the FP32 rate), `frac_bound` = that bound / the measured time.  The
+    kernels issue packed FP32 instructions (two lanes' worth of operations
+    each), which halves their instruction count but not the FP32 pipe's
+    work: the rate is 128 lane-operations per SM per clock, at the SM clock
+    sampled during the run."""
     import torch
     peak, kind = peaks()
 
@@ -159,7 +180,7 @@ def compositor_block(ctx, img, tmp, out, flush):
         return float(np.median(t[2:]))
 
     px = RES * RES
-    fp32_ops = 152 * 128 * 2.07e9  # FP32 operations per second, nominal
+    fp32_ops = sms * 128 * clk_mhz * 1e6  # FP32 lane-operations per second
     blur_ops = 2 * BLUR_SIZE * 3 * 2  # two passes, a multiply and an add per tap and channel
     res = {}
     for name, fn, bpp, ops in (
@@ -173,6 +194,83 @@ def compositor_block(ctx, img, tmp, out, flush):
                      "fp32_ops_per_pixel": ops, "bound_us": bound_us, "frac_bound": bound_us / (ms * 1e3)}
     res["peak_gbs"] = peak
     res["peak_kind"] = kind
+    return res
+
+
+def profile_facts(name):
+    """The `key value` lines of a profiles/ summary (ncu-derived constants)."""
+    p = os.path.join(ROOT, "profiles", name)
+    d = {}
+    if os.path.exists(p):
+        for ln in open(p):
+            f = ln.split()
+            if len(f) >= 2 and not ln.startswith("#"):
+                try:
+                    d[f[0]] = float(f[1])
+                except ValueError:
+                    pass
+    return d
+
+
+def l2_probe(ctx):
+    """Read bandwidth of a plain streaming kernel (rtx_probe_read_bandwidth,
+    16-byte ld.global.cg loads, L2-only caching) over buffers that fit the L2
+    (32 and 64 MiB), one the size of the traversal working set (112 MiB:
+    4-wide nodes + triangles of the bench scene) and one far beyond it (4 GiB,
+    HBM), each read many times in one launch after an untimed pass.  The L2
+    peak is the larger of the two L2-resident figures."""
+    res = {}
+    for mib, passes in ((32, 4000), (64, 2000), (112, 1000), (4096, 12)):
+        res[f"{mib}MiB"] = ctx.probe_read_bandwidth(mib << 20, passes)
+    return {"peak_gbs": max(res["32MiB"], res["64MiB"]), "probe_gbs": res,
+            "how": "rtx_probe_read_bandwidth: grid-stride 16-byte ld.global.cg reads, 8 blocks x 256 "
+                   "threads per SM, repeated passes in one launch, CUDA events"}
+
+
+def traversal_roofline(bytes_frame, launches_frame, ms_frame, hbm, hbm_kind, l2):
+    """Algorithmic bytes per launch / average launch time, against HBM and L2."""
+    per_launch = bytes_frame / launches_frame
+    avg_ms = ms_frame / launches_frame
+    ach = per_launch / (avg_ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": hbm, "peak_kind": hbm_kind, "unit": "GB/s",
+            "frac": ach / hbm, "bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
+            "l2": {"achieved": ach, "peak": l2["peak_gbs"], "peak_kind": "measured in this run (L2 probe)",
+                   "unit": "GB/s", "frac": ach / l2["peak_gbs"]}}
+
+
+def c1_block(local, sms, clk_mhz, reps=10):
+    """The Cornell box (36 triangles, 256^2, 16 spp, depth 8).  The whole
+    scene sits in L1/L2, so the frame is bound by instruction issue and lane
+    divergence: SM issue utilisation = warp instructions per frame / (SMs x 4
+    issue slots x SM clock x frame time), active lanes per warp = thread
+    instructions / warp instructions.  Instructions per frame come from an
+    ncu capture of the same frame (profiles/cornell_c1_issue.txt; the counts
+    are fixed by the seed), the frame time from CUDA events here (median)."""
+    import rendertoy_gb300 as rt
+    from rendertoy_gb300 import scenes
+    W = H = 256
+    spp, depth = 16, 8
+    with rt.Context(local) as c:
+        c.upload(scenes.cornell_box())
+        import torch
+        out = torch.empty((H, W, 3), dtype=torch.float32, device="cuda")
+        for i in range(3):
+            c.render_pt(W, H, spp, depth, seed=1 + i, out=out)
+        ms = []
+        for i in range(reps):
+            c.render_pt(W, H, spp, depth, seed=1, out=out)
+            ms.append(c.stats()["last_gpu_ms"])
+        launches = c.stats()["kernel_launches"]
+    med = float(np.median(ms))
+    res = {"workload": "Cornell box (36 triangles), 256x256, 16 spp, max depth 8, seed 1",
+           "ms_per_frame": med, "msamples_per_s": W * H * spp / (med / 1e3) / 1e6,
+           "kernel_launches": launches, "l2": "scene resident in L1/L2 (not flushed)"}
+    f = profile_facts("cornell_c1_issue.txt")
+    if "warp_inst_per_frame" in f:
+        res["issue_utilisation"] = f["warp_inst_per_frame"] / (sms * 4 * clk_mhz * 1e6 * med / 1e3)
+        res["active_lanes_per_warp_inst"] = f["thread_inst_per_frame"] / f["warp_inst_per_frame"]
+        res["warp_inst_per_frame"] = f["warp_inst_per_frame"]
+        res["source"] = "profiles/cornell_c1_issue.txt (ncu instruction counts) / this run's frame time"
     return res
 
 
@@ -256,9 +354,22 @@ def job_rate(units_per_rank, slowest_seconds, ws):
     return units_per_rank * ws / slowest_seconds
 
 
-def cpu_sample_rate(sc, seconds=12.0, threads=0, kind="oracle"):
+def cpu_calibration():
+    """The restatement's speed relative to RenderToy's own build on the same
+    work, measured where RenderToy's sources are (oracle/calibrate_cpu.py)."""
+    p = os.path.join(ROOT, "oracle", "cpu_calibration.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return {"restatement_over_reference_speed": {k: d[k]["speedup"] for k in ("paths_d12", "paths_d5",
+                                                                            "render_d5") if k in d},
+            "measured_on": d.get("machine"), "source": "oracle/cpu_calibration.json"}
+
+
+def cpu_sample_rate(sc, seconds=12.0, threads=0, kind="oracle", depth=DEPTH):
     """Msamples/s of RenderToy's CPU path (restated) on a bounded sample of
-    the workload: random pixels of the 1024^2 film, 1 sample each, depth 12."""
+    the workload: random pixels of the 1024^2 film, 1 sample each, at the
+    given max depth (the workload's 12, or RenderToy's native 5)."""
     from oracle import bind
     if kind == "reference":
         chk = bind.load("ref")
@@ -272,7 +383,7 @@ def cpu_sample_rate(sc, seconds=12.0, threads=0, kind="oracle"):
     while True:
         pix = rng.choice(RES * RES, n, replace=False).astype(np.int32)
         t0 = time.perf_counter()
-        s.trace_paths(RES, RES, 0, 1, DEPTH, 1, pixels=pix, threads=threads)
+        s.trace_paths(RES, RES, 0, 1, depth, 1, pixels=pix, threads=threads)
         dt = time.perf_counter() - t0
         total_samples += n
         total_t += dt
@@ -287,7 +398,7 @@ def cpu_sample_rate(sc, seconds=12.0, threads=0, kind="oracle"):
 BATCH_DEPTH = 8
 
 
-def batched(args, ws, rank, local):
+def run_batched(local, rank, n_scenes, steps, warmup, ws=1):
     """The batched config: seeded procedural scenes (1e3-2e6 triangles each,
     textures, 1-4 blackbody quad lights), each frame at its own resolution
     (256^2 .. 1920 x 1080) and spp (1..64), max depth 8, all traced through one
@@ -299,46 +410,50 @@ def batched(args, ws, rank, local):
     from rendertoy_gb300 import scenes
     t0 = time.perf_counter()
     scs, jobs = [], []
-    for k in range(args.scenes):
+    for k in range(n_scenes):
         sc, job = scenes.procedural_scene(1000 * rank + k)
         scs.append(sc)
         jobs.append(dict(scene=k, W=job["W"], H=job["H"], spp=job["spp"], seed=k + 1))
     gen_s = time.perf_counter() - t0
-    ctx = rt.Context(local)
-    t0 = time.perf_counter()
-    ctx.batch_upload(scs)
-    upload_s = time.perf_counter() - t0
-    tris = sum(sc.n_tris for sc in scs)
-    pix = sum(j["W"] * j["H"] for j in jobs)
-    samples = sum(j["W"] * j["H"] * j["spp"] for j in jobs)
-    small = [dict(j, spp=max(1, j["spp"] // 8)) for j in jobs]
-    tune = ctx.batch_autotune(small, BATCH_DEPTH)
-    ctx.set_option(rt.OPT_GRAPH, 1)
-    out = torch.empty(pix * 3, dtype=torch.float32, device="cuda")
-    for i in range(args.warmup):
-        ctx.render_batch([dict(j, seed=j["seed"] + 1000 * i) for j in jobs], BATCH_DEPTH, out=out)
-    ctx.synchronize()
-    ms = []
-    with Clocks(local) as clk:
-        for i in range(args.steps):
-            ctx.render_batch([dict(j, seed=j["seed"] + 7919 * (i + 1)) for j in jobs], BATCH_DEPTH, out=out)
-            ms.append(ctx.stats()["last_gpu_ms"])
+    with rt.Context(local) as ctx:
+        t0 = time.perf_counter()
+        ctx.batch_upload(scs)
+        upload_s = time.perf_counter() - t0
+        tris = sum(sc.n_tris for sc in scs)
+        pix = sum(j["W"] * j["H"] for j in jobs)
+        samples = sum(j["W"] * j["H"] * j["spp"] for j in jobs)
+        small = [dict(j, spp=max(1, j["spp"] // 8)) for j in jobs]
+        tune = ctx.batch_autotune(small, BATCH_DEPTH)
+        ctx.set_option(rt.OPT_GRAPH, 1)
+        out = torch.empty(pix * 3, dtype=torch.float32, device="cuda")
+        for i in range(warmup):
+            ctx.render_batch([dict(j, seed=j["seed"] + 1000 * i) for j in jobs], BATCH_DEPTH, out=out)
+        ctx.synchronize()
+        ms = []
+        with Clocks(local) as clk:
+            for i in range(steps):
+                ctx.render_batch([dict(j, seed=j["seed"] + 7919 * (i + 1)) for j in jobs], BATCH_DEPTH, out=out)
+                ms.append(ctx.stats()["last_gpu_ms"])
     total_ms = reduce_max(sum(ms), ws)
-    value = job_rate(samples * args.steps, total_ms / 1e3, ws) / 1e6
+    value = job_rate(samples * steps, total_ms / 1e3, ws) / 1e6
+    config = {"workload": f"{n_scenes} procedural scenes in one batch frame, max depth {BATCH_DEPTH}",
+              "triangles": tris, "pixels": pix, "samples_per_frame": samples,
+              "resolutions": sorted({f"{j['W']}x{j['H']}" for j in jobs}),
+              "spp_range": [min(j["spp"] for j in jobs), max(j["spp"] for j in jobs)],
+              "scene_gen_s": round(gen_s, 1), "upload_and_bvh_s": round(upload_s, 1),
+              "l2": "frame data far larger than L2"}
+    return value, total_ms / steps, config, tune, clk.summary()
+
+
+def batched(args, ws, rank, local):
+    value, ms, config, tune, clocks = run_batched(local, rank, args.scenes, args.steps, args.warmup, ws)
     if rank == 0:
         line = {
             "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded procedural scenes; no dataset)",
-            "config": {"workload": f"{args.scenes} procedural scenes in one batch frame, max depth {BATCH_DEPTH}",
-                       "triangles": tris, "pixels": pix, "samples_per_frame": samples,
-                       "resolutions": sorted({f"{j['W']}x{j['H']}" for j in jobs}),
-                       "spp_range": [min(j["spp"] for j in jobs), max(j["spp"] for j in jobs)],
-                       "scene_gen_s": round(gen_s, 1), "upload_and_bvh_s": round(upload_s, 1),
-                       "l2": "frame data far larger than L2"},
-            "autotune": tune, "graph": True,
-            "clocks": clk.summary(),
+            "config": config, "autotune": tune, "graph": True, "clocks": clocks,
         }
         print(json.dumps(line))
 
@@ -355,6 +470,9 @@ def main():
                     help="render one step of the workload and exit (for ncu)")
     ap.add_argument("--res", type=int, default=RES, help="with --profile: film size")
     ap.add_argument("--spp", type=int, default=SPP, help="with --profile: samples per pixel")
+    ap.add_argument("--depth", type=int, default=DEPTH, help="with --profile: max path depth")
+    ap.add_argument("--scene", default="icosphere", choices=["icosphere", "cornell"],
+                    help="with --profile: the scene rendered (cornell: the 36-triangle Cornell box, no filters)")
     ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batched"],
                     help="batched: 64 procedural scenes in one wavefront per frame (not the default)")
     ap.add_argument("--scenes", type=int, default=64, help="with --workload batched")
@@ -395,7 +513,9 @@ def main():
                 "config": {"workload": WORKLOAD, "sample": "random pixels of the film, 1 spp each"},
                 "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": cores,
                                  "kind": "reference" if kind == "reference" else "port",
-                                 "sample": f"{tot_s} samples (random pixels x 1 spp) in {tot_t:.1f} s"},
+                                 "sample": f"{tot_s} samples (random pixels x 1 spp, depth {DEPTH}) "
+                                           f"in {tot_t:.1f} s",
+                                 "calibration": cpu_calibration()},
                 "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -414,7 +534,8 @@ def main():
         return batched(args, ws, rank, local)
 
     t0 = time.perf_counter()
-    sc = scenes.displaced_icosphere(subdiv=args.subdiv)
+    sc = scenes.cornell_box() if (args.profile and args.scene == "cornell") else \
+        scenes.displaced_icosphere(subdiv=args.subdiv)
     gen_s = time.perf_counter() - t0
     ctx = rt.Context(local)
     opts = {}
@@ -425,14 +546,16 @@ def main():
     ctx.upload(sc)
     st0 = ctx.stats()
     if args.profile:
-        import torch
         out = torch.empty((args.res, args.res, 3), dtype=torch.float32, device="cuda")
-        ctx.render_pt(args.res, args.res, args.spp, DEPTH, seed=1, out=out)
-        tmp = torch.empty_like(out)
-        ctx.gaussian_blur(out, BLUR_SIZE, BLUR_SIGMA, out=tmp)
-        ctx.convolve(tmp, EDGE5, absval=True, out=out)
+        ctx.render_pt(args.res, args.res, args.spp, args.depth, seed=1, out=out)
+        st = ctx.stats()
+        if args.scene == "icosphere":
+            tmp = torch.empty_like(out)
+            ctx.gaussian_blur(out, BLUR_SIZE, BLUR_SIGMA, out=tmp)
+            ctx.convolve(tmp, EDGE5, absval=True, out=out)
         ctx.synchronize()
-        print(json.dumps({"profile": True, "res": args.res, "spp": args.spp, **ctx.stats()}))
+        print(json.dumps({"profile": True, "scene": args.scene, "res": args.res, "spp": args.spp,
+                          "depth": args.depth, **st}))
         return
     stream = torch.cuda.ExternalStream(ctx.stream)
     dev = torch.device("cuda", local)
@@ -456,7 +579,9 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
 
-    step_ms, ext_ms, ext_launch, rays_e, rays_s = [], 0.0, 0, 0, 0
+    step_ms, rays_e, rays_s = [], 0, 0
+    kt = {k: 0.0 for k in ("extend_ms", "shade_ms", "connect_ms", "extend_launches", "shade_launches",
+                           "connect_launches")}
     with Clocks(local) as clk:
         for i in range(args.steps):
             with torch.cuda.stream(stream):
@@ -472,14 +597,18 @@ def main():
             step_ms.append(e0.elapsed_time(e1))
             # the filters leave the render's timers and ray counters untouched
             s = ctx.stats()
-            ext_ms += s["extend_ms"]
-            ext_launch += s["extend_launches"]
+            for k in kt:
+                kt[k] += s[k]
             rays_e += s["extension_rays"]
             rays_s += s["shadow_rays"]
     total_ms = reduce_max(sum(step_ms), ws)
     samples = RES * RES * SPP * args.steps
     value = job_rate(samples, total_ms / 1e3, ws) / 1e6
     mrays = (rays_e + rays_s) * ws / (total_ms / 1e3) / 1e6
+
+    clocks = clk.summary()
+    clk_mhz = clocks["sm_mhz"] or 2070.0  # unsampled: the GB300's maximum SM clock
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
 
     # instrumented run (untimed): node visits and triangle tests per frame
     ctx.set_option(rt.OPT_COUNT_VISITS, 1)
@@ -489,31 +618,62 @@ def main():
     ctx.set_option(rt.OPT_COUNT_VISITS, 0)
     # kernels per step: the render's launches + blur (2) + convolution (1)
     launches = (cs["kernel_launches"] + 3) * args.steps
+    frames = args.steps
+    per_frame = {k: v / frames for k, v in kt.items()}
     ext_bytes_frame = (cs["ext_node_visits"] * cs["node_bytes"] + cs["ext_tri_tests"] * 48 +
                        cs["extension_rays"] * 52)
-    frames = args.steps
-    ext_launch_per_frame = ext_launch / frames
-    avg_launch_ms = ext_ms / ext_launch
-    bytes_per_launch = ext_bytes_frame / ext_launch_per_frame
-    achieved = bytes_per_launch / (avg_launch_ms / 1e3) / 1e9
+    con_bytes_frame = (cs["shadow_node_visits"] * cs["node_bytes"] + cs["shadow_tri_tests"] * 48 +
+                       cs["shadow_rays"] * 80)
     peak, peak_kind = peaks()
+    l2 = l2_probe(ctx)
+    roof = traversal_roofline(ext_bytes_frame, per_frame["extend_launches"], per_frame["extend_ms"], peak,
+                              peak_kind, l2)
+    roof_con = traversal_roofline(con_bytes_frame, per_frame["connect_launches"], per_frame["connect_ms"],
+                                  peak, peak_kind, l2)
     # DRAM bytes per launch from the ncu capture in profiles/ (fixed + per-ray
     # fit, cold L2 per launch), scaled to this run's rays per launch
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "k_extend_traffic.txt")
-    if os.path.exists(tf):
-        fit = {ln.split()[0]: float(ln.split()[1]) for ln in open(tf) if ln.startswith("dram_bytes")}
-        if "dram_bytes_per_extension_ray" in fit:
-            traffic = (fit.get("dram_bytes_per_launch_fixed", 0.0) +
-                       fit["dram_bytes_per_extension_ray"] * cs["extension_rays"] / ext_launch_per_frame)
+    fit = profile_facts("k_extend_traffic.txt")
+    if "dram_bytes_per_extension_ray" in fit:
+        traffic = (fit.get("dram_bytes_per_launch_fixed", 0.0) +
+                   fit["dram_bytes_per_extension_ray"] * cs["extension_rays"] / per_frame["extend_launches"])
+    roof.update({"kernel": "k_extend", "traffic": traffic,
+                 "extend_share_of_step": kt["extend_ms"] / sum(step_ms),
+                 "per_extension_ray": {"node_visits": cs["ext_node_visits"] / cs["extension_rays"],
+                                       "tri_tests": cs["ext_tri_tests"] / cs["extension_rays"]}})
+    roof_con.update({"kernel": "k_connect", "traffic": None,
+                     "connect_share_of_step": kt["connect_ms"] / sum(step_ms),
+                     "per_shadow_ray": {"node_visits": cs["shadow_node_visits"] / cs["shadow_rays"],
+                                        "tri_tests": cs["shadow_tri_tests"] / cs["shadow_rays"]}})
+    # shading: issue- and FP32-bound; instructions per sample from ncu
+    shade = {"kernel": "k_shade", "bound": "issue", "shade_share_of_step": kt["shade_ms"] / sum(step_ms),
+             "avg_launch_ms": per_frame["shade_ms"] / per_frame["shade_launches"],
+             "sm_mhz": clk_mhz, "sms": sms}
+    sf = profile_facts("k_shade_issue.txt")
+    if "warp_inst_per_sample" in sf:
+        spf = RES * RES * SPP
+        t = per_frame["shade_ms"] / 1e3
+        issue_peak = sms * 4 * clk_mhz * 1e6  # warp instructions per second
+        fp32_peak = sms * 128 * clk_mhz * 1e6  # FP32 lane-operations per second
+        ach_issue = sf["warp_inst_per_sample"] * spf / t
+        ach_fp32 = sf["fp32_ops_per_sample"] * spf / t
+        shade.update({"achieved": ach_issue / 1e9, "peak": issue_peak / 1e9, "unit": "G warp inst/s",
+                      "frac": ach_issue / issue_peak, "peak_kind": "4 issue slots x SMs x sampled SM clock",
+                      "fp32": {"achieved": ach_fp32 / 1e12, "peak": fp32_peak / 1e12, "unit": "T lane-ops/s",
+                               "frac": ach_fp32 / fp32_peak},
+                      "active_lanes_per_warp_inst": sf.get("active_lanes_per_warp_inst"),
+                      "source": "profiles/k_shade_issue.txt (ncu instructions per sample) / this run's "
+                                "k_shade time"})
 
     # end to end through the C ABI with pinned host buffers
     ctx.set_option(rt.OPT_ASYNC, 0)
     h_img = torch.empty((RES, RES, 3), dtype=torch.float32, pin_memory=True)
     h_blur = torch.empty_like(h_img, pin_memory=True)
     h_edge = torch.empty_like(h_img, pin_memory=True)
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, args.steps)
     ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed, out=h_img)
+    if ws > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     for i in range(e2e_steps):
         ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed + 1000 * i, out=h_img)
@@ -525,15 +685,22 @@ def main():
            "h2d_bytes_per_step": 2 * img_bytes + 84 + BLUR_SIZE * 4 + 25 * 4,
            "d2h_bytes_per_step": 3 * img_bytes, "steps": e2e_steps}
 
-    comp = compositor_block(ctx, img, blur, edge, flush)
+    comp = compositor_block(ctx, img, blur, edge, flush, sms, clk_mhz)
     dn = denoiser_block(ctx, rank)
+    c1 = c1_block(local, sms, clk_mhz)
+    bval, bms, bconf, btune, bclk = run_batched(local, rank, 16, 2, 1)
+    batch = {"value": bval, "unit": "Msamples/s", "ms_per_frame": bms, "steps": 2, "warmup": 1,
+             "config": bconf, "autotune": btune, "clocks": bclk, "graph": True}
 
     cpu = None
     if rank == 0:
         v, ns, t, cores = cpu_sample_rate(sc, seconds=args.cpu_seconds)
+        v5, ns5, t5, _ = cpu_sample_rate(sc, seconds=max(2.0, args.cpu_seconds / 3), depth=5)
         cpu = {"value": v, "unit": "Msamples/s", "cores": cores, "kind": "port",
                "sample": f"{ns} samples (random pixels of the 1024^2 film x 1 spp, depth {DEPTH}) "
-                         f"in {t:.1f} s; octree build excluded"}
+                         f"in {t:.1f} s; octree build excluded",
+               "depth5": {"value": v5, "sample": f"{ns5} samples at RenderToy's native depth 5 in {t5:.1f} s"},
+               "calibration": cpu_calibration()}
 
     if rank == 0:
         line = {
@@ -549,17 +716,15 @@ def main():
             "mrays_per_s": mrays,
             "rays_per_step": {"extension": rays_e / args.steps, "shadow": rays_s / args.steps},
             "e2e": e2e,
-            "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic,
-                         "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_ms,
-                         "extend_share_of_step": ext_ms / sum(step_ms),
-                         "per_extension_ray": {
-                             "node_visits": cs["ext_node_visits"] / cs["extension_rays"],
-                             "tri_tests": cs["ext_tri_tests"] / cs["extension_rays"]}},
+            "roofline": roof,
+            "roofline_connect": roof_con,
+            "roofline_shade": shade,
+            "l2_probe": l2,
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clocks,
             "gpu_launches": launches,
+            "c1": c1,
+            "batched": batch,
             "denoiser": dn,
             "compositor": comp,
         }

@@ -61,7 +61,7 @@
 extern "C" {
 #endif
 
-#define RTX_VERSION 1
+#define RTX_VERSION 2
 #define RTX_MATERIAL_FLOATS 24
 #define RTX_CAMERA_FLOATS 21
 
@@ -101,11 +101,17 @@ enum rtx_option {
   RTX_OPT_GRAPH = 12,         /* 0/1: rtx_render_batch captures its launch
                                  sequence as a CUDA graph and replays it for
                                  later frames of the same shape */
-  RTX_OPT_SORT_RAYS = 13      /* 0/1 (default 1): counting-sort the extension
+  RTX_OPT_SORT_RAYS = 13,     /* 0/1 (default 1): counting-sort the extension
                                  rays after the primary ones and the shadow
                                  rays by origin cell and direction octant
                                  before they are traced (results unchanged;
                                  only the visiting order) */
+  RTX_OPT_STACK_LIMIT = 14    /* traversal stack entries a ray may use, 2..64
+                                 (default 64, the whole stack).  A ray that
+                                 needs more stops, and the call returns
+                                 RTX_ERR_DEVICE "traversal stack overflow".
+                                 Lower values exist to exercise that error
+                                 path; results are undefined after it. */
 };
 
 typedef struct rtx_context rtx_context;
@@ -132,6 +138,8 @@ typedef struct rtx_stats {
   int32_t tri_bytes;         /* bytes per triangle record */
   int32_t reserved;
   uint64_t ext_rays_by_depth[16]; /* closest-hit rays per path vertex 0..15 */
+  uint64_t shade_launches;   /* shading launches of the last call (one per */
+  uint64_t connect_launches; /*   path vertex and wave), occlusion launches */
 } rtx_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -301,6 +309,40 @@ int rtx_primary_hits(rtx_context* ctx, const float* camera, int W, int H,
 int rtx_intersect(rtx_context* ctx, int n, const float* rays,
                   const int32_t* exclude, int32_t* out_tri, float* out_tuv);
 
+/* PrincipledBSDF::Eval (src/material.cpp:143-204) of n independent cases,
+ * by the device code the shading kernel inlines -- for checking the BSDF on
+ * its own.  Case i: mats[24 i ..] (a material record; a device array must be
+ * 16-byte aligned), eta[i], shading normal N[3 i ..], outgoing V[3 i ..] and
+ * incoming L[3 i ..] (world space); out_f[3 i ..] = f * |L.z| and
+ * out_pdf[i], as Eval returns them. */
+int rtx_bsdf_eval(rtx_context* ctx, int n, const float* mats, const float* eta,
+                  const float* N, const float* V, const float* L, float* out_f,
+                  float* out_pdf);
+/* PrincipledBSDF::Sample (src/material.cpp:206-295) of n cases: case i
+ * samples from direction in_dir[3 i ..] with the two numbers that path
+ * (pixel i, sample `sample`) of seed `seed` draws first (the Random::Float
+ * calls of material.cpp:214-215).  out_ok[i] = Sample's return value. */
+int rtx_bsdf_sample(rtx_context* ctx, int n, const float* mats, const float* eta,
+                    const float* N, const float* in_dir, uint64_t seed, int sample,
+                    int32_t* out_ok, float* out_dir, float* out_color,
+                    float* out_pdf);
+
+/* Measurement aid, no RenderToy counterpart: the read bandwidth (GB/s) of a
+ * plain streaming kernel over one `bytes` device buffer (a multiple of 16),
+ * read `passes` times in one launch after one untimed pass.  A buffer that
+ * fits the L2 cache measures L2 bandwidth: the bound of traversal over a tree
+ * and triangle array that stay L2-resident. */
+int rtx_probe_read_bandwidth(rtx_context* ctx, size_t bytes, int passes,
+                             double* gbs);
+
+/* Diagnostic, no RenderToy counterpart: one block waits on a shared-memory
+ * mbarrier that nothing arrives on, through the bounded wait every
+ * tensor-core kernel uses, giving up after `polls` polls (1..2^20).  The
+ * call then returns what such a kernel's failed wait returns:
+ * RTX_ERR_DEVICE with "tensor-core barrier wait timed out", and the context
+ * stays usable. */
+int rtx_selftest_wait_timeout(rtx_context* ctx, int polls);
+
 /* rtx_render_pt, and in the same pass as the last accumulation the display
  * resolve of the mean (see rtx_image_resolve): display (W x H RGB FP32) and
  * bytes (format as rtx_image_resolve) may each be NULL; out is the radiance. */
@@ -340,9 +382,12 @@ int rtx_encode_ppm(rtx_context* ctx, const float* in, int W, int H, char* file,
 
 /* ---- compositor ------------------------------------------------------------
  * Image operations (include/RenderToy/compositor.h:107-178,
- * src/compositor.cpp:42-77) on packed float3 W x H images, in != out.
- * Edge taps use the reference's reflect mapping (compositor.h:25-39); a tap
- * whose linear index falls outside the image reads zero. */
+ * src/compositor.cpp:42-77) on packed float3 W x H images (H <= 65535:
+ * the row passes launch one block row per image row; RTX_ERR_INVALID above).
+ * in == out is allowed (the input is copied first, as RenderToy filters a
+ * copy of the image).  Edge taps use the reference's reflect mapping
+ * (compositor.h:25-39); a tap whose linear index falls outside the image
+ * reads zero. */
 /* Image::Convolute<normalize, length, abs>(k): k is kr x kc, row-major */
 int rtx_image_convolve(rtx_context* ctx, const float* in, float* out, int W,
                        int H, const float* kernel, int kr, int kc,
@@ -436,19 +481,21 @@ int rtx_denoise(rtx_context* ctx, const float* radiance, const float* albedo,
 /* ---- without allocation -----------------------------------------------------
  * No counterpart in RenderToy.  Image::GaussianBlur (as rtx_image_gaussian_blur)
  * for callers that cannot allocate device memory when they call in: a plugin
- * whose host application owns the device-memory budget, a real-time loop in
- * which cudaMalloc / cudaFree would synchronise the device, or code that runs
- * while another component captures a stream.  d_in / d_out are device images
- * on the current device (in == out allowed); the work is enqueued on `stream`
- * (a cudaStream_t; NULL = the default stream) and the call returns without
- * waiting.  The intermediate image lives in a fixed 24 MiB device array that
- * the library keeps on every GPU that loads it until the process exits:
- * W * H <= 2097152 and size <= 255, otherwise RTX_ERR_INVALID.  All calls
- * share that array, so calls whose work overlaps on the GPU race: serialise
- * them.  The first call on a device looks the array's address up
- * (cudaGetSymbolAddress); make it before any stream capture.  msg (may be
- * NULL) receives a message on failure.  Calls no cudaMalloc, cudaFree or other
- * allocating routine. */
+ * whose host application owns the device-memory budget, or a real-time loop in
+ * which cudaMalloc / cudaFree would synchronise the device.  d_in / d_out are
+ * device images on the current device (in == out allowed); the work is
+ * enqueued on `stream` (a cudaStream_t; NULL = the default stream) and the
+ * call returns without waiting.  The intermediate image lives in a fixed
+ * 24 MiB device array that the library keeps on every GPU that loads it until
+ * the process exits: W * H <= 2097152, H <= 65535 and size <= 255, otherwise
+ * RTX_ERR_INVALID.  All calls share that array, so calls whose work overlaps
+ * on the GPU race: serialise them.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress) and keeps it for the process:
+ * make that first call before any stream capture, and do not call across a
+ * cudaDeviceReset.  If a CUDA error of earlier work is pending on the calling
+ * thread, the call enqueues nothing, leaves that error in place and returns
+ * RTX_ERR_CUDA.  msg (may be NULL) receives a message on failure.  Calls no
+ * cudaMalloc, cudaFree or other allocating routine. */
 int rtx_image_gaussian_blur_noalloc(const float* d_in, float* d_out, int W,
                                     int H, int size, float sigma, void* stream,
                                     char* msg, size_t msg_len);

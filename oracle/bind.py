@@ -92,6 +92,8 @@ class Checker:
         if kind == "oracle":
             fn("render_pt", None, [vp, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                    _f32p, C.c_int])
+        else:
+            fn("render_pt", C.c_double, [vp, _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp])
 
     # -- scene -------------------------------------------------------------
     def scene(self, sc):
@@ -276,9 +278,20 @@ class CheckerScene:
     def render_pt(self, W, H, spp, max_depth, seed, cam=None, threads=0):
         cam = self.sc.camera if cam is None else cam
         out = np.zeros((H, W, 3), np.float32)
+        if self.chk.kind != "oracle":
+            raise ValueError("the reference renders with Render(); use render_native")
         self.chk._fn["render_pt"](self.h, np.ascontiguousarray(cam, np.float32), W, H, spp,
                                   max_depth, seed, out, threads)
         return out
+
+    def render_native(self, W, H, spp, max_depth, cam=None, threads=0):
+        """The reference's own PathTracingRenderer::Render (reference builds
+        only): (image, seconds inside Render)."""
+        cam = self.sc.camera if cam is None else cam
+        out = np.zeros((H, W, 3), np.float32)
+        sec = self.chk._fn["render_pt"](self.h, np.ascontiguousarray(cam, np.float32), W, H, spp,
+                                        max_depth, threads, out.ctypes.data)
+        return out, sec
 
 
 def load(kind: str = "oracle") -> Checker:

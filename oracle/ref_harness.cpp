@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -81,19 +82,28 @@ uint32_t next_u32() {
   return w;
 }
 
+struct Ctx;
+
 struct RefScene {
   World world;
   std::vector<PrincipledBSDF*> mats;
   std::vector<Mesh*> meshes;
   std::map<const Triangle*, int> id;
   BVH* bvh = nullptr;
-  ~RefScene() {
-    delete bvh;
-    for (auto t : world.triangles) delete t;
-    for (auto m : meshes) delete m;
-    for (auto m : mats) delete m;
-  }
+  // The RenderContext of the last per-path call, kept while the camera and
+  // film stay the same: its constructor builds an octree (renderer.cpp:77-85),
+  // which repeated calls need not pay again.
+  Ctx* path_ctx = nullptr;
+  std::vector<float> path_key;
+  ~RefScene();
 };
+
+void destroy_scene_contents(RefScene* s) {
+    delete s->bvh;
+    for (auto t : s->world.triangles) delete t;
+    for (auto m : s->meshes) delete m;
+    for (auto m : s->mats) delete m;
+}
 
 Camera make_camera(const float* c) {
   Camera cam(Matrix4x4f::I, c[16], Vector2f(c[17], c[18]), c[19], c[20]);
@@ -113,6 +123,28 @@ struct Ctx {
   }
   ~Ctx() { delete rc; }
 };
+
+RefScene::~RefScene() {
+  delete path_ctx;
+  destroy_scene_contents(this);
+}
+
+// The cached per-path context for (camera, W, H), rebuilt when they change.
+Ctx& path_context(RefScene* s, const float* cam, int W, int H) {
+  std::vector<float> key(cam, cam + 21);
+  key.push_back((float)W);
+  key.push_back((float)H);
+  if (!s->path_ctx || key != s->path_key) {
+    delete s->path_ctx;
+    s->path_ctx = new Ctx(s, cam, W, H);
+    s->path_key = key;
+  } else {
+    // other calls may have installed their own camera in the shared World
+    s->world.cameras.clear();
+    s->world.cameras.push_back(make_camera(cam));
+  }
+  return *s->path_ctx;
+}
 
 Ray primary_ray(Renderer& r, int W, int H, int x, int y) {
   Camera* cam = &(r.render_context->world->cameras[r.render_context->camera_id]);
@@ -289,7 +321,7 @@ void ref_trace_paths(void* scene, const float* cam, int W, int H,
                      int n_samples, int max_depth, uint64_t seed, float* out,
                      int threads) {
   RefScene* s = (RefScene*)scene;
-  Ctx c(s, cam, W, H);
+  Ctx& c = path_context(s, cam, W, H);
   PathTracingRenderer r(c.rc, 1);
   rtx_ref_depth_cap = max_depth - 1;
   if (!pixels) npix = W * H;
@@ -311,6 +343,34 @@ void ref_trace_paths(void* scene, const float* cam, int W, int H,
     out[3 * q + 1] = L.y();
     out[3 * q + 2] = L.z();
   }
+}
+
+// PathTracingRenderer::Render itself (src/renderer.cpp:236-270): RenderToy's
+// own OpenMP renderer, unmodified, on the scene's RenderContext -- the loop
+// over samples and pixels with its shared-buffer accumulation.  Used to time
+// the reference against the restatement; its image is not deterministic
+// (renderer.cpp:247-261 races), so only the timing is meaningful.  The
+// wrapped Random draws one stream per thread here (no per-path key).  The
+// recursion cap is the build's: 4 in libref_orig, `max_depth - 1` in libref.
+// Returns the seconds spent inside Render(), timed with steady_clock.
+double ref_render_pt(void* scene, const float* cam, int W, int H, int spp, int max_depth,
+                     int threads, float* out) {
+  RefScene* s = (RefScene*)scene;
+  Ctx c(s, cam, W, H);
+  rtx_ref_depth_cap = max_depth - 1;
+#ifdef _OPENMP
+  const int saved = omp_get_max_threads();
+  omp_set_num_threads(nthreads(threads));
+#endif
+  PathTracingRenderer r(c.rc, spp);
+  auto t0 = std::chrono::steady_clock::now();
+  r.Render();
+  double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+#ifdef _OPENMP
+  omp_set_num_threads(saved);
+#endif
+  if (out) copy_buffer(c.rc, W, H, out);
+  return sec;
 }
 
 void ref_bsdf_eval(const float* mat, float eta, const float* N, const float* V,

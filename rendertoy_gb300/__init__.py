@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(HERE, "librtx.so")
 
 OPT_GRAPH = 12
 OPT_SORT_RAYS = 13
+OPT_STACK_LIMIT = 14
 OPT_ASYNC, OPT_WAVE_PATHS, OPT_BLOCK, OPT_SORT_MATERIAL, OPT_COUNT_VISITS, OPT_LEAF_SIZE, \
     OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING, OPT_ACCUMULATE, OPT_TRAVERSAL, OPT_MIN_BUSY = \
     1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11
@@ -32,7 +33,8 @@ EXPORTS = [
     "rtx_create", "rtx_destroy", "rtx_last_error", "rtx_version", "rtx_set_option",
     "rtx_get_option", "rtx_get_stream", "rtx_set_stream", "rtx_synchronize", "rtx_get_stats",
     "rtx_scene_upload", "rtx_scene_emitters", "rtx_scene_set_emitters", "rtx_render_pt", "rtx_trace_paths",
-    "rtx_render_aov", "rtx_primary_hits", "rtx_intersect", "rtx_image_convolve",
+    "rtx_render_aov", "rtx_primary_hits", "rtx_intersect", "rtx_bsdf_eval", "rtx_bsdf_sample",
+    "rtx_probe_read_bandwidth", "rtx_selftest_wait_timeout", "rtx_image_convolve",
     "rtx_image_gaussian_blur", "rtx_image_edge_detect", "rtx_image_bloom",
     "rtx_image_gaussian_blur_noalloc", "rtx_nn_gemm_bf16", "rtx_nn_conv3x3_fwd",
     "rtx_nn_conv3x3_dgrad", "rtx_nn_conv3x3_wgrad", "rtx_dn_init", "rtx_dn_info", "rtx_dn_layer",
@@ -77,7 +79,8 @@ class Stats(C.Structure):
                 ("last_gpu_ms", C.c_double), ("extend_ms", C.c_double), ("shade_ms", C.c_double),
                 ("connect_ms", C.c_double), ("bvh_build_ms", C.c_double), ("bvh_nodes", C.c_int32), ("bvh_leaves", C.c_int32),
                 ("bvh_depth", C.c_int32), ("node_bytes", C.c_int32), ("tri_bytes", C.c_int32),
-                ("reserved", C.c_int32), ("ext_rays_by_depth", C.c_uint64 * 16)]
+                ("reserved", C.c_int32), ("ext_rays_by_depth", C.c_uint64 * 16),
+                ("shade_launches", C.c_uint64), ("connect_launches", C.c_uint64)]
 
 
 _lib = None
@@ -111,6 +114,10 @@ def lib() -> C.CDLL:
         "rtx_render_aov": (i, [vp, vp, i, i, f, f, vp, vp, vp]),
         "rtx_primary_hits": (i, [vp, vp, i, i, vp, vp]),
         "rtx_intersect": (i, [vp, i, vp, vp, vp, vp]),
+        "rtx_bsdf_eval": (i, [vp, i, vp, vp, vp, vp, vp, vp, vp]),
+        "rtx_bsdf_sample": (i, [vp, i, vp, vp, vp, vp, u64, i, vp, vp, vp, vp]),
+        "rtx_probe_read_bandwidth": (i, [vp, C.c_size_t, i, C.POINTER(C.c_double)]),
+        "rtx_selftest_wait_timeout": (i, [vp, i]),
         "rtx_image_convolve": (i, [vp, vp, vp, i, i, vp, i, i, i, i, i]),
         "rtx_image_gaussian_blur": (i, [vp, vp, vp, i, i, i, f]),
         "rtx_image_edge_detect": (i, [vp, vp, vp, i, i]),
@@ -344,6 +351,37 @@ class Context:
         tuv = np.zeros((n, 3), np.float32)
         self._check(self.L.rtx_intersect(self.h, n, _ptr(rays), _ptr(ex), _ptr(tri), _ptr(tuv)))
         return tri, tuv
+
+    def bsdf_eval(self, mats, eta, N, V, L):
+        """PrincipledBSDF::Eval of n cases on the device: (f [n, 3], pdf [n])."""
+        mats = _f32(mats).reshape(-1, 24)
+        n = len(mats)
+        f = np.zeros((n, 3), np.float32)
+        pdf = np.zeros(n, np.float32)
+        args = [_f32(a).reshape(n, -1) for a in (eta, N, V, L)]
+        self._check(self.L.rtx_bsdf_eval(self.h, n, _ptr(mats), *[_ptr(a) for a in args], _ptr(f), _ptr(pdf)))
+        return f, pdf
+
+    def bsdf_sample(self, mats, eta, N, in_dir, seed, sample):
+        """PrincipledBSDF::Sample of n cases on the device (case i draws as
+        path (pixel i, sample)): (ok [n], dir [n, 3], color [n, 3], pdf [n])."""
+        mats = _f32(mats).reshape(-1, 24)
+        n = len(mats)
+        ok = np.zeros(n, np.int32)
+        od = np.zeros((n, 3), np.float32)
+        col = np.zeros((n, 3), np.float32)
+        pdf = np.zeros(n, np.float32)
+        args = [_f32(a).reshape(n, -1) for a in (eta, N, in_dir)]
+        self._check(self.L.rtx_bsdf_sample(self.h, n, _ptr(mats), *[_ptr(a) for a in args], int(seed),
+                                           int(sample), _ptr(ok), _ptr(od), _ptr(col), _ptr(pdf)))
+        return ok, od, col, pdf
+
+    def probe_read_bandwidth(self, nbytes, passes):
+        """GB/s of a plain streaming read of an nbytes device buffer, `passes`
+        times over in one launch (an L2-resident size measures L2)."""
+        gbs = C.c_double()
+        self._check(self.L.rtx_probe_read_bandwidth(self.h, int(nbytes), int(passes), C.byref(gbs)))
+        return gbs.value
 
     # -- denoiser building blocks ---------------------------------------------
     def gemm_bf16(self, A, B, a_mn=False, b_mn=False, out=None):

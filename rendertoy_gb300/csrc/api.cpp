@@ -86,6 +86,7 @@ struct rtx_context {
   bool accumulate = false;
   int traversal = 2;
   int min_busy = 20;
+  int stack_limit = kStackSize;
   KernelTimer timer;
   // scene
   bool has_scene = false;
@@ -421,6 +422,12 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
       if (v < 0 || v > 32) return fail(c, RTX_ERR_INVALID, "min busy lanes must be in [0, 32]");
       c->min_busy = (int)v;
       return RTX_OK;
+    case RTX_OPT_STACK_LIMIT:
+      if (v < 2 || v > kStackSize) return fail(c, RTX_ERR_INVALID, "stack limit must be in [2, 64]");
+      c->stack_limit = (int)v;
+      c->ds.stack_limit = c->stack_limit;
+      c->bds.stack_limit = c->stack_limit;
+      return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -441,6 +448,7 @@ int rtx_get_option(rtx_context* c, int option, int64_t* v) {
     case RTX_OPT_ACCUMULATE: *v = c->accumulate; return RTX_OK;
     case RTX_OPT_TRAVERSAL: *v = c->traversal; return RTX_OK;
     case RTX_OPT_MIN_BUSY: *v = c->min_busy; return RTX_OK;
+    case RTX_OPT_STACK_LIMIT: *v = c->stack_limit; return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -647,6 +655,7 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
     s.sky[k] = sky[k];
     s.ground[k] = ground[k];
   }
+  s.stack_limit = c->stack_limit;
   c->has_scene = true;
   c->stats.bvh_build_ms = b.ms;
   c->stats.bvh_nodes = b.n_nodes;
@@ -773,6 +782,7 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   if ((r = upload_buf(c, c->b_emit, emit.data(), emit.size() * sizeof(int32_t), "upload batch emitters"))) return r;
   DeviceScene& s = c->bds;
   s = DeviceScene{};
+  s.stack_limit = c->stack_limit;
   s.nodes = (const float4*)c->b_nodes.p;
   s.nodes4 = (const float4*)c->b_nodes4.p;
   s.root4 = kEmptyRoot;
@@ -938,13 +948,15 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   p.traversal = c->traversal;
   p.min_busy = c->min_busy;
   RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
-  int launches = 0, ext_launches = 0;
+  int launches = 0, ext_launches = 0, vtx_launches = 0;
   std::string why;
   c->timer.reset();  // times are per render; rtx_get_stats collects them
   cudaError_t e = pt_render(c->pt, c->ds, cp, p, (float*)o.dev, c->d_err, c->d_counters,
-                            &c->timer, c->stream, &launches, &ext_launches, &why);
+                            &c->timer, c->stream, &launches, &ext_launches, &vtx_launches, &why);
   c->stats.kernel_launches = launches;
   c->stats.extend_launches = ext_launches;
+  c->stats.shade_launches = vtx_launches;
+  c->stats.connect_launches = vtx_launches;
   if (e != cudaSuccess) {
     if (!why.empty()) return fail(c, RTX_ERR_INVALID, why);
     return cuda_fail(c, e, "pt_render");
@@ -1055,7 +1067,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
                               c->accumulate, c->sort_material, c->sort_rays, c->traversal,
                               (int64_t)(intptr_t)o.dev};
   for (int j = 0; j < n_jobs; ++j) key.insert(key.end(), {jobs[j].scene, jobs[j].W, jobs[j].H, jobs[j].spp});
-  int launches = 0, ext_launches = 0;
+  int launches = 0, ext_launches = 0, vtx_launches = 0;
   std::string why;
   cudaError_t e = cudaSuccess;
   const bool graphable = c->use_graph && !c->timer.on;
@@ -1065,9 +1077,11 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
     c->stats.kernel_launches = 0;  // kernels are graph nodes
   } else {
     e = pt_render(c->pt, c->bds, CamParams{}, p, (float*)o.dev, c->d_err, c->d_counters, &c->timer, c->stream,
-                  &launches, &ext_launches, &why);
+                  &launches, &ext_launches, &vtx_launches, &why);
     c->stats.kernel_launches = launches;
     c->stats.extend_launches = ext_launches;
+    c->stats.shade_launches = vtx_launches;
+    c->stats.connect_launches = vtx_launches;
     if (e != cudaSuccess) {
       if (!why.empty()) return fail(c, RTX_ERR_INVALID, why);
       return cuda_fail(c, e, "pt_render (batch)");
@@ -1081,10 +1095,10 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
       PtParams pc = p;
       pc.wave_paths = (int)pt_last_wave(c->pt);
       cudaGraph_t g = nullptr;
-      int l2 = 0, x2 = 0;
+      int l2 = 0, x2 = 0, v2 = 0;
       RTX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
       cudaError_t ec = pt_render(c->pt, c->bds, CamParams{}, pc, (float*)o.dev, c->d_err, c->d_counters,
-                                 &c->timer, c->stream, &l2, &x2, &why);
+                                 &c->timer, c->stream, &l2, &x2, &v2, &why);
       cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
       if (ec != cudaSuccess || ee != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -1378,6 +1392,108 @@ int rtx_intersect(rtx_context* c, int n, const float* rays, const int32_t* exclu
   return finish(c, all_device({&ar, &ae, &at, &au}));
 }
 
+static int check_bsdf_args(rtx_context* c, int n, const float* mats, const float* eta,
+                           const float* N, const float* dir) {
+  if (!c) return RTX_ERR_INVALID;
+  if (n < 0 || n > (1 << 26)) return fail(c, RTX_ERR_INVALID, "case count out of range");
+  if (n > 0 && (!mats || !eta || !N || !dir)) return fail(c, RTX_ERR_INVALID, "NULL buffer");
+  // material records are read as float4 vectors
+  if (n > 0 && is_device_ptr(mats) && ((uintptr_t)mats & 15))
+    return fail(c, RTX_ERR_INVALID, "device material array not 16-byte aligned");
+  return RTX_OK;
+}
+
+int rtx_bsdf_eval(rtx_context* c, int n, const float* mats, const float* eta, const float* N,
+                  const float* V, const float* L, float* out_f, float* out_pdf) {
+  int r;
+  if ((r = check_bsdf_args(c, n, mats, eta, N, V))) return r;
+  if (n > 0 && (!L || !out_f || !out_pdf)) return fail(c, RTX_ERR_INVALID, "NULL buffer");
+  if (n == 0) return RTX_OK;
+  if ((r = begin(c))) return r;
+  Arg am, ae, an, av, al, af, ap;
+  if ((r = bind_in(c, mats, (size_t)n * 96, 0, am))) return r;
+  if ((r = bind_in(c, eta, (size_t)n * 4, 1, ae))) return r;
+  if ((r = bind_in(c, N, (size_t)n * 12, 2, an))) return r;
+  if ((r = bind_in(c, V, (size_t)n * 12, 3, av))) return r;
+  if ((r = bind_in(c, L, (size_t)n * 12, 4, al))) return r;
+  if ((r = bind_out(c, out_f, (size_t)n * 12, 5, af))) return r;
+  if ((r = bind_out(c, out_pdf, (size_t)n * 4, 6, ap))) return r;
+  cudaError_t e = launch_bsdf_eval(n, (const float*)am.dev, (const float*)ae.dev, (const float*)an.dev,
+                                   (const float*)av.dev, (const float*)al.dev, (float*)af.dev,
+                                   (float*)ap.dev, c->stream);
+  c->stats.kernel_launches = 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "bsdf eval kernel");
+  if ((r = copy_back(c, af))) return r;
+  if ((r = copy_back(c, ap))) return r;
+  return finish(c, all_device({&am, &ae, &an, &av, &al, &af, &ap}));
+}
+
+int rtx_bsdf_sample(rtx_context* c, int n, const float* mats, const float* eta, const float* N,
+                    const float* in_dir, uint64_t seed, int sample, int32_t* out_ok,
+                    float* out_dir, float* out_color, float* out_pdf) {
+  int r;
+  if ((r = check_bsdf_args(c, n, mats, eta, N, in_dir))) return r;
+  if (n > 0 && (!out_ok || !out_dir || !out_color || !out_pdf))
+    return fail(c, RTX_ERR_INVALID, "NULL buffer");
+  if (n == 0) return RTX_OK;
+  if ((r = begin(c))) return r;
+  Arg am, ae, an, ai, ao, ad, ac, ap;
+  if ((r = bind_in(c, mats, (size_t)n * 96, 0, am))) return r;
+  if ((r = bind_in(c, eta, (size_t)n * 4, 1, ae))) return r;
+  if ((r = bind_in(c, N, (size_t)n * 12, 2, an))) return r;
+  if ((r = bind_in(c, in_dir, (size_t)n * 12, 3, ai))) return r;
+  if ((r = bind_out(c, out_ok, (size_t)n * 4, 4, ao))) return r;
+  if ((r = bind_out(c, out_dir, (size_t)n * 12, 5, ad))) return r;
+  if ((r = bind_out(c, out_color, (size_t)n * 12, 6, ac))) return r;
+  if ((r = bind_out(c, out_pdf, (size_t)n * 4, 7, ap))) return r;
+  cudaError_t e = launch_bsdf_sample(n, (const float*)am.dev, (const float*)ae.dev,
+                                     (const float*)an.dev, (const float*)ai.dev, seed, sample,
+                                     (int*)ao.dev, (float*)ad.dev, (float*)ac.dev, (float*)ap.dev,
+                                     c->stream);
+  c->stats.kernel_launches = 1;
+  if (e != cudaSuccess) return cuda_fail(c, e, "bsdf sample kernel");
+  for (const Arg* a : {&ao, &ad, &ac, &ap})
+    if ((r = copy_back(c, *a))) return r;
+  return finish(c, all_device({&am, &ae, &an, &ai, &ao, &ad, &ac, &ap}));
+}
+
+int rtx_probe_read_bandwidth(rtx_context* c, size_t bytes, int passes, double* gbs) {
+  if (!c) return RTX_ERR_INVALID;
+  if (!gbs || passes < 1 || passes > 100000 || bytes < 4096 || bytes > ((size_t)1 << 34) || (bytes & 15))
+    return fail(c, RTX_ERR_INVALID, "bad probe size");
+  int r;
+  if ((r = begin(c))) return r;
+  int sms = 0;
+  RTX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device), "attribute");
+  RTX_CUDA(c->stage[0].ensure(bytes), "probe buffer");
+  RTX_CUDA(c->stage[1].ensure(1024), "probe sink");
+  RTX_CUDA(cudaMemsetAsync(c->stage[0].p, 0x5a, bytes, c->stream), "memset");
+  // one pass first, so that an L2-sized buffer is resident when timing starts
+  RTX_CUDA(launch_read_probe(c->stage[0].p, bytes, 1, (uint32_t*)c->stage[1].p, sms, c->stream),
+           "probe kernel");
+  RTX_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
+  RTX_CUDA(launch_read_probe(c->stage[0].p, bytes, passes, (uint32_t*)c->stage[1].p, sms, c->stream),
+           "probe kernel");
+  RTX_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
+  RTX_CUDA(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  float ms = 0.0f;
+  RTX_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "cudaEventElapsedTime");
+  c->stats.last_gpu_ms = ms;
+  c->stats.kernel_launches = 2;
+  *gbs = (double)bytes * passes / (ms * 1e-3) / 1e9;
+  return RTX_OK;
+}
+
+int rtx_selftest_wait_timeout(rtx_context* c, int polls) {
+  if (!c) return RTX_ERR_INVALID;
+  if (polls < 1 || polls > (1 << 20)) return fail(c, RTX_ERR_INVALID, "polls must be in [1, 2^20]");
+  int r;
+  if ((r = begin(c))) return r;
+  RTX_CUDA(launch_wait_timeout(polls, c->d_err, c->stream), "wait kernel");
+  c->stats.kernel_launches = 1;
+  return finish(c, false);
+}
+
 // Bind an image input; when it aliases the output (the reference filters in
 // place) it is first copied so that no kernel reads what it writes.
 static int bind_image_in(rtx_context* c, const float* in, float* out, size_t bytes, int slot,
@@ -1397,6 +1513,7 @@ static int check_image(rtx_context* c, const float* in, float* out, int W, int H
   if (!in || !out) return fail(c, RTX_ERR_INVALID, "NULL image");
   if (W <= 0 || H <= 0) return fail(c, RTX_ERR_INVALID, "image size must be positive");
   if ((long long)W * H > (1LL << 30)) return fail(c, RTX_ERR_INVALID, "image too large");
+  if (H > 65535) return fail(c, RTX_ERR_INVALID, "image taller than 65535 rows");
   return RTX_OK;
 }
 

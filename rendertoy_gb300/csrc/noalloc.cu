@@ -1,10 +1,10 @@
 // noalloc.cu — a Gaussian blur entry point that allocates nothing.
 //
 // Some callers cannot allocate device memory when they call in: a plugin
-// whose host application owns the whole device-memory budget, a real-time
-// frame loop where cudaMalloc / cudaFree would synchronise the device and
-// stall other streams, or code that runs while another component is
-// capturing a stream.  rtx_image_gaussian_blur_noalloc serves them: the
+// whose host application owns the whole device-memory budget and hands out
+// no more, or a real-time frame loop where cudaMalloc / cudaFree would
+// synchronise the device and stall the other streams.
+// rtx_image_gaussian_blur_noalloc serves them: the
 // caller passes device input and output images, and the intermediate image of
 // the two separable passes lives in a fixed array in the library's device
 // memory instead of in a buffer allocated per call.
@@ -13,7 +13,9 @@
 // (24 MiB), resident on every GPU that loads the library until the process
 // exits.  Host code cannot use its name as a device address, so the first call
 // on a device looks the address up with cudaGetSymbolAddress (with that device
-// current) and keeps it; make that first call before any stream capture.
+// current) and keeps it for the life of the process; make that first call
+// before any stream capture, and do not use the entry point across a
+// cudaDeviceReset (the kept address would no longer name the array).
 // All calls share the array, so calls whose work overlaps on the GPU (other
 // streams, other threads) race; serialise them.  Every pixel of the
 // intermediate image is written by the first pass before the second pass reads
@@ -28,6 +30,7 @@ namespace {
 
 constexpr int kNoAllocMaxPixels = 2097152;  // 24 MiB of float3 (2048 x 1024)
 constexpr int kNoAllocMaxTaps = 255;
+constexpr int kMaxRows = 65535;  // the row passes launch one block row per image row
 
 static __device__ __align__(256) float g_noalloc_image[3 * (size_t)kNoAllocMaxPixels];
 static __device__ __align__(256) float g_noalloc_weights[kNoAllocMaxTaps];
@@ -72,9 +75,22 @@ extern "C" int rtx_image_gaussian_blur_noalloc(const float* d_in, float* d_out, 
     set_msg(msg, msg_len, "image larger than the fixed scratch (2097152 pixels)");
     return RTX_ERR_INVALID;
   }
+  if (H > kMaxRows) {
+    set_msg(msg, msg_len, "image taller than 65535 rows");
+    return RTX_ERR_INVALID;
+  }
   if (size <= 0 || size > kNoAllocMaxTaps) {
     set_msg(msg, msg_len, "kernel size must be in [1, 255]");
     return RTX_ERR_INVALID;
+  }
+  // A launch error is read back through the thread's last-error slot, which
+  // may already hold an error of the caller's own earlier work.  Leave such an
+  // error where it is (the caller reads it) and do nothing, rather than
+  // report it as this call's failure or clear it.
+  cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    set_msg(msg, msg_len, "an earlier CUDA error is pending on this thread; nothing was enqueued");
+    return RTX_ERR_CUDA;
   }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {

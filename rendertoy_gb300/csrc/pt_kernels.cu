@@ -1032,7 +1032,7 @@ template <bool kJobs>
 static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene& s, const CamParams& cam,
                                  const float4* prim, PtWorkspace* ws, KernelTimer* timer, cudaStream_t st,
                                  int grid_ext, int grid_con, int grid_sh, int block, int nw, int* launches,
-                                 int* extend_launches) {
+                                 int* extend_launches, int* vertex_launches) {
   cudaError_t e;
   a.queue_in = ws->queue[0];
   a.queue_out = ws->queue[1];
@@ -1123,6 +1123,7 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
     }
     if ((e = timer->mark(2, st, false))) return e;
     *launches += 2;
+    ++*vertex_launches;  // one shading and one occlusion launch per path vertex
   }
   return cudaSuccess;
 }
@@ -1130,7 +1131,7 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
 cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& cam,
                       const PtParams& p, float* d_out, int* err, Counters* d_counters,
                       KernelTimer* timer, cudaStream_t st, int* launches, int* extend_launches,
-                      std::string* why) {
+                      int* vertex_launches, std::string* why) {
   cudaError_t e;
   if (p.max_depth < 1 || p.max_depth > kMaxDepthSlots - 1) {
     *why = "max_depth must be in [1, 63]";
@@ -1255,9 +1256,9 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     a.n_wave = nw;
     if ((e = cudaMemsetAsync(ws->counters, 0, 4 * kMaxDepthSlots * sizeof(int), st))) return e;
     e = jobs ? wave_launches<true>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,
-                                   extend_launches)
+                                   extend_launches, vertex_launches)
              : wave_launches<false>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,
-                                    extend_launches);
+                                    extend_launches, vertex_launches);
     if (e) return e;
     if (jobs) {
       k_accumulate_jobs<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(ws->rad, q0, nw, p.d_jobs, p.n_jobs,

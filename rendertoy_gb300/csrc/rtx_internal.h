@@ -57,6 +57,9 @@ struct DeviceScene {
   int n_tris, n_emitters, n_mats;
   int textured;  // some material has a procedural texture
   float sky[3], ground[3];
+  // traversal stack entries a ray may use before it reports kErrStackOverflow
+  // (kStackSize; lower only through RTX_OPT_STACK_LIMIT, to exercise that path)
+  int stack_limit = kStackSize;
 };
 
 // Camera reduced to what ray generation needs (src/renderer.cpp:103-124,
@@ -180,7 +183,7 @@ void pt_workspace_destroy(PtWorkspace* ws);
 cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& cam,
                       const PtParams& p, float* d_out, int* err, Counters* d_counters,
                       KernelTimer* timer, cudaStream_t st, int* launches, int* extend_launches,
-                      std::string* why);
+                      int* vertex_launches, std::string* why);
 
 cudaError_t launch_resolve(const float* in, int W, int H, const Resolve& r, cudaStream_t st);
 cudaError_t launch_convolve(const float* in, float* out, int W, int H, const float* d_k,
@@ -192,6 +195,14 @@ cudaError_t launch_edge(const float* in, float* out, int W, int H, cudaStream_t 
                         int* launches);
 cudaError_t launch_texture_sample(int kind, float param, const uint8_t* perm, int n, const float* uv,
                                   float* out, cudaStream_t st);
+cudaError_t launch_bsdf_eval(int n, const float* mats, const float* eta, const float* N,
+                             const float* V, const float* L, float* f, float* pdf, cudaStream_t st);
+cudaError_t launch_bsdf_sample(int n, const float* mats, const float* eta, const float* N,
+                               const float* in_dir, uint64_t seed, int sample, int* ok, float* dir,
+                               float* color, float* pdf, cudaStream_t st);
+cudaError_t launch_read_probe(const void* buf, size_t bytes, int passes, uint32_t* sink, int sms,
+                              cudaStream_t st);
+cudaError_t launch_wait_timeout(int polls, int* err, cudaStream_t st);
 cudaError_t launch_gemm_bf16(const void* A, const void* B, float* C, int M, int N, int K, int a_mn,
                              int b_mn, int* err, cudaStream_t st);
 

@@ -119,7 +119,7 @@ RTX_DEV int closest_hit(const DeviceScene& s, F3 o, F3 d, int exclude, float& t,
           nearc = c1;
           farc = c0;
         }
-        if (sp >= kStackSize) {
+        if (sp >= s.stack_limit) {
           atomicOr(err, kErrStackOverflow);
           return best;
         }
@@ -185,7 +185,7 @@ RTX_DEV bool occluded(const DeviceScene& s, F3 o, F3 d, int exclude, int target,
           nearc = c1;
           farc = c0;
         }
-        if (sp >= kStackSize) {
+        if (sp >= s.stack_limit) {
           atomicOr(err, kErrStackOverflow);
           return true;
         }
@@ -360,7 +360,7 @@ RTX_DEV int trace4(const DeviceScene& s, F3 o, F3 d, int exclude, int target, fl
       int c0, c1, c2, c3;
       int nh = node4<!kAnyHit>(rb, s.nodes4 + 7 * (size_t)node, t, c0, c1, c2, c3);
       if (nh > 0) {
-        if (sp + 3 > kStackSize) {
+        if (sp + 3 > s.stack_limit) {
           atomicOr(err, kErrStackOverflow);
           return kAnyHit ? 1 : best;
         }
@@ -466,7 +466,7 @@ RTX_DEV bool trav_run(Trav& r, int* stack, const DeviceScene& s, int* err, Visit
             r.node = c1;
             farc = c0;
           }
-          if (r.sp + 1 >= kStackSize) {
+          if (r.sp + 1 >= s.stack_limit) {
             atomicOr(err, kErrStackOverflow);
             r.node = kSentinel;
             r.leaf = 0;

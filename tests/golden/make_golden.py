@@ -461,10 +461,17 @@ def demo_obj_case(ref_root):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None,
+                    help="the RenderToy tree (default: the one oracle/Makefile reads, "
+                         "RENDERTOY_SRC or the recipe's location)")
     ap.add_argument("--only", default="", help="regenerate one case: textures, resolve, obj")
     args = ap.parse_args()
-    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={args.ref}", "all", "ref"])
+    oracle_dir = os.path.join(ROOT, "oracle")
+    if args.ref is None:
+        args.ref = subprocess.check_output(["make", "-s", "-C", oracle_dir, "print-ref"], text=True).strip()
+    if not os.path.isfile(os.path.join(args.ref, "src", "renderer.cpp")):
+        raise SystemExit(f"no RenderToy tree at {args.ref!r}: pass --ref or set RENDERTOY_SRC")
+    subprocess.check_call(["make", "-s", "-C", oracle_dir, f"RENDERTOY_SRC={args.ref}", "all", "ref"])
     ref, refo, orc = bind.load("ref"), bind.load("ref_orig"), bind.load("oracle")
     if args.only == "obj":
         obj_case(ref, args.ref)

@@ -14,6 +14,15 @@ def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.uint32)
 
 
+def same_bits(a, b):
+    """Bit-equal arrays, except that NaN payloads need not agree (NaN
+    positions must)."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    na, nb = np.isnan(a), np.isnan(b)
+    return bool(np.array_equal(na, nb) and np.array_equal(bits(a)[~na], bits(b)[~nb]))
+
+
 def rel_close(a, b, rtol, atol=0.0):
     """Elementwise |a - b| <= rtol * max(|a|, |b|) + atol, NaN == NaN."""
     a = np.asarray(a, np.float64)

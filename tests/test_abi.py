@@ -29,7 +29,7 @@ def test_library_exports_header():
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
     assert set(rt.EXPORTS) == names
-    assert lib.rtx_version() == 1
+    assert lib.rtx_version() == 2
 
 
 def test_no_gpu_fails_loudly():

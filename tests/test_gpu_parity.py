@@ -253,32 +253,6 @@ def test_edge_cases(ctx, oracle):
         ctx.upload(bad)
 
 
-@pytest.fixture(scope="module")
-def icosphere_scene():
-    return scenes.displaced_icosphere(subdiv=8)
-
-
-def test_full_size_icosphere(ctx, oracle, icosphere_scene):
-    """The 1.3M-triangle displaced icosphere: primary hits of a 256 x 256 film
-    and per-path radiance of 256 pixels at max depth 12 against the oracle."""
-    sc = icosphere_scene
-    assert sc.n_tris == 20 * 4 ** 8 + 12
-    ctx.upload(sc)
-    osc = oracle.scene(sc)
-    tri, tuv = ctx.primary(256, 256)
-    rtri, rtuv = osc.primary(256, 256)
-    same = tri == rtri
-    assert same.mean() >= 0.9999, same.mean()
-    assert rel_close(tuv[..., 0][same], rtuv[..., 0][same], 1e-5).all()
-    W = H = 256
-    pix = np.random.RandomState(2).choice(W * H, 256, replace=False).astype(np.int32)
-    got = ctx.trace_paths(W, H, 0, 1, 12, seed=5).reshape(W * H, 3)[pix]
-    ref = osc.trace_paths(W, H, 0, 1, 12, 5, pixels=pix)[0]
-    ok = rel_close(got, ref, 1e-4, 1e-6).all(-1)
-    print(f"icosphere depth 12: {ok.mean() * 100:.2f} % of paths within 1e-4")
-    assert ok.mean() >= 0.97
-
-
 @pytest.mark.gpu
 def test_traversal_variants_agree(ctx):
     """The binary batch walk (0), the binary while-while walk with ray refill

@@ -1,13 +1,13 @@
 """rtx_image_gaussian_blur_noalloc: the Gaussian blur for callers that cannot
 allocate device memory when they call in (a plugin whose host application owns
 the device-memory budget, a real-time loop that must not synchronise the
-device, code running during someone else's stream capture).  It keeps its
-intermediate image in a fixed device array instead of allocating one.
+device).  It keeps its intermediate image in a fixed device array instead of
+allocating one.
 
-Called through the C ABI twice in a row on device buffers the test owns; each
-result must equal, bit for bit, what rtx_image_gaussian_blur returns for the
-same image (the tolerance of every compositor test here).  Collected last so a
-failing run has already run every other test; it also passes alone.
+Called through the C ABI several times in a row on device buffers the test
+owns; each result must equal, bit for bit, what rtx_image_gaussian_blur returns
+for the same image (the tolerance of every compositor test here).  Collected
+last so a failing run has already run every other test; it also passes alone.
 """
 import ctypes as C
 
@@ -43,6 +43,16 @@ def test_noalloc_blur_matches_allocating_entry_point():
             want = ctx.gaussian_blur(img, size, sigma)
             got = d_out.cpu().numpy()
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (W, H, size)
+        # in place (d_in == d_out) with the largest kernel: its column pass
+        # needs more than the default 48 KB of shared memory
+        img = rng.exponential(0.7, (96, 160, 3)).astype(np.float32)
+        d_io = torch.from_numpy(img).cuda()
+        r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(d_io.data_ptr()), C.c_void_p(d_io.data_ptr()),
+                                              160, 96, 255, 40.0, C.c_void_p(stream), msg, len(msg))
+        assert r == 0, msg.value
+        torch.cuda.synchronize()
+        want = ctx.gaussian_blur(img, 255, 40.0)
+        assert np.array_equal(d_io.cpu().numpy().view(np.uint32), want.view(np.uint32))
         # sizes beyond the fixed scratch are refused, with a message
         big = torch.zeros((2049, 1024, 3), device="cuda")
         r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(big.data_ptr()), C.c_void_p(big.data_ptr()),
@@ -51,5 +61,10 @@ def test_noalloc_blur_matches_allocating_entry_point():
         r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(big.data_ptr()), C.c_void_p(big.data_ptr()),
                                               64, 64, 256, 1.5, C.c_void_p(stream), msg, len(msg))
         assert r == 1
+        # within the pixel limit but taller than a grid's rows: refused too
+        tall = torch.zeros((70000, 16, 3), device="cuda")
+        r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(tall.data_ptr()), C.c_void_p(tall.data_ptr()),
+                                              16, 70000, 7, 1.5, C.c_void_p(stream), msg, len(msg))
+        assert r == 1 and b"65535" in msg.value
     finally:
         ctx.close()
