@@ -95,8 +95,9 @@ def denoiser_block(ctx, rank):
     fwd = sum(2 * 9 * L["cin_pad"] * L["cout_pad"] / 4 ** L["level"] for L in ctx.dn_layers())
     g = torch.Generator(device="cuda").manual_seed(rank)
     N, H, W = 32, 256, 256
-    raw = torch.rand(N, H, W, 10, device="cuda", generator=g)
+    raw = torch.rand(N, H, W, 11, device="cuda", generator=g)
     raw[..., :3] *= 4.0
+    raw[..., 10] = 4.0
     tgt = torch.rand(N, H, W, 3, device="cuda", generator=g)
 
     def med(fn, n=10):
@@ -110,7 +111,8 @@ def denoiser_block(ctx, rank):
 
     train_ms = med(lambda: ctx.dn_train_step(raw, tgt, lr=3e-4))
     train_launches = ctx.stats()["kernel_launches"]
-    fr = torch.rand(1, 1088, 1920, 10, device="cuda", generator=g)
+    fr = torch.rand(1, 1088, 1920, 11, device="cuda", generator=g)
+    fr[..., 10] = 4.0
     out = torch.empty(1, 1088, 1920, 3, device="cuda")
     infer_ms = med(lambda: ctx.dn_infer(fr, out))
     peak, kind = peaks("bf16_tflops")

@@ -439,11 +439,16 @@ int rtx_nn_conv3x3_wgrad(rtx_context* ctx, int N, int H, int W,
  * U-Net (3 x 3 convolutions of 32 / 64 / 96 / 128 / 160 channels, 2 x 2
  * average pooling, nearest upsampling, skip concatenation; 14 layers), run
  * and trained on the tensor cores in BF16 with FP32 accumulation.
- * Input, per pixel, 10 FP32 channels: radiance RGB, albedo RGB, normal RGB
- * (encoded (n + 1) / 2 as the normal pass writes it), depth; the network
- * predicts log(1 + radiance) and is trained with an L1 loss on
- * log(1 + target) and Adam (beta 0.9 / 0.999, eps 1e-8).
- * Batches are [N][H][W][10] with H and W multiples of 16.  Parameters are one
+ * Input, per pixel, 11 FP32 channels: radiance RGB (linear), albedo RGB,
+ * normal RGB (encoded (n + 1) / 2 as the normal pass writes it), depth, and
+ * the radiance's samples per pixel (the same over a frame).  The network
+ * predicts, per pixel, a 5 x 5 filter (the softmax of 25 logits) that is
+ * applied to the input radiance (taps clamped to the frame): the denoised
+ * radiance is a weighted mean of input pixels.  Training minimises the
+ * relative squared error (o - t)^2 / (o^2 + 0.01) of the filtered radiance o
+ * against the target t, the prediction in the denominator held constant, with
+ * Adam (beta 0.9 / 0.999, eps 1e-8).
+ * Batches are [N][H][W][11] with H and W multiples of 16.  Parameters are one
  * FP32 array in the padded layout rtx_dn_layer describes. */
 int rtx_dn_init(rtx_context* ctx, uint64_t seed);
 /* n_params: FP32 entries of the padded array; n_real: parameters of the
@@ -462,21 +467,23 @@ int rtx_dn_get_adam(rtx_context* ctx, float* m, float* v);
 int rtx_dn_set_adam(rtx_context* ctx, const float* m, const float* v,
                     int step);
 /* forward + loss + backward without an update (the gradients stay readable
- * with rtx_dn_get_grads) */
+ * with rtx_dn_get_grads); *loss = mean over pixels and channels */
 int rtx_dn_loss_grads(rtx_context* ctx, const float* input, const float* target,
                       int N, int H, int W, double* loss);
 /* one Adam step on a minibatch; *loss = the minibatch loss before the step */
 int rtx_dn_train_step(rtx_context* ctx, const float* input, const float* target,
                       int N, int H, int W, float lr, double* loss);
-/* out [N][H][W][3] = exp(prediction) - 1 */
+/* out [N][H][W][3] = the denoised radiance */
 int rtx_dn_infer(rtx_context* ctx, const float* input, float* out, int N, int H,
                  int W);
 /* Denoise one frame from the renderer's passes, each W x H RGB FP32 as
- * rtx_render_pt / rtx_render_aov write them (depth: channel 0 is used).  Any
- * W, H: the frame is padded with zeros to multiples of 16 on the device. */
+ * rtx_render_pt / rtx_render_aov write them (depth: channel 0 is used), the
+ * radiance rendered at `spp` samples per pixel.  Any W, H: the frame is
+ * padded to multiples of 16 on the device (the filters never read the
+ * padding). */
 int rtx_denoise(rtx_context* ctx, const float* radiance, const float* albedo,
-                const float* normal, const float* depth, float* out, int W,
-                int H);
+                const float* normal, const float* depth, int spp, float* out,
+                int W, int H);
 
 /* ---- without allocation -----------------------------------------------------
  * No counterpart in RenderToy.  Image::GaussianBlur (as rtx_image_gaussian_blur)

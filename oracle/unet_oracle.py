@@ -82,11 +82,58 @@ def upsample2_grad(dy):
     return dy.reshape(n, h // 2, 2, w // 2, 2, c).sum(axis=(2, 4))
 
 
-def l1_log_loss(pred, target):
-    """mean |pred - log(1 + target)|; pred is in log space."""
-    t = np.log1p(np.maximum(np.asarray(target, np.float64), 0.0))
-    d = np.asarray(pred, np.float64) - t
-    return np.abs(d).mean(), np.sign(d) / d.size
+KP_WIDTH = 5
+KP_TAPS = KP_WIDTH * KP_WIDTH
+REL_EPS = 1e-2
+
+
+def sane(x):
+    """Radiance made safe to filter: NaN and negatives 0, +inf the BF16 range."""
+    x = np.nan_to_num(np.asarray(x, np.float64), nan=0.0, posinf=65504.0, neginf=0.0)
+    return np.clip(x, 0.0, 65504.0)
+
+
+def kp_taps(rad):
+    """rad [N][H][W][3] -> [N][H][W][25][3]: tap k = offset
+    (k // 5 - 2, k % 5 - 2) in (y, x), clamped to the frame."""
+    r = KP_WIDTH // 2
+    N, H, W, _ = rad.shape
+    pad = np.pad(rad, ((0, 0), (r, r), (r, r), (0, 0)), mode="edge")
+    return np.stack([pad[:, k // KP_WIDTH:k // KP_WIDTH + H, k % KP_WIDTH:k % KP_WIDTH + W]
+                     for k in range(KP_TAPS)], axis=3)
+
+
+def softmax(logits):
+    z = logits - logits.max(-1, keepdims=True)
+    e = np.exp(z)
+    return e / e.sum(-1, keepdims=True)
+
+
+def kp_apply(logits, raw):
+    """The denoised radiance: softmax(logits[..., :25]) over the 5 x 5
+    neighbourhood of the input radiance."""
+    w = softmax(np.asarray(logits, np.float64)[..., :KP_TAPS])
+    taps = kp_taps(sane(np.asarray(raw)[..., :3]))
+    return (w[..., None] * taps).sum(3)
+
+
+def kp_loss(logits, raw, target):
+    """mean over pixels and channels of (o - t)^2 / (o^2 + eps), o the
+    filtered radiance, the denominator held constant; returns the loss and
+    its gradient with respect to the logits (zero beyond the 25 taps)."""
+    logits = np.asarray(logits, np.float64)
+    w = softmax(logits[..., :KP_TAPS])
+    taps = kp_taps(sane(np.asarray(raw)[..., :3]))
+    o = (w[..., None] * taps).sum(3)
+    t = sane(target)
+    den = o * o + REL_EPS
+    d = o - t
+    loss = (d * d / den).mean()
+    g = 2.0 * d / den / d.size
+    dw = (g[..., None, :] * taps).sum(-1)
+    dl = np.zeros_like(logits)
+    dl[..., :KP_TAPS] = w * (dw - (w * dw).sum(-1, keepdims=True))
+    return loss, dl
 
 
 def adam(p, g, m, v, step, lr=3e-4, b1=0.9, b2=0.999, eps=1e-8):
@@ -103,8 +150,8 @@ def adam(p, g, m, v, step, lr=3e-4, b1=0.9, b2=0.999, eps=1e-8):
 # Architecture (the denoiser's definition): 3 x 3 convolutions with ReLU
 # except the last, 2 x 2 average pooling, nearest upsampling, skip
 # concatenation after the upsampled channels.  Tensors carry padded channel
-# counts (multiples of 8; the 10-channel input is padded to 16, the 3-channel
-# output to 16), and the parameters live in one flat array:
+# counts (multiples of 8; the 11-channel input is padded to 16, the 25 filter
+# logits of the output to 32), and the parameters live in one flat array:
 # per layer w [cout_pad][9][cin_pad] then b [cout_pad], each start aligned to
 # 4 floats.  With bf16=True every value the GPU stores in BF16 (the encoded
 # input, the weights, activations, data gradients) is rounded to BF16
@@ -121,13 +168,13 @@ TENSORS = {
 POOLED = {"P1": "S0", "P2": "S1", "P3": "S2", "P4": "S3"}
 # (s1, s1 upsampled, s2, out, cout_pad, cout, cin, relu)
 LAYERS = [
-    ("X", 0, None, "A0a", 32, 32, 10, 1), ("A0a", 0, None, "S0", 32, 32, 32, 1),
+    ("X", 0, None, "A0a", 32, 32, 11, 1), ("A0a", 0, None, "S0", 32, 32, 32, 1),
     ("P1", 0, None, "A1a", 64, 64, 32, 1), ("A1a", 0, None, "S1", 64, 64, 64, 1),
     ("P2", 0, None, "A2a", 96, 96, 64, 1), ("A2a", 0, None, "S2", 96, 96, 96, 1),
     ("P3", 0, None, "A3a", 128, 128, 96, 1), ("A3a", 0, None, "S3", 128, 128, 128, 1),
     ("P4", 0, None, "B", 160, 160, 128, 1), ("B", 1, "S3", "U3", 128, 128, 288, 1),
     ("U3", 1, "S2", "U2", 96, 96, 224, 1), ("U2", 1, "S1", "U1", 64, 64, 160, 1),
-    ("U1", 1, "S0", "U0", 32, 32, 96, 1), ("U0", 0, None, None, 16, 3, 32, 0),
+    ("U1", 1, "S0", "U0", 32, 32, 96, 1), ("U0", 0, None, None, 32, KP_TAPS, 32, 0),
 ]
 
 
@@ -177,12 +224,14 @@ def init_params(seed=0):
 
 
 def encode_input(raw):
-    """raw [N][H][W][10] -> [N][H][W][16]: log(1 + max(radiance, 0)), the
-    other 7 channels as they are, 6 zero channels."""
+    """raw [N][H][W][11] -> [N][H][W][16]: log(1 + radiance) of the sane
+    radiance, albedo / normal / depth as they are, log2(spp) / 16, 5 zero
+    channels."""
     raw = np.asarray(raw, np.float64)
     x = np.zeros(raw.shape[:3] + (16,))
-    x[..., :3] = np.log1p(np.maximum(raw[..., :3], 0.0))
+    x[..., :3] = np.log1p(sane(raw[..., :3]))
     x[..., 3:10] = raw[..., 3:10]
+    x[..., 10] = np.log2(np.maximum(raw[..., 10], 1.0)) / 16.0
     return x
 
 
@@ -221,20 +270,17 @@ class UNet:
         self.act = act
         return act["pred"]
 
+    def denoise(self, raw):
+        """The denoised radiance of a batch (the predicted filters applied)."""
+        return kp_apply(self.forward(raw), raw)
+
     def loss_and_grads(self, raw, target):
-        """L1 on log(1 + target) of the first 3 output channels; returns the
-        loss and the gradient of the flat parameter array."""
+        """The relative squared error of the filtered radiance (kp_loss);
+        returns the loss and the gradient of the flat parameter array."""
         pred = self.forward(raw)
         act = self.act
-        P = pred.shape[0] * pred.shape[1] * pred.shape[2]
-        t = np.log1p(np.maximum(np.asarray(target, np.float64), 0.0))
-        d = pred[..., :3] - t
-        loss = np.abs(d).mean()
-        inv = float(np.float32(1.0) / np.float32(3.0 * P))
-        if self.bf16:
-            inv = float(to_bf16(inv))
-        dpred = np.zeros_like(pred)
-        dpred[..., :3] = np.sign(d) * inv
+        loss, dpred = kp_loss(pred, raw, target)
+        dpred = self.r(dpred)
         grad = np.zeros_like(self.p)
         dact = {}
         for i in range(len(LAYERS) - 1, -1, -1):

@@ -138,7 +138,7 @@ def lib() -> C.CDLL:
         "rtx_dn_loss_grads": (i, [vp, vp, vp, i, i, i, C.POINTER(C.c_double)]),
         "rtx_dn_train_step": (i, [vp, vp, vp, i, i, i, f, C.POINTER(C.c_double)]),
         "rtx_dn_infer": (i, [vp, vp, vp, i, i, i]),
-        "rtx_denoise": (i, [vp, vp, vp, vp, vp, vp, i, i]),
+        "rtx_denoise": (i, [vp, vp, vp, vp, vp, i, vp, i, i]),
         "rtx_scene_set_texture_table": (i, [vp, vp]),
         "rtx_texture_sample": (i, [vp, i, f, i, vp, vp]),
         "rtx_render_pt_resolved": (i, [vp, vp, i, i, i, i, u64, vp, f, f, vp, vp, i]),
@@ -609,7 +609,7 @@ class Context:
         return x if hasattr(x, "data_ptr") else _f32(x)
 
     def dn_loss_grads(self, inp, target):
-        """Loss of a batch (inp [N][H][W][10], target [N][H][W][3]); the
+        """Loss of a batch (inp [N][H][W][11], target [N][H][W][3]); the
         gradients are then read with dn_get_grads."""
         inp, target = self._batch(inp), self._batch(target)
         N, H, W = inp.shape[:3]
@@ -633,13 +633,15 @@ class Context:
         self._check(self.L.rtx_dn_infer(self.h, _ptr(inp), _ptr(out), N, H, W))
         return out
 
-    def denoise(self, radiance, albedo, normal, depth, out=None):
-        """Denoise a frame from its passes (each H x W x 3 FP32)."""
+    def denoise(self, radiance, albedo, normal, depth, spp, out=None):
+        """Denoise a frame from its passes (each H x W x 3 FP32), the radiance
+        rendered at `spp` samples per pixel."""
         rad, alb, nrm, dep = (x if hasattr(x, "data_ptr") else _f32(x) for x in (radiance, albedo, normal, depth))
         H, W = rad.shape[:2]
         if out is None:
             out = np.zeros((H, W, 3), np.float32)
-        self._check(self.L.rtx_denoise(self.h, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(dep), _ptr(out), W, H))
+        self._check(self.L.rtx_denoise(self.h, _ptr(rad), _ptr(alb), _ptr(nrm), _ptr(dep), int(spp), _ptr(out),
+                                       W, H))
         return out
 
     # -- compositor -------------------------------------------------------------

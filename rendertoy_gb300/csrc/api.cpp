@@ -1837,7 +1837,7 @@ static int dn_run(rtx_context* c, const float* input, const float* target, int N
   const size_t P = (size_t)N * H * W;
   if ((r = begin(c))) return r;
   Arg ai, at;
-  if ((r = bind_in(c, input, P * 40, 0, ai))) return r;
+  if ((r = bind_in(c, input, P * 4 * rtx::nn::kRawCh, 0, ai))) return r;
   if ((r = bind_in(c, target, P * 12, 1, at))) return r;
   RTX_CUDA(c->dn->reserve((long long)P), "denoiser buffers");
   double l = 0.0;
@@ -1871,11 +1871,11 @@ int rtx_dn_infer(rtx_context* c, const float* input, float* out, int N, int H, i
   const size_t P = (size_t)N * H * W;
   if ((r = begin(c))) return r;
   Arg ai, ao;
-  if ((r = bind_in(c, input, P * 40, 0, ai))) return r;
+  if ((r = bind_in(c, input, P * 4 * rtx::nn::kRawCh, 0, ai))) return r;
   if ((r = bind_out(c, out, P * 12, 1, ao))) return r;
   RTX_CUDA(c->dn->reserve((long long)P), "denoiser buffers");
   cudaError_t e = c->dn->forward((const float*)ai.dev, N, H, W, c->d_err, c->stream);
-  if (e == cudaSuccess) e = c->dn->decode((float*)ao.dev, (long long)P, c->stream);
+  if (e == cudaSuccess) e = c->dn->decode((const float*)ai.dev, (float*)ao.dev, N, H, W, H, W, c->stream);
   c->stats.kernel_launches = c->dn->last_launches() + 1;
   if (e != cudaSuccess) return cuda_fail(c, e, "denoiser inference");
   if ((r = copy_back(c, ao))) return r;
@@ -1883,11 +1883,12 @@ int rtx_dn_infer(rtx_context* c, const float* input, float* out, int N, int H, i
 }
 
 int rtx_denoise(rtx_context* c, const float* radiance, const float* albedo, const float* normal,
-                const float* depth, float* out, int W, int H) {
+                const float* depth, int spp, float* out, int W, int H) {
   int r;
   if ((r = need_dn(c))) return r;
   if (W <= 0 || H <= 0 || (long long)W * H > (1LL << 28)) return fail(c, RTX_ERR_INVALID, "bad image size");
   if (!radiance || !albedo || !normal || !depth || !out) return fail(c, RTX_ERR_INVALID, "NULL image");
+  if (spp < 1) return fail(c, RTX_ERR_INVALID, "spp must be >= 1");
   const int Wp = (W + 15) / 16 * 16, Hp = (H + 15) / 16 * 16;
   const size_t bytes = (size_t)W * H * 12;
   if ((r = begin(c))) return r;
@@ -1897,13 +1898,13 @@ int rtx_denoise(rtx_context* c, const float* radiance, const float* albedo, cons
   if ((r = bind_in(c, normal, bytes, 2, an))) return r;
   if ((r = bind_in(c, depth, bytes, 3, ad))) return r;
   if ((r = bind_out(c, out, bytes, 4, ao))) return r;
-  RTX_CUDA(c->stage[5].ensure((size_t)Wp * Hp * 40), "stage alloc");
+  RTX_CUDA(c->stage[5].ensure((size_t)Wp * Hp * 4 * rtx::nn::kRawCh), "stage alloc");
   RTX_CUDA(c->dn->reserve((long long)Wp * Hp), "denoiser buffers");
   float* raw = (float*)c->stage[5].p;
   cudaError_t e = rtx::nn::pack_passes((const float*)ar.dev, (const float*)aa.dev, (const float*)an.dev,
-                                       (const float*)ad.dev, raw, W, H, Wp, Hp, c->stream);
+                                       (const float*)ad.dev, (float)spp, raw, W, H, Wp, Hp, c->stream);
   if (e == cudaSuccess) e = c->dn->forward(raw, 1, Hp, Wp, c->d_err, c->stream);
-  if (e == cudaSuccess) e = rtx::nn::decode_crop(c->dn->prediction(), (float*)ao.dev, W, H, Wp, c->stream);
+  if (e == cudaSuccess) e = c->dn->decode(raw, (float*)ao.dev, 1, H, W, Hp, Wp, c->stream);
   c->stats.kernel_launches = c->dn->last_launches() + 2;
   if (e != cudaSuccess) return cuda_fail(c, e, "denoise");
   if ((r = copy_back(c, ao))) return r;

@@ -11,6 +11,27 @@ namespace nn {
 
 using bf16 = __nv_bfloat16;
 
+// Network input and output records.
+//   raw input, FP32 per pixel: radiance 3 (linear), albedo 3, normal 3 (as the
+//   normal pass encodes it), depth 1, and the radiance's samples per pixel 1
+//   (the same value over a frame; it tells the network how noisy the
+//   radiance is).
+//   prediction, FP32 per pixel: kKpTaps filter logits (padded to kPredCh).
+//   The denoised radiance is the softmax of the logits applied to the
+//   kKpWidth x kKpWidth neighbourhood of the input radiance (taps clamped to
+//   the frame): a kernel-predicting output (Bako et al., SIGGRAPH 2017),
+//   which can only average input pixels and so approaches its input as the
+//   input's noise vanishes.
+constexpr int kRawCh = 11;
+constexpr int kKpWidth = 5;
+constexpr int kKpTaps = kKpWidth * kKpWidth;
+constexpr int kPredCh = 32;
+// Loss: relative squared error with the prediction (not differentiated) in
+// the denominator, (o - t)^2 / (o^2 + kRelEps): its minimiser over noisy
+// targets is their mean, so unbiased targets of any noise level train it
+// toward the clean image.
+constexpr float kRelEps = 1e-2f;
+
 // One input of a convolution: C channels; `up` = stored at half resolution
 // and read upsampled (nearest) to the convolution's resolution.
 struct Src {

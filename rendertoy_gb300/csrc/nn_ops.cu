@@ -1,8 +1,9 @@
 // nn_ops.cu — the denoiser's memory-bound operators: input encoding, 2 x 2
 // average pooling and its gradient, the gradient of nearest upsampling and of
-// channel concatenation, the L1-on-log loss, bias gradients, Adam and the
-// BF16 weight layouts the convolutions read.  One thread per 8 channels of a
-// pixel (16-byte BF16 accesses) unless noted.
+// channel concatenation, the kernel-predicting output with its relative-L2
+// loss, bias gradients, Adam and the BF16 weight layouts the convolutions
+// read.  One thread per 8 channels of a pixel (16-byte BF16 accesses) unless
+// noted.
 #include <algorithm>
 
 #include "nn.h"
@@ -34,19 +35,58 @@ __device__ __forceinline__ void st8(bf16* p, const float* f) {
 
 unsigned blocks(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
+// A radiance value made safe to filter and to learn from: NaN and negative
+// values (the renderer's rare NaN pixels) read 0, +inf reads the BF16 range.
+__device__ __forceinline__ float sane(float v) { return fminf(fmaxf(v, 0.0f), 65504.0f); }
+
+// Pixel (n, y, x) of frames of Hs x Ws stored pixels, RGB of its raw record
+__device__ __forceinline__ void raw_rgb(const float* raw, long long pix, float* c) {
+  const float* r = raw + (long long)kRawCh * pix;
+  c[0] = sane(r[0]);
+  c[1] = sane(r[1]);
+  c[2] = sane(r[2]);
+}
+
+// Softmax of the pixel's kKpTaps logits (max subtracted first).
+__device__ __forceinline__ void kp_weights(const float* __restrict__ logits, float* w) {
+  float m = logits[0];
+#pragma unroll
+  for (int k = 1; k < kKpTaps; ++k) m = fmaxf(m, logits[k]);
+  float s = 0.0f;
+#pragma unroll
+  for (int k = 0; k < kKpTaps; ++k) {
+    w[k] = expf(logits[k] - m);
+    s += w[k];
+  }
+  const float inv = 1.0f / s;
+#pragma unroll
+  for (int k = 0; k < kKpTaps; ++k) w[k] *= inv;
+}
+
+// Tap k of pixel (x, y) of an Hc x Wc frame stored with row stride Ws:
+// offset (k / kKpWidth - r, k % kKpWidth - r), clamped to the frame.
+__device__ __forceinline__ long long kp_tap(long long frame0, int x, int y, int k, int Wc, int Hc, int Ws) {
+  constexpr int r = kKpWidth / 2;
+  const int ty = min(max(y + k / kKpWidth - r, 0), Hc - 1);
+  const int tx = min(max(x + k % kKpWidth - r, 0), Wc - 1);
+  return frame0 + (long long)ty * Ws + tx;
+}
+
 }  // namespace
 
-// raw [P][10] (radiance 3, albedo 3, normal 3, depth 1) -> [P][16] BF16,
-// radiance as log(1 + max(x, 0)), channels 10..15 zero
+// raw [P][kRawCh] -> [P][16] BF16: radiance as log(1 + x), albedo, normal and
+// depth as they are, the samples per pixel as log2(spp) / 16, channels
+// 11..15 zero
 __global__ void k_encode_input(const float* __restrict__ raw, bf16* __restrict__ x, long long P) {
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= P) return;
-  const float* r = raw + 10 * p;
+  const float* r = raw + (long long)kRawCh * p;
   float f[16];
 #pragma unroll
   for (int i = 0; i < 16; ++i) f[i] = 0.0f;
-  for (int i = 0; i < 3; ++i) f[i] = log1pf(fmaxf(r[i], 0.0f));
+  for (int i = 0; i < 3; ++i) f[i] = log1pf(sane(r[i]));
   for (int i = 3; i < 10; ++i) f[i] = r[i];
+  f[10] = log2f(fmaxf(r[10], 1.0f)) * (1.0f / 16.0f);
   st8(x + 16 * p, f);
   st8(x + 16 * p + 8, f + 8);
 }
@@ -135,22 +175,55 @@ __global__ void k_pool_grad_acc(const bf16* __restrict__ dpool, const bf16* __re
 // L1 on log(1 + target): pred [P][16] FP32 (channels 0..2), target [P][3];
 // d_pred = sign(pred - log1p(target)) / (3P) as BF16 [P][16]; loss summed
 // into *loss (FP64)
-__global__ void k_l1log_loss(const float* __restrict__ pred, const float* __restrict__ target,
-                             bf16* __restrict__ dpred, long long P, double* loss) {
+// The loss of the kernel-predicting output, per pixel p of N frames of H x W:
+// o = sum_k w_k r(tap k), loss = sum_c (o_c - t_c)^2 / (o_c^2 + kRelEps),
+// with the denominator held constant; the gradient of the mean over pixels
+// and channels is taken through the filter and the softmax to the logits
+// (dl_k = w_k (dw_k - sum_j w_j dw_j), dw_k = sum_c g_c r_c(tap k)), stored
+// as BF16 [P][kPredCh] (zero beyond the taps).
+__global__ void __launch_bounds__(256) k_kp_loss(const float* __restrict__ pred, const float* __restrict__ raw,
+                                                 const float* __restrict__ target, bf16* __restrict__ dpred,
+                                                 int N, int H, int W, double* loss) {
+  const long long P = (long long)N * H * W;
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   float part = 0.0f;
   if (p < P) {
-    float g[16];
+    const int x = (int)(p % W);
+    const long long q = p / W;
+    const int y = (int)(q % H);
+    const long long frame0 = (q / H) * (long long)H * W;
+    float w[kKpTaps];
+    kp_weights(pred + (long long)kPredCh * p, w);
+    float o[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int i = 0; i < 16; ++i) g[i] = 0.0f;
-    float inv = 1.0f / (3.0f * (float)P);
-    for (int i = 0; i < 3; ++i) {
-      float d = pred[16 * p + i] - log1pf(fmaxf(target[3 * p + i], 0.0f));
-      part += fabsf(d);
-      g[i] = d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f);
+    for (int k = 0; k < kKpTaps; ++k) {
+      float c[3];
+      raw_rgb(raw, kp_tap(frame0, x, y, k, W, H, W), c);
+      o[0] += w[k] * c[0];
+      o[1] += w[k] * c[1];
+      o[2] += w[k] * c[2];
     }
-    st8(dpred + 16 * p, g);
-    st8(dpred + 16 * p + 8, g + 8);
+    const float inv = 1.0f / (3.0f * (float)P);
+    float g[3];
+    for (int i = 0; i < 3; ++i) {
+      const float d = o[i] - sane(target[3 * p + i]);
+      const float den = o[i] * o[i] + kRelEps;
+      part += d * d / den;
+      g[i] = 2.0f * d / den * inv;
+    }
+    float dw[kKpTaps], s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kKpTaps; ++k) {
+      float c[3];
+      raw_rgb(raw, kp_tap(frame0, x, y, k, W, H, W), c);
+      dw[k] = g[0] * c[0] + g[1] * c[1] + g[2] * c[2];
+      s += w[k] * dw[k];
+    }
+    float dl[kPredCh];
+#pragma unroll
+    for (int k = 0; k < kPredCh; ++k) dl[k] = k < kKpTaps ? w[k] * (dw[k] - s) : 0.0f;
+#pragma unroll
+    for (int k = 0; k < kPredCh; k += 8) st8(dpred + (long long)kPredCh * p + k, dl + k);
   }
   for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, (double)part);
@@ -215,23 +288,46 @@ __global__ void k_weights_bf16(const float* __restrict__ master, bf16* __restric
 }
 
 // prediction (log space) [P][16] -> radiance [P][3] = exp(pred) - 1
-__global__ void k_decode_output(const float* __restrict__ pred, float* __restrict__ out, long long P) {
-  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p >= P) return;
-  for (int i = 0; i < 3; ++i) out[3 * p + i] = expm1f(pred[16 * p + i]);
+// The denoised radiance: the predicted filter applied to the input radiance,
+// for N frames of Hc x Wc pixels stored as Hs x Ws (the frame is the top-left
+// corner; taps are clamped to it); out [N][Hc][Wc][3].
+__global__ void k_kp_apply(const float* __restrict__ pred, const float* __restrict__ raw, float* __restrict__ out,
+                           int N, int Hc, int Wc, int Hs, int Ws) {
+  const long long P = (long long)N * Hc * Wc;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  const int x = (int)(i % Wc);
+  const long long q = i / Wc;
+  const int y = (int)(q % Hc);
+  const long long frame0 = (q / Hc) * (long long)Hs * Ws;
+  const long long p = frame0 + (long long)y * Ws + x;
+  float w[kKpTaps];
+  kp_weights(pred + (long long)kPredCh * p, w);
+  float o[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < kKpTaps; ++k) {
+    float c[3];
+    raw_rgb(raw, kp_tap(frame0, x, y, k, Wc, Hc, Ws), c);
+    o[0] += w[k] * c[0];
+    o[1] += w[k] * c[1];
+    o[2] += w[k] * c[2];
+  }
+  out[3 * i] = o[0];
+  out[3 * i + 1] = o[1];
+  out[3 * i + 2] = o[2];
 }
 
-// the renderer's passes (W x H RGB FP32 each) -> raw [Hp][Wp][10], zero
-// outside the W x H frame
+// the renderer's passes (W x H RGB FP32 each) + their samples per pixel ->
+// raw [Hp][Wp][kRawCh], zero outside the W x H frame
 __global__ void k_pack_passes(const float* __restrict__ rad, const float* __restrict__ alb,
-                              const float* __restrict__ nrm, const float* __restrict__ dep,
+                              const float* __restrict__ nrm, const float* __restrict__ dep, float spp,
                               float* __restrict__ raw, int W, int H, int Wp, int Hp) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= (long long)Wp * Hp) return;
   int x = (int)(i % Wp), y = (int)(i / Wp);
-  float* r = raw + 10 * i;
+  float* r = raw + (long long)kRawCh * i;
   if (x >= W || y >= H) {
-    for (int k = 0; k < 10; ++k) r[k] = 0.0f;
+    for (int k = 0; k < kRawCh; ++k) r[k] = 0.0f;
     return;
   }
   long long s = ((long long)y * W + x) * 3;
@@ -241,17 +337,10 @@ __global__ void k_pack_passes(const float* __restrict__ rad, const float* __rest
     r[6 + k] = nrm[s + k];
   }
   r[9] = dep[s];
+  r[10] = spp;
 }
 
 // prediction [Hp][Wp][16] (log space) -> radiance W x H RGB
-__global__ void k_decode_crop(const float* __restrict__ pred, float* __restrict__ out, int W, int H, int Wp) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= (long long)W * H) return;
-  int x = (int)(i % W), y = (int)(i / W);
-  const float* q = pred + 16 * ((long long)y * Wp + x);
-  for (int k = 0; k < 3; ++k) out[3 * i + k] = expm1f(q[k]);
-}
-
 // ---- launchers ------------------------------------------------------------
 cudaError_t encode_input(const float* raw, bf16* x, long long P, cudaStream_t st) {
   k_encode_input<<<blocks(P), 256, 0, st>>>(raw, x, P);
@@ -278,9 +367,9 @@ cudaError_t pool_grad_acc(const bf16* dpool, const bf16* skip, bf16* dskip, int 
   k_pool_grad_acc<<<blocks(n), 256, 0, st>>>(dpool, skip, dskip, N, H, W, C);
   return cudaGetLastError();
 }
-cudaError_t l1log_loss(const float* pred, const float* target, bf16* dpred, long long P, double* loss,
-                       cudaStream_t st) {
-  k_l1log_loss<<<blocks(P), 256, 0, st>>>(pred, target, dpred, P, loss);
+cudaError_t kp_loss(const float* pred, const float* raw, const float* target, bf16* dpred, int N, int H,
+                    int W, double* loss, cudaStream_t st) {
+  k_kp_loss<<<blocks((long long)N * H * W), 256, 0, st>>>(pred, raw, target, dpred, N, H, W, loss);
   return cudaGetLastError();
 }
 cudaError_t bias_grad(const bf16* dout, long long P, int C, float* db, cudaStream_t st) {
@@ -301,18 +390,15 @@ cudaError_t weights_bf16(const float* master, bf16* w, bf16* wt, int Cout, int C
   k_weights_bf16<<<blocks((long long)Cout * 9 * Cin), 256, 0, st>>>(master, w, wt, Cout, Cin);
   return cudaGetLastError();
 }
-cudaError_t decode_output(const float* pred, float* out, long long P, cudaStream_t st) {
-  k_decode_output<<<blocks(P), 256, 0, st>>>(pred, out, P);
+cudaError_t kp_apply(const float* pred, const float* raw, float* out, int N, int Hc, int Wc, int Hs, int Ws,
+                     cudaStream_t st) {
+  k_kp_apply<<<blocks((long long)N * Hc * Wc), 256, 0, st>>>(pred, raw, out, N, Hc, Wc, Hs, Ws);
   return cudaGetLastError();
 }
 
-cudaError_t pack_passes(const float* rad, const float* alb, const float* nrm, const float* dep, float* raw,
-                        int W, int H, int Wp, int Hp, cudaStream_t st) {
-  k_pack_passes<<<blocks((long long)Wp * Hp), 256, 0, st>>>(rad, alb, nrm, dep, raw, W, H, Wp, Hp);
-  return cudaGetLastError();
-}
-cudaError_t decode_crop(const float* pred, float* out, int W, int H, int Wp, cudaStream_t st) {
-  k_decode_crop<<<blocks((long long)W * H), 256, 0, st>>>(pred, out, W, H, Wp);
+cudaError_t pack_passes(const float* rad, const float* alb, const float* nrm, const float* dep, float spp,
+                        float* raw, int W, int H, int Wp, int Hp, cudaStream_t st) {
+  k_pack_passes<<<blocks((long long)Wp * Hp), 256, 0, st>>>(rad, alb, nrm, dep, spp, raw, W, H, Wp, Hp);
   return cudaGetLastError();
 }
 

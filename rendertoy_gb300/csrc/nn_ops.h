@@ -12,16 +12,20 @@ cudaError_t upsample_grad(const bf16* dcat, int Ccat, int c0, bf16* dlow, int N,
 cudaError_t take_channels(const bf16* dcat, int Ccat, int c0, bf16* dst, long long P, int C, cudaStream_t st);
 cudaError_t pool_grad_acc(const bf16* dpool, const bf16* skip, bf16* dskip, int N, int H, int W, int C,
                           cudaStream_t st);
-cudaError_t l1log_loss(const float* pred, const float* target, bf16* dpred, long long P, double* loss,
-                       cudaStream_t st);
+// loss of the kernel-predicting output of N frames of H x W (see nn.h);
+// adds the summed per-pixel, per-channel loss to *loss
+cudaError_t kp_loss(const float* pred, const float* raw, const float* target, bf16* dpred, int N, int H,
+                    int W, double* loss, cudaStream_t st);
 cudaError_t bias_grad(const bf16* dout, long long P, int C, float* db, cudaStream_t st);
 cudaError_t adam(float* p, const float* g, float* m, float* v, long long n, float lr, int step,
                  cudaStream_t st);
 cudaError_t weights_bf16(const float* master, bf16* w, bf16* wt, int Cout, int Cin, cudaStream_t st);
-cudaError_t decode_output(const float* pred, float* out, long long P, cudaStream_t st);
-cudaError_t pack_passes(const float* rad, const float* alb, const float* nrm, const float* dep, float* raw,
-                        int W, int H, int Wp, int Hp, cudaStream_t st);
-cudaError_t decode_crop(const float* pred, float* out, int W, int H, int Wp, cudaStream_t st);
+// out [N][Hc][Wc][3] = the predicted filters applied to the input radiance of
+// frames stored as Hs x Ws pixels (pred and raw share that layout)
+cudaError_t kp_apply(const float* pred, const float* raw, float* out, int N, int Hc, int Wc, int Hs, int Ws,
+                     cudaStream_t st);
+cudaError_t pack_passes(const float* rad, const float* alb, const float* nrm, const float* dep, float spp,
+                        float* raw, int W, int H, int Wp, int Hp, cudaStream_t st);
 
 }  // namespace nn
 }  // namespace rtx

@@ -1,18 +1,21 @@
 // nn_unet.cu — the learned denoiser: a 5-level U-Net over the renderer's
-// 4-spp radiance and its albedo / normal / depth passes, trained and run with
-// the tcgen05 convolutions of nn_conv.cu.  RenderToy has no counterpart (its
-// demos call Intel OIDN, an external binary).
+// low-spp radiance, its albedo / normal / depth passes and its samples per
+// pixel, trained and run with the tcgen05 convolutions of nn_conv.cu.
+// RenderToy has no counterpart (its demos call Intel OIDN, an external
+// binary).
 //
 // Layers (3 x 3 convolutions, ReLU except the last; pooling 2 x 2 average,
 // upsampling nearest; channels 32 / 64 / 96 / 128 / 160):
-//   level 0: e0a 10->32, e0b 32->32 = S0         (H   x W)
+//   level 0: e0a 11->32, e0b 32->32 = S0         (H   x W)
 //   level 1: e1a 32->64, e1b 64->64 = S1         (H/2)
 //   level 2: e2a 64->96, e2b 96->96 = S2         (H/4)
 //   level 3: e3a 96->128, e3b 128->128 = S3      (H/8)
 //   level 4: bottleneck 128->160 = B             (H/16)
 //   decoder: d3 [up(B), S3] 288->128, d2 [up, S2] 224->96,
-//            d1 [up, S1] 160->64, d0 [up, S0] 96->32, out 32->3 (linear)
-// The output is log(1 + radiance); the loss is L1 against log(1 + target).
+//            d1 [up, S1] 160->64, d0 [up, S0] 96->32, out 32->25 (linear)
+// The output is a 5 x 5 filter per pixel (softmax of 25 logits) applied to the
+// input radiance; the loss is the relative squared error of the filtered
+// radiance against the target (nn.h).
 // Parameters live as FP32 masters in one flat array in the padded layout the
 // kernels read (w [Cout][9][Cin] then b [Cout] per layer, padding zero and
 // kept zero by construction); BF16 copies (and transposes for the data
@@ -44,13 +47,13 @@ struct LayerDef {
   int cout_pad, cout_real, cin_real, relu;
 };
 const LayerDef kLayers[] = {
-    {tX, 0, -1, tA0a, 32, 32, 10, 1},    {tA0a, 0, -1, tS0, 32, 32, 32, 1},
+    {tX, 0, -1, tA0a, 32, 32, kRawCh, 1}, {tA0a, 0, -1, tS0, 32, 32, 32, 1},
     {tP1, 0, -1, tA1a, 64, 64, 32, 1},   {tA1a, 0, -1, tS1, 64, 64, 64, 1},
     {tP2, 0, -1, tA2a, 96, 96, 64, 1},   {tA2a, 0, -1, tS2, 96, 96, 96, 1},
     {tP3, 0, -1, tA3a, 128, 128, 96, 1}, {tA3a, 0, -1, tS3, 128, 128, 128, 1},
     {tP4, 0, -1, tB, 160, 160, 128, 1},  {tB, 1, tS3, tU3, 128, 128, 288, 1},
     {tU3, 1, tS2, tU2, 96, 96, 224, 1},  {tU2, 1, tS1, tU1, 64, 64, 160, 1},
-    {tU1, 1, tS0, tU0, 32, 32, 96, 1},   {tU0, 0, -1, -1, 16, 3, 32, 0},
+    {tU1, 1, tS0, tU0, 32, 32, 96, 1},   {tU0, 0, -1, -1, kPredCh, kKpTaps, 32, 0},
 };
 constexpr int kNumLayers = 14;
 
@@ -76,9 +79,9 @@ struct UNet::Impl {
   bf16* act[kTensors] = {};
   bf16* dact[kTensors] = {};
   bf16* dcat = nullptr;
-  float* pred = nullptr;
+  float* pred = nullptr;     // filter logits [P][kPredCh]
   bf16* dpred = nullptr;
-  float* raw = nullptr;     // staged input [P][10]
+  float* raw = nullptr;     // staged input [P][kRawCh]
   float* target = nullptr;  // staged target [P][3]
   double* loss = nullptr;
 
@@ -122,9 +125,9 @@ struct UNet::Impl {
     size_t ncat = std::max({(size_t)P0 * 96, (size_t)(P0 >> 2) * 160, (size_t)(P0 >> 4) * 224,
                             (size_t)(P0 >> 6) * 288});
     if ((e = cudaMalloc(&dcat, ncat * sizeof(bf16)))) return e;
-    if ((e = cudaMalloc(&pred, (size_t)P0 * 16 * sizeof(float)))) return e;
-    if ((e = cudaMalloc(&dpred, (size_t)P0 * 16 * sizeof(bf16)))) return e;
-    if ((e = cudaMalloc(&raw, (size_t)P0 * 10 * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&pred, (size_t)P0 * kPredCh * sizeof(float)))) return e;
+    if ((e = cudaMalloc(&dpred, (size_t)P0 * kPredCh * sizeof(bf16)))) return e;
+    if ((e = cudaMalloc(&raw, (size_t)P0 * kRawCh * sizeof(float)))) return e;
     if ((e = cudaMalloc(&target, (size_t)P0 * 3 * sizeof(float)))) return e;
     cap = P0;
     return cudaSuccess;
@@ -348,7 +351,7 @@ cudaError_t UNet::train_step(const float* d_raw, const float* d_target, int N, i
   long long P0 = (long long)N * H * W;
   if ((e = forward(d_raw, N, H, W, err, st))) return e;
   if ((e = cudaMemsetAsync(I.loss, 0, sizeof(double), st))) return e;
-  if ((e = l1log_loss(I.pred, d_target, I.dpred, P0, I.loss, st))) return e;
+  if ((e = kp_loss(I.pred, d_raw, d_target, I.dpred, N, H, W, I.loss, st))) return e;
   int fwd = I.launches;
   if ((e = backward(N, H, W, err, st))) return e;
   ++I.step;
@@ -371,7 +374,7 @@ cudaError_t UNet::loss_and_grads(const float* d_raw, const float* d_target, int 
   long long P0 = (long long)N * H * W;
   if ((e = forward(d_raw, N, H, W, err, st))) return e;
   if ((e = cudaMemsetAsync(I.loss, 0, sizeof(double), st))) return e;
-  if ((e = l1log_loss(I.pred, d_target, I.dpred, P0, I.loss, st))) return e;
+  if ((e = kp_loss(I.pred, d_raw, d_target, I.dpred, N, H, W, I.loss, st))) return e;
   int fwd = I.launches;
   if ((e = backward(N, H, W, err, st))) return e;
   I.launches += fwd + 1;
@@ -387,8 +390,9 @@ float* UNet::scratch_target() { return p_->target; }
 const float* UNet::prediction() const { return p_->pred; }
 cudaError_t UNet::reserve(long long P0) { return p_->ensure(P0); }
 
-cudaError_t UNet::decode(float* d_out, long long P0, cudaStream_t st) const {
-  return decode_output(p_->pred, d_out, P0, st);
+cudaError_t UNet::decode(const float* d_raw, float* d_out, int N, int Hc, int Wc, int Hs, int Ws,
+                         cudaStream_t st) const {
+  return kp_apply(p_->pred, d_raw, d_out, N, Hc, Wc, Hs, Ws, st);
 }
 
 }  // namespace nn

@@ -32,23 +32,25 @@ class UNet {
   cudaError_t get_state(float* host_m, float* host_v, cudaStream_t st) const;
   cudaError_t set_state(const float* host_m, const float* host_v, int step, cudaStream_t st);
 
-  // raw [N*H*W][10] = radiance 3, albedo 3, normal 3, depth 1 (FP32)
+  // raw [N*H*W][kRawCh] = radiance 3, albedo 3, normal 3, depth 1, spp 1 (FP32)
   cudaError_t forward(const float* d_raw, int N, int H, int W, int* err, cudaStream_t st);
   // gradients of the loss of the last forward (d_pred set by the loss)
   cudaError_t backward(int N, int H, int W, int* err, cudaStream_t st);
-  // forward + L1-log loss against target [N*H*W][3] + backward (no update)
+  // forward + loss against target [N*H*W][3] + backward (no update)
   cudaError_t loss_and_grads(const float* d_raw, const float* d_target, int N, int H, int W,
                              double* loss, int* err, cudaStream_t st);
   // forward + loss + backward + Adam + BF16 weight refresh
   cudaError_t train_step(const float* d_raw, const float* d_target, int N, int H, int W, float lr,
                          double* loss, int* err, cudaStream_t st);
-  // radiance [P][3] = exp(prediction) - 1 of the last forward
-  cudaError_t decode(float* d_out, long long P, cudaStream_t st) const;
+  // out [N][Hc][Wc][3] = the last forward's predicted filters applied to the
+  // radiance of d_raw (the same input), frames stored as Hs x Ws pixels
+  cudaError_t decode(const float* d_raw, float* d_out, int N, int Hc, int Wc, int Hs, int Ws,
+                     cudaStream_t st) const;
 
   cudaError_t reserve(long long P0);  // activation buffers for P0 pixels
-  float* scratch_raw();               // [P0][10] staging for host inputs
+  float* scratch_raw();               // [P0][kRawCh] staging for host inputs
   float* scratch_target();            // [P0][3]
-  const float* prediction() const;    // [P0][16] FP32, log space
+  const float* prediction() const;    // [P0][kPredCh] FP32 filter logits
 
  private:
   cudaError_t refresh_weights(cudaStream_t st);

@@ -1,11 +1,15 @@
 """The learned denoiser's data, training and evaluation (host side).
 
 Training pairs come from the renderer itself on procedural scenes
-(``scenes.procedural_scene``): the input is a low-spp radiance render plus the
-albedo, normal and depth passes of the same camera (10 channels), the target a
-high-spp render with an independent seed.  Minibatches are gathered on the
-device and stepped through ``Context.dn_train_step`` (forward, backward and
-Adam on the tensor cores).
+(``scenes.procedural_scene``): the input is a radiance render at some spp plus
+the albedo, normal and depth passes of the same camera and that spp (11
+channels), the target a high-spp render with an independent seed.  The pairs
+stay on the device; minibatches of random crops are gathered there and stepped
+through ``Context.dn_train_step`` (forward, backward and Adam on the tensor
+cores).  The network predicts a 5 x 5 filter per pixel that is applied to the
+input radiance, trained on the relative squared error (its minimiser over
+noisy targets is their mean, so the 4,096-spp targets' noise averages out
+instead of biasing the result).
 
 ``study`` measures the denoised form against the plain one at equal accuracy
 on one scene: a high-spp FP32 reference rendered as two independent halves
@@ -15,7 +19,8 @@ network + bloom), their relMSE against the reference and their frame times;
 a frame whose denoised relMSE exceeds that of the plain render of equal time
 falls back to the plain render.
 
-    python -m rendertoy_gb300.denoise train --scenes 256 --steps 2000 --in-spp 1,1024 --out DIR
+    python -m rendertoy_gb300.denoise train --scenes 4000 --steps 20000 --in-spp 4,8192 \
+        --target-spp 4096 --out DIR
     python -m rendertoy_gb300.denoise study --params DIR/params.npy --out DIR
     python -m rendertoy_gb300.denoise step --batch 8 --steps 2   # profiling
 
@@ -74,42 +79,75 @@ def frame_passes(ctx, sc, W, H):
     return a, n, d
 
 
-def network_input(rad, albedo, normal, depth):
-    return np.concatenate([rad, albedo, normal, depth[..., :1]], -1).astype(np.float32)
+def network_input(rad, albedo, normal, depth, spp):
+    """One frame's network input [H][W][11] from its passes (host arrays)."""
+    spp_plane = np.full(rad.shape[:2] + (1,), float(spp), np.float32)
+    return np.concatenate([rad, albedo, normal, depth[..., :1], spp_plane], -1).astype(np.float32)
+
+
+def pair_spp(seed, in_spp):
+    """The input spp of pair `seed`: in_spp itself, or for a range (lo, hi)
+    a log-uniform draw (seeded by the scene) so that one network serves
+    many noise levels."""
+    if isinstance(in_spp, (tuple, list)):
+        lo, hi = np.log(in_spp[0]), np.log(in_spp[1])
+        return int(round(np.exp(np.random.RandomState(int(seed)).uniform(lo, hi))))
+    return int(in_spp)
 
 
 def make_pairs(ctx, seeds, W=256, H=256, in_spp=4, target_spp=1024, max_depth=8,
-               tri_range=(1e3, 2e5), log=print):
+               tri_range=(1e3, 2e5), log=print, device=False):
     """Render (input, target) pairs of the procedural scenes `seeds`:
-    X [n][H][W][10], Y [n][H][W][3].  in_spp: the input's samples per pixel,
-    or a range (lo, hi) from which each pair draws its own, log-uniformly
-    (seeded by the scene), so that one network serves many noise levels."""
-    X = np.zeros((len(seeds), H, W, 10), np.float32)
-    Y = np.zeros((len(seeds), H, W, 3), np.float32)
+    X [n][H][W][11], Y [n][H][W][3] (numpy arrays, or device tensors with
+    device=True: then nothing is copied to the host).  Scene generation for
+    the next scene runs on a host thread while the GPU renders."""
+    import concurrent.futures as cf
+    import torch
+    seeds = [int(s) for s in seeds]
+    dev = torch.device("cuda")
+    X = torch.empty((len(seeds), H, W, 11), dtype=torch.float32, device=dev)
+    Y = torch.empty((len(seeds), H, W, 3), dtype=torch.float32, device=dev)
+    img = [torch.empty((H, W, 3), dtype=torch.float32, device=dev) for _ in range(4)]
     t0 = time.time()
-    for i, s in enumerate(seeds):
-        sc, _ = scenes.procedural_scene(int(s), tri_range=tri_range)
-        ctx.upload(sc)
-        spp = in_spp
-        if isinstance(in_spp, (tuple, list)):
-            lo, hi = np.log(in_spp[0]), np.log(in_spp[1])
-            spp = int(round(np.exp(np.random.RandomState(int(s)).uniform(lo, hi))))
-        rad = ctx.render_pt(W, H, spp, max_depth, seed=2 * int(s) + 1)
-        X[i] = network_input(rad, *frame_passes(ctx, sc, W, H))
-        Y[i] = ctx.render_pt(W, H, target_spp, max_depth, seed=2 * int(s) + 2)
-        if log and (i + 1) % max(1, len(seeds) // 8) == 0:
-            log(f"  pairs {i + 1}/{len(seeds)}  {time.time() - t0:.1f} s")
-    return X, Y
+    spps = []
+    with cf.ThreadPoolExecutor(1) as pool:
+        nxt = pool.submit(scenes.procedural_scene, seeds[0], tri_range=tri_range) if seeds else None
+        for i, s in enumerate(seeds):
+            sc, _ = nxt.result()
+            if i + 1 < len(seeds):
+                nxt = pool.submit(scenes.procedural_scene, seeds[i + 1], tri_range=tri_range)
+            ctx.upload(sc)
+            spp = pair_spp(s, in_spp)
+            spps.append(spp)
+            rad, nrm, alb, dep = img
+            ctx.render_pt(W, H, spp, max_depth, seed=2 * s + 1, out=rad)
+            ctx.aov(W, H, float(sc.camera[19]), float(sc.camera[20]), out=(nrm, alb, dep))
+            ctx.synchronize()
+            X[i, ..., 0:3] = rad
+            X[i, ..., 3:6] = alb
+            X[i, ..., 6:9] = nrm
+            X[i, ..., 9] = dep[..., 0]
+            X[i, ..., 10] = float(spp)
+            torch.cuda.current_stream().synchronize()  # before the next render reuses the buffers
+            ctx.render_pt(W, H, target_spp, max_depth, seed=2 * s + 2, out=Y[i])
+            if log and (i + 1) % max(1, len(seeds) // 8) == 0:
+                log(f"  pairs {i + 1}/{len(seeds)}  {time.time() - t0:.1f} s")
+    torch.cuda.synchronize()
+    if device:
+        return X, Y
+    return X.cpu().numpy(), Y.cpu().numpy()
 
 
-def train(ctx, X, Y, steps, batch=32, crop=256, lr=3e-4, seed=0, log_every=200, log=print):
-    """Adam steps on random crops of random pairs (device-resident data).
-    Returns the per-step minibatch losses and the mean step time (ms)."""
+def train(ctx, X, Y, steps, batch=32, crop=256, lr=3e-4, seed=0, log_every=200, log=print, decay_from=1.0):
+    """Adam steps on random crops of random pairs (device-resident data; X, Y
+    numpy arrays or device tensors).  The learning rate drops to lr / 10 for
+    the steps after `decay_from` x steps.  Returns the per-step minibatch
+    losses and the mean step time (ms)."""
     import torch
     n, H, W = X.shape[:3]
     crop = min(crop, H, W) // 16 * 16
-    Xd = torch.from_numpy(X).cuda()
-    Yd = torch.from_numpy(Y).cuda()
+    Xd = X if hasattr(X, "data_ptr") else torch.from_numpy(X).cuda()
+    Yd = Y if hasattr(Y, "data_ptr") else torch.from_numpy(Y).cuda()
     g = torch.Generator().manual_seed(seed)
     losses, ms = [], []
     for it in range(steps):
@@ -118,7 +156,8 @@ def train(ctx, X, Y, steps, batch=32, crop=256, lr=3e-4, seed=0, log_every=200, 
         x0 = int(torch.randint(0, W - crop + 1, (1,), generator=g))
         xb = Xd[idx, y0:y0 + crop, x0:x0 + crop].contiguous()
         yb = Yd[idx, y0:y0 + crop, x0:x0 + crop].contiguous()
-        losses.append(ctx.dn_train_step(xb, yb, lr=lr))
+        rate = lr if it < decay_from * steps else lr / 10
+        losses.append(ctx.dn_train_step(xb, yb, lr=rate))
         ms.append(ctx.stats()["last_gpu_ms"])
         if log and (it + 1) % log_every == 0:
             log(f"  step {it + 1}/{steps}  loss {np.mean(losses[-log_every:]):.4f}  "
@@ -148,7 +187,8 @@ def _time_to(points, target):
     return None
 
 
-def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 4, 16, 64, 256, 1024, 4096),
+def study(ctx, sc, W, H, ref_spp=16384, max_depth=12,
+          denoise_spp=(1, 4, 16, 64, 256, 1024, 2048, 4096, 8192),
           plain_spp=(1, 4, 16, 64, 256, 1024, 4096), reps=20,
           bloom=(49, 8.0, 1.0), target=1e-3, seed=1, log=print):
     """Denoised vs plain at equal accuracy on one scene (see the module text).
@@ -199,7 +239,7 @@ def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 4, 16, 64,
         def frame():
             ctx.render_pt(W, H, spp, max_depth, seed=seed, out=rad)
             ctx.aov(W, H, near, far, out=(nrm, alb, dep))
-            ctx.denoise(rad, alb, nrm, dep, out=den)
+            ctx.denoise(rad, alb, nrm, dep, spp, out=den)
             if bloom:
                 ctx.bloom(den, *bloom, out=fin)
         t_med, t_99 = timed_reps(frame)
@@ -231,19 +271,24 @@ def study(ctx, sc, W, H, ref_spp=16384, max_depth=12, denoise_spp=(1, 4, 16, 64,
 def _main():
     import rendertoy_gb300 as rt
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train", "study", "step"])
+    ap.add_argument("cmd", choices=["train", "study", "step", "full"],
+                    help="full: render the pairs once, train one network per --subsets size on the first "
+                         "that many scenes, and study each (one process: the pairs never leave the device)")
     ap.add_argument("--out", default="denoise_out")
     ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--subsets", default="", help="with full: scene counts to train on, e.g. 192,1000,4000")
     ap.add_argument("--res", type=int, default=256)
-    ap.add_argument("--target-spp", type=int, default=1024)
-    ap.add_argument("--in-spp", default="4",
+    ap.add_argument("--target-spp", type=int, default=4096)
+    ap.add_argument("--in-spp", default="4,8192",
                     help="input samples per pixel of the training pairs: N, or LO,HI (log-uniform per pair)")
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--lr", type=float, default=3e-4)
+    ap.add_argument("--decay-from", type=float, default=0.9)
     ap.add_argument("--params", default="")
     ap.add_argument("--study-res", default="1920x1080")
     ap.add_argument("--ref-spp", type=int, default=16384)
+    ap.add_argument("--denoise-spp", default="1,4,16,64,256,1024,2048,4096,8192")
     a = ap.parse_args()
     ctx = rt.Context(0)
     ctx.dn_init(0)
@@ -252,7 +297,8 @@ def _main():
     if a.cmd == "step":
         import torch
         g = torch.Generator(device="cuda").manual_seed(0)
-        xb = torch.rand(a.batch, a.res, a.res, 10, device="cuda", generator=g)
+        xb = torch.rand(a.batch, a.res, a.res, 11, device="cuda", generator=g)
+        xb[..., 10] = 64.0
         yb = 2 * torch.rand(a.batch, a.res, a.res, 3, device="cuda", generator=g)
         ms = []
         for _ in range(a.steps):
@@ -261,24 +307,46 @@ def _main():
         print(json.dumps({"batch": a.batch, "res": a.res, "steps": a.steps, "loss": loss, "ms": ms}))
         return
     os.makedirs(a.out, exist_ok=True)
-    if a.cmd == "train":
+    in_spp = tuple(int(v) for v in a.in_spp.split(","))
+    in_spp = in_spp[0] if len(in_spp) == 1 else in_spp
+    W, H = (int(v) for v in a.study_res.split("x"))
+    dspp = tuple(int(v) for v in a.denoise_spp.split(","))
+
+    def run_train(X, Y, n, tag):
+        ctx.dn_init(0)
         t0 = time.time()
-        in_spp = tuple(int(v) for v in a.in_spp.split(","))
-        in_spp = in_spp[0] if len(in_spp) == 1 else in_spp
-        X, Y = make_pairs(ctx, range(a.scenes), W=a.res, H=a.res, in_spp=in_spp, target_spp=a.target_spp)
-        t_data = time.time() - t0
-        losses, ms = train(ctx, X, Y, a.steps, batch=a.batch, lr=a.lr)
-        np.save(os.path.join(a.out, "params.npy"), ctx.dn_get_params())
-        res = {"scenes": a.scenes, "res": a.res, "in_spp": a.in_spp, "target_spp": a.target_spp, "steps": a.steps,
-               "batch": a.batch, "lr": a.lr, "data_s": t_data, "ms_per_step": ms,
-               "loss_first100": float(losses[:100].mean()), "loss_last100": float(losses[-100:].mean())}
-        json.dump(res, open(os.path.join(a.out, "train.json"), "w"), indent=1)
-        print(json.dumps(res))
+        losses, ms = train(ctx, X[:n], Y[:n], a.steps, batch=a.batch, lr=a.lr, decay_from=a.decay_from)
+        np.save(os.path.join(a.out, f"params{tag}.npy"), ctx.dn_get_params())
+        res = {"scenes": n, "res": a.res, "in_spp": a.in_spp, "target_spp": a.target_spp, "steps": a.steps,
+               "batch": a.batch, "lr": a.lr, "decay_from": a.decay_from, "train_s": time.time() - t0,
+               "ms_per_step": ms, "loss_first100": float(losses[:100].mean()),
+               "loss_last100": float(losses[-100:].mean()),
+               "loss_curve": [float(losses[i:i + 500].mean()) for i in range(0, len(losses), 500)]}
+        json.dump(res, open(os.path.join(a.out, f"train{tag}.json"), "w"), indent=1)
+        print(json.dumps({k: v for k, v in res.items() if k != "loss_curve"}), flush=True)
+        return res
+
+    def run_study(tag):
+        res = study(ctx, scenes.displaced_icosphere(), W, H, ref_spp=a.ref_spp, denoise_spp=dspp)
+        json.dump(res, open(os.path.join(a.out, f"study{tag}.json"), "w"), indent=1)
+        print(json.dumps({k: v for k, v in res.items() if k not in ("plain", "denoised")}), flush=True)
+        return res
+
+    if a.cmd in ("train", "full"):
+        t0 = time.time()
+        X, Y = make_pairs(ctx, range(a.scenes), W=a.res, H=a.res, in_spp=in_spp, target_spp=a.target_spp,
+                          device=True)
+        data = {"scenes": a.scenes, "data_s": time.time() - t0}
+        json.dump(data, open(os.path.join(a.out, "data.json"), "w"))
+        print(json.dumps(data), flush=True)
+        subsets = [int(v) for v in a.subsets.split(",")] if (a.cmd == "full" and a.subsets) else [a.scenes]
+        for n in subsets:
+            tag = f"_{n}" if a.cmd == "full" else ""
+            run_train(X, Y, n, tag)
+            if a.cmd == "full":
+                run_study(tag)
     else:
-        W, H = (int(v) for v in a.study_res.split("x"))
-        res = study(ctx, scenes.displaced_icosphere(), W, H, ref_spp=a.ref_spp)
-        json.dump(res, open(os.path.join(a.out, "study.json"), "w"), indent=1)
-        print(json.dumps({k: v for k, v in res.items() if k not in ("plain", "denoised")}))
+        run_study("")
 
 
 if __name__ == "__main__":

@@ -1,9 +1,9 @@
 """What the trained denoiser gains over the method without it.
 
 The network is trained briefly on pairs the renderer generates from
-procedural scenes (4-spp radiance + albedo / normal / depth passes -> 256-spp
-radiance), then run on held-out scenes: its output must be closer to a
-1024-spp render than the 4-spp input it was given (relMSE, eps 1e-2) by at
+procedural scenes (4-spp radiance + albedo / normal / depth passes + spp ->
+256-spp radiance), then run on held-out scenes: its output must be closer to
+a 1024-spp render than the 4-spp input it was given (relMSE, eps 1e-2) by at
 least 2x, and training must lower the loss.
 """
 import numpy as np
@@ -27,7 +27,7 @@ def test_trained_network_beats_its_input(ctx):
         ctx.upload(sc)
         rad = ctx.render_pt(128, 128, 4, 6, seed=7)
         a, n, d = D.frame_passes(ctx, sc, 128, 128)
-        den = ctx.denoise(rad, a, n, d)
+        den = ctx.denoise(rad, a, n, d, 4)
         ref = ctx.render_pt(128, 128, 1024, 6, seed=8)
         e_in, _ = D.relmse(rad, ref)
         # the renders may hold RenderToy's NaN paths (relmse masks them); the

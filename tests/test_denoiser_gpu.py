@@ -108,11 +108,12 @@ def test_conv_weight_gradient(ctx, c):
 
 def _batch(seed, N=2, H=32, W=32):
     rng = np.random.RandomState(seed)
-    raw = np.zeros((N, H, W, 10), np.float32)
+    raw = np.zeros((N, H, W, 11), np.float32)
     raw[..., :3] = rng.exponential(0.6, (N, H, W, 3))
     raw[..., 3:6] = rng.uniform(0, 1, (N, H, W, 3))
     raw[..., 6:9] = rng.uniform(0, 1, (N, H, W, 3))
     raw[..., 9] = rng.uniform(0, 1, (N, H, W))
+    raw[..., 10] = 2.0 ** rng.randint(0, 13)
     target = (raw[..., :3] * rng.uniform(0.5, 1.5, (N, H, W, 3))).astype(np.float32)
     return raw, target
 
@@ -212,40 +213,64 @@ def test_training_reduces_loss(dn):
     first = dn.dn_train_step(raw, target, lr=1e-3)
     for _ in range(60):
         last = dn.dn_train_step(raw, target, lr=1e-3)
-    assert last < 0.7 * first, (first, last)
+    assert last < 0.8 * first, (first, last)
 
 
 def test_inference_matches_oracle(dn):
-    """The prediction against the exact FP64 network: no further from it (RMS
-    over pixels and channels) than twice the BF16-emulating network is.  BF16
-    storage noise compounds over the 14 layers, so the emulation does not
-    track the GPU element for element at the output."""
+    """The denoised radiance against the exact FP64 network: no further from
+    it (RMS over pixels and channels) than twice the BF16-emulating network
+    is.  BF16 storage noise compounds over the 14 layers, so the emulation does
+    not track the GPU element for element at the output."""
     dn.dn_init(41)
     p = _with_biases(dn.dn_get_params(), 16)
     dn.dn_set_params(p)
     raw, _ = _batch(17, N=1, H=48, W=32)
     out = dn.dn_infer(raw)
-    exact = U.UNet(p.astype(np.float64), bf16=False).forward(raw)[..., :3]
-    emu = U.UNet(p.astype(np.float64), bf16=True).forward(raw)[..., :3]
+    exact = U.UNet(p.astype(np.float64), bf16=False).denoise(raw)
+    emu = U.UNet(p.astype(np.float64), bf16=True).denoise(raw)
     rms = lambda x: float(np.sqrt(np.mean(x * x)))  # noqa: E731
-    e_gpu, e_emu = rms(np.log1p(out.astype(np.float64)) - exact), rms(emu - exact)
+    e_gpu, e_emu = rms(out.astype(np.float64) - exact), rms(emu - exact)
     assert e_gpu <= 2.0 * e_emu + 1e-5 * np.abs(exact).max(), (e_gpu, e_emu)
+    # a filtered pixel is a weighted mean of its 5 x 5 input neighbourhood
+    rad = raw[0, ..., :3]
+    assert (out >= 0).all() and (out <= rad.max() * (1 + 1e-5)).all()
 
 
-def test_denoise_frame_pads_and_crops(dn):
-    """A 40 x 24 frame (not multiples of 16) equals inference on the frame
-    zero-padded to 48 x 32, cropped."""
-    rng = np.random.RandomState(18)
-    H, W = 24, 40
+def _frame(rng, H, W):
     rad = rng.exponential(0.5, (H, W, 3)).astype(np.float32)
     alb = rng.uniform(0, 1, (H, W, 3)).astype(np.float32)
     nrm = rng.uniform(0, 1, (H, W, 3)).astype(np.float32)
     dep = np.repeat(rng.uniform(0, 1, (H, W, 1)), 3, axis=2).astype(np.float32)
-    out = dn.denoise(rad, alb, nrm, dep)
-    raw = np.zeros((1, 32, 48, 10), np.float32)
+    return rad, alb, nrm, dep
+
+
+def _raw(rad, alb, nrm, dep, spp, Hp, Wp):
+    H, W = rad.shape[:2]
+    raw = np.zeros((1, Hp, Wp, 11), np.float32)
     raw[0, :H, :W, 0:3], raw[0, :H, :W, 3:6], raw[0, :H, :W, 6:9], raw[0, :H, :W, 9] = rad, alb, nrm, dep[..., 0]
-    ref = dn.dn_infer(raw)[0, :H, :W]
-    assert np.array_equal(out, ref)
+    raw[0, :H, :W, 10] = spp
+    return raw
+
+
+def test_denoise_frame_pads_and_crops(dn):
+    """A frame of multiples of 16 denoises exactly as batch inference does.  A
+    40 x 24 frame is zero-padded to 48 x 32 for the network, so its filters
+    equal those of inference on the padded frame; they are applied to the
+    frame itself (taps clamped to it), so pixels whose 5 x 5 footprint lies
+    inside the frame equal the padded inference exactly, and no output reads
+    the padding (the frame's top-right corner stays within its neighbours)."""
+    rng = np.random.RandomState(18)
+    f = _frame(rng, 32, 48)
+    assert np.array_equal(dn.denoise(*f, 64), dn.dn_infer(_raw(*f, 64, 32, 48))[0])
+    H, W = 24, 40
+    f = _frame(rng, H, W)
+    out = dn.denoise(*f, 64)
+    ref = dn.dn_infer(_raw(*f, 64, 32, 48))[0, :H, :W]
+    assert np.array_equal(out[:H - 2, :W - 2], ref[:H - 2, :W - 2])
+    rad = f[0]
+    corner = rad[H - 3:, W - 3:].reshape(-1, 3)
+    assert (out[H - 1, W - 1] <= corner.max(0) * (1 + 1e-5)).all()
+    assert (out[H - 1, W - 1] >= corner.min(0) * (1 - 1e-5)).all()
 
 
 def test_checkpoint_resume(ctx, dn):

@@ -40,12 +40,39 @@ def test_pool_upsample_loss_adam():
     assert np.allclose(U.avgpool2_grad(r), _fd(lambda: float((U.avgpool2(x) * r).sum()), x))
     r2 = rng.normal(size=(1, 8, 12, 2))
     assert np.allclose(U.upsample2_grad(r2), _fd(lambda: float((U.upsample2(x) * r2).sum()), x))
-    t = np.abs(rng.normal(size=x.shape))
-    val, g = U.l1_log_loss(x, t)
-    assert np.isclose(val, np.abs(x - np.log1p(t)).mean())
-    assert np.allclose(g, _fd(lambda: U.l1_log_loss(x, t)[0], x), atol=1e-6)
     p, m, v = U.adam(np.ones(3), np.array([1.0, -2.0, 0.0]), np.zeros(3), np.zeros(3), 1)
     assert np.allclose(p, [1 - 3e-4, 1 + 3e-4, 1.0])
+
+
+def test_kernel_predicting_loss():
+    """The filtered radiance is a convex combination of the 5 x 5 taps
+    (clamped at the frame's edge); the loss gradient with respect to the
+    logits matches central differences of the loss with its denominator held
+    at the base point's output; NaN / infinite radiance is made safe."""
+    rng = np.random.RandomState(2)
+    logits = rng.normal(size=(2, 6, 5, 32))
+    raw = rng.uniform(0, 2, (2, 6, 5, 11))
+    raw[0, 0, 0, 0] = np.nan
+    raw[1, 2, 3, 1] = np.inf
+    t = rng.uniform(0, 2, (2, 6, 5, 3))
+    o = U.kp_apply(logits, raw)
+    assert np.isfinite(o).all()
+    rad = U.sane(raw[..., :3])
+    assert (o <= rad.max() + 1e-9).all() and (o >= 0).all()
+    # a filter that puts all weight on the centre tap returns the input
+    centre = np.full((2, 6, 5, 32), -60.0)
+    centre[..., 12] = 60.0
+    assert np.allclose(U.kp_apply(centre, raw), rad)
+    # the corner pixel's up-left tap is clamped onto the corner itself
+    corner = np.full((2, 6, 5, 32), -60.0)
+    corner[..., 0] = 60.0
+    assert np.allclose(U.kp_apply(corner, raw)[:, 0, 0], rad[:, 0, 0])
+    loss, g = U.kp_loss(logits, raw, t)
+    den = o * o + U.REL_EPS
+    assert np.isclose(loss, ((o - t) ** 2 / den).mean())
+    assert (g[..., 25:] == 0).all()
+    fd = _fd(lambda: float(((U.kp_apply(logits, raw) - t) ** 2 / den).mean()), logits)
+    assert np.allclose(g, fd, atol=1e-9)
 
 
 def test_bf16_rounding_is_nearest_even():
@@ -69,27 +96,33 @@ def test_layer_table_layout():
         end = r["b_off"] + r["cout_pad"]
     assert end <= n
     # 32 / 64 / 96 / 128 / 160 channels, about 1.3M parameters
-    assert [r["cout"] for r in rows] == [32, 32, 64, 64, 96, 96, 128, 128, 160, 128, 96, 64, 32, 3]
+    assert [r["cout"] for r in rows] == [32, 32, 64, 64, 96, 96, 128, 128, 160, 128, 96, 64, 32, 25]
+    assert rows[0]["cin"] == 11 and rows[-1]["cout_pad"] == 32
     assert 1.2e6 < U.real_param_count() < 1.4e6
 
 
 def test_network_gradients_match_finite_differences():
-    """The whole U-Net (FP64, no rounding): the analytic gradient of the L1-log
-    loss against central differences, for weights and biases of every layer."""
+    """The whole U-Net (FP64, no rounding): the analytic gradient of the
+    relative squared error of the filtered radiance (its denominator held at
+    the base point's output) against central differences, for weights and
+    biases of every layer."""
     rng = np.random.RandomState(3)
     p = U.init_params(5)
     rows, _ = U.layer_table()
     for r in rows:  # non-zero biases so that every bias gradient is exercised
         p[r["b_off"]:r["b_off"] + r["cout"]] = rng.normal(0, 0.05, r["cout"])
-    raw = rng.uniform(0, 1, (1, 16, 16, 10))
+    raw = rng.uniform(0, 1, (1, 16, 16, 11))
     raw[..., :3] *= 4.0
+    raw[..., 10] = 16.0
     target = rng.uniform(0, 3, (1, 16, 16, 3))
     net = U.UNet(p)
     loss, g = net.loss_and_grads(raw, target)
     assert np.isfinite(loss)
+    o0 = U.UNet(p).denoise(raw)
+    den = o0 * o0 + U.REL_EPS
 
     def f():
-        return np.abs(U.UNet(p).forward(raw)[..., :3] - np.log1p(target)).mean()
+        return (((U.UNet(p).denoise(raw) - target) ** 2) / den).mean()
 
     picks = []
     for r in rows:
