@@ -106,12 +106,20 @@ enum rtx_option {
                                  rays by origin cell and direction octant
                                  before they are traced (results unchanged;
                                  only the visiting order) */
-  RTX_OPT_STACK_LIMIT = 14    /* traversal stack entries a ray may use, 2..64
+  RTX_OPT_STACK_LIMIT = 14,   /* traversal stack entries a ray may use, 2..64
                                  (default 64, the whole stack).  A ray that
                                  needs more stops, and the call returns
                                  RTX_ERR_DEVICE "traversal stack overflow".
                                  Lower values exist to exercise that error
                                  path; results are undefined after it. */
+  RTX_OPT_COMPOSITOR_FMA = 15 /* 0/1 (default 0): the 3 x 3 and 5 x 5
+                                 convolutions and the separable Gaussian /
+                                 bloom passes fuse each tap's multiply and
+                                 add (one rounding instead of two).  Results
+                                 then differ from RenderToy's by at most
+                                 ~1e-5 of the sum of the taps' magnitudes;
+                                 0 keeps them bit-exact.  Other kernel shapes
+                                 are always computed unfused. */
 };
 
 typedef struct rtx_context rtx_context;

@@ -87,6 +87,7 @@ struct rtx_context {
   int traversal = 2;
   int min_busy = 20;
   int stack_limit = kStackSize;
+  bool compositor_fma = false;
   KernelTimer timer;
   // scene
   bool has_scene = false;
@@ -422,6 +423,7 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
       if (v < 0 || v > 32) return fail(c, RTX_ERR_INVALID, "min busy lanes must be in [0, 32]");
       c->min_busy = (int)v;
       return RTX_OK;
+    case RTX_OPT_COMPOSITOR_FMA: c->compositor_fma = v != 0; return RTX_OK;
     case RTX_OPT_STACK_LIMIT:
       if (v < 2 || v > kStackSize) return fail(c, RTX_ERR_INVALID, "stack limit must be in [2, 64]");
       c->stack_limit = (int)v;
@@ -449,6 +451,7 @@ int rtx_get_option(rtx_context* c, int option, int64_t* v) {
     case RTX_OPT_TRAVERSAL: *v = c->traversal; return RTX_OK;
     case RTX_OPT_MIN_BUSY: *v = c->min_busy; return RTX_OK;
     case RTX_OPT_STACK_LIMIT: *v = c->stack_limit; return RTX_OK;
+    case RTX_OPT_COMPOSITOR_FMA: *v = c->compositor_fma; return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -1533,7 +1536,8 @@ int rtx_image_convolve(rtx_context* c, const float* in, float* out, int W, int H
   int flags = (absval ? 1 : 0) | (length ? 2 : 0) | (normalize ? 4 : 0);
   int launches = 0;
   cudaError_t e = launch_convolve((const float*)ai.dev, (float*)ao.dev, W, H,
-                                  (const float*)c->weights.p, kr, kc, flags, c->stream, &launches);
+                                  (const float*)c->weights.p, kr, kc, flags, c->compositor_fma, c->stream,
+                                  &launches);
   c->stats.kernel_launches = launches;
   if (e != cudaSuccess) return cuda_fail(c, e, "convolve kernel");
   if ((r = copy_back(c, ao))) return r;
@@ -1559,7 +1563,7 @@ static int gaussian_common(rtx_context* c, const float* in, float* out, int W, i
   cudaError_t e = launch_gaussian((const float*)ai.dev, (float*)c->stage[2].p,
                                   bloom ? (float*)c->stage[3].p : nullptr, (float*)ao.dev, W, H,
                                   (const float*)c->weights.p, size, bloom ? 1 : 0, threshold,
-                                  c->stream, &launches);
+                                  c->compositor_fma, c->stream, &launches);
   c->stats.kernel_launches = launches;
   if (e != cudaSuccess) return cuda_fail(c, e, "gaussian kernels");
   if ((r = copy_back(c, ao))) return r;

@@ -134,6 +134,17 @@ __global__ void __launch_bounds__(kConvTX * kConvTY) k_convolve_tiled(const floa
 // (unknown to the compiler): that rounds p * w once, as a multiply does
 // (x + -0 == x, also for x = +0 and -0), and leaves nothing to contract.
 RTX_DEV f2_t f2_mul_add(f2_t acc, f2_t p, f2_t w, f2_t nz) { return f2_add(acc, f2_fma(p, w, nz)); }
+// One tap into an accumulator pair: RenderToy's rounding (kFma = false) or one
+// fused multiply-add per tap (kFma = true: RTX_OPT_COMPOSITOR_FMA), which
+// halves the FP32 work of the register-blocked filters.
+template <bool kFma>
+RTX_DEV f2_t f2_tap(f2_t acc, f2_t p, f2_t w, f2_t nz) {
+  return kFma ? f2_fma(p, w, acc) : f2_mul_add(acc, p, w, nz);
+}
+template <bool kFma>
+RTX_DEV float f_tap(float acc, float p, float w) {
+  return kFma ? __fmaf_rn(p, w, acc) : acc + p * w;
+}
 RTX_DEV float f3c(F3 p, int c) { return c == 0 ? p.x : (c == 1 ? p.y : p.z); }
 
 // Small 2-D kernels (3 x 3, 5 x 5), register-blocked: a thread computes
@@ -144,7 +155,7 @@ RTX_DEV float f3c(F3 p, int c) { return c == 0 ? p.x : (c == 1 ? p.y : p.z); }
 constexpr int kConvR = 4, kConvRegThreads = 256, kConvRegW = 32,
               kConvRegH = (kConvRegThreads / kConvRegW) * kConvR;
 
-template <int KR, int KC>
+template <int KR, int KC, bool kFma>
 __global__ void __launch_bounds__(kConvRegThreads, 4) k_convolve_reg(const float* __restrict__ in,
                                                                   float* __restrict__ out, int W, int H,
                                                                   const float* __restrict__ k, int flags,
@@ -185,14 +196,14 @@ __global__ void __launch_bounds__(kConvRegThreads, 4) k_convolve_reg(const float
         if (v0 && v1) {
           const f2_t ww = f2_pack(wk[i0 * KC + jj], wk[i1 * KC + jj]);
 #pragma unroll
-          for (int c = 0; c < 3; ++c) acc[c][q] = f2_mul_add(acc[c][q], pp[c], ww, nz);
+          for (int c = 0; c < 3; ++c) acc[c][q] = f2_tap<kFma>(acc[c][q], pp[c], ww, nz);
         } else if (v0 || v1) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             float a, b;
             f2_unpack(acc[c][q], a, b);
-            if (v0) a = a + f3c(p, c) * wk[i0 * KC + jj];
-            if (v1) b = b + f3c(p, c) * wk[i1 * KC + jj];
+            if (v0) a = f_tap<kFma>(a, f3c(p, c), wk[i0 * KC + jj]);
+            if (v1) b = f_tap<kFma>(b, f3c(p, c), wk[i1 * KC + jj]);
             acc[c][q] = f2_pack(a, b);
           }
         }
@@ -240,7 +251,7 @@ struct SepAcc {
 
 // Add window pixels j0 .. j0 + kSepR - 1 into the accumulators.  kAll: every
 // (pixel, output) pair of the chunk is a tap (no range test, no early exit).
-template <bool kAll, class Px>
+template <bool kAll, bool kFma, class Px>
 RTX_DEV void sep_chunk(SepAcc& A, const float* __restrict__ wsm, int size, int j0, int nj, f2_t nz, Px px) {
   float wv[2 * kSepR - 1];  // wv[k]: weight of tap j0 - (kSepR - 1) + k
 #pragma unroll
@@ -265,15 +276,15 @@ RTX_DEV void sep_chunk(SepAcc& A, const float* __restrict__ wsm, int size, int j
       const bool v1 = kAll || (j - o1 >= 0 && j - o1 < size);
       if (v0 && v1) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) A.v[c][q] = f2_mul_add(A.v[c][q], pp[c], wp[k0], nz);
+        for (int c = 0; c < 3; ++c) A.v[c][q] = f2_tap<kFma>(A.v[c][q], pp[c], wp[k0], nz);
       } else if (v0 || v1) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           float a, b;
           f2_unpack(A.v[c][q], a, b);
           const float pc = f3c(p, c);
-          if (v0) a = a + pc * wv[k0];
-          if (v1) b = b + pc * wv[k0 - 1];
+          if (v0) a = f_tap<kFma>(a, pc, wv[k0]);
+          if (v1) b = f_tap<kFma>(b, pc, wv[k0 - 1]);
           A.v[c][q] = f2_pack(a, b);
         }
       }
@@ -281,7 +292,7 @@ RTX_DEV void sep_chunk(SepAcc& A, const float* __restrict__ wsm, int size, int j
   }
 }
 
-template <class Px>
+template <bool kFma, class Px>
 RTX_DEV void sep_window(SepAcc& A, const float* __restrict__ wsm, int size, float negzero, Px px) {
   const f2_t nz = f2_pack(negzero, negzero);
 #pragma unroll
@@ -291,9 +302,9 @@ RTX_DEV void sep_window(SepAcc& A, const float* __restrict__ wsm, int size, floa
   const int nj = size + kSepR - 1;
   for (int j0 = 0; j0 < nj; j0 += kSepR) {
     if (j0 >= kSepR - 1 && j0 + kSepR - 1 < size)
-      sep_chunk<true>(A, wsm, size, j0, nj, nz, px);
+      sep_chunk<true, kFma>(A, wsm, size, j0, nj, nz, px);
     else
-      sep_chunk<false>(A, wsm, size, j0, nj, nz, px);
+      sep_chunk<false, kFma>(A, wsm, size, j0, nj, nz, px);
   }
 }
 
@@ -304,6 +315,7 @@ RTX_DEV void sep_window(SepAcc& A, const float* __restrict__ wsm, int size, floa
 constexpr int kRowThreads = 128, kRowTile = kRowThreads * kSepR;
 RTX_DEV int row_slot(int i) { return 3 * (i + i / kSepR); }
 
+template <bool kFma>
 __global__ void __launch_bounds__(kRowThreads, 8) k_gauss_x(const float* __restrict__ in,
                                                          float* __restrict__ out, int W, int H,
                                                          const float* __restrict__ w, int size,
@@ -331,7 +343,7 @@ __global__ void __launch_bounds__(kRowThreads, 8) k_gauss_x(const float* __restr
   SepAcc acc;
   const int b = kSepR * tid;
   if (b < n_out) {
-    sep_window(acc, wsm, size, negzero, [&](int j) {
+    sep_window<kFma>(acc, wsm, size, negzero, [&](int j) {
       const float* s = tile + row_slot(b + j);
       return f3(s[0], s[1], s[2]);
     });
@@ -360,6 +372,7 @@ __global__ void __launch_bounds__(kRowThreads, 8) k_gauss_x(const float* __restr
 // from a shared-memory strip of kColH + size - 1 rows.
 constexpr int kColW = 32, kColThreads = 128, kColH = (kColThreads / kColW) * kSepR;
 
+template <bool kFma>
 __global__ void __launch_bounds__(kColThreads, 7) k_gauss_y(const float* __restrict__ in,
                                                          const float* __restrict__ orig,
                                                          float* __restrict__ out, int W, int H,
@@ -382,7 +395,7 @@ __global__ void __launch_bounds__(kColThreads, 7) k_gauss_y(const float* __restr
   const int x = x0 + cc, yb = y0 + kSepR * g;
   if (x >= W || yb >= H) return;
   SepAcc acc;
-  sep_window(acc, wsm, size, negzero, [&](int j) {
+  sep_window<kFma>(acc, wsm, size, negzero, [&](int j) {
     const float* s = strip + 3 * ((kSepR * g + j) * kColW + cc);
     return f3(s[0], s[1], s[2]);
   });
@@ -442,13 +455,19 @@ __global__ void k_add(const float* __restrict__ a, const float* __restrict__ b,
 }
 
 cudaError_t launch_convolve(const float* in, float* out, int W, int H, const float* d_k, int kr,
-                            int kc, int flags, cudaStream_t st, int* launches) {
+                            int kc, int flags, bool fma, cudaStream_t st, int* launches) {
   const size_t smem = sizeof(float) * ((size_t)kr * kc + 3 * (size_t)(kConvTY + kr - 1) * (kConvTX + kc - 1));
   const dim3 rgrid((W + kConvRegW - 1) / kConvRegW, (H + kConvRegH - 1) / kConvRegH);
   if (kr == 5 && kc == 5) {
-    k_convolve_reg<5, 5><<<rgrid, kConvRegThreads, 0, st>>>(in, out, W, H, d_k, flags, -0.0f);
+    if (fma)
+      k_convolve_reg<5, 5, true><<<rgrid, kConvRegThreads, 0, st>>>(in, out, W, H, d_k, flags, -0.0f);
+    else
+      k_convolve_reg<5, 5, false><<<rgrid, kConvRegThreads, 0, st>>>(in, out, W, H, d_k, flags, -0.0f);
   } else if (kr == 3 && kc == 3) {
-    k_convolve_reg<3, 3><<<rgrid, kConvRegThreads, 0, st>>>(in, out, W, H, d_k, flags, -0.0f);
+    if (fma)
+      k_convolve_reg<3, 3, true><<<rgrid, kConvRegThreads, 0, st>>>(in, out, W, H, d_k, flags, -0.0f);
+    else
+      k_convolve_reg<3, 3, false><<<rgrid, kConvRegThreads, 0, st>>>(in, out, W, H, d_k, flags, -0.0f);
   } else if (smem <= 48 * 1024) {
     dim3 grid((W + kConvTX - 1) / kConvTX, (H + kConvTY - 1) / kConvTY);
     k_convolve_tiled<<<grid, kConvTX * kConvTY, smem, st>>>(in, out, W, H, d_k, kr, kc, flags);
@@ -474,7 +493,7 @@ static size_t smem_y(int size) {
 // extraction and the final addition as separate elementwise passes (tmp2 is
 // then required).
 cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out, int W, int H,
-                            const float* d_w, int size, int extract_mode, float threshold,
+                            const float* d_w, int size, int extract_mode, float threshold, bool fma,
                             cudaStream_t st, int* launches) {
   cudaError_t e;
   size_t sx = smem_x(size), sy = smem_y(size);
@@ -490,20 +509,20 @@ cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out
     return cudaGetLastError();
   }
   if (sx <= kMaxSmem) {
-    if (sx > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(k_gauss_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
+    auto kx = fma ? k_gauss_x<true> : k_gauss_x<false>;
+    if (sx > 48 * 1024 && (e = cudaFuncSetAttribute(kx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sx)))
       return e;
-    k_gauss_x<<<dim3((W + kRowTile - 1) / kRowTile, H), kRowThreads, sx, st>>>(in, tmp, W, H, d_w, size,
-                                                                              extract_mode, threshold, -0.0f);
+    kx<<<dim3((W + kRowTile - 1) / kRowTile, H), kRowThreads, sx, st>>>(in, tmp, W, H, d_w, size, extract_mode,
+                                                                       threshold, -0.0f);
   } else {
     k_convolve<<<dim3((W + 127) / 128, H), 128, 0, st>>>(in, tmp, W, H, d_w, 1, size, 0);
   }
   ++*launches;
   if (sy <= kMaxSmem) {
-    if (sy > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(k_gauss_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy)))
+    auto ky = fma ? k_gauss_y<true> : k_gauss_y<false>;
+    if (sy > 48 * 1024 && (e = cudaFuncSetAttribute(ky, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sy)))
       return e;
-    k_gauss_y<<<dim3((W + kColW - 1) / kColW, (H + kColH - 1) / kColH), kColThreads, sy, st>>>(
+    ky<<<dim3((W + kColW - 1) / kColW, (H + kColH - 1) / kColH), kColThreads, sy, st>>>(
         tmp, extract_mode ? in : nullptr, out, W, H, d_w, size, -0.0f);
   } else {
     k_convolve<<<dim3((W + 127) / 128, H), 128, 0, st>>>(tmp, out, W, H, d_w, size, 1, 0);

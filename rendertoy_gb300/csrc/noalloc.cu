@@ -133,7 +133,7 @@ extern "C" int rtx_image_gaussian_blur_noalloc(const float* d_in, float* d_out, 
   int launches = 0;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
-    e = launch_gaussian(d_in, img, nullptr, d_out, W, H, wts, size, 0, 0.0f, st, &launches);
+    e = launch_gaussian(d_in, img, nullptr, d_out, W, H, wts, size, 0, 0.0f, false, st, &launches);
   if (e != cudaSuccess) {
     set_msg(msg, msg_len, cudaGetErrorString(e));
     return RTX_ERR_CUDA;

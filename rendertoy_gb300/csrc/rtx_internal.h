@@ -186,10 +186,13 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
                       int* vertex_launches, std::string* why);
 
 cudaError_t launch_resolve(const float* in, int W, int H, const Resolve& r, cudaStream_t st);
+// fma: each tap's multiply-add fused (RTX_OPT_COMPOSITOR_FMA) in the
+// register-blocked kernels (3 x 3, 5 x 5, separable passes); false keeps the
+// reference's separately rounded multiply and add
 cudaError_t launch_convolve(const float* in, float* out, int W, int H, const float* d_k,
-                            int kr, int kc, int flags, cudaStream_t st, int* launches);
+                            int kr, int kc, int flags, bool fma, cudaStream_t st, int* launches);
 cudaError_t launch_gaussian(const float* in, float* tmp, float* tmp2, float* out, int W, int H,
-                            const float* d_w, int size, int extract_mode, float threshold,
+                            const float* d_w, int size, int extract_mode, float threshold, bool fma,
                             cudaStream_t st, int* launches);
 cudaError_t launch_edge(const float* in, float* out, int W, int H, cudaStream_t st,
                         int* launches);

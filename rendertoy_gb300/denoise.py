@@ -190,20 +190,25 @@ def _time_to(points, target):
 def study(ctx, sc, W, H, ref_spp=16384, max_depth=12,
           denoise_spp=(1, 4, 16, 64, 256, 1024, 2048, 4096, 8192),
           plain_spp=(1, 4, 16, 64, 256, 1024, 4096), reps=20,
-          bloom=(49, 8.0, 1.0), target=1e-3, seed=1, log=print):
+          bloom=(49, 8.0, 1.0), target=1e-3, seed=1, log=print, cache=None):
     """Denoised vs plain at equal accuracy on one scene (see the module text).
     The reference is two renders of ref_spp / 2 samples with independent
     random streams; errors are reported raw and with the reference's own
     noise removed (relmse_corrected), and times to the target use the
     corrected errors.  Times are device-synchronised wall times of the whole
     frame, its buffers resident on the device (median of `reps` runs for
-    frames under a second, of 3 above)."""
+    frames under a second, of 3 above).  `cache` (a dict) keeps the reference
+    and the plain sweep for later studies of other networks on the same
+    scene and settings."""
     ctx.upload(sc)
-    t0 = time.time()
+    cache = {} if cache is None else cache
     half = ref_spp // 2
-    ref_a = ctx.render_pt(W, H, half, max_depth, seed=10_000 + seed)
-    ref_b = ctx.render_pt(W, H, half, max_depth, seed=20_000 + seed)
-    log(f"  reference 2 x {half} spp: {time.time() - t0:.1f} s")
+    if "ref" not in cache:
+        t0 = time.time()
+        cache["ref"] = (ctx.render_pt(W, H, half, max_depth, seed=10_000 + seed),
+                        ctx.render_pt(W, H, half, max_depth, seed=20_000 + seed))
+        log(f"  reference 2 x {half} spp: {time.time() - t0:.1f} s")
+    ref_a, ref_b = cache["ref"]
     out = {"scene": sc.name, "W": W, "H": H, "ref_spp": 2 * half, "max_depth": max_depth, "eps": EPS,
            "target_relmse": target, "plain": [], "denoised": []}
     import torch
@@ -218,12 +223,15 @@ def study(ctx, sc, W, H, ref_spp=16384, max_depth=12,
         return float(np.median(times)), float(np.percentile(times, 99))
 
     # plain: relMSE and frame time per spp (device-resident frame)
-    for spp in plain_spp:
-        ms, _ = timed_reps(lambda: ctx.render_pt(W, H, spp, max_depth, seed=seed, out=img))
-        raw, corr, noise, bad = relmse_corrected(img.cpu().numpy(), ref_a, ref_b)
-        out["plain"].append({"spp": spp, "ms": ms, "relmse_raw": raw, "relmse": corr, "nan_px": bad})
-        log(f"  plain {spp:5d} spp  {ms:9.2f} ms  relMSE {corr:.3e} (raw {raw:.3e})")
-    out["ref_noise_relmse"] = noise
+    if "plain" not in cache:
+        plain = []
+        for spp in plain_spp:
+            ms, p99 = timed_reps(lambda: ctx.render_pt(W, H, spp, max_depth, seed=seed, out=img))
+            raw, corr, noise, bad = relmse_corrected(img.cpu().numpy(), ref_a, ref_b)
+            plain.append({"spp": spp, "ms": ms, "ms_p99": p99, "relmse_raw": raw, "relmse": corr, "nan_px": bad})
+            log(f"  plain {spp:5d} spp  {ms:9.2f} ms  relMSE {corr:.3e} (raw {raw:.3e})")
+        cache["plain"] = (plain, noise)
+    out["plain"], out["ref_noise_relmse"] = cache["plain"]
     # plain relMSE ~ c / spp (Monte Carlo): fitted on the corrected errors
     p = out["plain"]
     fit = [q for q in p if q["spp"] >= 16 and q["relmse"] > 0]
@@ -326,8 +334,11 @@ def _main():
         print(json.dumps({k: v for k, v in res.items() if k != "loss_curve"}), flush=True)
         return res
 
+    study_cache = {}
+    icosphere = scenes.displaced_icosphere()
+
     def run_study(tag):
-        res = study(ctx, scenes.displaced_icosphere(), W, H, ref_spp=a.ref_spp, denoise_spp=dspp)
+        res = study(ctx, icosphere, W, H, ref_spp=a.ref_spp, denoise_spp=dspp, cache=study_cache)
         json.dump(res, open(os.path.join(a.out, f"study{tag}.json"), "w"), indent=1)
         print(json.dumps({k: v for k, v in res.items() if k not in ("plain", "denoised")}), flush=True)
         return res
