@@ -618,6 +618,26 @@ def main():
 
     clocks = clk.summary()
     clk_mhz = clocks["sm_mhz"] or 2070.0  # unsampled: the GB300's maximum SM clock
+
+    # Per-kernel launch times for the rooflines come from frames with the
+    # occlusion launches serialised (RTX_OPT_OVERLAP = 0): in the timed frames
+    # above a vertex's occlusion launch shares the GPU with the next vertex's
+    # closest-hit launch, so each one's event-to-event time includes the other.
+    kt_overlapped = kt
+    serial_frames = max(1, min(args.steps, 5))
+    kt = {k: 0.0 for k in kt_overlapped}
+    serial_ms = []
+    ctx.set_option(rt.OPT_OVERLAP, 0)
+    for i in range(serial_frames):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.render_pt(RES, RES, SPP, DEPTH, seed=seed + 1000 * i, out=img)
+        ctx.synchronize()
+        s = ctx.stats()
+        serial_ms.append(s["last_gpu_ms"])
+        for k in kt:
+            kt[k] += s[k] * args.steps / serial_frames  # scaled to the timed frames' count
+    ctx.set_option(rt.OPT_OVERLAP, 1)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
 
     # instrumented run (untimed): node visits and triangle tests per frame
@@ -648,10 +668,14 @@ def main():
         traffic = (fit.get("dram_bytes_per_launch_fixed", 0.0) +
                    fit["dram_bytes_per_extension_ray"] * cs["extension_rays"] / per_frame["extend_launches"])
     roof.update({"kernel": "k_extend", "traffic": traffic,
+                 "launch_times": f"{serial_frames} frames with the occlusion launches serialised "
+                                 "(RTX_OPT_OVERLAP=0); the timed frames overlap them",
+                 "overlapped_avg_launch_ms": kt_overlapped["extend_ms"] / kt_overlapped["extend_launches"],
                  "extend_share_of_step": kt["extend_ms"] / sum(step_ms),
                  "per_extension_ray": {"node_visits": cs["ext_node_visits"] / cs["extension_rays"],
                                        "tri_tests": cs["ext_tri_tests"] / cs["extension_rays"]}})
     roof_con.update({"kernel": "k_connect", "traffic": None,
+                     "overlapped_avg_launch_ms": kt_overlapped["connect_ms"] / kt_overlapped["connect_launches"],
                      "connect_share_of_step": kt["connect_ms"] / sum(step_ms),
                      "per_shadow_ray": {"node_visits": cs["shadow_node_visits"] / cs["shadow_rays"],
                                         "tri_tests": cs["shadow_tri_tests"] / cs["shadow_rays"]}})
@@ -724,6 +748,10 @@ def main():
                        "bvh_build_ms": st0["bvh_build_ms"], "bvh_nodes": st0["bvh_nodes"],
                        "scene_gen_s": round(gen_s, 2), "options": opts},
             "mrays_per_s": mrays,
+            "overlap": {"step_ms": total_ms / args.steps,
+                        "render_ms_serialised": float(np.median(serial_ms)),
+                        "note": "RTX_OPT_OVERLAP: each vertex's occlusion launch on a second stream beside "
+                                "the next vertex's closest-hit launch (timed frames); serialised for comparison"},
             "rays_per_step": {"extension": rays_e / args.steps, "shadow": rays_s / args.steps},
             "e2e": e2e,
             "roofline": roof,

@@ -112,7 +112,7 @@ enum rtx_option {
                                  RTX_ERR_DEVICE "traversal stack overflow".
                                  Lower values exist to exercise that error
                                  path; results are undefined after it. */
-  RTX_OPT_COMPOSITOR_FMA = 15 /* 0/1 (default 0): the 3 x 3 and 5 x 5
+  RTX_OPT_COMPOSITOR_FMA = 15,/* 0/1 (default 0): the 3 x 3 and 5 x 5
                                  convolutions and the separable Gaussian /
                                  bloom passes fuse each tap's multiply and
                                  add (one rounding instead of two).  Results
@@ -120,6 +120,12 @@ enum rtx_option {
                                  ~1e-5 of the sum of the taps' magnitudes;
                                  0 keeps them bit-exact.  Other kernel shapes
                                  are always computed unfused. */
+  RTX_OPT_OVERLAP = 16        /* 0/1 (default 1): each path vertex's shadow-ray
+                                 sort and occlusion launch run on a second
+                                 stream beside the next vertex's ray sort and
+                                 closest-hit launch (they share no data), so
+                                 one fills the other's idle tail; shading
+                                 waits for both.  Results are unchanged. */
 };
 
 typedef struct rtx_context rtx_context;

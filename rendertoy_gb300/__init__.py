@@ -22,6 +22,7 @@ OPT_GRAPH = 12
 OPT_SORT_RAYS = 13
 OPT_STACK_LIMIT = 14
 OPT_COMPOSITOR_FMA = 15
+OPT_OVERLAP = 16
 OPT_ASYNC, OPT_WAVE_PATHS, OPT_BLOCK, OPT_SORT_MATERIAL, OPT_COUNT_VISITS, OPT_LEAF_SIZE, \
     OPT_PRIMARY_CACHE, OPT_KERNEL_TIMING, OPT_ACCUMULATE, OPT_TRAVERSAL, OPT_MIN_BUSY = \
     1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11

@@ -88,6 +88,7 @@ struct rtx_context {
   int min_busy = 20;
   int stack_limit = kStackSize;
   bool compositor_fma = false;
+  bool overlap = true;
   KernelTimer timer;
   // scene
   bool has_scene = false;
@@ -424,6 +425,7 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
       c->min_busy = (int)v;
       return RTX_OK;
     case RTX_OPT_COMPOSITOR_FMA: c->compositor_fma = v != 0; return RTX_OK;
+    case RTX_OPT_OVERLAP: c->overlap = v != 0; return RTX_OK;
     case RTX_OPT_STACK_LIMIT:
       if (v < 2 || v > kStackSize) return fail(c, RTX_ERR_INVALID, "stack limit must be in [2, 64]");
       c->stack_limit = (int)v;
@@ -452,6 +454,7 @@ int rtx_get_option(rtx_context* c, int option, int64_t* v) {
     case RTX_OPT_MIN_BUSY: *v = c->min_busy; return RTX_OK;
     case RTX_OPT_STACK_LIMIT: *v = c->stack_limit; return RTX_OK;
     case RTX_OPT_COMPOSITOR_FMA: *v = c->compositor_fma; return RTX_OK;
+    case RTX_OPT_OVERLAP: *v = c->overlap; return RTX_OK;
   }
   return fail(c, RTX_ERR_INVALID, "unknown option");
 }
@@ -948,6 +951,7 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   p.primary_cache = c->primary_cache;
   p.sort_material = c->sort_material;
   p.sort_rays = c->sort_rays;
+  p.overlap = c->overlap;
   p.traversal = c->traversal;
   p.min_busy = c->min_busy;
   RTX_CUDA(cudaMemsetAsync(c->d_counters, 0, sizeof(Counters), c->stream), "reset counters");
@@ -1056,6 +1060,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   p.primary_cache = c->primary_cache;
   p.sort_material = c->sort_material;
   p.sort_rays = c->sort_rays;
+  p.overlap = c->overlap;
   p.traversal = c->traversal;
   p.min_busy = c->min_busy;
   p.accumulate = c->accumulate;

@@ -47,7 +47,7 @@ constexpr int kMaxSortBins = 4096;
 #endif
 // path state 6 x 16 B + shadow record 4 x 16 B + six 4-byte entries (two
 // queues, the material order, the ray order, the ray keys, the shadow order)
-constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 6 * 4;
+constexpr size_t kPathBytes = 6 * 16 + 4 * 16 + 7 * 4;
 
 struct PtWorkspace {
   size_t cap = 0;
@@ -61,6 +61,13 @@ struct PtWorkspace {
   int* keys = nullptr;        // ray keys of the extension queue / shadow records
   int* shadow_order = nullptr;  // shadow records ordered by ray key
   int* mat_hist = nullptr;  // kMaxSortBins + 1 bins: counts, then write offsets
+  // The occlusion launch of a vertex runs on `side`, beside the next vertex's
+  // ray sort and closest-hit launch (RTX_OPT_OVERLAP): its shadow-ray sort
+  // has its own keys and histogram, and two events order the streams.
+  int* keys2 = nullptr;
+  int* mat_hist2 = nullptr;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_shaded = nullptr, ev_connected = nullptr;
   float4* shadow = nullptr;
   int* counters = nullptr;  // counts[64] | shadow_counts[64] | work[2 * 64]
   int num_sms = 0;
@@ -84,7 +91,9 @@ static void ws_free(PtWorkspace* w) {
   if (w->shadow_order) cudaFree(w->shadow_order);
   w->shadow_order = nullptr;
   if (w->mat_hist) cudaFree(w->mat_hist);
-  w->sorted = w->ray_sorted = w->keys = w->mat_hist = nullptr;
+  if (w->keys2) cudaFree(w->keys2);
+  if (w->mat_hist2) cudaFree(w->mat_hist2);
+  w->sorted = w->ray_sorted = w->keys = w->mat_hist = w->keys2 = w->mat_hist2 = nullptr;
   if (w->counters) cudaFree(w->counters);
   w->ray_o = w->ray_d = w->thr = w->rad = w->absb = w->hit = w->shadow = nullptr;
   w->queue[0] = w->queue[1] = nullptr;
@@ -96,6 +105,9 @@ void pt_workspace_destroy(PtWorkspace* ws) {
   if (!ws) return;
   ws_free(ws);
   if (ws->prim) cudaFree(ws->prim);
+  if (ws->ev_shaded) cudaEventDestroy(ws->ev_shaded);
+  if (ws->ev_connected) cudaEventDestroy(ws->ev_connected);
+  if (ws->side) cudaStreamDestroy(ws->side);
   delete ws;
 }
 
@@ -114,6 +126,8 @@ static cudaError_t ws_reserve(PtWorkspace* w, size_t cap) {
   if ((e = cudaMalloc(&w->keys, cap * sizeof(int))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->shadow_order, cap * sizeof(int))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->mat_hist, 2 * (kMaxSortBins + 1) * sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->keys2, cap * sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->mat_hist2, 2 * (kMaxSortBins + 1) * sizeof(int))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->counters, 4 * kMaxDepthSlots * sizeof(int))) != cudaSuccess) return e;
   w->cap = cap;
   return cudaSuccess;
@@ -1032,7 +1046,7 @@ template <bool kJobs>
 static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene& s, const CamParams& cam,
                                  const float4* prim, PtWorkspace* ws, KernelTimer* timer, cudaStream_t st,
                                  int grid_ext, int grid_con, int grid_sh, int block, int nw, int* launches,
-                                 int* extend_launches, int* vertex_launches) {
+                                 int* extend_launches, int* vertex_launches, bool overlap) {
   cudaError_t e;
   a.queue_in = ws->queue[0];
   a.queue_out = ws->queue[1];
@@ -1074,6 +1088,9 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
       ++*extend_launches;
       ++*launches;
     }
+    // the previous vertex's occlusion launch (on the side stream) adds to the
+    // radiance this vertex's shading reads and writes: wait for it here
+    if (overlap && depth > 0 && (e = cudaStreamWaitEvent(st, ws->ev_connected, 0))) return e;
     if ((e = timer->mark(1, st, true))) return e;
     a.queue_in = path_order;
     if (p.sort_material && s.n_mats + 1 <= kMaxSortBins) {
@@ -1096,35 +1113,51 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
       k_shade<kJobs, false><<<grid_sh, block, 0, st>>>(a, s);
     }
     if ((e = timer->mark(1, st, false))) return e;
+    // The vertex's shadow rays: sorted and traced on the side stream, beside
+    // the next vertex's sort and closest-hit launch, which touch neither the
+    // shadow records nor the radiance.
+    cudaStream_t cs = st;
+    int* skeys = ws->keys;
+    int* shist = ws->mat_hist;
+    if (overlap) {
+      if ((e = cudaEventRecord(ws->ev_shaded, st))) return e;
+      if ((e = cudaStreamWaitEvent(ws->side, ws->ev_shaded, 0))) return e;
+      cs = ws->side;
+      skeys = ws->keys2;
+      shist = ws->mat_hist2;
+    }
     a.shadow_order = nullptr;
     if (p.sort_rays) {
-      if ((e = cudaMemsetAsync(ws->mat_hist, 0, (kMaxSortBins + 1) * sizeof(int), st))) return e;
-      k_raykey_hist<kJobs, true><<<grid_sh, 256, 0, st>>>(a, s, ws->mat_hist, ws->keys);
-      k_sort_scan<<<1, 1024, 0, st>>>(kRayKeyBins, ws->mat_hist);
-      k_raykey_scatter<true><<<grid_sh, 256, 0, st>>>(a, ws->keys, ws->mat_hist, ws->shadow_order);
+      if ((e = cudaMemsetAsync(shist, 0, (kMaxSortBins + 1) * sizeof(int), cs))) return e;
+      k_raykey_hist<kJobs, true><<<grid_sh, 256, 0, cs>>>(a, s, shist, skeys);
+      k_sort_scan<<<1, 1024, 0, cs>>>(kRayKeyBins, shist);
+      k_raykey_scatter<true><<<grid_sh, 256, 0, cs>>>(a, skeys, shist, ws->shadow_order);
       *launches += 3;
       a.shadow_order = ws->shadow_order;  // the occlusion kernel visits records in key order
     }
-    if ((e = timer->mark(2, st, true))) return e;
+    if ((e = timer->mark(2, cs, true))) return e;
     if (p.traversal == 2) {
       if (p.count_visits)
-        k_connect_batch<true, true, kJobs><<<grid_con, block, 0, st>>>(a, s);
+        k_connect_batch<true, true, kJobs><<<grid_con, block, 0, cs>>>(a, s);
       else
-        k_connect_batch<false, true, kJobs><<<grid_con, block, 0, st>>>(a, s);
+        k_connect_batch<false, true, kJobs><<<grid_con, block, 0, cs>>>(a, s);
     } else if (p.traversal == 0 || kJobs) {
       if (p.count_visits)
-        k_connect_batch<true, false, kJobs><<<grid_con, block, 0, st>>>(a, s);
+        k_connect_batch<true, false, kJobs><<<grid_con, block, 0, cs>>>(a, s);
       else
-        k_connect_batch<false, false, kJobs><<<grid_con, block, 0, st>>>(a, s);
+        k_connect_batch<false, false, kJobs><<<grid_con, block, 0, cs>>>(a, s);
     } else if (p.count_visits) {
-      k_connect<true><<<grid_con, block, 0, st>>>(a, s);
+      k_connect<true><<<grid_con, block, 0, cs>>>(a, s);
     } else {
-      k_connect<false><<<grid_con, block, 0, st>>>(a, s);
+      k_connect<false><<<grid_con, block, 0, cs>>>(a, s);
     }
-    if ((e = timer->mark(2, st, false))) return e;
+    if ((e = timer->mark(2, cs, false))) return e;
+    if (overlap && (e = cudaEventRecord(ws->ev_connected, cs))) return e;
     *launches += 2;
     ++*vertex_launches;  // one shading and one occlusion launch per path vertex
   }
+  // the last occlusion launch before the accumulation reads the radiance
+  if (overlap && (e = cudaStreamWaitEvent(st, ws->ev_connected, 0))) return e;
   return cudaSuccess;
 }
 
@@ -1155,7 +1188,7 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
   if (total == 0) return cudaSuccess;
   // Paths in flight: the whole render when it fits (every vertex launch has an
   // idle tail, so fewer, larger waves are faster), at most 2^26 paths and a
-  // quarter of the free device memory (kPathBytes = 184 B per path).
+  // quarter of the free device memory (kPathBytes = 188 B per path).
   long long wave = p.wave_paths;
   if (wave <= 0) {
     size_t free_b = 0, total_b = 0;
@@ -1196,6 +1229,20 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
       ws->occ_shade = std::min(ws->occ_shade, o1);
     }
     ws->block_cached = block;
+  }
+  // The side stream and its events are made outside any stream capture (a
+  // render captured before any uncaptured one runs without the overlap).
+  bool overlap = p.overlap;
+  if (overlap && !ws->side) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(st, &cap))) return e;
+    if (cap != cudaStreamCaptureStatusNone) {
+      overlap = false;
+    } else {
+      if ((e = cudaStreamCreateWithFlags(&ws->side, cudaStreamNonBlocking))) return e;
+      if ((e = cudaEventCreateWithFlags(&ws->ev_shaded, cudaEventDisableTiming))) return e;
+      if ((e = cudaEventCreateWithFlags(&ws->ev_connected, cudaEventDisableTiming))) return e;
+    }
   }
   int grid_ext = ws->num_sms * std::max(ws->occ_extend, 1);
   int grid_con = ws->num_sms * std::max(ws->occ_connect, 1);
@@ -1256,9 +1303,9 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     a.n_wave = nw;
     if ((e = cudaMemsetAsync(ws->counters, 0, 4 * kMaxDepthSlots * sizeof(int), st))) return e;
     e = jobs ? wave_launches<true>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,
-                                   extend_launches, vertex_launches)
+                                   extend_launches, vertex_launches, overlap)
              : wave_launches<false>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,
-                                    extend_launches, vertex_launches);
+                                    extend_launches, vertex_launches, overlap);
     if (e) return e;
     if (jobs) {
       k_accumulate_jobs<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(ws->rad, q0, nw, p.d_jobs, p.n_jobs,

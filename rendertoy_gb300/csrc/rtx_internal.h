@@ -167,6 +167,7 @@ struct PtParams {
   bool primary_cache;
   bool sort_material = false;  // counting-sort the shading queue by material
   bool sort_rays = false;      // counting-sort the extension queue by ray key
+  bool overlap = false;        // a vertex's occlusion launch beside the next vertex's closest-hit launch
   int traversal;  // RTX_OPT_TRAVERSAL
   int min_busy;   // RTX_OPT_MIN_BUSY
   Resolve resolve;  // fused into the last accumulation when display or bytes is set
