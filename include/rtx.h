@@ -302,6 +302,18 @@ int rtx_batch_autotune(rtx_context* ctx, int n_scenes,
  * src/renderer.cpp:274). */
 int rtx_render_pt(rtx_context* ctx, const float* camera, int W, int H, int spp,
                   int max_depth, uint64_t seed, float* out_rgb);
+/* Progressive rendering, checkpoint and resume.  RenderToy renders all of a
+ * frame's samples in one call (src/renderer.cpp:236-270) and keeps nothing to
+ * resume from.  Here out[p] += sum over s = first_sample ..
+ * first_sample + n_samples - 1 of L(p, s) / spp, in sample order
+ * (first_sample = 0 overwrites out instead), 0 <= first_sample <
+ * first_sample + n_samples <= spp.  A checkpoint is the image, the next
+ * sample index and the call's camera, size, spp, max_depth and seed;
+ * continuing from it -- in this or any other context with the same scene --
+ * gives, bit for bit, the image one rtx_render_pt(spp) call renders. */
+int rtx_render_pt_progressive(rtx_context* ctx, const float* camera, int W,
+                              int H, int first_sample, int n_samples, int spp,
+                              int max_depth, uint64_t seed, float* out_rgb);
 /* Per-path radiance L(p, s) for samples first_sample .. first_sample+n-1:
  * out[(s - first_sample) * W*H + p] (PathTracingRenderer::Radiance,
  * src/renderer.cpp:272-333, one call per (pixel, sample)). */

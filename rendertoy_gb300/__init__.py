@@ -36,6 +36,7 @@ EXPORTS = [
     "rtx_get_option", "rtx_get_stream", "rtx_set_stream", "rtx_synchronize", "rtx_get_stats",
     "rtx_scene_upload", "rtx_scene_emitters", "rtx_scene_set_emitters", "rtx_render_pt", "rtx_trace_paths",
     "rtx_render_aov", "rtx_primary_hits", "rtx_intersect", "rtx_bsdf_eval", "rtx_bsdf_sample",
+    "rtx_render_pt_progressive",
     "rtx_probe_read_bandwidth", "rtx_selftest_wait_timeout", "rtx_image_convolve",
     "rtx_image_gaussian_blur", "rtx_image_edge_detect", "rtx_image_bloom",
     "rtx_image_gaussian_blur_noalloc", "rtx_nn_gemm_bf16", "rtx_nn_conv3x3_fwd",
@@ -113,6 +114,7 @@ def lib() -> C.CDLL:
         "rtx_scene_set_emitters": (i, [vp, vp, i]),
         "rtx_render_pt": (i, [vp, vp, i, i, i, i, u64, vp]),
         "rtx_trace_paths": (i, [vp, vp, i, i, i, i, i, u64, vp]),
+        "rtx_render_pt_progressive": (i, [vp, vp, i, i, i, i, i, i, u64, vp]),
         "rtx_render_aov": (i, [vp, vp, i, i, f, f, vp, vp, vp]),
         "rtx_primary_hits": (i, [vp, vp, i, i, vp, vp]),
         "rtx_intersect": (i, [vp, i, vp, vp, vp, vp]),
@@ -318,6 +320,16 @@ class Context:
         cam = self._cam(camera)
         o = np.zeros((H, W, 3), np.float32) if out is None else out
         self._check(self.L.rtx_render_pt(self.h, _ptr(cam), W, H, spp, max_depth, seed, _ptr(o)))
+        return o
+
+    def render_pt_progressive(self, W, H, first_sample, n_samples, spp, max_depth, seed=0, camera=None,
+                              out=None):
+        """Samples [first_sample, first_sample + n_samples) of an spp-sample
+        frame added into `out` (overwritten when first_sample is 0)."""
+        cam = self._cam(camera)
+        o = np.zeros((H, W, 3), np.float32) if out is None else out
+        self._check(self.L.rtx_render_pt_progressive(self.h, _ptr(cam), W, H, first_sample, n_samples, spp,
+                                                     max_depth, seed, _ptr(o)))
         return o
 
     def trace_paths(self, W, H, first_sample, n_samples, max_depth, seed=0, camera=None, out=None):

@@ -980,6 +980,19 @@ int rtx_render_pt(rtx_context* c, const float* cam, int W, int H, int spp, int m
   return render_paths(c, cam, W, H, 0, spp, spp, max_depth, seed, out, false);
 }
 
+int rtx_render_pt_progressive(rtx_context* c, const float* cam, int W, int H, int first_sample, int n_samples,
+                              int spp, int max_depth, uint64_t seed, float* out) {
+  if (!c) return RTX_ERR_INVALID;
+  if (spp <= 0 || n_samples <= 0 || first_sample < 0 || (long long)first_sample + n_samples > spp)
+    return fail(c, RTX_ERR_INVALID, "need 0 <= first_sample < first_sample + n_samples <= spp");
+  // samples after the first add to the image rendered so far
+  const bool saved = c->accumulate;
+  c->accumulate = first_sample > 0;
+  int r = render_paths(c, cam, W, H, first_sample, n_samples, spp, max_depth, seed, out, false);
+  c->accumulate = saved;
+  return r;
+}
+
 int rtx_render_pt_resolved(rtx_context* c, const float* cam, int W, int H, int spp, int max_depth,
                            uint64_t seed, float* out, float limit, float gamma, float* display,
                            uint8_t* bytes, int format) {
@@ -1072,8 +1085,8 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   c->timer.reset();
   // the launch shape: everything the captured kernels bake in
   std::vector<int64_t> key = {n_jobs, max_depth, c->wave_paths, c->block, c->primary_cache, c->count_visits,
-                              c->accumulate, c->sort_material, c->sort_rays, c->traversal,
-                              (int64_t)(intptr_t)o.dev};
+                              c->accumulate, c->sort_material, c->sort_rays, c->traversal, c->overlap,
+                              c->stack_limit, (int64_t)(intptr_t)o.dev};
   for (int j = 0; j < n_jobs; ++j) key.insert(key.end(), {jobs[j].scene, jobs[j].W, jobs[j].H, jobs[j].spp});
   int launches = 0, ext_launches = 0, vtx_launches = 0;
   std::string why;

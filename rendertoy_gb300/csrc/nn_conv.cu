@@ -824,8 +824,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_wgrad(ConvWgrad a) {
 // three times and dout Cin / CR times, against nine and 9 Cin / 128 times in
 // k_conv_wgrad.  The accumulator lives in TMEM across all of the CTA's tiles;
 // one set of FP32 atomics per CTA combines the runs.
+//
+// kSwap (narrow outputs, Cout <= 56, and Cin >= 64): the operands trade
+// places.  M = the CTA's source channels (up to 128 accumulator lanes; the
+// MMA reads 128 rows of the halo, and rows past CR land in lanes that are
+// never read), N = Cout, A = the halo read at each tap's shift, B = the dout
+// tile; tap t accumulates in columns [t * Cout, t * Cout + Cout), 9 Cout <=
+// 512.  With M = Cout = 32 three quarters of every MMA would be padding; with
+// M = 96 source channels one quarter is, and one CTA covers all channels, so
+// dout is read once per tile.
 // ---------------------------------------------------------------------------
-template <int S>
+template <int S, bool kSwap>
 __global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[S], empty[S];
@@ -839,7 +848,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
   const int T = a.N * a.H * TR;
   const int tb = blockIdx.y * a.tiles_per_cta;
   const int n_tiles = max(0, min(a.tiles_per_cta, T - tb));
-  const uint32_t ncols = 9 * a.cr <= 256 ? 256 : 512;
+  const uint32_t ncols = (!kSwap && 9 * a.cr <= 256) ? 256 : 512;
   const uint32_t dout_bytes = (uint32_t)a.Cout * TW * 2;
   const uint32_t stage = dout_bytes + 3u * (a.cr >> 3) * TW2 * 16;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
@@ -854,7 +863,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = tmem_slot;
-  const uint32_t idesc = tc::make_idesc_bf16(128, CR, true, true);
+  const uint32_t idesc = tc::make_idesc_bf16(128, kSwap ? a.Cout : CR, true, true);
   const uint32_t s0 = tc::smem_u32(smem);
   // a producer's starting item and the per-iteration step of the two copy
   // loops (items: dout = (pixel k, chunk g), g fastest; halo = (row r, pixel
@@ -908,15 +917,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
 #pragma unroll 1
     for (int t = 0; t < 9; ++t) {
       const int dy = t / 3 - 1, dx = t % 3 - 1;
-      const uint64_t bd = bh + ((dy + 1) * nch * TW2 + 1 + dx);
-      const uint32_t d = tmem + t * CR;
-      tc::mma_bf16(d, ad0, bd, idesc, !first);
+      const uint64_t hd = bh + ((dy + 1) * nch * TW2 + 1 + dx);
+      if (kSwap) {  // A = the shifted halo (M = channels), B = the dout tile
+        const uint32_t d = tmem + t * a.Cout;
+        tc::mma_bf16(d, hd, ad0, idesc, !first);
 #pragma unroll 8
-      for (int ks = 1; ks < nks; ++ks) tc::mma_bf16(d, ad0 + 16 * ks, bd + 16 * ks, idesc, true);
+        for (int ks = 1; ks < nks; ++ks) tc::mma_bf16(d, hd + 16 * ks, ad0 + 16 * ks, idesc, true);
+      } else {
+        const uint32_t d = tmem + t * CR;
+        tc::mma_bf16(d, ad0, hd, idesc, !first);
+#pragma unroll 8
+        for (int ks = 1; ks < nks; ++ks) tc::mma_bf16(d, ad0 + 16 * ks, hd + 16 * ks, idesc, true);
+      }
     }
   };
   const bool ok = ws_ring<S>(n_tiles, full, empty, load, mma, a.err);
   const int lw = warp & 3;
+  if (kSwap) {
+    // warp w reads lanes 32 (w % 4) .. + 31 (source channel c0 + ch), half
+    // w / 4 of the 9 Cout / 8 column chunks (tap t, output channels o0 ..)
+    const int ch = lw * 32 + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(lw * 32) << 16);
+    const int nq = 9 * nco, q0 = (warp >> 2) * (nq >> 1), q1 = (warp >> 2) ? nq : (nq >> 1);
+    if (ok && n_tiles > 0 && lw * 32 < CR) {
+      for (int q = q0; q < q1; ++q) {
+        float v[8];
+        tc::tmem_ld8(taddr + q * 8, v);  // warp-wide: every lane loads, valid lanes add
+        if (ch < CR) {
+          const int t = q / nco, o0 = (q - t * nco) * 8;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) atomicAdd(a.dw + ((size_t)(o0 + k) * 9 + t) * a.Cin + c0 + ch, v[k]);
+        }
+      }
+    }
+    tc_end(tmem, ncols);
+    return;
+  }
   if (ok && n_tiles > 0 && lw * 32 < a.Cout) {
     // warp w reads lanes 32 (w % 4) .. + 31 (output channel o), half w / 4 of
     // the 9 CR / 8 column chunks
@@ -1090,6 +1126,27 @@ static int wgrad_row_channels(int Cin, int Cout) {
 cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
   long long P = (long long)a0.N * a0.H * a0.W;
   if (P >= (1LL << 31) || a0.Cout % 16 || a0.Cout > 256) return cudaErrorInvalidValue;
+  if (use_rows(a0.W, a0.Cin) && 9 * a0.Cout <= 512 && a0.Cin >= 64) {
+    // narrow outputs: source channels on the accumulator lanes (kSwap)
+    ConvWgrad a = a0;
+    a.tw = 64;
+    const int nr = (a.Cin + 127) / 128;
+    a.cr = (a.Cin + nr - 1) / nr;
+    a.cr = (a.cr + 15) / 16 * 16;
+    const long long T = (long long)a.N * a.H * ((a.W + a.tw - 1) / a.tw);
+    const int nch = a.cr / 8, TW2 = a.tw + 2;
+    const size_t stage = (size_t)a.Cout * a.tw * 2 + (size_t)3 * nch * TW2 * 16;
+    const int S = 4 * stage <= 190 * 1024 ? 4 : (3 * stage <= 190 * 1024 ? 3 : 2);
+    // the MMA's A operand spans 128 channel rows of a halo row: at the last
+    // stage's last halo row that reaches past the halo by this much
+    const size_t a_over = ((size_t)(16 - std::min(nch, 16)) * TW2 + a.tw + 2) * 16;
+    const long long ctas = (long long)sm_count();  // 512 TMEM columns: one CTA per SM
+    const long long npg = std::max(1LL, ctas / nr);
+    a.tiles_per_cta = (int)((T + npg - 1) / npg);
+    const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
+    return launch_staged(k_conv_wgrad_row<4, true>, k_conv_wgrad_row<3, true>, k_conv_wgrad_row<2, true>, S,
+                         dim3(nr, gy), stage, a, st, a_over);
+  }
   if (use_rows(a0.W, a0.Cin) && a0.Cout <= 128) {
     ConvWgrad a = a0;
     a.tw = a.W >= 128 ? 128 : 64;
@@ -1111,8 +1168,8 @@ cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
     const long long npg = std::max(1LL, ctas / nr);
     a.tiles_per_cta = (int)((T + npg - 1) / npg);
     const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
-    return launch_staged(k_conv_wgrad_row<4>, k_conv_wgrad_row<3>, k_conv_wgrad_row<2>, S, dim3(nr, gy), stage, a,
-                         st, extra);
+    return launch_staged(k_conv_wgrad_row<4, false>, k_conv_wgrad_row<3, false>, k_conv_wgrad_row<2, false>, S,
+                         dim3(nr, gy), stage, a, st, extra);
   }
   const ConvWgrad& a = a0;
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;

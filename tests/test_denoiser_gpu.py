@@ -43,6 +43,11 @@ CASES = [  # N, H, W, C1, up1, C2, Cout, relu
     (1, 2, 96, 16, 0, 0, 16, 0),       # the output layer's shape
     (1, 2, 128, 96, 1, 64, 64, 1),     # 160 inputs: five weight-gradient channel ranges
     (8, 64, 256, 32, 0, 0, 32, 1),     # several row tiles per weight-gradient CTA (ring wraps)
+    # narrow outputs from 64+ inputs: the weight gradient puts the source
+    # channels on the accumulator lanes
+    (2, 2, 128, 64, 1, 32, 32, 1),     # d0's shape: upsampled 64 + skip 32 -> 32
+    (4, 16, 256, 64, 1, 32, 32, 1),    # the same over many tiles per CTA (ring wraps)
+    (1, 2, 64, 128, 0, 32, 48, 1),     # 160 inputs in two channel ranges, Cout 48
 ]
 
 

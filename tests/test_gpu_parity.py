@@ -271,3 +271,27 @@ def test_traversal_variants_agree(ctx):
     for trav in (1, 2):
         assert np.array_equal(np.nan_to_num(out[trav], nan=-7).view(np.uint32),
                               np.nan_to_num(out[0], nan=-7).view(np.uint32)), trav
+
+
+def test_progressive_checkpoint_resume(ctx):
+    """A frame rendered in chunks of samples, checkpointed to the host after
+    each chunk and resumed in a fresh context, equals the frame rendered in
+    one call bit for bit (also when each chunk runs in several waves)."""
+    import rendertoy_gb300 as rt
+    from helpers import same_bits
+    sc = scenes.cornell_mixed()
+    ctx.upload(sc)
+    W, H, spp, depth, seed = 40, 30, 16, 8, 77
+    whole = ctx.render_pt(W, H, spp, depth, seed=seed)
+    chunks = [(0, 5), (5, 6), (11, 5)]
+    img = None
+    for k, (first, n) in enumerate(chunks):
+        with rt.Context(0) as other:  # a new process would do the same
+            other.upload(sc)
+            if k == 1:
+                other.set_option(rt.OPT_WAVE_PATHS, 777)
+            buf = np.zeros((H, W, 3), np.float32) if img is None else img.copy()  # the checkpoint
+            img = other.render_pt_progressive(W, H, first, n, spp, depth, seed=seed, out=buf)
+    assert same_bits(img, whole)
+    with pytest.raises(rt.RtxError):
+        ctx.render_pt_progressive(W, H, 10, 7, spp, depth)  # past the frame's samples
