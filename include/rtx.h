@@ -277,11 +277,11 @@ int rtx_render_batch(rtx_context* ctx, int n_jobs, const rtx_job* jobs,
  * `scenes` for each; scenes = NULL keeps the uploaded batch and its leaf
  * size -- then threads per block 64 / 128 x paths per wave 2^20, 2^22, 2^24,
  * auto, then the binary or 4-wide tree, then material-sorted shading on /
- * off, then ray-sorted traversal on / off, coordinate-wise from the
- * context's current options.  The fastest setting stays on the context
- * (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK, RTX_OPT_WAVE_PATHS, RTX_OPT_TRAVERSAL,
- * RTX_OPT_SORT_MATERIAL, RTX_OPT_SORT_RAYS) and the batch is left built with
- * it. */
+ * off, then ray-sorted traversal on / off, then the occlusion / closest-hit
+ * overlap on / off, coordinate-wise from the context's current options.  The
+ * fastest setting stays on the context (RTX_OPT_LEAF_SIZE, RTX_OPT_BLOCK,
+ * RTX_OPT_WAVE_PATHS, RTX_OPT_TRAVERSAL, RTX_OPT_SORT_MATERIAL,
+ * RTX_OPT_SORT_RAYS, RTX_OPT_OVERLAP) and the batch is left built with it. */
 typedef struct rtx_tune_result {
   int64_t block, wave_paths, leaf_size;
   double ms, ms_default;       /* frame time chosen / at the starting options */
@@ -289,6 +289,7 @@ typedef struct rtx_tune_result {
   int sort_material;           /* RTX_OPT_SORT_MATERIAL chosen */
   int traversal;               /* RTX_OPT_TRAVERSAL chosen (0 or 2) */
   int sort_rays;               /* RTX_OPT_SORT_RAYS chosen */
+  int overlap;                 /* RTX_OPT_OVERLAP chosen */
 } rtx_tune_result;
 int rtx_batch_autotune(rtx_context* ctx, int n_scenes,
                        const rtx_scene_desc* scenes, int n_jobs,

@@ -65,7 +65,7 @@ class Job(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("block", C.c_int64), ("wave_paths", C.c_int64), ("leaf_size", C.c_int64), ("ms", C.c_double),
                 ("ms_default", C.c_double), ("trials", C.c_int), ("sort_material", C.c_int),
-                ("traversal", C.c_int), ("sort_rays", C.c_int)]
+                ("traversal", C.c_int), ("sort_rays", C.c_int), ("overlap", C.c_int)]
 
 
 class RtxError(RuntimeError):

@@ -1245,6 +1245,16 @@ int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scene
     res.sort_rays = c->sort_rays ? 1 : 0;
   }
   c->sort_rays = res.sort_rays != 0;
+  // occlusion launches beside the next vertex's closest-hit launches
+  res.overlap = c->overlap ? 1 : 0;
+  c->overlap = !c->overlap;
+  if ((r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms))) return done(r);
+  ++res.trials;
+  if (ms < res.ms) {
+    res.ms = ms;
+    res.overlap = c->overlap ? 1 : 0;
+  }
+  c->overlap = res.overlap != 0;
   *out = res;
   return done(RTX_OK);
 }

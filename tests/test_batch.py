@@ -134,6 +134,7 @@ def test_autotune(ctx):
         assert res["trials"] >= 10 and res["ms"] <= res["ms_default"]
         assert ctx.get_option(rt.OPT_SORT_MATERIAL) == res["sort_material"]
         assert ctx.get_option(rt.OPT_SORT_RAYS) == res["sort_rays"]
+        assert ctx.get_option(rt.OPT_OVERLAP) == res["overlap"]
         assert ctx.get_option(rt.OPT_TRAVERSAL) == res["traversal"] and res["traversal"] in (0, 2)
         assert res["leaf_size"] in (2, 4, 8) and res["block"] in (64, 128)
         assert ctx.get_option(rt.OPT_BLOCK) == res["block"]
@@ -146,6 +147,7 @@ def test_autotune(ctx):
         ctx.set_option(rt.OPT_BLOCK, 128)
         ctx.set_option(rt.OPT_WAVE_PATHS, 0)
         ctx.set_option(rt.OPT_LEAF_SIZE, 4)
+        ctx.set_option(rt.OPT_OVERLAP, 1)
         ctx.set_option(rt.OPT_SORT_MATERIAL, 0)
         ctx.set_option(rt.OPT_SORT_RAYS, 1)
         ctx.set_option(rt.OPT_TRAVERSAL, 2)
