@@ -1,5 +1,7 @@
 """The benchmark's host-side arithmetic (no GPU): the per-layer roofline bound
-of the denoiser and the whole-job rate of a weak-scaling run."""
+of the denoiser, the whole-job rate of a weak-scaling run, the per-launch
+traversal roofline against HBM and L2, and the profile constants and CPU
+calibration the benchmark line reads."""
 import os
 import sys
 
@@ -50,3 +52,40 @@ def test_job_rate_is_weak_scaling_over_the_slowest_rank():
     assert bench.job_rate(100, 2.0, 1) == 50.0
     assert bench.job_rate(100, 2.0, 4) == 200.0
     assert bench.reduce_max(3.5, 1) == 3.5
+
+
+def test_traversal_roofline_per_launch_against_hbm_and_l2():
+    l2 = {"peak_gbs": 20000.0}
+    r = bench.traversal_roofline(bytes_frame=22e9, launches_frame=11, ms_frame=33.0, hbm=6800.0,
+                                 hbm_kind="measured", l2=l2)
+    # 2 GB per launch in 3 ms: 666.7 GB/s
+    assert abs(r["bytes_per_launch"] - 2e9) < 1e-3 and abs(r["avg_launch_ms"] - 3.0) < 1e-12
+    assert abs(r["achieved"] - 2e9 / 3e-3 / 1e9) < 1e-9
+    assert abs(r["frac"] - r["achieved"] / 6800.0) < 1e-12
+    assert abs(r["l2"]["frac"] - r["achieved"] / 20000.0) < 1e-12
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s"
+
+
+def test_profile_facts_reads_key_value_lines(tmp_path, monkeypatch):
+    prof = tmp_path / "profiles"
+    prof.mkdir()
+    (prof / "x.txt").write_text("# a comment 1.0\nwarp_inst_per_sample 356.2\nnot_a_number abc\n\nfoo 2e3 trailing\n")
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert bench.profile_facts("x.txt") == {"warp_inst_per_sample": 356.2, "foo": 2000.0}
+    assert bench.profile_facts("missing.txt") == {}
+
+
+def test_committed_profile_constants_are_readable():
+    """The constants the bench combines with its own timings exist."""
+    f = bench.profile_facts("k_shade_issue.txt")
+    assert f["warp_inst_per_sample"] > 0 and f["fp32_ops_per_sample"] > 0
+    c = bench.profile_facts("cornell_c1_issue.txt")
+    assert c["thread_inst_per_frame"] > c["warp_inst_per_frame"] > 0
+    assert bench.profile_facts("k_extend_traffic.txt")["dram_bytes_per_extension_ray"] > 0
+
+
+def test_cpu_calibration_reports_the_three_ratios():
+    c = bench.cpu_calibration()
+    assert c is not None
+    assert set(c["restatement_over_reference_speed"]) == {"paths_d12", "paths_d5", "render_d5"}
+    assert all(v > 0 for v in c["restatement_over_reference_speed"].values())
