@@ -233,14 +233,14 @@ __global__ void __launch_bounds__(256) k_kp_loss(const float* __restrict__ pred,
 // 8-channel group t % (C / 8) and walks pixels t / (C / 8), + 256 / (C / 8),
 // ... of the block's range; the block then sums its partials in shared memory
 // and adds one value per channel (C <= 256).
-__global__ void __launch_bounds__(256) k_bias_grad(const bf16* __restrict__ dout, long long P, int C,
-                                                   long long per_block, float* __restrict__ db) {
+__device__ __forceinline__ void bias_grad_block(const bf16* __restrict__ dout, long long P, int C,
+                                                long long per_block, int block, float* __restrict__ db) {
   __shared__ float part[256][9];
   const int groups = C >> 3, lanes = 256 / groups, tid = threadIdx.x;
   const int g = tid % groups, l = tid / groups;
   float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
   if (l < lanes) {
-    long long p0 = blockIdx.x * per_block, p1 = min(P, p0 + per_block);
+    long long p0 = block * per_block, p1 = min(P, p0 + per_block);
     for (long long p = p0 + l; p < p1; p += lanes) {
       ld8(dout + p * C + 8 * g, v);
 #pragma unroll
@@ -256,6 +256,19 @@ __global__ void __launch_bounds__(256) k_bias_grad(const bf16* __restrict__ dout
     for (int j = 0; j < lanes; ++j) s += part[j * groups + gg][k];
     atomicAdd(db + tid, s);
   }
+}
+
+__global__ void __launch_bounds__(256) k_bias_grad(const bf16* __restrict__ dout, long long P, int C,
+                                                   long long per_block, float* __restrict__ db) {
+  bias_grad_block(dout, P, C, per_block, blockIdx.x, db);
+}
+
+// Every layer's bias gradient in one launch: blockIdx.y picks the layer,
+// blockIdx.x its pixel range (blocks past a layer's own count return).
+__global__ void __launch_bounds__(256) k_bias_grads(BiasGrads j) {
+  const int i = blockIdx.y;
+  if ((long long)blockIdx.x * j.per_block[i] >= j.P[i]) return;
+  bias_grad_block(j.dout[i], j.P[i], j.C[i], j.per_block[i], blockIdx.x, j.db[i]);
 }
 
 // Adam (Kingma & Ba) on the FP32 master parameters
@@ -377,6 +390,18 @@ cudaError_t bias_grad(const bf16* dout, long long P, int C, float* db, cudaStrea
   long long nb = std::min<long long>(2 * 152, (P + 255) / 256);
   long long per = (P + nb - 1) / nb;
   k_bias_grad<<<(unsigned)nb, 256, 0, st>>>(dout, P, C, per, db);
+  return cudaGetLastError();
+}
+cudaError_t bias_grads(BiasGrads j, cudaStream_t st) {
+  if (j.n <= 0 || j.n > BiasGrads::kMax) return cudaErrorInvalidValue;
+  long long nbmax = 1;
+  for (int i = 0; i < j.n; ++i) {
+    if (j.C[i] % 8 || j.C[i] > 256) return cudaErrorInvalidValue;
+    const long long nb = std::min<long long>(2 * 152, (j.P[i] + 255) / 256);
+    j.per_block[i] = (j.P[i] + nb - 1) / nb;
+    nbmax = std::max(nbmax, nb);
+  }
+  k_bias_grads<<<dim3((unsigned)nbmax, (unsigned)j.n), 256, 0, st>>>(j);
   return cudaGetLastError();
 }
 cudaError_t adam(float* p, const float* g, float* m, float* v, long long n, float lr, int step,

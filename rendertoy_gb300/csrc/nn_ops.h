@@ -17,6 +17,17 @@ cudaError_t pool_grad_acc(const bf16* dpool, const bf16* skip, bf16* dskip, int 
 cudaError_t kp_loss(const float* pred, const float* raw, const float* target, bf16* dpred, int N, int H,
                     int W, double* loss, cudaStream_t st);
 cudaError_t bias_grad(const bf16* dout, long long P, int C, float* db, cudaStream_t st);
+// Several layers' bias gradients (db_i[c] += sum_p dout_i[p, c]) in one launch
+struct BiasGrads {
+  static constexpr int kMax = 16;
+  int n = 0;
+  const bf16* dout[kMax];
+  long long P[kMax];
+  int C[kMax];
+  long long per_block[kMax];  // set by bias_grads
+  float* db[kMax];
+};
+cudaError_t bias_grads(BiasGrads jobs, cudaStream_t st);
 cudaError_t adam(float* p, const float* g, float* m, float* v, long long n, float lr, int step,
                  cudaStream_t st);
 cudaError_t weights_bf16(const float* master, bf16* w, bf16* wt, int Cout, int Cin, cudaStream_t st);

@@ -283,6 +283,10 @@ cudaError_t UNet::backward(int N, int H, int W, int* err, cudaStream_t st) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(I.grad, 0, I.n_params * 4, st))) return e;
   I.launches = 0;
+  // Bias gradients are summed for all layers in one launch at the end: each
+  // layer's output gradient holds its final value once its own step is done
+  // (later steps write only the gradients of earlier layers' outputs).
+  BiasGrads bias;
   for (int i = kNumLayers - 1; i >= 0; --i) {
     const Impl::Layer& l = I.L[i];
     int lev = kTL[l.d.out >= 0 ? l.d.out : tU0];
@@ -305,8 +309,12 @@ cudaError_t UNet::backward(int N, int H, int W, int* err, cudaStream_t st) {
     g.dw = I.grad + l.w_off;
     g.err = err;
     if ((e = conv_wgrad(g, st))) return e;
-    if ((e = bias_grad(dout, P, l.d.cout_pad, I.grad + l.b_off, st))) return e;
-    I.launches += 2;
+    bias.dout[bias.n] = dout;
+    bias.P[bias.n] = P;
+    bias.C[bias.n] = l.d.cout_pad;
+    bias.db[bias.n] = I.grad + l.b_off;
+    ++bias.n;
+    ++I.launches;
     if (i == 0) break;  // the input needs no gradient
     // data gradient into the sources
     bool pooled = l.d.s1 == tP1 || l.d.s1 == tP2 || l.d.s1 == tP3 || l.d.s1 == tP4;
@@ -341,6 +349,8 @@ cudaError_t UNet::backward(int N, int H, int W, int* err, cudaStream_t st) {
       }
     }
   }
+  if ((e = bias_grads(bias, st))) return e;
+  ++I.launches;
   return cudaSuccess;
 }
 
