@@ -286,9 +286,8 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 }
 
 // master [Cout][9][Cin] FP32 -> w [Cout][9][Cin] and wt [Cin][9][Cout] BF16
-__global__ void k_weights_bf16(const float* __restrict__ master, bf16* __restrict__ w, bf16* __restrict__ wt,
-                               int Cout, int Cin) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void weight_bf16(const float* __restrict__ master, bf16* __restrict__ w,
+                                            bf16* __restrict__ wt, int Cout, int Cin, long long i) {
   long long n = (long long)Cout * 9 * Cin;
   if (i >= n) return;
   int c = (int)(i % Cin);
@@ -300,7 +299,17 @@ __global__ void k_weights_bf16(const float* __restrict__ master, bf16* __restric
   if (wt) wt[((size_t)c * 9 + t) * Cout + o] = b;
 }
 
-// prediction (log space) [P][16] -> radiance [P][3] = exp(pred) - 1
+__global__ void k_weights_bf16(const float* __restrict__ master, bf16* __restrict__ w, bf16* __restrict__ wt,
+                               int Cout, int Cin) {
+  weight_bf16(master, w, wt, Cout, Cin, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+}
+
+// Every layer's BF16 weights and transposes in one launch (blockIdx.y = layer)
+__global__ void k_weights_bf16_all(WeightLayouts j) {
+  const int l = blockIdx.y;
+  weight_bf16(j.master[l], j.w[l], j.wt[l], j.Cout[l], j.Cin[l], blockIdx.x * (long long)blockDim.x + threadIdx.x);
+}
+
 // The denoised radiance: the predicted filter applied to the input radiance,
 // for N frames of Hc x Wc pixels stored as Hs x Ws (the frame is the top-left
 // corner; taps are clamped to it); out [N][Hc][Wc][3].
@@ -413,6 +422,13 @@ cudaError_t adam(float* p, const float* g, float* m, float* v, long long n, floa
 }
 cudaError_t weights_bf16(const float* master, bf16* w, bf16* wt, int Cout, int Cin, cudaStream_t st) {
   k_weights_bf16<<<blocks((long long)Cout * 9 * Cin), 256, 0, st>>>(master, w, wt, Cout, Cin);
+  return cudaGetLastError();
+}
+cudaError_t weights_bf16_all(const WeightLayouts& j, cudaStream_t st) {
+  if (j.n <= 0 || j.n > WeightLayouts::kMax) return cudaErrorInvalidValue;
+  long long nmax = 1;
+  for (int l = 0; l < j.n; ++l) nmax = std::max(nmax, (long long)j.Cout[l] * 9 * j.Cin[l]);
+  k_weights_bf16_all<<<dim3(blocks(nmax), (unsigned)j.n), 256, 0, st>>>(j);
   return cudaGetLastError();
 }
 cudaError_t kp_apply(const float* pred, const float* raw, float* out, int N, int Hc, int Wc, int Hs, int Ws,

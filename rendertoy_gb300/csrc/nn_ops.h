@@ -31,6 +31,17 @@ cudaError_t bias_grads(BiasGrads jobs, cudaStream_t st);
 cudaError_t adam(float* p, const float* g, float* m, float* v, long long n, float lr, int step,
                  cudaStream_t st);
 cudaError_t weights_bf16(const float* master, bf16* w, bf16* wt, int Cout, int Cin, cudaStream_t st);
+// Several layers' BF16 weights w [Cout][9][Cin] and transposes wt [Cin][9][Cout]
+// from their FP32 masters in one launch
+struct WeightLayouts {
+  static constexpr int kMax = 16;
+  int n = 0;
+  const float* master[kMax];
+  bf16* w[kMax];
+  bf16* wt[kMax];
+  int Cout[kMax], Cin[kMax];
+};
+cudaError_t weights_bf16_all(const WeightLayouts& layers, cudaStream_t st);
 // out [N][Hc][Wc][3] = the predicted filters applied to the input radiance of
 // frames stored as Hs x Ws pixels (pred and raw share that layout)
 cudaError_t kp_apply(const float* pred, const float* raw, float* out, int N, int Hc, int Wc, int Hs, int Ws,

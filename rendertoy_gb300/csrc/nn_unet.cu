@@ -209,13 +209,17 @@ cudaError_t UNet::init(uint64_t seed, cudaStream_t st) {
 
 cudaError_t UNet::refresh_weights(cudaStream_t st) {
   Impl& I = *p_;
+  WeightLayouts j;
   for (int i = 0; i < kNumLayers; ++i) {
     const Impl::Layer& l = I.L[i];
-    cudaError_t e = weights_bf16(I.master + l.w_off, I.wbf + l.wb_off, I.wbf + l.wt_off, l.d.cout_pad,
-                                 l.cin_pad, st);
-    if (e) return e;
+    j.master[i] = I.master + l.w_off;
+    j.w[i] = I.wbf + l.wb_off;
+    j.wt[i] = I.wbf + l.wt_off;
+    j.Cout[i] = l.d.cout_pad;
+    j.Cin[i] = l.cin_pad;
   }
-  return cudaSuccess;
+  j.n = kNumLayers;
+  return weights_bf16_all(j, st);
 }
 
 cudaError_t UNet::set_params(const float* host, cudaStream_t st) {
@@ -367,7 +371,7 @@ cudaError_t UNet::train_step(const float* d_raw, const float* d_target, int N, i
   ++I.step;
   if ((e = adam(I.master, I.grad, I.m, I.v, (long long)I.n_params, lr, I.step, st))) return e;
   if ((e = refresh_weights(st))) return e;
-  I.launches += fwd + 2 + kNumLayers;  // loss, Adam, weight refresh
+  I.launches += fwd + 3;  // loss, Adam, weight refresh
   if (loss_out) {
     double s = 0.0;
     if ((e = cudaMemcpyAsync(&s, I.loss, sizeof(double), cudaMemcpyDeviceToHost, st))) return e;
