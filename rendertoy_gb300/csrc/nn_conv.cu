@@ -1123,20 +1123,45 @@ static int wgrad_row_channels(int Cin, int Cout) {
   return best;
 }
 
+// The row-tile weight gradient with S ring stages (2..7): each stage has its
+// own producer warp, so a deeper ring is also more warps copying at once.
+template <bool kSwap>
+static cudaError_t launch_wgrad_row(int S, dim3 grid, size_t smem, const ConvWgrad& a, cudaStream_t st) {
+  auto go = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    kern<<<grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+  };
+  switch (S) {
+    case 7: return go(k_conv_wgrad_row<7, kSwap>);
+    case 6: return go(k_conv_wgrad_row<6, kSwap>);
+    case 5: return go(k_conv_wgrad_row<5, kSwap>);
+    case 4: return go(k_conv_wgrad_row<4, kSwap>);
+    case 3: return go(k_conv_wgrad_row<3, kSwap>);
+    default: return go(k_conv_wgrad_row<2, kSwap>);
+  }
+}
+
 cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
   long long P = (long long)a0.N * a0.H * a0.W;
   if (P >= (1LL << 31) || a0.Cout % 16 || a0.Cout > 256) return cudaErrorInvalidValue;
+  constexpr size_t kRing = 190 * 1024;  // shared memory for the ring
+  auto stages = [&](size_t stage) { return (int)std::min<size_t>(kProducerWarps, kRing / stage); };
   if (use_rows(a0.W, a0.Cin) && 9 * a0.Cout <= 512 && a0.Cin >= 64) {
     // narrow outputs: source channels on the accumulator lanes (kSwap)
     ConvWgrad a = a0;
-    a.tw = 64;
     const int nr = (a.Cin + 127) / 128;
     a.cr = (a.Cin + nr - 1) / nr;
     a.cr = (a.cr + 15) / 16 * 16;
+    const int nch = a.cr / 8;
+    auto stage_of = [&](int tw) { return (size_t)a.Cout * tw * 2 + (size_t)3 * nch * (tw + 2) * 16; };
+    // the tile width whose ring is deepest (ties: the wider tile)
+    a.tw = stages(stage_of(32)) > stages(stage_of(64)) ? 32 : 64;
+    const size_t stage = stage_of(a.tw);
+    const int S = std::max(2, stages(stage));
     const long long T = (long long)a.N * a.H * ((a.W + a.tw - 1) / a.tw);
-    const int nch = a.cr / 8, TW2 = a.tw + 2;
-    const size_t stage = (size_t)a.Cout * a.tw * 2 + (size_t)3 * nch * TW2 * 16;
-    const int S = 4 * stage <= 190 * 1024 ? 4 : (3 * stage <= 190 * 1024 ? 3 : 2);
+    const int TW2 = a.tw + 2;
     // the MMA's A operand spans 128 channel rows of a halo row: at the last
     // stage's last halo row that reaches past the halo by this much
     const size_t a_over = ((size_t)(16 - std::min(nch, 16)) * TW2 + a.tw + 2) * 16;
@@ -1144,32 +1169,46 @@ cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
     const long long npg = std::max(1LL, ctas / nr);
     a.tiles_per_cta = (int)((T + npg - 1) / npg);
     const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
-    return launch_staged(k_conv_wgrad_row<4, true>, k_conv_wgrad_row<3, true>, k_conv_wgrad_row<2, true>, S,
-                         dim3(nr, gy), stage, a, st, a_over);
+    return launch_wgrad_row<true>(S, dim3(nr, gy), S * stage + a_over, a, st);
   }
   if (use_rows(a0.W, a0.Cin) && a0.Cout <= 128) {
     ConvWgrad a = a0;
-    a.tw = a.W >= 128 ? 128 : 64;
     a.cr = wgrad_row_channels(a.Cin, a.Cout);
     const int nr = (a.Cin + a.cr - 1) / a.cr;
+    struct Cfg {
+      int tw, S, per_sm;
+      size_t stage, extra;
+    };
+    auto cfg_of = [&](int tw) {
+      Cfg c;
+      c.tw = tw;
+      c.stage = (size_t)a.Cout * tw * 2 + (size_t)3 * (a.cr / 8) * (tw + 2) * 16;
+      c.S = std::max(2, stages(c.stage));
+      // the MMA's A operand spans 128 rows of TW pixels; rows past Cout are
+      // read (and their accumulator lanes ignored), so they must lie inside
+      // the allocation
+      const size_t a_span = (size_t)256 * tw;
+      c.extra = a_span > c.stage ? a_span - c.stage : 0;
+      c.per_sm = (9 * a.cr <= 256 && c.S * c.stage + c.extra <= 110 * 1024) ? 2 : 1;
+      // one CTA per SM when it takes all 512 TMEM columns: a second CTA on
+      // the SM would wait in its allocation for the first to finish
+      if (c.per_sm == 1 && c.S * c.stage + c.extra < 116 * 1024) c.extra = 116 * 1024 - c.S * c.stage;
+      return c;
+    };
+    // the tile width with the most producer warps per SM (ties: the wider)
+    Cfg best = cfg_of(a.W >= 128 ? 128 : 64);
+    for (int tw : {64, 32})
+      if (tw < best.tw) {
+        const Cfg c = cfg_of(tw);
+        if (c.S * c.per_sm > best.S * best.per_sm) best = c;
+      }
+    a.tw = best.tw;
     const long long T = (long long)a.N * a.H * ((a.W + a.tw - 1) / a.tw);
-    const size_t stage = (size_t)a.Cout * a.tw * 2 + (size_t)3 * (a.cr / 8) * (a.tw + 2) * 16;
-    const int S = 4 * stage <= 190 * 1024 ? 4 : (3 * stage <= 190 * 1024 ? 3 : 2);
-    // the MMA's A operand spans 128 rows of TW pixels; rows past Cout are
-    // read (and their accumulator lanes ignored), so they must lie inside the
-    // allocation
-    const size_t a_span = (size_t)256 * a.tw;
-    size_t extra = a_span > stage ? a_span - stage : 0;
-    const int per_sm = (9 * a.cr <= 256 && S * stage + extra <= 110 * 1024) ? 2 : 1;
-    // one CTA per SM when it takes all 512 TMEM columns: a second CTA on the
-    // SM would wait in its allocation for the first to finish
-    if (per_sm == 1 && S * stage + extra < 116 * 1024) extra = 116 * 1024 - S * stage;
-    const long long ctas = (long long)sm_count() * per_sm;
+    const long long ctas = (long long)sm_count() * best.per_sm;
     const long long npg = std::max(1LL, ctas / nr);
     a.tiles_per_cta = (int)((T + npg - 1) / npg);
     const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
-    return launch_staged(k_conv_wgrad_row<4, false>, k_conv_wgrad_row<3, false>, k_conv_wgrad_row<2, false>, S,
-                         dim3(nr, gy), stage, a, st, extra);
+    return launch_wgrad_row<false>(best.S, dim3(nr, gy), best.S * best.stage + best.extra, a, st);
   }
   const ConvWgrad& a = a0;
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
