@@ -657,6 +657,7 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   s.n_mats = n_mat;
   s.textured = 0;
   for (int m = 0; m < n_mat; ++m) s.textured |= mats[RTX_MATERIAL_FLOATS * (size_t)m + 21] != 0.0f;
+  s.lobes = material_lobes(mats, n_mat);
   for (int k = 0; k < 3; ++k) {
     s.sky[k] = sky[k];
     s.ground[k] = ground[k];
@@ -805,6 +806,7 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   s.textured = 0;
   for (size_t m = 0; m < mats.size() / RTX_MATERIAL_FLOATS; ++m)
     s.textured |= mats[RTX_MATERIAL_FLOATS * m + 21] != 0.0f;
+  s.lobes = material_lobes(mats.data(), (int)(mats.size() / RTX_MATERIAL_FLOATS));
   c->has_batch = true;
   if (c->graph) {
     cudaGraphExecDestroy(c->graph);

@@ -489,11 +489,29 @@ RTX_DEV ShadingFrame make_frame(const Mat& m, float eta, F3 N, F3 V) {
   return fr;
 }
 
+// Lobe sets.  A material with spec_trans == 0 (either sign) has a refraction
+// weight strw of +-0 or NaN, and one with clearcoat == 0 a clearcoat weight
+// cw of +-0 or NaN: Eval never adds those lobes (each needs its weight > 0),
+// Sample never takes the refraction branch (cdf2 = cdf1 + strw compares as
+// cdf1), and Sample's clearcoat branch multiplies its pdf by cw, so it returns
+// pdf +-0 or NaN.  The shading kernel uses neither Eval's value nor Sample's
+// direction unless the pdf is > 0, so when no material of the scene has the
+// lobe, leaving it out (kTrans / kCoat false) changes no result; it shrinks
+// the inlined shading code.
+#ifndef RTX_LOBE_BITS
+#define RTX_LOBE_BITS
+constexpr int kLobeTrans = 1, kLobeCoat = 2, kLobeAll = 3;
+#endif
+
+template <int kLobes = kLobeAll>
 RTX_DEV F3 BsdfEvalFrame(const Mat& m, float eta, const ShadingFrame& fr, F3 L, float& bsdf_pdf) {
+  constexpr bool kTrans = (kLobes & kLobeTrans) != 0, kCoat = (kLobes & kLobeCoat) != 0;
   bsdf_pdf = 0.0f;
   F3 f = f3s(0.0f);
   F3 V = fr.V;
   L = ToLocal(fr.T, fr.B, fr.N, L);
+  // without refraction every lobe needs L.z > 0: pdf 0 below the horizon
+  if (!kTrans && !(L.z > 0.0f)) return f;
   F3 H;
   if (L.z > 0.0f)
     H = normalized(L + V);
@@ -513,18 +531,20 @@ RTX_DEV F3 BsdfEvalFrame(const Mat& m, float eta, const ShadingFrame& fr, F3 L, 
     f = f + EvalSpecReflection(m, eta, spec_color, V, L, H, pdf);
     bsdf_pdf = bsdf_pdf + pdf * srw;
   }
-  if (strw > 0.0f && L.z < 0.0f) {
+  if (kTrans && strw > 0.0f && L.z < 0.0f) {
     f = f + EvalSpecRefraction(m, eta, V, L, H, pdf);
     bsdf_pdf = bsdf_pdf + pdf * strw;
   }
-  if (cw > 0.0f && L.z > 0.0f && V.z > 0.0f) {
+  if (kCoat && cw > 0.0f && L.z > 0.0f && V.z > 0.0f) {
     f = f + EvalClearcoat(m, V, L, H, pdf);
     bsdf_pdf = bsdf_pdf + pdf * cw;
   }
   return f * fabsf(L.z);
 }
+template <int kLobes = kLobeAll>
 RTX_DEV bool BsdfSampleFrame(const Mat& m, float eta, const ShadingFrame& fr, float r1, float r2,
                              F3& out_dir, F3& color_o, float& pdf) {
+  constexpr bool kTrans = (kLobes & kLobeTrans) != 0, kCoat = (kLobes & kLobeCoat) != 0;
   pdf = 0.0f;
   F3 f = f3s(0.0f);
   F3 V = fr.V;
@@ -549,13 +569,15 @@ RTX_DEV bool BsdfSampleFrame(const Mat& m, float eta, const ShadingFrame& fr, fl
     out_dir = normalized(Reflect(-V, H));
     f = EvalSpecReflection(m, eta, specCol, V, out_dir, H, pdf);
     pdf *= srw;
-  } else if (r1 < cdf2) {
+  } else if (kTrans && r1 < cdf2) {
     r1 = (r1 - cdf1) / (cdf2 - cdf1);
     F3 H = SampleGGXVNDF(V, m.roughness, r1, r2);
     if (H.z < 0.0f) H = -H;
     out_dir = normalized(Refract(-V, H, eta));
     f = EvalSpecRefraction(m, eta, V, out_dir, H, pdf);
     pdf *= strw;
+  } else if (!kCoat) {
+    return false;  // the clearcoat branch's pdf would be +-0 or NaN
   } else {
     // material.cpp:279 divides in double and narrows to float
     float num = r1 - cdf2;

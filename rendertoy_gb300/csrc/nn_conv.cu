@@ -1175,40 +1175,26 @@ cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
     ConvWgrad a = a0;
     a.cr = wgrad_row_channels(a.Cin, a.Cout);
     const int nr = (a.Cin + a.cr - 1) / a.cr;
-    struct Cfg {
-      int tw, S, per_sm;
-      size_t stage, extra;
-    };
-    auto cfg_of = [&](int tw) {
-      Cfg c;
-      c.tw = tw;
-      c.stage = (size_t)a.Cout * tw * 2 + (size_t)3 * (a.cr / 8) * (tw + 2) * 16;
-      c.S = std::max(2, stages(c.stage));
-      // the MMA's A operand spans 128 rows of TW pixels; rows past Cout are
-      // read (and their accumulator lanes ignored), so they must lie inside
-      // the allocation
-      const size_t a_span = (size_t)256 * tw;
-      c.extra = a_span > c.stage ? a_span - c.stage : 0;
-      c.per_sm = (9 * a.cr <= 256 && c.S * c.stage + c.extra <= 110 * 1024) ? 2 : 1;
-      // one CTA per SM when it takes all 512 TMEM columns: a second CTA on
-      // the SM would wait in its allocation for the first to finish
-      if (c.per_sm == 1 && c.S * c.stage + c.extra < 116 * 1024) c.extra = 116 * 1024 - c.S * c.stage;
-      return c;
-    };
-    // the tile width with the most producer warps per SM (ties: the wider)
-    Cfg best = cfg_of(a.W >= 128 ? 128 : 64);
-    for (int tw : {64, 32})
-      if (tw < best.tw) {
-        const Cfg c = cfg_of(tw);
-        if (c.S * c.per_sm > best.S * best.per_sm) best = c;
-      }
-    a.tw = best.tw;
+    a.tw = a.W >= 128 ? 128 : 64;
+    const size_t stage = (size_t)a.Cout * a.tw * 2 + (size_t)3 * (a.cr / 8) * (a.tw + 2) * 16;
+    // at most 4 stages here: deeper rings (narrower tiles, or more stages of
+    // the same tile) measured 0-10 % slower on these layers
+    const int S = std::max(2, std::min(4, stages(stage)));
+    // the MMA's A operand spans 128 rows of TW pixels; rows past Cout are
+    // read (and their accumulator lanes ignored), so they must lie inside the
+    // allocation
+    const size_t a_span = (size_t)256 * a.tw;
+    size_t extra = a_span > stage ? a_span - stage : 0;
+    const int per_sm = (9 * a.cr <= 256 && S * stage + extra <= 110 * 1024) ? 2 : 1;
+    // one CTA per SM when it takes all 512 TMEM columns: a second CTA on the
+    // SM would wait in its allocation for the first to finish
+    if (per_sm == 1 && S * stage + extra < 116 * 1024) extra = 116 * 1024 - S * stage;
     const long long T = (long long)a.N * a.H * ((a.W + a.tw - 1) / a.tw);
-    const long long ctas = (long long)sm_count() * best.per_sm;
+    const long long ctas = (long long)sm_count() * per_sm;
     const long long npg = std::max(1LL, ctas / nr);
     a.tiles_per_cta = (int)((T + npg - 1) / npg);
     const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
-    return launch_wgrad_row<false>(best.S, dim3(nr, gy), best.S * best.stage + best.extra, a, st);
+    return launch_wgrad_row<false>(S, dim3(nr, gy), S * stage + extra, a, st);
   }
   const ConvWgrad& a = a0;
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;

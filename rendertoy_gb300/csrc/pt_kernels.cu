@@ -388,8 +388,13 @@ __global__ void __launch_bounds__(64) k_primary_cache_job(DeviceScene s, const P
   primary_px(sj, J.cam, prim + J.pix_begin, err, ctr);
 }
 
-template <bool kJobs, bool kTex>
+// kFeat: the scene's lobe set (kLobeTrans, kLobeCoat) | kShadeTex when some
+// material has a procedural texture
+constexpr int kShadeTex = 4;
+template <bool kJobs, int kFeat>
 __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceScene s) {
+  constexpr bool kTex = (kFeat & kShadeTex) != 0;
+  constexpr int kLobes = kFeat & kLobeAll;
   int n = a.counts[a.depth];
   const int depth = a.depth;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -464,7 +469,7 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
       F3 emit_pos = (f3(g1.x, g1.y, g1.z) * aa + f3(g2.x, g2.y, g2.z) * bb) + f3(g0.x, g0.y, g0.z);
       F3 dl = normalized(emit_pos - pos);
       float bpdf;
-      F3 f = BsdfEvalFrame(m, eta, fr, dl, bpdf);
+      F3 f = BsdfEvalFrame<kLobes>(m, eta, fr, dl, bpdf);
       if (bpdf > 0.0f) {
         int slot = warp_append(a.shadow_counts + depth);
         F3 tb = T * br;
@@ -480,7 +485,7 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
     F3 nd, color;
     float pdf;
     bool cont = false;
-    if (BsdfSampleFrame(m, eta, fr, r1, r2, nd, color, pdf)) {
+    if (BsdfSampleFrame<kLobes>(m, eta, fr, r1, r2, nd, color, pdf)) {
       // log(1) is exactly +0: skip the call for the default extinction
       F3 lg = f3(m.extinction.x == 1.0f ? 0.0f : logf(m.extinction.x),
                  m.extinction.y == 1.0f ? 0.0f : logf(m.extinction.y),
@@ -508,6 +513,35 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
       a.queue_out[slot] = p;
     }
   }
+}
+
+// The shading variant a scene needs: its lobe set and whether it is textured.
+static int shade_features(const DeviceScene& s) { return (s.lobes & kLobeAll) | (s.textured ? kShadeTex : 0); }
+
+template <bool kJobs>
+static void launch_shade(int feat, dim3 grid, dim3 block, cudaStream_t st, const PtArgs& a, const DeviceScene& s) {
+  switch (feat) {
+    case 0: k_shade<kJobs, 0><<<grid, block, 0, st>>>(a, s); break;
+    case 1: k_shade<kJobs, 1><<<grid, block, 0, st>>>(a, s); break;
+    case 2: k_shade<kJobs, 2><<<grid, block, 0, st>>>(a, s); break;
+    case 3: k_shade<kJobs, 3><<<grid, block, 0, st>>>(a, s); break;
+    case 4: k_shade<kJobs, 4><<<grid, block, 0, st>>>(a, s); break;
+    case 5: k_shade<kJobs, 5><<<grid, block, 0, st>>>(a, s); break;
+    case 6: k_shade<kJobs, 6><<<grid, block, 0, st>>>(a, s); break;
+    default: k_shade<kJobs, 7><<<grid, block, 0, st>>>(a, s); break;
+  }
+}
+
+// resident blocks per SM of the least-resident shading variant
+template <bool kJobs>
+static int shade_occupancy(int block) {
+  int occ = 1 << 30, o = 0;
+  for (auto k : {k_shade<kJobs, 0>, k_shade<kJobs, 1>, k_shade<kJobs, 2>, k_shade<kJobs, 3>, k_shade<kJobs, 4>,
+                 k_shade<kJobs, 5>, k_shade<kJobs, 6>, k_shade<kJobs, 7>}) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, block, 0);
+    occ = std::min(occ, o);
+  }
+  return occ;
 }
 
 // Emitter's own exact test for a shadow record: the emitter is the target of
@@ -1103,14 +1137,9 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
       *launches += 3;
       PtArgs as = a;
       as.queue_in = ws->sorted;
-      if (s.textured)
-        k_shade<kJobs, true><<<grid_sh, block, 0, st>>>(as, s);
-      else
-        k_shade<kJobs, false><<<grid_sh, block, 0, st>>>(as, s);
-    } else if (s.textured) {
-      k_shade<kJobs, true><<<grid_sh, block, 0, st>>>(a, s);
+      launch_shade<kJobs>(shade_features(s), grid_sh, block, st, as, s);
     } else {
-      k_shade<kJobs, false><<<grid_sh, block, 0, st>>>(a, s);
+      launch_shade<kJobs>(shade_features(s), grid_sh, block, st, a, s);
     }
     if ((e = timer->mark(1, st, false))) return e;
     // The vertex's shadow rays: sorted and traced on the side stream, beside
@@ -1223,11 +1252,7 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     ws->occ_connect = std::min(ws->occ_connect, o2);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_connect_batch<false, true, true>, block, 0);
     ws->occ_connect = std::min(ws->occ_connect, o2);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ws->occ_shade, k_shade<false, false>, block, 0);
-    for (auto k : {k_shade<true, false>, k_shade<false, true>, k_shade<true, true>}) {
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k, block, 0);
-      ws->occ_shade = std::min(ws->occ_shade, o1);
-    }
+    ws->occ_shade = std::min(shade_occupancy<false>(block), shade_occupancy<true>(block));
     ws->block_cached = block;
   }
   // The side stream and its events are made outside any stream capture (a

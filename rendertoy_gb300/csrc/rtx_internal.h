@@ -43,6 +43,23 @@ enum DeviceError : int {
   kErrBadIndex = 4,
 };
 
+// Principled-BSDF lobes a scene's materials use beyond diffuse and specular
+// reflection (DeviceScene::lobes)
+#ifndef RTX_LOBE_BITS
+#define RTX_LOBE_BITS
+constexpr int kLobeTrans = 1, kLobeCoat = 2, kLobeAll = 3;
+#endif
+// kLobeTrans when some record (24 floats) has spec_trans (float 15) != 0,
+// kLobeCoat when some has clearcoat (float 13) != 0; NaN counts as nonzero
+inline int material_lobes(const float* mats, int n) {
+  int r = 0;
+  for (int m = 0; m < n; ++m) {
+    if (!(mats[24 * (size_t)m + 15] == 0.0f)) r |= kLobeTrans;
+    if (!(mats[24 * (size_t)m + 13] == 0.0f)) r |= kLobeCoat;
+  }
+  return r;
+}
+
 struct DeviceScene {
   const float4* __restrict__ nodes;
   const float4* __restrict__ nodes4;
@@ -56,6 +73,7 @@ struct DeviceScene {
   int root;  // node index (>= 0), leaf ref (< 0) or kEmptyRoot
   int n_tris, n_emitters, n_mats;
   int textured;  // some material has a procedural texture
+  int lobes;     // kLobeTrans: some material has spec_trans != 0; kLobeCoat: clearcoat != 0
   float sky[3], ground[3];
   // traversal stack entries a ray may use before it reports kErrStackOverflow
   // (kStackSize; lower only through RTX_OPT_STACK_LIMIT, to exercise that path)

@@ -295,3 +295,28 @@ def test_progressive_checkpoint_resume(ctx):
     assert same_bits(img, whole)
     with pytest.raises(rt.RtxError):
         ctx.render_pt_progressive(W, H, 10, 7, spp, depth)  # past the frame's samples
+
+
+def test_lobe_variants_agree(ctx):
+    """The shading kernel leaves out the refraction and clearcoat lobes when
+    no material of the scene uses them (spec_trans / clearcoat all zero).
+    The same scene with one more, unused material that has both lobes runs
+    the full kernel: single renders, per-path traces and textured batch
+    frames are bit-identical between the two."""
+    import dataclasses
+
+    from helpers import same_bits
+    extra = scenes.material((0.5, 0.5, 0.5), spec_trans=1.0, clearcoat=1.0)[None]
+    cases = [scenes.cornell_box(), scenes.displaced_icosphere(subdiv=3),
+             scenes.procedural_scene(3, n_tris=5000)[0]]
+    try:
+        for sc in cases:
+            full = dataclasses.replace(sc, mats=np.vstack([sc.mats, extra]).astype(np.float32))
+            out = []
+            for s in (sc, full):
+                ctx.upload(s)
+                out.append((ctx.trace_paths(40, 30, 0, 3, 12, seed=9), ctx.render_pt(48, 40, 4, 12, seed=9)))
+            for x, y in zip(*out):
+                assert same_bits(x, y), sc.name
+    finally:
+        ctx.upload(scenes.cornell_box())
