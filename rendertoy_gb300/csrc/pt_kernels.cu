@@ -388,6 +388,19 @@ __global__ void __launch_bounds__(64) k_primary_cache_job(DeviceScene s, const P
   primary_px(sj, J.cam, prim + J.pix_begin, err, ctr);
 }
 
+// Beer-Lambert factors pow(e, -absorption * distance) per channel and the
+// log of a material's extinction: out of line, so that the shading kernel's
+// common path (no absorption, extinction 1) does not carry six inlined
+// transcendental functions through the instruction cache.
+static __device__ __noinline__ F3 transmittance(F3 expo) {
+  return f3(expo.x == 0.0f ? 1.0f : powf(kE, expo.x), expo.y == 0.0f ? 1.0f : powf(kE, expo.y),
+            expo.z == 0.0f ? 1.0f : powf(kE, expo.z));
+}
+static __device__ __noinline__ F3 log_extinction(F3 ext) {
+  return f3(ext.x == 1.0f ? 0.0f : logf(ext.x), ext.y == 1.0f ? 0.0f : logf(ext.y),
+            ext.z == 1.0f ? 0.0f : logf(ext.z));
+}
+
 // kFeat: the scene's lobe set (kLobeTrans, kLobeCoat) | kShadeTex when some
 // material has a procedural texture
 constexpr int kShadeTex = 4;
@@ -443,9 +456,8 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
     acc = acc + T * E;
     float dist = length(pos - o);
     F3 expo = (-absorption) * dist;
-    // pow(e, +-0) is exactly 1: skip the call for the common no-absorption case
-    F3 br = f3(expo.x == 0.0f ? 1.0f : powf(kE, expo.x), expo.y == 0.0f ? 1.0f : powf(kE, expo.y),
-               expo.z == 0.0f ? 1.0f : powf(kE, expo.z));
+    // pow(e, +-0) is exactly 1: no call for the common no-absorption case
+    F3 br = (expo.x == 0.0f && expo.y == 0.0f && expo.z == 0.0f) ? f3s(1.0f) : transmittance(expo);
     ShadingFrame fr = make_frame(m, eta, ff, -d);
 
     long long q = J.q;
@@ -486,10 +498,10 @@ __global__ void __launch_bounds__(128, RTX_SHADE_MINB) k_shade(PtArgs a, DeviceS
     float pdf;
     bool cont = false;
     if (BsdfSampleFrame<kLobes>(m, eta, fr, r1, r2, nd, color, pdf)) {
-      // log(1) is exactly +0: skip the call for the default extinction
-      F3 lg = f3(m.extinction.x == 1.0f ? 0.0f : logf(m.extinction.x),
-                 m.extinction.y == 1.0f ? 0.0f : logf(m.extinction.y),
-                 m.extinction.z == 1.0f ? 0.0f : logf(m.extinction.z));
+      // log(1) is exactly +0: no call for the default extinction
+      F3 lg = (m.extinction.x == 1.0f && m.extinction.y == 1.0f && m.extinction.z == 1.0f)
+                  ? f3s(0.0f)
+                  : log_extinction(m.extinction);
       absorption = (-lg) / m.at_distance;
       if (pdf > 0.0f) {
         F3 w = (br * color) / pdf;
