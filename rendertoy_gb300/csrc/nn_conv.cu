@@ -29,6 +29,8 @@
 // MMAs that read it have completed.  The gathers of later slices therefore
 // overlap the MMAs of earlier ones, and no thread stalls on its own loads.
 #include <algorithm>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "nn.h"
 #include "tc_core.cuh"
@@ -199,6 +201,10 @@ __device__ __forceinline__ bool conv_ring(int n, uint64_t* bars, Load&& load, Mm
 // load(unit, stage, lane) copies with item stride kLoadStride.
 constexpr int kProducerWarps = 7;
 constexpr int kLoadStride = 32;
+#ifndef RTX_CONV_TMA
+#define RTX_CONV_TMA 1
+#endif
+constexpr bool kConvTma = RTX_CONV_TMA != 0;  // tensor copies where a source allows them
 
 // pre(pw, lane) issues copies every MMA needs (resident weights, split over
 // the producer warps); the warp waits for them and its 32 lanes arrive on
@@ -226,6 +232,42 @@ __device__ __forceinline__ bool produce(int n, uint64_t* full, uint64_t* empty, 
     tc::mbar_arrive(&full[pw]);
   }
   return true;
+}
+
+// produce() for units that arrive as tensor copies: the producer warps
+// still copy what every MMA needs (pre, then wbar), then thread 32 alone
+// issues each unit's copies (issue(unit, stage, bar)) into its stage once
+// the stage is free, with one arrival carrying the unit's `tx` bytes.
+// `issued` counts the units it issued.
+template <int S, class Pre, class Issue>
+__device__ __forceinline__ bool produce_tma(int n, uint64_t* full, uint64_t* empty, uint64_t* wbar, uint32_t tx,
+                                            Pre&& pre, Issue&& issue, int& issued) {
+  const int pw = (threadIdx.x >> 5) - 1, lane = threadIdx.x & 31;
+  issued = 0;
+  if (wbar) {
+    pre(pw, lane);
+    tc::cp_async_commit();
+    tc::cp_async_wait<0>();
+    tc::fence_proxy_async();
+    tc::mbar_arrive(wbar);
+  }
+  if (threadIdx.x != 32) return true;
+  for (int u = 0; u < n; ++u) {
+    const int st = u % S;
+    if (u >= S && !tc::mbar_wait(&empty[st], (uint32_t)(u / S - 1) & 1u)) return false;
+    tc::mbar_arrive_expect_tx(&full[st], tx);
+    issue(u, st, &full[st]);
+    issued = u + 1;
+  }
+  return true;
+}
+
+// After a timed-out wait: thread 32 waits (bounded) for the tensor copies it
+// issued last on each stage, so that none lands after the CTA has left.
+template <int S>
+__device__ __forceinline__ void drain_tma(uint64_t* full, int issued) {
+  if (threadIdx.x != 32) return;
+  for (int u = max(0, issued - S); u < issued; ++u) tc::mbar_wait(&full[u % S], (uint32_t)(u / S) & 1u);
 }
 
 // One accumulation over n slices (the weight gradient).  Returns true,
@@ -261,6 +303,53 @@ __device__ __forceinline__ bool ws_ring(int n, uint64_t* full, uint64_t* empty, 
   return fin;
 }
 
+// The same accumulation fed by tensor copies (TMA): thread 32 issues unit
+// it's copies into stage it % S once the MMAs of unit it - S have released
+// it (one arrival carrying the unit's byte count, `tx`), thread 0 issues the
+// MMAs.  On a timed-out wait the issuing thread waits (bounded) for the
+// copies it issued last on each stage before the CTA leaves, so that none
+// lands in released shared memory.
+template <int S, class Issue, class Mma>
+__device__ __forceinline__ bool tma_ring(int n, uint64_t* full, uint64_t* empty, uint32_t tx, Issue&& issue,
+                                         Mma&& mma, int* err) {
+  const int tid = threadIdx.x;
+  bool ok = true;
+  int issued = 0;
+  if (tid == 0) {
+    for (int it = 0; it < n; ++it) {
+      const int st = it % S;
+      if (!tc::mbar_wait(&full[st], (uint32_t)(it / S) & 1u)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+      mma(it, st);
+      tc::mma_commit(&empty[st]);
+    }
+  } else if (tid == 32) {
+    for (int it = 0; it < n; ++it) {
+      const int st = it % S;
+      if (it >= S && !tc::mbar_wait(&empty[st], (uint32_t)(it / S - 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      tc::mbar_arrive_expect_tx(&full[st], tx);
+      issue(it, st, &full[st]);
+      issued = it + 1;
+    }
+  }
+  bool fin = __syncthreads_and(ok);
+  if (fin && n > 0) fin = tc::mbar_wait(&empty[(n - 1) % S], (uint32_t)((n - 1) / S) & 1u);
+  fin = __syncthreads_and(fin);
+  if (!fin) {
+    if (tid == 32)
+      for (int it = max(0, issued - S); it < issued; ++it) tc::mbar_wait(&full[it % S], (uint32_t)(it / S) & 1u);
+    if ((tid & 31) == 0) atomicOr(err, tc::kErrMbarTimeout);
+  }
+  tc::fence_after();
+  return fin;
+}
+
 // Persistent tiles (kTileThreads = 12 warps): thread 0 issues MMAs, warps
 // 1 .. 7 produce, warps 8 .. 11 run the epilogue, warp 8 + q reading
 // accumulator lanes 32 q .. 32 q + 31.  A CTA walks n_tiles output tiles of
@@ -278,10 +367,10 @@ struct TileBars {
 };
 
 template <int S>
-__device__ __forceinline__ void tile_bars_init(TileBars& b) {
+__device__ __forceinline__ void tile_bars_init(TileBars& b, uint32_t full_count = kLoadStride) {
   if (threadIdx.x == 0) {
     for (int i = 0; i < S; ++i) {
-      tc::mbar_init(&b.full[i], kLoadStride);
+      tc::mbar_init(&b.full[i], full_count);
       tc::mbar_init(&b.empty[i], 1);
     }
     for (int i = 0; i < 2; ++i) {
@@ -293,12 +382,13 @@ __device__ __forceinline__ void tile_bars_init(TileBars& b) {
   }
 }
 
-template <int S, class Pre, class Load, class Mma, class Epi>
+template <int S, bool kTma = false, class Pre, class Load, class Mma, class Epi, class Issue>
 __device__ __forceinline__ bool ws_tiles(int n_tiles, int nsl, TileBars& b, Pre&& pre, Load&& load, Mma&& mma,
-                                         Epi&& epi, int* err) {
+                                         Epi&& epi, int* err, Issue&& issue, uint32_t tx) {
   const int tid = threadIdx.x, warp = tid >> 5;
   const int n = n_tiles * nsl;
   bool ok = true;
+  int issued = 0;
   if (warp == 0) {
     if (tid == 0) {
       if (n > 0) ok = tc::mbar_wait(&b.wbar, 0u);
@@ -314,7 +404,10 @@ __device__ __forceinline__ bool ws_tiles(int n_tiles, int nsl, TileBars& b, Pre&
       }
     }
   } else if (warp <= kProducerWarps) {
-    ok = produce<S>(n, b.full, b.empty, &b.wbar, pre, load);
+    if constexpr (kTma)
+      ok = produce_tma<S>(n, b.full, b.empty, &b.wbar, tx, pre, issue, issued);
+    else
+      ok = produce<S>(n, b.full, b.empty, &b.wbar, pre, load);
   } else {
     for (int i = 0; i < n_tiles; ++i) {
       const int buf = i & 1;
@@ -329,7 +422,10 @@ __device__ __forceinline__ bool ws_tiles(int n_tiles, int nsl, TileBars& b, Pre&
     }
   }
   ok = __syncthreads_and(ok);
-  if (!ok && (tid & 31) == 0) atomicOr(err, tc::kErrMbarTimeout);
+  if (!ok) {
+    if constexpr (kTma) drain_tma<S>(b.full, issued);
+    if ((tid & 31) == 0) atomicOr(err, tc::kErrMbarTimeout);
+  }
   return ok;
 }
 
@@ -437,12 +533,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_fwd(ConvFwd a) {
 // ---------------------------------------------------------------------------
 constexpr int kHalo = 130;                                  // pixels x0 - 1 .. x0 + 128
 constexpr uint32_t kHaloBytes = 3 * 2 * kHalo * 16;          // rows x chunks x pixels x 16 B
+constexpr uint32_t kHaloStage = (kHaloBytes + 1023) & ~1023u;  // 1 KB aligned for tensor copies
 
 // smem byte offset of chunk c (of 2) of halo pixel h in halo row r
 __device__ __forceinline__ uint32_t halo_off(int r, int c, int h) { return ((r * 2 + c) * kHalo + h) * 16; }
 
-template <int S, bool kRes>
-__global__ void __launch_bounds__(kTileThreads, 1) k_conv_fwd_rows(ConvFwd a) {
+template <int S, bool kRes, bool kTma = false>
+__global__ void __launch_bounds__(kTileThreads, 1)
+    k_conv_fwd_rows(ConvFwd a, const __grid_constant__ CUtensorMap tm_halo) {
+  static_assert(!kTma || kRes, "tensor copies carry the halo only");
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) TileBars bars;
   __shared__ uint32_t tmem_slot;
@@ -453,9 +552,9 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_fwd_rows(ConvFwd a) {
   const int nsl = a.Cin / 16;
   const uint32_t ncols = a.Cout <= 32 ? 32 : (a.Cout <= 64 ? 64 : (a.Cout <= 128 ? 128 : 256));
   const uint32_t tap_bytes = (uint32_t)a.Cout * 32;
-  const uint32_t stage = kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes;
+  const uint32_t stage = kTma ? kHaloStage : (kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes);
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
-  tile_bars_init<S>(bars);
+  tile_bars_init<S>(bars, kTma ? 1 : kLoadStride);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -534,7 +633,14 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_fwd_rows(ConvFwd a) {
       }
     }
   };
-  ws_tiles<S>(n_tiles, nsl, bars, pre, load, mma, epi, a.err);
+  // tensor-copy form: the unit's halo slice as one box of the source map
+  auto issue = [&](int u, int st, uint64_t* bar) {
+    const int i = u / nsl, s = u - i * nsl;
+    int n, y, x0;
+    tile_of(i, n, y, x0);
+    tc::tma_load_5d(s0 + st * stage, &tm_halo, 0, x0 - 1, 2 * s, y - 1, n, bar);
+  };
+  ws_tiles<S, kTma>(n_tiles, nsl, bars, pre, load, mma, epi, a.err, issue, kHaloBytes);
   tc_end(tmem, 2 * ncols);
 }
 
@@ -543,8 +649,10 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_fwd_rows(ConvFwd a) {
 // tile is (image row, 128 pixels, 256 input channels); the channel tile
 // varies fastest, so neighbouring CTAs read the same dout halo.  Resident
 // weights: [channel tile][slice][tap] tiles of NTmax x 16.
-template <int S, bool kRes>
-__global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a) {
+template <int S, bool kRes, bool kTma = false>
+__global__ void __launch_bounds__(kTileThreads, 1)
+    k_conv_dgrad_rows(ConvDgrad a, const __grid_constant__ CUtensorMap tm_halo) {
+  static_assert(!kTma || kRes, "tensor copies carry the halo only");
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) TileBars bars;
   __shared__ uint32_t tmem_slot;
@@ -556,9 +664,9 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a
   const int ntm = min(a.ctw, a.Cin);  // widest channel tile
   const uint32_t ncols = ntm <= 32 ? 32 : (ntm <= 64 ? 64 : (ntm <= 128 ? 128 : 256));
   const uint32_t tap_bytes = (uint32_t)ntm * 32;
-  const uint32_t stage = kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes;
+  const uint32_t stage = kTma ? kHaloStage : (kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes);
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
-  tile_bars_init<S>(bars);
+  tile_bars_init<S>(bars, kTma ? 1 : kLoadStride);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -644,7 +752,14 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_conv_dgrad_rows(ConvDgrad a
       }
     }
   };
-  ws_tiles<S>(n_tiles, nsl, bars, pre, load, mma, epi, a.err);
+  // tensor-copy form: the unit's dout halo slice as one box of dout's map
+  auto issue = [&](int u, int st, uint64_t* bar) {
+    const int i = u / nsl, s = u - i * nsl;
+    int n, y, x0, ct;
+    tile_of(i, n, y, x0, ct);
+    tc::tma_load_5d(s0 + st * stage, &tm_halo, 0, x0 - 1, 2 * s, y - 1, n, bar);
+  };
+  ws_tiles<S, kTma>(n_tiles, nsl, bars, pre, load, mma, epi, a.err, issue, kHaloBytes);
   tc_end(tmem, 2 * ncols);
 }
 
@@ -833,9 +948,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_conv_wgrad(ConvWgrad a) {
 // 512.  With M = Cout = 32 three quarters of every MMA would be padding; with
 // M = 96 source channels one quarter is, and one CTA covers all channels, so
 // dout is read once per tile.
+//
+// kTma (single, full-resolution source; Cin a multiple of the CTA's
+// channels): each unit's halo and dout tile arrive as two tensor copies
+// into the same layouts.  The source map is NHWC viewed as 5-D (8 channels,
+// x, channel chunk, y, image), so a box of (8, TW + 2, CR / 8, 3, 1) lands
+// row, chunk, pixel major -- the layout above -- with zeros outside the
+// image; dout's map is the same view of [rows][W][Cout] with a box of
+// (8, TW, Cout / 8, 1, 1).  Stages are 1 KB aligned for the copies.
 // ---------------------------------------------------------------------------
-template <int S, bool kSwap>
-__global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
+template <int S, bool kSwap, bool kTma>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_conv_wgrad_row(ConvWgrad a, const __grid_constant__ CUtensorMap tm_src,
+                     const __grid_constant__ CUtensorMap tm_dout) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[S], empty[S];
   __shared__ uint32_t tmem_slot;
@@ -850,11 +975,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
   const int n_tiles = max(0, min(a.tiles_per_cta, T - tb));
   const uint32_t ncols = (!kSwap && 9 * a.cr <= 256) ? 256 : 512;
   const uint32_t dout_bytes = (uint32_t)a.Cout * TW * 2;
-  const uint32_t stage = dout_bytes + 3u * (a.cr >> 3) * TW2 * 16;
+  const uint32_t tx = dout_bytes + 3u * (a.cr >> 3) * TW2 * 16;  // one unit's bytes
+  const uint32_t stage = kTma ? (tx + 1023u) & ~1023u : tx;
   if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
   if (tid == 0) {
     for (int i = 0; i < S; ++i) {
-      tc::mbar_init(&full[i], kLoadStride);
+      tc::mbar_init(&full[i], kTma ? 1 : kLoadStride);
       tc::mbar_init(&empty[i], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -931,7 +1057,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_wgrad_row(ConvWgrad a) {
       }
     }
   };
-  const bool ok = ws_ring<S>(n_tiles, full, empty, load, mma, a.err);
+  // the tensor-copy form: unit `slice` of this CTA (its row tile) as two boxes
+  auto issue = [&](int slice, int st, uint64_t* bar) {
+    const uint32_t sd = s0 + st * stage, sh = sd + dout_bytes;
+    const int j = tb + slice;
+    const int row = j / TR, x0 = (j - row * TR) * TW;  // row = n * H + y
+    const int n = row / a.H, y = row - n * a.H;
+    tc::tma_load_5d(sh, &tm_src, 0, x0 - 1, c0 >> 3, y - 1, n, bar);
+    tc::tma_load_5d(sd, &tm_dout, 0, x0, 0, row, 0, bar);
+  };
+  bool ok;
+  if constexpr (kTma)
+    ok = tma_ring<S>(n_tiles, full, empty, tx, issue, mma, a.err);
+  else
+    ok = ws_ring<S>(n_tiles, full, empty, load, mma, a.err);
   const int lw = warp & 3;
   if (kSwap) {
     // warp w reads lanes 32 (w % 4) .. + 31 (source channel c0 + ch), half
@@ -1023,7 +1162,7 @@ static bool use_rows(int W, int Ck) { return W >= 64 && Ck % 16 == 0; }
 // deepest ring (6, 4 or 2 stages) that fits 200 KB.
 template <class KR, class K6, class K4, class K2, class Args>
 static cudaError_t launch_tiles(KR kr, K6 k6, K4 k4, K2 k2, bool res, size_t stage, size_t res_bytes, long long T,
-                                const Args& a, cudaStream_t st) {
+                                const Args& a, const CUtensorMap& tm, cudaStream_t st) {
   if (T <= 0) return cudaSuccess;
   int S = 7;
   size_t smem = 7 * stage + res_bytes;
@@ -1036,7 +1175,7 @@ static cudaError_t launch_tiles(KR kr, K6 k6, K4 k4, K2 k2, bool res, size_t sta
   cudaError_t e;
 #define RTX_LAUNCH_TILES(K)                                                                          \
   if ((e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e; \
-  K<<<grid, kTileThreads, smem, st>>>(a);
+  K<<<grid, kTileThreads, smem, st>>>(a, tm);
   if (res) {
     RTX_LAUNCH_TILES(kr)
   } else if (S == 6) {
@@ -1050,6 +1189,40 @@ static cudaError_t launch_tiles(KR kr, K6 k6, K4 k4, K2 k2, bool res, size_t sta
   return cudaGetLastError();
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (null if
+// the driver does not provide it)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of an [imgs][H][W][C] BF16 tensor (C a multiple of 8) viewed as
+// 5-D (8 channels, x, channel chunk, y, image), with a box of (8, box_w,
+// box_chunks, box_rows, 1): the box lands in shared memory row, chunk,
+// pixel major, 16 bytes per (pixel, chunk).  False if it cannot be encoded.
+static bool chunk_major_map(CUtensorMap* m, const void* base, int imgs, int H, int W, int C, int box_w,
+                            int box_chunks, int box_rows) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(base) & 15) || C % 8 || box_w > 256 || box_chunks > 256 ||
+      box_rows > 256)
+    return false;
+  const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)(C / 8), (cuuint64_t)H, (cuuint64_t)imgs};
+  const cuuint64_t strides[4] = {(cuuint64_t)C * 2, 16, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+  const cuuint32_t box[5] = {8, (cuuint32_t)box_w, (cuuint32_t)box_chunks, (cuuint32_t)box_rows, 1};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // weights kept in shared memory by the persistent kernels up to this size
 constexpr size_t kResidentWeights = 96 * 1024;
 
@@ -1059,10 +1232,16 @@ cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st) {
   if (use_rows(a.W, a.Cin)) {
     const size_t wbytes = (size_t)9 * a.Cin * a.Cout * 2;
     const bool res = wbytes <= kResidentWeights;
-    const size_t stage = res ? kHaloBytes : kHaloBytes + (size_t)9 * a.Cout * 32;
+    // resident weights and one full-resolution source: halo slices arrive as
+    // tensor copies, if the map encodes
+    CUtensorMap tm{};
+    const bool tma = kConvTma && res && !a.s2.ptr && !a.s1.up && a.s1.C == a.Cin &&
+                     chunk_major_map(&tm, a.s1.ptr, a.N, a.H, a.W, a.Cin, kHalo, 2, 3);
+    const size_t stage = res ? (tma ? kHaloStage : kHaloBytes) : kHaloBytes + (size_t)9 * a.Cout * 32;
     const long long T = (long long)a.N * a.H * ((a.W + 127) / 128);
-    return launch_tiles(k_conv_fwd_rows<7, true>, k_conv_fwd_rows<6, false>, k_conv_fwd_rows<4, false>,
-                        k_conv_fwd_rows<2, false>, res, stage, res ? wbytes : 0, T, a, st);
+    return launch_tiles(tma ? k_conv_fwd_rows<7, true, true> : k_conv_fwd_rows<7, true>, k_conv_fwd_rows<6, false>,
+                        k_conv_fwd_rows<4, false>, k_conv_fwd_rows<2, false>, res, stage, res ? wbytes : 0, T, a,
+                        tm, st);
   }
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
   return launch_staged(k_conv_fwd<4>, k_conv_fwd<3>, k_conv_fwd<2>, stages_for(a.Cout),
@@ -1089,10 +1268,16 @@ cudaError_t conv_dgrad(const ConvDgrad& a, cudaStream_t st) {
       }
     }
     const int ntb = (a.Cin + b.ctw - 1) / b.ctw;
-    const size_t stage = res ? kHaloBytes : kHaloBytes + (size_t)9 * b.ctw * 32;
+    // resident weights: dout's halo slices arrive as tensor copies, if the
+    // map encodes
+    CUtensorMap tm{};
+    const bool tma = kConvTma && res && a.Cout % 16 == 0 &&
+                     chunk_major_map(&tm, a.dout, a.N, a.H, a.W, a.Cout, kHalo, 2, 3);
+    const size_t stage = res ? (tma ? kHaloStage : kHaloBytes) : kHaloBytes + (size_t)9 * b.ctw * 32;
     const long long T = (long long)a.N * a.H * ((a.W + 127) / 128) * ntb;
-    return launch_tiles(k_conv_dgrad_rows<7, true>, k_conv_dgrad_rows<6, false>, k_conv_dgrad_rows<4, false>,
-                        k_conv_dgrad_rows<2, false>, res, stage, res ? wbytes : 0, T, b, st);
+    return launch_tiles(tma ? k_conv_dgrad_rows<7, true, true> : k_conv_dgrad_rows<7, true>,
+                        k_conv_dgrad_rows<6, false>, k_conv_dgrad_rows<4, false>, k_conv_dgrad_rows<2, false>, res,
+                        stage, res ? wbytes : 0, T, b, tm, st);
   }
   int nb = std::min(256, a.Cin);
   size_t stage = 128 * kSlice * 2 + (size_t)nb * kSlice * 2;
@@ -1124,22 +1309,24 @@ static int wgrad_row_channels(int Cin, int Cout) {
 }
 
 // The row-tile weight gradient with S ring stages (2..7): each stage has its
-// own producer warp, so a deeper ring is also more warps copying at once.
-template <bool kSwap>
-static cudaError_t launch_wgrad_row(int S, dim3 grid, size_t smem, const ConvWgrad& a, cudaStream_t st) {
+// own producer warp, so a deeper ring is also more warps copying at once
+// (tensor-copy form: one issuing thread for all stages).
+template <bool kSwap, bool kTma>
+static cudaError_t launch_wgrad_row(int S, dim3 grid, size_t smem, const ConvWgrad& a, const CUtensorMap& ms,
+                                    const CUtensorMap& md, cudaStream_t st) {
   auto go = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e) return e;
-    kern<<<grid, kThreads, smem, st>>>(a);
+    kern<<<grid, kThreads, smem, st>>>(a, ms, md);
     return cudaGetLastError();
   };
   switch (S) {
-    case 7: return go(k_conv_wgrad_row<7, kSwap>);
-    case 6: return go(k_conv_wgrad_row<6, kSwap>);
-    case 5: return go(k_conv_wgrad_row<5, kSwap>);
-    case 4: return go(k_conv_wgrad_row<4, kSwap>);
-    case 3: return go(k_conv_wgrad_row<3, kSwap>);
-    default: return go(k_conv_wgrad_row<2, kSwap>);
+    case 7: return go(k_conv_wgrad_row<7, kSwap, kTma>);
+    case 6: return go(k_conv_wgrad_row<6, kSwap, kTma>);
+    case 5: return go(k_conv_wgrad_row<5, kSwap, kTma>);
+    case 4: return go(k_conv_wgrad_row<4, kSwap, kTma>);
+    case 3: return go(k_conv_wgrad_row<3, kSwap, kTma>);
+    default: return go(k_conv_wgrad_row<2, kSwap, kTma>);
   }
 }
 
@@ -1169,22 +1356,34 @@ cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
     const long long npg = std::max(1LL, ctas / nr);
     a.tiles_per_cta = (int)((T + npg - 1) / npg);
     const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
-    return launch_wgrad_row<true>(S, dim3(nr, gy), S * stage + a_over, a, st);
+    const CUtensorMap none{};
+    return launch_wgrad_row<true, false>(S, dim3(nr, gy), S * stage + a_over, a, none, none, st);
   }
   if (use_rows(a0.W, a0.Cin) && a0.Cout <= 128) {
     ConvWgrad a = a0;
     a.cr = wgrad_row_channels(a.Cin, a.Cout);
     const int nr = (a.Cin + a.cr - 1) / a.cr;
     a.tw = a.W >= 128 ? 128 : 64;
-    const size_t stage = (size_t)a.Cout * a.tw * 2 + (size_t)3 * (a.cr / 8) * (a.tw + 2) * 16;
-    // at most 4 stages here: deeper rings (narrower tiles, or more stages of
-    // the same tile) measured 0-10 % slower on these layers
-    const int S = std::max(2, std::min(4, stages(stage)));
+    // a single full-resolution source whose channels split evenly over the
+    // CTAs: the tensor-copy form, if both maps encode
+    CUtensorMap ms{}, md{};
+    const bool tma = kConvTma && !a.s2.ptr && !a.s1.up && a.Cin % a.cr == 0 &&
+                     chunk_major_map(&ms, a.s1.ptr, a.N, a.H, a.W, a.Cin, a.tw + 2, a.cr / 8, 3) &&
+                     chunk_major_map(&md, a.dout, 1, a.N * a.H, a.W, a.Cout, a.tw, a.Cout / 8, 1);
+    const size_t tx = (size_t)a.Cout * a.tw * 2 + (size_t)3 * (a.cr / 8) * (a.tw + 2) * 16;
+    const size_t stage = tma ? (tx + 1023) / 1024 * 1024 : tx;
     // the MMA's A operand spans 128 rows of TW pixels; rows past Cout are
     // read (and their accumulator lanes ignored), so they must lie inside the
     // allocation
     const size_t a_span = (size_t)256 * a.tw;
     size_t extra = a_span > stage ? a_span - stage : 0;
+    // at most 4 stages with producer warps: deeper rings (narrower tiles, or
+    // more stages of the same tile) measured 0-10 % slower on these layers.
+    // Tensor copies: as deep as fits, but not so deep that it costs the
+    // second CTA per SM that a 256-column accumulator allows.
+    int S = std::max(2, tma ? stages(stage) : std::min(4, stages(stage)));
+    if (tma && 9 * a.cr <= 256 && 2 * stage + extra <= 110 * 1024)
+      S = std::min(S, (int)((110 * 1024 - extra) / stage));
     const int per_sm = (9 * a.cr <= 256 && S * stage + extra <= 110 * 1024) ? 2 : 1;
     // one CTA per SM when it takes all 512 TMEM columns: a second CTA on the
     // SM would wait in its allocation for the first to finish
@@ -1194,7 +1393,8 @@ cudaError_t conv_wgrad(const ConvWgrad& a0, cudaStream_t st) {
     const long long npg = std::max(1LL, ctas / nr);
     a.tiles_per_cta = (int)((T + npg - 1) / npg);
     const unsigned gy = (unsigned)((T + a.tiles_per_cta - 1) / a.tiles_per_cta);
-    return launch_wgrad_row<false>(S, dim3(nr, gy), S * stage + extra, a, st);
+    if (tma) return launch_wgrad_row<false, true>(S, dim3(nr, gy), S * stage + extra, a, ms, md, st);
+    return launch_wgrad_row<false, false>(S, dim3(nr, gy), S * stage + extra, a, ms, md, st);
   }
   const ConvWgrad& a = a0;
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;

@@ -105,6 +105,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return mbar_wait_bounded(bar, parity, kWaitLimit);
 }
 
+// Arrive on the barrier and add `bytes` to the transaction count its phase
+// waits for (the bytes of the tensor copies that complete on it).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Tensor copy (TMA) of one box of a 5-D tensor map into shared memory at
+// dst, completing its bytes on `bar`.  The map is a __grid_constant__ kernel
+// parameter; c0 is the innermost coordinate (kept 16-byte aligned: 0 here).
+// Coordinates outside the tensor read zeros.
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const void* tmap, int c0, int c1, int c2, int c3, int c4,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+      "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // D (TMEM) [+]= A (smem desc) * B (smem desc)^T, one M x N x 16 step.
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          bool accumulate) {

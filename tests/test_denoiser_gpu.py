@@ -43,6 +43,10 @@ CASES = [  # N, H, W, C1, up1, C2, Cout, relu
     (1, 2, 96, 16, 0, 0, 16, 0),       # the output layer's shape
     (1, 2, 128, 96, 1, 64, 64, 1),     # 160 inputs: five weight-gradient channel ranges
     (8, 64, 256, 32, 0, 0, 32, 1),     # several row tiles per weight-gradient CTA (ring wraps)
+    # one full-resolution source: the weight gradient's tensor-copy form,
+    # over several channel ranges (chunk coordinates past 0)
+    (2, 4, 128, 64, 0, 0, 64, 1),      # e1b's shape: 2 ranges of 32 channels
+    (2, 5, 64, 96, 0, 0, 96, 1),       # e2b's shape: 2 ranges of 48 channels
     # narrow outputs from 64+ inputs: the weight gradient puts the source
     # channels on the accumulator lanes
     (2, 2, 128, 64, 1, 32, 32, 1),     # d0's shape: upsampled 64 + skip 32 -> 32
