@@ -94,10 +94,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cmds.append([_nvcc(), *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", *extra,
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3",
                      *inc, "-c", os.path.join(CSRC, f), "-o", o])
+    # macro definitions among the extra flags reach the host sources too, so
+    # that host and device code never disagree on a layout constant
+    host_defs = [f for f in os.environ.get("RTX_NVCC_FLAGS", "").split() if f.startswith(("-D", "-U"))]
     for f in cpp:
         o = os.path.join(OBJ, f + ".o")
         objs.append(o)
-        cmds.append(["g++", "-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-fopenmp",
+        cmds.append(["g++", "-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-fopenmp", *host_defs,
                      "-I" + os.path.join(CUDA_HOME, "include"), *inc, "-c",
                      os.path.join(CSRC, f), "-o", o])
     with cf.ThreadPoolExecutor(max_workers=min(8, len(cmds))) as ex:

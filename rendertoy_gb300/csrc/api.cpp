@@ -501,7 +501,7 @@ int rtx_get_stats(rtx_context* c, rtx_stats* out) {
   c->stats.shadow_tri_tests = h.sh_tri_tests;
   for (int d = 0; d < 16; ++d) c->stats.ext_rays_by_depth[d] = h.ext_rays_by_depth[d];
   // node visits count records of the tree in use: 4 x 16 B binary, 7 x 16 B 4-wide
-  c->stats.node_bytes = c->traversal == 2 ? 112 : 64;
+  c->stats.node_bytes = c->traversal == 2 ? 112 : 64;  // bytes a node visit reads
   RTX_CUDA(c->timer.collect(), "kernel timing");
   c->stats.extend_ms = c->timer.ms[0];
   c->stats.shade_ms = c->timer.ms[1];
@@ -725,10 +725,10 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
       std::memcpy(&n3.x, ch, 8);
       nodes.insert(nodes.end(), {n0, n1, n2, n3});
     }
-    // 4-wide nodes: seven float4, child references in the last one (empty
-    // slots hold 0 behind a box that is never hit)
-    int node4_base = (int)(nodes4.size() / 7);
-    for (size_t k = 0; k < h.b.nodes4.size(); k += 7) {
+    // 4-wide nodes: six float4 of planes, child references in the seventh
+    // (empty slots hold 0 behind a box that is never hit)
+    int node4_base = (int)(nodes4.size() / kNode4Vecs);
+    for (size_t k = 0; k < h.b.nodes4.size(); k += kNode4Vecs) {
       for (int r = 0; r < 6; ++r) nodes4.push_back(h.b.nodes4[k + r]);
       float4 m = h.b.nodes4[k + 6];
       int ch[4];

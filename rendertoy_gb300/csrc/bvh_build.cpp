@@ -216,8 +216,8 @@ struct Collapser {
 
   int collapse(int b, int depth) {
     max_depth = std::max(max_depth, depth);
-    int idx = (int)(out.size() / 7);
-    out.resize(out.size() + 7);
+    int idx = (int)(out.size() / kNode4Vecs);
+    out.resize(out.size() + kNode4Vecs);
     Child ch[4];
     int n = 2;
     ch[0] = child_of(b, 0);
@@ -237,7 +237,7 @@ struct Collapser {
     }
     int refs[4];
     for (int k = 0; k < 4; ++k) refs[k] = k < n ? (ch[k].ref >= 0 ? collapse(ch[k].ref, depth + 1) : ch[k].ref) : 0;
-    float4* nd = &out[7 * (size_t)idx];
+    float4* nd = &out[kNode4Vecs * (size_t)idx];
     float v[6][4];
     for (int k = 0; k < 4; ++k)
       for (int a = 0; a < 3; ++a) {
@@ -290,13 +290,13 @@ BvhBuildResult build_bvh(const float* verts, int n, int max_leaf) {
   res.depth = b.max_depth;
   if (res.root >= 0) {
     Collapser col{res.nodes, res.nodes4};
-    res.nodes4.reserve(res.nodes.size() * 7 / 4 / 2 + 7);
+    res.nodes4.reserve(res.nodes.size() * kNode4Vecs / 4 / 2 + kNode4Vecs);
     res.root4 = col.collapse(res.root, 0);
     res.depth4 = col.max_depth;
   } else {
     res.root4 = res.root;
   }
-  res.n_nodes4 = (int)(res.nodes4.size() / 7);
+  res.n_nodes4 = (int)(res.nodes4.size() / kNode4Vecs);
   res.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return res;
 }

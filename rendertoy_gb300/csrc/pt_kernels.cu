@@ -30,6 +30,7 @@
 namespace rtx {
 
 constexpr int kMaxDepthSlots = 64;
+constexpr int kCounterInts = 4 * kMaxDepthSlots;
 // material sort: at most this many materials (+1 bin for misses)
 constexpr int kMaxSortBins = 4096;
 // Minimum resident blocks of 128 threads per SM, i.e. the register budget
@@ -128,7 +129,7 @@ static cudaError_t ws_reserve(PtWorkspace* w, size_t cap) {
   if ((e = cudaMalloc(&w->mat_hist, 2 * (kMaxSortBins + 1) * sizeof(int))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->keys2, cap * sizeof(int))) != cudaSuccess) return e;
   if ((e = cudaMalloc(&w->mat_hist2, 2 * (kMaxSortBins + 1) * sizeof(int))) != cudaSuccess) return e;
-  if ((e = cudaMalloc(&w->counters, 4 * kMaxDepthSlots * sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&w->counters, kCounterInts * sizeof(int))) != cudaSuccess) return e;
   w->cap = cap;
   return cudaSuccess;
 }
@@ -934,7 +935,7 @@ RTX_DEV int ray_key(const DeviceScene& s, float4 o, float4 d) {
   if (s.root4 < 0) return 0;
   // scene bounds: the union of the 4-wide root's children (empty slots hold
   // planes at 1e30 and are skipped)
-  const float4* n = s.nodes4 + 7 * (size_t)s.root4;
+  const float4* n = s.nodes4 + kNode4Vecs * (size_t)s.root4;
   const float4 lx = __ldg(n), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3);
   const float4 lz = __ldg(n + 4), hz = __ldg(n + 5);
   const float big = 1e29f;
@@ -1338,7 +1339,7 @@ cudaError_t pt_render(PtWorkspace* ws, const DeviceScene& s, const CamParams& ca
     int nw = (int)std::min(wave, total - q0);
     a.q0 = q0;
     a.n_wave = nw;
-    if ((e = cudaMemsetAsync(ws->counters, 0, 4 * kMaxDepthSlots * sizeof(int), st))) return e;
+    if ((e = cudaMemsetAsync(ws->counters, 0, kCounterInts * sizeof(int), st))) return e;
     e = jobs ? wave_launches<true>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,
                                    extend_launches, vertex_launches, overlap)
              : wave_launches<false>(p, a, s, cam, prim, ws, timer, st, grid_ext, grid_con, grid_sh, block, nw, launches,

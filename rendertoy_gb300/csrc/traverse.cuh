@@ -358,7 +358,7 @@ RTX_DEV int trace4(const DeviceScene& s, F3 o, F3 d, int exclude, int target, fl
     if (node >= 0) {
       if (kCount) vc.nodes++;
       int c0, c1, c2, c3;
-      int nh = node4<!kAnyHit>(rb, s.nodes4 + 7 * (size_t)node, t, c0, c1, c2, c3);
+      int nh = node4<!kAnyHit>(rb, s.nodes4 + kNode4Vecs * (size_t)node, t, c0, c1, c2, c3);
       if (nh > 0) {
         if (sp + 3 > s.stack_limit) {
           atomicOr(err, kErrStackOverflow);
