@@ -35,10 +35,11 @@ constexpr int kCounterInts = 4 * kMaxDepthSlots;
 constexpr int kMaxSortBins = 4096;
 // Minimum resident blocks of 128 threads per SM, i.e. the register budget
 // (measured on the 1.3M-triangle frame: the traversal kernels are latency
-// bound and gain from more warps until spills begin; shading at 8 blocks
-// spills ~170 B yet beats 6 and 5 blocks by 3-7 %).
+// bound and gain from more warps until spills begin; shading, with the
+// lobe-set variants, is fastest at 7 blocks (72 registers): 1.7 % faster
+// than 8, 4 % faster than 6).
 #ifndef RTX_SHADE_MINB
-#define RTX_SHADE_MINB 8
+#define RTX_SHADE_MINB 7
 #endif
 #ifndef RTX_EXTEND_MINB
 #define RTX_EXTEND_MINB 10
