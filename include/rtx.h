@@ -101,11 +101,14 @@ enum rtx_option {
   RTX_OPT_GRAPH = 12,         /* 0/1: rtx_render_batch captures its launch
                                  sequence as a CUDA graph and replays it for
                                  later frames of the same shape */
-  RTX_OPT_SORT_RAYS = 13,     /* 0/1 (default 1): counting-sort the extension
-                                 rays after the primary ones and the shadow
-                                 rays by origin cell and direction octant
+  RTX_OPT_SORT_RAYS = 13,     /* 0 off, 1 on, 2 (default) on for scenes of
+                                 4,096 triangles or more: counting-sort the
+                                 extension rays after the primary ones and
+                                 the shadow rays by origin cell and direction
                                  before they are traced (results unchanged;
-                                 only the visiting order) */
+                                 only the visiting order; below ~4,000
+                                 triangles the tree sits in L1 and the sorts
+                                 cost more than they save) */
   RTX_OPT_STACK_LIMIT = 14,   /* traversal stack entries a ray may use, 2..64
                                  (default 64, the whole stack).  A ray that
                                  needs more stops, and the call returns
