@@ -320,3 +320,20 @@ def test_lobe_variants_agree(ctx):
                 assert same_bits(x, y), sc.name
     finally:
         ctx.upload(scenes.cornell_box())
+
+
+def test_ray_sort_auto_by_scene_size():
+    """RTX_OPT_SORT_RAYS defaults to 2 (sort when the scene has 4,096
+    triangles or more); a small and a large scene render the same bits with
+    the option at 0, 1 and 2."""
+    import rendertoy_gb300 as rt
+    from helpers import same_bits
+    with rt.Context(0) as c:
+        assert c.get_option(rt.OPT_SORT_RAYS) == 2
+        for sc in (scenes.cornell_box(), scenes.displaced_icosphere(subdiv=4)):
+            c.upload(sc)
+            out = []
+            for v in (2, 0, 1):
+                c.set_option(rt.OPT_SORT_RAYS, v)
+                out.append(c.render_pt(48, 40, 4, 8, seed=3))
+            assert same_bits(out[0], out[1]) and same_bits(out[0], out[2]), sc.name
