@@ -47,8 +47,21 @@ __device__ __forceinline__ void raw_rgb(const float* raw, long long pix, float* 
   c[2] = sane(r[2]);
 }
 
-// Softmax of the pixel's kKpTaps logits (max subtracted first).
-__device__ __forceinline__ void kp_weights(const float* __restrict__ logits, float* w) {
+// Softmax of the pixel's kKpTaps logits (max subtracted first); the logits
+// are read as seven 16-byte loads (the record is kPredCh = 32 floats, 128-byte
+// aligned).
+__device__ __forceinline__ void kp_weights(const float* __restrict__ logits_g, float* w) {
+  static_assert(kPredCh % 4 == 0 && kKpTaps <= 28 && kPredCh >= 28, "seven float4 of logits");
+  float logits[28];
+  const float4* l4 = reinterpret_cast<const float4*>(logits_g);
+#pragma unroll
+  for (int i = 0; i < 7; ++i) {
+    const float4 v = __ldg(l4 + i);
+    logits[4 * i] = v.x;
+    logits[4 * i + 1] = v.y;
+    logits[4 * i + 2] = v.z;
+    logits[4 * i + 3] = v.w;
+  }
   float m = logits[0];
 #pragma unroll
   for (int k = 1; k < kKpTaps; ++k) m = fmaxf(m, logits[k]);
@@ -181,11 +194,44 @@ __global__ void k_pool_grad_acc(const bf16* __restrict__ dpool, const bf16* __re
 // and channels is taken through the filter and the softmax to the logits
 // (dl_k = w_k (dw_k - sum_j w_j dw_j), dw_k = sum_c g_c r_c(tap k)), stored
 // as BF16 [P][kPredCh] (zero beyond the taps).
-__global__ void __launch_bounds__(256) k_kp_loss(const float* __restrict__ pred, const float* __restrict__ raw,
-                                                 const float* __restrict__ target, bf16* __restrict__ dpred,
-                                                 int N, int H, int W, double* loss) {
+// kTile (W a multiple of the 256-pixel block, so a block is one run of one
+// image row): the block first stages the RGB of its kKpWidth clamped rows x
+// (256 + kKpWidth - 1) clamped columns in shared memory, once, instead of
+// every pixel reading its 25 taps twice through L1.
+constexpr int kKpBlock = 256, kKpTileW = kKpBlock + kKpWidth - 1;
+
+template <bool kTile>
+__global__ void __launch_bounds__(kKpBlock) k_kp_loss(const float* __restrict__ pred, const float* __restrict__ raw,
+                                                      const float* __restrict__ target, bf16* __restrict__ dpred,
+                                                      int N, int H, int W, double* loss) {
+  __shared__ float tile[kTile ? kKpWidth : 1][kTile ? kKpTileW : 1][3];
   const long long P = (long long)N * H * W;
   long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (kTile) {
+    constexpr int r = kKpWidth / 2;
+    const long long pb = blockIdx.x * (long long)blockDim.x;
+    const int x0 = (int)(pb % W);
+    const long long qb = pb / W;
+    const int yb = (int)(qb % H);
+    const long long fb = (qb / H) * (long long)H * W;
+    for (int e = threadIdx.x; e < kKpWidth * kKpTileW; e += blockDim.x) {
+      const int rr = e / kKpTileW, cc = e - rr * kKpTileW;
+      const int ty = min(max(yb + rr - r, 0), H - 1), tx = min(max(x0 + cc - r, 0), W - 1);
+      raw_rgb(raw, fb + (long long)ty * W + tx, tile[rr][cc]);
+    }
+    __syncthreads();
+  }
+  // tap k of this pixel: from the staged tile, or through kp_tap
+  auto tap = [&](long long frame0, int x, int y, int k, float* c) {
+    if (kTile) {
+      const float* t = tile[k / kKpWidth][threadIdx.x + k % kKpWidth];
+      c[0] = t[0];
+      c[1] = t[1];
+      c[2] = t[2];
+    } else {
+      raw_rgb(raw, kp_tap(frame0, x, y, k, W, H, W), c);
+    }
+  };
   float part = 0.0f;
   if (p < P) {
     const int x = (int)(p % W);
@@ -198,7 +244,7 @@ __global__ void __launch_bounds__(256) k_kp_loss(const float* __restrict__ pred,
 #pragma unroll
     for (int k = 0; k < kKpTaps; ++k) {
       float c[3];
-      raw_rgb(raw, kp_tap(frame0, x, y, k, W, H, W), c);
+      tap(frame0, x, y, k, c);
       o[0] += w[k] * c[0];
       o[1] += w[k] * c[1];
       o[2] += w[k] * c[2];
@@ -215,7 +261,7 @@ __global__ void __launch_bounds__(256) k_kp_loss(const float* __restrict__ pred,
 #pragma unroll
     for (int k = 0; k < kKpTaps; ++k) {
       float c[3];
-      raw_rgb(raw, kp_tap(frame0, x, y, k, W, H, W), c);
+      tap(frame0, x, y, k, c);
       dw[k] = g[0] * c[0] + g[1] * c[1] + g[2] * c[2];
       s += w[k] * dw[k];
     }
@@ -391,7 +437,10 @@ cudaError_t pool_grad_acc(const bf16* dpool, const bf16* skip, bf16* dskip, int 
 }
 cudaError_t kp_loss(const float* pred, const float* raw, const float* target, bf16* dpred, int N, int H,
                     int W, double* loss, cudaStream_t st) {
-  k_kp_loss<<<blocks((long long)N * H * W), 256, 0, st>>>(pred, raw, target, dpred, N, H, W, loss);
+  if (W % kKpBlock == 0)
+    k_kp_loss<true><<<blocks((long long)N * H * W), kKpBlock, 0, st>>>(pred, raw, target, dpred, N, H, W, loss);
+  else
+    k_kp_loss<false><<<blocks((long long)N * H * W), kKpBlock, 0, st>>>(pred, raw, target, dpred, N, H, W, loss);
   return cudaGetLastError();
 }
 cudaError_t bias_grad(const bf16* dout, long long P, int C, float* db, cudaStream_t st) {
