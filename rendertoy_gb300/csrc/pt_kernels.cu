@@ -145,6 +145,10 @@ struct PtArgs {
   int *queue_in, *queue_out;
   const int* shadow_order = nullptr;  // occlusion: record visiting order (nullptr: record order)
   int *counts, *shadow_counts, *work;
+  // a single render's camera and per-pixel primary hits: the first shading
+  // launch makes its paths' camera rays itself (k_shade<.., kFirst>)
+  CamParams cam{};
+  const float4* prim = nullptr;
   int* err;
   Counters* ctr;
   long long q0;
@@ -411,16 +415,38 @@ static __device__ __noinline__ F3 log_extinction(F3 ext) {
 // kFeat: the scene's lobe set (kLobeTrans, kLobeCoat) | kShadeTex when some
 // material has a procedural texture
 constexpr int kShadeTex = 4;
-template <bool kJobs, int kFeat>
+// kFirst (single renders with the primary-hit cache): the wave's first
+// vertex, path i of the wave taking its camera ray and cached primary hit
+// directly -- the state k_raygen would have written and this launch would
+// have read back.
+template <bool kJobs, int kFeat, bool kFirst = false>
 __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_MINB) k_shade(PtArgs a, DeviceScene s) {
+  static_assert(!(kFirst && kJobs), "the first-vertex form serves single renders");
   constexpr bool kTex = (kFeat & kShadeTex) != 0;
   constexpr int kLobes = kFeat & kLobeAll;
-  int n = a.counts[a.depth];
+  const int n = kFirst ? a.n_wave : a.counts[a.depth];
+  if (kFirst && blockIdx.x == 0 && threadIdx.x == 0) a.counts[0] = a.n_wave;
   const int depth = a.depth;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int p = a.queue_in[i];
+    const int p = kFirst ? i : a.queue_in[i];
     const JobView J = job_of<kJobs>(a, s, a.q0 + p);
-    float4 ro = a.ray_o[p], rd = a.ray_d[p], h = a.hit[p], th = a.thr[p], rr = a.rad[p];
+    float4 ro, rd, h, th, rr;
+    if (kFirst) {
+      const int pix = (int)((a.q0 + p) % a.npix);
+      F3 co, cd;
+      camera_ray(a.cam, pix % a.W, pix / a.W, co, cd);
+      ro = make_float4(co.x, co.y, co.z, 0.0f);
+      rd = make_float4(cd.x, cd.y, cd.z, __int_as_float(-1));
+      h = __ldg(a.prim + pix);
+      th = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
+      rr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    } else {
+      ro = a.ray_o[p];
+      rd = a.ray_d[p];
+      h = a.hit[p];
+      th = a.thr[p];
+      rr = a.rad[p];
+    }
     F3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z);
     float last_pdf = ro.w;
     int tri = __float_as_int(h.x);
@@ -434,7 +460,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
       a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
       continue;
     }
-    float4 ab = a.absb[p];
+    float4 ab = kFirst ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : a.absb[p];
     F3 absorption = f3(ab.x, ab.y, ab.z);
     float t = h.y, u = h.z, v = h.w;
     float4 s0 = __ldg(s.shade + 4 * (size_t)tri), s1 = __ldg(s.shade + 4 * (size_t)tri + 1);
@@ -538,7 +564,22 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
 static int shade_features(const DeviceScene& s) { return (s.lobes & kLobeAll) | (s.textured ? kShadeTex : 0); }
 
 template <bool kJobs>
-static void launch_shade(int feat, dim3 grid, dim3 block, cudaStream_t st, const PtArgs& a, const DeviceScene& s) {
+static void launch_shade(int feat, dim3 grid, dim3 block, cudaStream_t st, const PtArgs& a, const DeviceScene& s,
+                         bool first = false) {
+  if constexpr (!kJobs) {
+    if (first) {
+      switch (feat) {
+        case 0: k_shade<false, 0, true><<<grid, block, 0, st>>>(a, s); return;
+        case 1: k_shade<false, 1, true><<<grid, block, 0, st>>>(a, s); return;
+        case 2: k_shade<false, 2, true><<<grid, block, 0, st>>>(a, s); return;
+        case 3: k_shade<false, 3, true><<<grid, block, 0, st>>>(a, s); return;
+        case 4: k_shade<false, 4, true><<<grid, block, 0, st>>>(a, s); return;
+        case 5: k_shade<false, 5, true><<<grid, block, 0, st>>>(a, s); return;
+        case 6: k_shade<false, 6, true><<<grid, block, 0, st>>>(a, s); return;
+        default: k_shade<false, 7, true><<<grid, block, 0, st>>>(a, s); return;
+      }
+    }
+  }
   switch (feat) {
     case 0: k_shade<kJobs, 0><<<grid, block, 0, st>>>(a, s); break;
     case 1: k_shade<kJobs, 1><<<grid, block, 0, st>>>(a, s); break;
@@ -1104,8 +1145,16 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
   a.queue_in = ws->queue[0];
   a.queue_out = ws->queue[1];
   a.depth = 0;
-  k_raygen<kJobs><<<(nw + 255) / 256, 256, 0, st>>>(a, cam, prim);
-  ++*launches;
+  // A single render with cached primary hits and path-order shading needs no
+  // path state before its first shading launch, which makes the camera rays
+  // itself; otherwise k_raygen writes the state (and the cached hits).
+  const bool first_in_shade = !kJobs && prim && !p.sort_material;
+  a.cam = cam;
+  a.prim = prim;
+  if (!first_in_shade) {
+    k_raygen<kJobs><<<(nw + 255) / 256, 256, 0, st>>>(a, cam, prim);
+    ++*launches;
+  }
   for (int depth = 0; depth < p.max_depth; ++depth) {
     a.depth = depth;
     a.queue_in = ws->queue[depth & 1];
@@ -1158,7 +1207,7 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
       as.queue_in = ws->sorted;
       launch_shade<kJobs>(shade_features(s), grid_sh, block, st, as, s);
     } else {
-      launch_shade<kJobs>(shade_features(s), grid_sh, block, st, a, s);
+      launch_shade<kJobs>(shade_features(s), grid_sh, block, st, a, s, first_in_shade && depth == 0);
     }
     if ((e = timer->mark(1, st, false))) return e;
     // The vertex's shadow rays: sorted and traced on the side stream, beside
