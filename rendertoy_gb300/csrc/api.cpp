@@ -164,6 +164,29 @@ static bool sort_rays_for(const rtx_context* c, int n_tris) {
   return c->sort_rays == 2 ? n_tris >= kSortRaysMinTris : c->sort_rays != 0;
 }
 
+// The ray sort's origin grids over the scene bounds: the union of the 4-wide
+// root's children (empty slots hold planes at 1e30 and are skipped), as the
+// device-side key computes it.
+static void set_sort_key_bounds(DeviceScene& s, const std::vector<float4>& nodes4, int root4) {
+  s.key_ok = 0;
+  if (root4 < 0 || nodes4.size() < (size_t)kNode4Vecs * (root4 + 1)) return;
+  const float4* n = &nodes4[(size_t)kNode4Vecs * root4];
+  const float big = 1e29f;
+  auto lo4 = [](float4 v) { return std::min(std::min(v.x, v.y), std::min(v.z, v.w)); };
+  auto hi4 = [&](float4 v) {
+    auto f = [&](float x) { return x < big ? x : -big; };
+    return std::max(std::max(f(v.x), f(v.y)), std::max(f(v.z), f(v.w)));
+  };
+  const float lo[3] = {lo4(n[0]), lo4(n[2]), lo4(n[4])}, hi[3] = {hi4(n[1]), hi4(n[3]), hi4(n[5])};
+  for (int k = 0; k < 3; ++k) {
+    const float ext = std::max(hi[k] - lo[k], 1e-20f);
+    s.key_lo[k] = lo[k];
+    s.key_inv4[k] = 4.0f / ext;
+    s.key_inv16[k] = 16.0f / ext;
+  }
+  s.key_ok = 1;
+}
+
 int begin(rtx_context* c) {
   RTX_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
   RTX_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream), "cudaMemsetAsync(err)");
@@ -672,6 +695,7 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
     s.ground[k] = ground[k];
   }
   s.stack_limit = c->stack_limit;
+  set_sort_key_bounds(s, b.nodes4, b.root4);
   c->has_scene = true;
   c->stats.bvh_build_ms = b.ms;
   c->stats.bvh_nodes = b.n_nodes;

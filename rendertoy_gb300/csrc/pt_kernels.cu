@@ -144,6 +144,10 @@ struct PtArgs {
   float4 *ray_o, *ray_d, *thr, *rad, *absb, *hit, *shadow;
   int *queue_in, *queue_out;
   const int* shadow_order = nullptr;  // occlusion: record visiting order (nullptr: record order)
+  // ray sort keys written by the shading kernel of a single render beside
+  // each new extension ray (at its slot of the next queue) and each shadow
+  // record (nullptr: the sort's histogram pass computes them)
+  int *ekeys = nullptr, *skeys = nullptr;
   int *counts, *shadow_counts, *work;
   // a single render's camera and per-pixel primary hits: the first shading
   // launch makes its paths' camera rays itself (k_shade<.., kFirst>)
@@ -399,6 +403,30 @@ __global__ void __launch_bounds__(64) k_primary_cache_job(DeviceScene s, const P
   primary_px(sj, J.cam, prim + J.pix_begin, err, ctr);
 }
 
+// Sort keys from the scene bounds the host computed (DeviceScene::key_*):
+// the same cells as ray_key, cheap enough to inline into the shading kernel
+// (the direction cell takes a fast reciprocal: a key only orders rays).
+template <int G>
+RTX_DEV uint32_t origin_cell(const DeviceScene& s, F3 o) {
+  const float* inv = G == 4 ? s.key_inv4 : s.key_inv16;
+  auto cell = [](float v, float a, float iv) { return (uint32_t)min(max((int)((v - a) * iv), 0), G - 1); };
+  auto spread = [](uint32_t v) { return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6); };
+  return spread(cell(o.x, s.key_lo[0], inv[0])) | (spread(cell(o.y, s.key_lo[1], inv[1])) << 1) |
+         (spread(cell(o.z, s.key_lo[2], inv[2])) << 2);
+}
+RTX_DEV int shadow_sort_key(const DeviceScene& s, F3 o) { return s.key_ok ? (int)origin_cell<16>(s, o) : 0; }
+RTX_DEV int ext_sort_key(const DeviceScene& s, F3 o, F3 d) {
+  if (!s.key_ok) return 0;
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  const bool fx = ax >= ay && ax >= az, fy = !fx && ay >= az;
+  const int face = fx ? (d.x < 0.0f) : (fy ? 2 + (d.y < 0.0f) : 4 + (d.z < 0.0f));
+  const float u = fx ? d.y : d.x, v = fx || fy ? d.z : d.y, mj = fx ? ax : (fy ? ay : az);
+  const float inv = __fdividef(1.0f, fmaxf(mj, 1e-30f));
+  const int cu = min(max((int)((u * inv + 1.0f) * 1.5f), 0), 2);
+  const int cv = min(max((int)((v * inv + 1.0f) * 1.5f), 0), 2);
+  return (int)((origin_cell<4>(s, o) << 6) | (uint32_t)(face * 9 + cu * 3 + cv));
+}
+
 // Beer-Lambert factors pow(e, -absorption * distance) per channel and the
 // log of a material's extinction: out of line, so that the shading kernel's
 // common path (no absorption, extinction 1) does not carry six inlined
@@ -523,6 +551,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
         r[1] = make_float4(emit_pos.x, emit_pos.y, emit_pos.z, __int_as_float(e));
         r[2] = make_float4(f.x, f.y, f.z, bpdf);
         r[3] = make_float4(tb.x, tb.y, tb.z, __int_as_float(tri));
+        if (!kJobs && a.skeys) a.skeys[slot] = shadow_sort_key(s, pos);
       }
     }
     float r1 = Rng::to_uniform(nee ? dv[3] : dv[0]);
@@ -556,6 +585,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
       a.absb[p] = make_float4(absorption.x, absorption.y, absorption.z, 0.0f);
       int slot = warp_append(a.counts + depth + 1);
       a.queue_out[slot] = p;
+      if (!kJobs && a.ekeys) a.ekeys[slot] = ext_sort_key(s, pos, nd);
     }
   }
 }
@@ -1047,14 +1077,29 @@ RTX_DEV int count_key(int* counter, int key) { return atomicAdd(counter + key, 1
 // flight at once.
 constexpr int kHistPer = 4;
 
-template <bool kJobs, bool kShadow>
+// kPre: the shading kernel already wrote the keys (single renders); only
+// their histogram is made here.
+template <bool kJobs, bool kShadow, bool kPre = false>
 __global__ void __launch_bounds__(256) k_raykey_hist(PtArgs a, DeviceScene s0, int* hist, int* keys) {
   __shared__ int sh[kRayKeyBins];
   for (int b = threadIdx.x; b < kRayKeyBins; b += blockDim.x) sh[b] = 0;
   __syncthreads();
   const int n = kShadow ? a.shadow_counts[a.depth] : a.counts[a.depth];
   const int step = gridDim.x * blockDim.x * kHistPer;
-  for (int base = blockIdx.x * blockDim.x * kHistPer; base < n; base += step) {
+  if (kPre) {
+    for (int base = blockIdx.x * blockDim.x * kHistPer; base < n; base += step) {
+      int k[kHistPer];
+#pragma unroll
+      for (int j = 0; j < kHistPer; ++j) {
+        const int i = base + j * blockDim.x + threadIdx.x;
+        k[j] = i < n ? keys[i] : -1;
+      }
+#pragma unroll
+      for (int j = 0; j < kHistPer; ++j)
+        if (k[j] >= 0) count_key(sh, k[j]);
+    }
+  }
+  for (int base = blockIdx.x * blockDim.x * kHistPer; !kPre && base < n; base += step) {
     int idx[kHistPer], path[kHistPer];
     float4 o[kHistPer], d[kHistPer];
 #pragma unroll
@@ -1151,6 +1196,11 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
   const bool first_in_shade = !kJobs && prim && !p.sort_material;
   a.cam = cam;
   a.prim = prim;
+  // single renders with ray sorting: the shading kernel writes the
+  // extension rays' keys to `keys` and the shadow records' to `keys2`; each
+  // is read by its sort before the next shading launch writes it again
+  a.ekeys = !kJobs && p.sort_rays ? ws->keys : nullptr;
+  a.skeys = !kJobs && p.sort_rays ? ws->keys2 : nullptr;
   if (!first_in_shade) {
     k_raygen<kJobs><<<(nw + 255) / 256, 256, 0, st>>>(a, cam, prim);
     ++*launches;
@@ -1163,7 +1213,10 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
     if (p.sort_rays && depth > 0) {
       static_assert(kRayKeyBins <= kMaxSortBins, "ray keys use the sort histogram");
       if ((e = cudaMemsetAsync(ws->mat_hist, 0, (kMaxSortBins + 1) * sizeof(int), st))) return e;
-      k_raykey_hist<kJobs, false><<<grid_sh, 256, 0, st>>>(a, s, ws->mat_hist, ws->keys);
+      if (a.ekeys)
+        k_raykey_hist<kJobs, false, true><<<grid_sh, 256, 0, st>>>(a, s, ws->mat_hist, ws->keys);
+      else
+        k_raykey_hist<kJobs, false><<<grid_sh, 256, 0, st>>>(a, s, ws->mat_hist, ws->keys);
       k_sort_scan<<<1, 1024, 0, st>>>(kRayKeyBins, ws->mat_hist);
       k_raykey_scatter<false><<<grid_sh, 256, 0, st>>>(a, ws->keys, ws->mat_hist, ws->ray_sorted);
       *launches += 3;
@@ -1214,7 +1267,9 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
     // the next vertex's sort and closest-hit launch, which touch neither the
     // shadow records nor the radiance.
     cudaStream_t cs = st;
-    int* skeys = ws->keys;
+    // shadow keys: written by the shading kernel into keys2, or made by the
+    // histogram pass (keys2 beside the overlap's next closest-hit sort)
+    int* skeys = a.skeys ? ws->keys2 : ws->keys;
     int* shist = ws->mat_hist;
     if (overlap) {
       if ((e = cudaEventRecord(ws->ev_shaded, st))) return e;
@@ -1226,7 +1281,10 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
     a.shadow_order = nullptr;
     if (p.sort_rays) {
       if ((e = cudaMemsetAsync(shist, 0, (kMaxSortBins + 1) * sizeof(int), cs))) return e;
-      k_raykey_hist<kJobs, true><<<grid_sh, 256, 0, cs>>>(a, s, shist, skeys);
+      if (a.skeys)
+        k_raykey_hist<kJobs, true, true><<<grid_sh, 256, 0, cs>>>(a, s, shist, skeys);
+      else
+        k_raykey_hist<kJobs, true><<<grid_sh, 256, 0, cs>>>(a, s, shist, skeys);
       k_sort_scan<<<1, 1024, 0, cs>>>(kRayKeyBins, shist);
       k_raykey_scatter<true><<<grid_sh, 256, 0, cs>>>(a, skeys, shist, ws->shadow_order);
       *launches += 3;

@@ -84,6 +84,11 @@ struct DeviceScene {
   // traversal stack entries a ray may use before it reports kErrStackOverflow
   // (kStackSize; lower only through RTX_OPT_STACK_LIMIT, to exercise that path)
   int stack_limit = kStackSize;
+  // ray sort keys (single renders): the scene bounds' low corner and the
+  // cells per unit length of the 4^3 and 16^3 origin grids; key_ok = 0 when
+  // the tree has no inner root (every key 0)
+  float key_lo[3] = {0.0f, 0.0f, 0.0f}, key_inv4[3] = {0.0f, 0.0f, 0.0f}, key_inv16[3] = {0.0f, 0.0f, 0.0f};
+  int key_ok = 0;
 };
 
 // Camera reduced to what ray generation needs (src/renderer.cpp:103-124,
