@@ -488,7 +488,11 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
       a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
       continue;
     }
-    float4 ab = kFirst ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : a.absb[p];
+    // bit 31 of the RNG counter word: the path carries an absorption that
+    // is not +-0 (only then was it stored); +-0 reads as +0, which gives
+    // the same transmittance (pow(e, +-0) = 1, and +-0 * inf = NaN either way)
+    const uint32_t thw = __float_as_uint(th.w);
+    float4 ab = (kFirst || !(thw >> 31)) ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : a.absb[p];
     F3 absorption = f3(ab.x, ab.y, ab.z);
     float t = h.y, u = h.z, v = h.w;
     float4 s0 = __ldg(s.shade + 4 * (size_t)tri), s1 = __ldg(s.shade + 4 * (size_t)tri + 1);
@@ -523,7 +527,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
 
     long long q = J.q;
     Rng rng{J.k0, J.k1, (uint32_t)(q % J.npix), (uint32_t)(J.first_sample + q / J.npix),
-            __float_as_uint(th.w)};
+            thw & 0x7fffffffu};
     // the vertex's draws, in the reference's order: Int (emitter), Float,
     // Float (point on it) when there are emitters, then Float, Float (BSDF)
     uint32_t dv[5];
@@ -581,8 +585,9 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
     if (cont) {
       a.ray_o[p] = make_float4(pos.x, pos.y, pos.z, pdf);
       a.ray_d[p] = make_float4(nd.x, nd.y, nd.z, __int_as_float(tri));
-      a.thr[p] = make_float4(T.x, T.y, T.z, __uint_as_float(rng.draw));
-      a.absb[p] = make_float4(absorption.x, absorption.y, absorption.z, 0.0f);
+      const bool ab_zero = absorption.x == 0.0f && absorption.y == 0.0f && absorption.z == 0.0f;
+      a.thr[p] = make_float4(T.x, T.y, T.z, __uint_as_float(rng.draw | (ab_zero ? 0u : 0x80000000u)));
+      if (!ab_zero) a.absb[p] = make_float4(absorption.x, absorption.y, absorption.z, 0.0f);
       int slot = warp_append(a.counts + depth + 1);
       a.queue_out[slot] = p;
       if (!kJobs && a.ekeys) a.ekeys[slot] = ext_sort_key(s, pos, nd);

@@ -337,3 +337,25 @@ def test_ray_sort_auto_by_scene_size():
                 c.set_option(rt.OPT_SORT_RAYS, v)
                 out.append(c.render_pt(48, 40, 4, 8, seed=3))
             assert same_bits(out[0], out[1]) and same_bits(out[0], out[2]), sc.name
+
+
+def test_absorbing_media(ctx, oracle):
+    """Beer-Lambert absorption inside refracting materials (extinction != 1,
+    RenderToy's renderer.cpp:293, 311, 319): per-path radiance against the oracle
+    in the mixed-lobe room with its glass made absorbing."""
+    sc = scenes.cornell_mixed()
+    glass = sc.mats[:, 15] > 0  # spec_trans: the refracting materials
+    assert glass.any()
+    sc.mats[glass, 17] = 80.0                       # at_distance
+    sc.mats[glass, 18:21] = (0.35, 0.6, 0.85)       # extinction per channel
+    ctx.upload(sc)
+    got = ctx.trace_paths(24, 20, 0, 4, 10, seed=7)
+    ref = oracle.scene(sc).trace_paths(24, 20, 0, 4, 10, 7)
+    close = rel_close(got, ref, 1e-4, 1e-6).all(-1)
+    assert close.mean() >= 0.99, close.mean()
+    # the absorption actually entered some paths: their radiance differs
+    # from the same room without it
+    sc2 = scenes.cornell_mixed()
+    ctx.upload(sc2)
+    plain = ctx.trace_paths(24, 20, 0, 4, 10, seed=7)
+    assert (np.abs(plain - got) > 1e-6).any()
