@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int p = kFirst ? i : a.queue_in[i];
     const JobView J = job_of<kJobs>(a, s, a.q0 + p);
-    float4 ro, rd, h, th, rr;
+    float4 ro, rd, h, th;
     if (kFirst) {
       const int pix = (int)((a.q0 + p) % a.npix);
       F3 co, cd;
@@ -467,25 +467,38 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
       rd = make_float4(cd.x, cd.y, cd.z, __int_as_float(-1));
       h = __ldg(a.prim + pix);
       th = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
-      rr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     } else {
       ro = a.ray_o[p];
       rd = a.ray_d[p];
       h = a.hit[p];
       th = a.thr[p];
-      rr = a.rad[p];
     }
     F3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z);
     float last_pdf = ro.w;
     int tri = __float_as_int(h.x);
     F3 T = f3(th.x, th.y, th.z);
-    F3 acc = f3(rr.x, rr.y, rr.z);
+    // The path's radiance is read and written back only when this vertex
+    // adds a term that is not exactly zero: the sum starts at +0 and never
+    // becomes -0 (x + y is -0 only when both are), so adding +-0 leaves it
+    // unchanged, bit for bit; a NaN term is added.  The first vertex always
+    // writes it (no earlier value exists).
+    F3 acc = f3s(0.0f);
+    bool touched = kFirst;
+    auto add_rad = [&](F3 x) {
+      if (x.x == 0.0f && x.y == 0.0f && x.z == 0.0f) return;
+      if (!touched) {
+        const float4 r0 = a.rad[p];
+        acc = f3(r0.x, r0.y, r0.z);
+        touched = true;
+      }
+      acc = acc + x;
+    };
     if (tri < 0) {
       // World::GetDefaultEmission (world.cpp:39-42) of -direction
       F3 env = (-d.z < 0.0f) ? f3(J.sky[0], J.sky[1], J.sky[2])
                              : f3(J.ground[0], J.ground[1], J.ground[2]);
-      acc = acc + T * env;
-      a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+      add_rad(T * env);
+      if (touched) a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
       continue;
     }
     // bit 31 of the RNG counter word: the path carries an absorption that
@@ -518,7 +531,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
     float self_pdf = fabsf(d2 / cos_area);
     F3 E = m.emission;
     if (depth > 0) E = E * PowerHeuristic(last_pdf, self_pdf);
-    acc = acc + T * E;
+    add_rad(T * E);
     float dist = length(pos - o);
     F3 expo = (-absorption) * dist;
     // pow(e, +-0) is exactly 1: no call for the common no-absorption case
@@ -577,11 +590,11 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
         } else {
           // the reference multiplies by the (zero) radiance beyond the cap,
           // which keeps an infinite or NaN weight visible as NaN
-          acc = acc + T * (w * 0.0f);
+          add_rad(T * (w * 0.0f));
         }
       }
     }
-    a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+    if (touched) a.rad[p] = make_float4(acc.x, acc.y, acc.z, 0.0f);
     if (cont) {
       a.ray_o[p] = make_float4(pos.x, pos.y, pos.z, pdf);
       a.ray_d[p] = make_float4(nd.x, nd.y, nd.z, __int_as_float(tri));
