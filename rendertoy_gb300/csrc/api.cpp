@@ -105,6 +105,7 @@ struct rtx_context {
   struct BatchScene {
     int root, root4, e_begin, n_emitters, n_tris;
     float sky[3], ground[3];
+    SortKeyBounds keyb;
   };
   bool has_batch = false;
   DeviceScene bds{};
@@ -164,12 +165,12 @@ static bool sort_rays_for(const rtx_context* c, int n_tris) {
   return c->sort_rays == 2 ? n_tris >= kSortRaysMinTris : c->sort_rays != 0;
 }
 
-// The ray sort's origin grids over the scene bounds: the union of the 4-wide
+// The ray sort's origin grids over a scene's bounds: the union of its 4-wide
 // root's children (empty slots hold planes at 1e30 and are skipped), as the
-// device-side key computes it.
-static void set_sort_key_bounds(DeviceScene& s, const std::vector<float4>& nodes4, int root4) {
-  s.key_ok = 0;
-  if (root4 < 0 || nodes4.size() < (size_t)kNode4Vecs * (root4 + 1)) return;
+// device-side key of the sort's histogram pass computes it.
+static SortKeyBounds sort_key_bounds(const std::vector<float4>& nodes4, int root4) {
+  SortKeyBounds kb;
+  if (root4 < 0 || nodes4.size() < (size_t)kNode4Vecs * (root4 + 1)) return kb;
   const float4* n = &nodes4[(size_t)kNode4Vecs * root4];
   const float big = 1e29f;
   auto lo4 = [](float4 v) { return std::min(std::min(v.x, v.y), std::min(v.z, v.w)); };
@@ -180,11 +181,12 @@ static void set_sort_key_bounds(DeviceScene& s, const std::vector<float4>& nodes
   const float lo[3] = {lo4(n[0]), lo4(n[2]), lo4(n[4])}, hi[3] = {hi4(n[1]), hi4(n[3]), hi4(n[5])};
   for (int k = 0; k < 3; ++k) {
     const float ext = std::max(hi[k] - lo[k], 1e-20f);
-    s.key_lo[k] = lo[k];
-    s.key_inv4[k] = 4.0f / ext;
-    s.key_inv16[k] = 16.0f / ext;
+    kb.lo[k] = lo[k];
+    kb.inv4[k] = 4.0f / ext;
+    kb.inv16[k] = 16.0f / ext;
   }
-  s.key_ok = 1;
+  kb.ok = 1;
+  return kb;
 }
 
 int begin(rtx_context* c) {
@@ -695,7 +697,7 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
     s.ground[k] = ground[k];
   }
   s.stack_limit = c->stack_limit;
-  set_sort_key_bounds(s, b.nodes4, b.root4);
+  s.keyb = sort_key_bounds(b.nodes4, b.root4);
   c->has_scene = true;
   c->stats.bvh_build_ms = b.ms;
   c->stats.bvh_nodes = b.n_nodes;
@@ -804,6 +806,7 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
       bs.n_emitters = (int)h.emitters.size();
     }
     bs.n_tris = h.n_tris;
+    bs.keyb = sort_key_bounds(h.b.nodes4, h.b.root4);
     for (int k = 0; k < 3; ++k) {
       bs.sky[k] = h.sky[k];
       bs.ground[k] = h.ground[k];
@@ -1070,6 +1073,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
       P.ground[k] = bs.ground[k];
     }
     P.cam = make_cam_params(J.camera, J.W, J.H);
+    P.keyb = bs.keyb;
     q += (long long)P.npix * J.spp;
     pix += P.npix;
   }

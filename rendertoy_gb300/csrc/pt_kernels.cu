@@ -144,13 +144,14 @@ struct PtArgs {
   float4 *ray_o, *ray_d, *thr, *rad, *absb, *hit, *shadow;
   int *queue_in, *queue_out;
   const int* shadow_order = nullptr;  // occlusion: record visiting order (nullptr: record order)
-  // ray sort keys written by the shading kernel of a single render beside
-  // each new extension ray (at its slot of the next queue) and each shadow
-  // record (nullptr: the sort's histogram pass computes them)
+  // ray sort keys written by the shading kernel beside each new extension
+  // ray (at its slot of the next queue) and each shadow record (nullptr: the
+  // sort's histogram pass computes them)
   int *ekeys = nullptr, *skeys = nullptr;
   int *counts, *shadow_counts, *work;
-  // a single render's camera and per-pixel primary hits: the first shading
-  // launch makes its paths' camera rays itself (k_shade<.., kFirst>)
+  // a single render's camera (batches: each frame's, in its job) and the
+  // per-pixel primary hits: the first shading launch makes its paths'
+  // camera rays itself (k_shade<.., kFirst>)
   CamParams cam{};
   const float4* prim = nullptr;
   int* err;
@@ -168,6 +169,7 @@ struct PtArgs {
 // and the render's own; in a batch those of q's frame (binary search on the
 // frames' first paths).
 struct JobView {
+  int job;  // the frame's index in the job table (batches; 0 otherwise)
   int root, root4, n_emitters;
   const int* emitters;
   float sky[3], ground[3];
@@ -193,6 +195,7 @@ RTX_DEV int job_index(const PtArgs& a, long long q) {
 template <bool kJobs>
 RTX_DEV JobView job_of(const PtArgs& a, const DeviceScene& s, long long q) {
   JobView v;
+  v.job = 0;
   if (!kJobs) {
     v.root = s.root;
     v.root4 = s.root4;
@@ -208,7 +211,8 @@ RTX_DEV JobView job_of(const PtArgs& a, const DeviceScene& s, long long q) {
     v.npix = a.npix;
     v.first_sample = a.first_sample;
   } else {
-    const PtJob& J = a.jobs[job_index<true>(a, q)];
+    v.job = job_index<true>(a, q);
+    const PtJob& J = a.jobs[v.job];
     v.root = J.root;
     v.root4 = J.root4;
     v.n_emitters = J.n_emitters;
@@ -403,20 +407,20 @@ __global__ void __launch_bounds__(64) k_primary_cache_job(DeviceScene s, const P
   primary_px(sj, J.cam, prim + J.pix_begin, err, ctr);
 }
 
-// Sort keys from the scene bounds the host computed (DeviceScene::key_*):
+// Sort keys from the scene bounds the host computed (SortKeyBounds):
 // the same cells as ray_key, cheap enough to inline into the shading kernel
 // (the direction cell takes a fast reciprocal: a key only orders rays).
 template <int G>
-RTX_DEV uint32_t origin_cell(const DeviceScene& s, F3 o) {
-  const float* inv = G == 4 ? s.key_inv4 : s.key_inv16;
+RTX_DEV uint32_t origin_cell(const SortKeyBounds& kb, F3 o) {
+  const float* inv = G == 4 ? kb.inv4 : kb.inv16;
   auto cell = [](float v, float a, float iv) { return (uint32_t)min(max((int)((v - a) * iv), 0), G - 1); };
   auto spread = [](uint32_t v) { return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6); };
-  return spread(cell(o.x, s.key_lo[0], inv[0])) | (spread(cell(o.y, s.key_lo[1], inv[1])) << 1) |
-         (spread(cell(o.z, s.key_lo[2], inv[2])) << 2);
+  return spread(cell(o.x, kb.lo[0], inv[0])) | (spread(cell(o.y, kb.lo[1], inv[1])) << 1) |
+         (spread(cell(o.z, kb.lo[2], inv[2])) << 2);
 }
-RTX_DEV int shadow_sort_key(const DeviceScene& s, F3 o) { return s.key_ok ? (int)origin_cell<16>(s, o) : 0; }
-RTX_DEV int ext_sort_key(const DeviceScene& s, F3 o, F3 d) {
-  if (!s.key_ok) return 0;
+RTX_DEV int shadow_sort_key(const SortKeyBounds& kb, F3 o) { return kb.ok ? (int)origin_cell<16>(kb, o) : 0; }
+RTX_DEV int ext_sort_key(const SortKeyBounds& kb, F3 o, F3 d) {
+  if (!kb.ok) return 0;
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   const bool fx = ax >= ay && ax >= az, fy = !fx && ay >= az;
   const int face = fx ? (d.x < 0.0f) : (fy ? 2 + (d.y < 0.0f) : 4 + (d.z < 0.0f));
@@ -424,7 +428,7 @@ RTX_DEV int ext_sort_key(const DeviceScene& s, F3 o, F3 d) {
   const float inv = __fdividef(1.0f, fmaxf(mj, 1e-30f));
   const int cu = min(max((int)((u * inv + 1.0f) * 1.5f), 0), 2);
   const int cv = min(max((int)((v * inv + 1.0f) * 1.5f), 0), 2);
-  return (int)((origin_cell<4>(s, o) << 6) | (uint32_t)(face * 9 + cu * 3 + cv));
+  return (int)((origin_cell<4>(kb, o) << 6) | (uint32_t)(face * 9 + cu * 3 + cv));
 }
 
 // Beer-Lambert factors pow(e, -absorption * distance) per channel and the
@@ -443,13 +447,12 @@ static __device__ __noinline__ F3 log_extinction(F3 ext) {
 // kFeat: the scene's lobe set (kLobeTrans, kLobeCoat) | kShadeTex when some
 // material has a procedural texture
 constexpr int kShadeTex = 4;
-// kFirst (single renders with the primary-hit cache): the wave's first
-// vertex, path i of the wave taking its camera ray and cached primary hit
-// directly -- the state k_raygen would have written and this launch would
-// have read back.
+// kFirst (renders with the primary-hit cache): the wave's first vertex,
+// path i of the wave taking its camera ray and cached primary hit directly
+// -- the state k_raygen would have written and this launch would have read
+// back.
 template <bool kJobs, int kFeat, bool kFirst = false>
 __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_MINB) k_shade(PtArgs a, DeviceScene s) {
-  static_assert(!(kFirst && kJobs), "the first-vertex form serves single renders");
   constexpr bool kTex = (kFeat & kShadeTex) != 0;
   constexpr int kLobes = kFeat & kLobeAll;
   const int n = kFirst ? a.n_wave : a.counts[a.depth];
@@ -460,12 +463,15 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
     const JobView J = job_of<kJobs>(a, s, a.q0 + p);
     float4 ro, rd, h, th;
     if (kFirst) {
-      const int pix = (int)((a.q0 + p) % a.npix);
+      // the frame's pixel of the path, as k_raygen numbers it
+      const PtJob* pj = kJobs ? a.jobs + J.job : nullptr;
+      const int pix = kJobs ? (int)(J.q % pj->npix) : (int)((a.q0 + p) % a.npix);
+      const int W = kJobs ? pj->W : a.W;
       F3 co, cd;
-      camera_ray(a.cam, pix % a.W, pix / a.W, co, cd);
+      camera_ray(kJobs ? pj->cam : a.cam, pix % W, pix / W, co, cd);
       ro = make_float4(co.x, co.y, co.z, 0.0f);
       rd = make_float4(cd.x, cd.y, cd.z, __int_as_float(-1));
-      h = __ldg(a.prim + pix);
+      h = __ldg(a.prim + (kJobs ? pj->pix_begin : 0) + pix);
       th = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(0u));
     } else {
       ro = a.ray_o[p];
@@ -568,7 +574,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
         r[1] = make_float4(emit_pos.x, emit_pos.y, emit_pos.z, __int_as_float(e));
         r[2] = make_float4(f.x, f.y, f.z, bpdf);
         r[3] = make_float4(tb.x, tb.y, tb.z, __int_as_float(tri));
-        if (!kJobs && a.skeys) a.skeys[slot] = shadow_sort_key(s, pos);
+        if (a.skeys) a.skeys[slot] = shadow_sort_key(kJobs ? a.jobs[J.job].keyb : s.keyb, pos);
       }
     }
     float r1 = Rng::to_uniform(nee ? dv[3] : dv[0]);
@@ -603,7 +609,7 @@ __global__ void __launch_bounds__(128, kJobs ? RTX_SHADE_MINB_JOBS : RTX_SHADE_M
       if (!ab_zero) a.absb[p] = make_float4(absorption.x, absorption.y, absorption.z, 0.0f);
       int slot = warp_append(a.counts + depth + 1);
       a.queue_out[slot] = p;
-      if (!kJobs && a.ekeys) a.ekeys[slot] = ext_sort_key(s, pos, nd);
+      if (a.ekeys) a.ekeys[slot] = ext_sort_key(kJobs ? a.jobs[J.job].keyb : s.keyb, pos, nd);
     }
   }
 }
@@ -614,18 +620,16 @@ static int shade_features(const DeviceScene& s) { return (s.lobes & kLobeAll) | 
 template <bool kJobs>
 static void launch_shade(int feat, dim3 grid, dim3 block, cudaStream_t st, const PtArgs& a, const DeviceScene& s,
                          bool first = false) {
-  if constexpr (!kJobs) {
-    if (first) {
-      switch (feat) {
-        case 0: k_shade<false, 0, true><<<grid, block, 0, st>>>(a, s); return;
-        case 1: k_shade<false, 1, true><<<grid, block, 0, st>>>(a, s); return;
-        case 2: k_shade<false, 2, true><<<grid, block, 0, st>>>(a, s); return;
-        case 3: k_shade<false, 3, true><<<grid, block, 0, st>>>(a, s); return;
-        case 4: k_shade<false, 4, true><<<grid, block, 0, st>>>(a, s); return;
-        case 5: k_shade<false, 5, true><<<grid, block, 0, st>>>(a, s); return;
-        case 6: k_shade<false, 6, true><<<grid, block, 0, st>>>(a, s); return;
-        default: k_shade<false, 7, true><<<grid, block, 0, st>>>(a, s); return;
-      }
+  if (first) {
+    switch (feat) {
+      case 0: k_shade<kJobs, 0, true><<<grid, block, 0, st>>>(a, s); return;
+      case 1: k_shade<kJobs, 1, true><<<grid, block, 0, st>>>(a, s); return;
+      case 2: k_shade<kJobs, 2, true><<<grid, block, 0, st>>>(a, s); return;
+      case 3: k_shade<kJobs, 3, true><<<grid, block, 0, st>>>(a, s); return;
+      case 4: k_shade<kJobs, 4, true><<<grid, block, 0, st>>>(a, s); return;
+      case 5: k_shade<kJobs, 5, true><<<grid, block, 0, st>>>(a, s); return;
+      case 6: k_shade<kJobs, 6, true><<<grid, block, 0, st>>>(a, s); return;
+      default: k_shade<kJobs, 7, true><<<grid, block, 0, st>>>(a, s); return;
     }
   }
   switch (feat) {
@@ -1208,17 +1212,18 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
   a.queue_in = ws->queue[0];
   a.queue_out = ws->queue[1];
   a.depth = 0;
-  // A single render with cached primary hits and path-order shading needs no
-  // path state before its first shading launch, which makes the camera rays
+  // A render with cached primary hits and path-order shading needs no path
+  // state before its first shading launch, which makes the camera rays
   // itself; otherwise k_raygen writes the state (and the cached hits).
-  const bool first_in_shade = !kJobs && prim && !p.sort_material;
+  const bool first_in_shade = prim && !p.sort_material;
   a.cam = cam;
   a.prim = prim;
-  // single renders with ray sorting: the shading kernel writes the
-  // extension rays' keys to `keys` and the shadow records' to `keys2`; each
-  // is read by its sort before the next shading launch writes it again
-  a.ekeys = !kJobs && p.sort_rays ? ws->keys : nullptr;
-  a.skeys = !kJobs && p.sort_rays ? ws->keys2 : nullptr;
+  // with ray sorting, the shading kernel writes the extension rays' keys to
+  // `keys` and the shadow records' to `keys2` (from each frame's scene
+  // grids); each is read by its sort before the next shading launch writes
+  // it again
+  a.ekeys = p.sort_rays ? ws->keys : nullptr;
+  a.skeys = p.sort_rays ? ws->keys2 : nullptr;
   if (!first_in_shade) {
     k_raygen<kJobs><<<(nw + 255) / 256, 256, 0, st>>>(a, cam, prim);
     ++*launches;

@@ -66,6 +66,14 @@ inline int material_lobes(const float* mats, int n) {
   return r;
 }
 
+// The ray sort's origin grids over a scene: its bounds' low corner and the
+// cells per unit length of the 4^3 and 16^3 grids; ok = 0 when the tree has
+// no inner root (every key 0)
+struct SortKeyBounds {
+  float lo[3] = {0.0f, 0.0f, 0.0f}, inv4[3] = {0.0f, 0.0f, 0.0f}, inv16[3] = {0.0f, 0.0f, 0.0f};
+  int ok = 0;
+};
+
 struct DeviceScene {
   const float4* __restrict__ nodes;
   const float4* __restrict__ nodes4;
@@ -84,11 +92,7 @@ struct DeviceScene {
   // traversal stack entries a ray may use before it reports kErrStackOverflow
   // (kStackSize; lower only through RTX_OPT_STACK_LIMIT, to exercise that path)
   int stack_limit = kStackSize;
-  // ray sort keys (single renders): the scene bounds' low corner and the
-  // cells per unit length of the 4^3 and 16^3 origin grids; key_ok = 0 when
-  // the tree has no inner root (every key 0)
-  float key_lo[3] = {0.0f, 0.0f, 0.0f}, key_inv4[3] = {0.0f, 0.0f, 0.0f}, key_inv16[3] = {0.0f, 0.0f, 0.0f};
-  int key_ok = 0;
+  SortKeyBounds keyb;  // the ray sort's origin grids over this scene
 };
 
 // Camera reduced to what ray generation needs (src/renderer.cpp:103-124,
@@ -183,6 +187,7 @@ struct PtJob {
   uint32_t k0, k1;
   float sky[3], ground[3];
   CamParams cam;
+  SortKeyBounds keyb;  // the frame's scene's ray sort grids
 };
 
 struct PtParams {
