@@ -145,8 +145,8 @@ struct PtArgs {
   int *queue_in, *queue_out;
   const int* shadow_order = nullptr;  // occlusion: record visiting order (nullptr: record order)
   // ray sort keys written by the shading kernel beside each new extension
-  // ray (at its slot of the next queue) and each shadow record (nullptr: the
-  // sort's histogram pass computes them)
+  // ray (at its slot of the next queue) and each shadow record (nullptr:
+  // rays not sorted)
   int *ekeys = nullptr, *skeys = nullptr;
   int *counts, *shadow_counts, *work;
   // a single render's camera (batches: each frame's, in its job) and the
@@ -407,9 +407,14 @@ __global__ void __launch_bounds__(64) k_primary_cache_job(DeviceScene s, const P
   primary_px(sj, J.cam, prim + J.pix_begin, err, ctr);
 }
 
-// Sort keys from the scene bounds the host computed (SortKeyBounds):
-// the same cells as ray_key, cheap enough to inline into the shading kernel
-// (the direction cell takes a fast reciprocal: a key only orders rays).
+// Sort keys (12 bits, 4,096 bins) from the scene bounds the host computed
+// (SortKeyBounds).  Extension rays: the Morton code of the origin's cell in
+// a 4^3 grid, then the direction's cube face (major axis and sign) and its
+// 3 x 3 cell on that face; shadow rays (which all head for the lights, so the
+// origin says most about the path): the origin's cell in a 16^3 grid
+// (measured against 8^3 cells + octant for both: 552.7 -> 567.6 Msamples/s).
+// Cheap enough to inline into the shading kernel; the direction cell takes
+// a fast reciprocal, since a key only orders rays.
 template <int G>
 RTX_DEV uint32_t origin_cell(const SortKeyBounds& kb, F3 o) {
   const float* inv = G == 4 ? kb.inv4 : kb.inv16;
@@ -1006,7 +1011,8 @@ __global__ void __launch_bounds__(256) k_sort_scatter(PtArgs a, DeviceScene s, i
 
 // ---------------------------------------------------------------------------
 // Ray sort (RTX_OPT_SORT_RAYS): counting sorts by a 12-bit key of the ray's
-// origin cell and direction (ray_key), so that a warp of a traversal kernel
+// origin cell and direction (ext_sort_key / shadow_sort_key, written by the
+// shading kernel beside each ray), so that a warp of a traversal kernel
 // takes rays that start close together and head the same way: fewer
 // divergent node visits and more cache hits.  Two sorts per path vertex: the extension
 // queue before the closest-hit kernel, and the shadow records before the
@@ -1019,146 +1025,35 @@ __global__ void __launch_bounds__(256) k_sort_scatter(PtArgs a, DeviceScene s, i
 // ---------------------------------------------------------------------------
 constexpr int kRayKeyBins = 4096;
 
-
-
-// Sort keys (12 bits, 4,096 bins).  kShadow = false, extension rays: the
-// Morton code of the origin's cell in a 4^3 grid over the scene bounds, then
-// the direction's cube face (major axis and sign) and its 3 x 3 cell on that
-// face.  kShadow = true, shadow rays (which all head for the lights, so the
-// origin says most about the path): the origin's cell in a 16^3 grid.
-// Measured on the 1.3M-triangle frame against 8^3 origin cells + octant for
-// both: 552.7 -> 567.6 Msamples/s; 8^3 cells + cube face only for extension
-// rays: 545.
-template <bool kShadow>
-RTX_DEV int ray_key(const DeviceScene& s, float4 o, float4 d) {
-  if (s.root4 < 0) return 0;
-  // scene bounds: the union of the 4-wide root's children (empty slots hold
-  // planes at 1e30 and are skipped)
-  const float4* n = s.nodes4 + kNode4Vecs * (size_t)s.root4;
-  const float4 lx = __ldg(n), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3);
-  const float4 lz = __ldg(n + 4), hz = __ldg(n + 5);
-  const float big = 1e29f;
-  auto lo4 = [&](float4 v) { return fminf(fminf(v.x, v.y), fminf(v.z, v.w)); };
-  auto hi4 = [&](float4 v) {
-    return fmaxf(fmaxf(v.x < big ? v.x : -big, v.y < big ? v.y : -big),
-                 fmaxf(v.z < big ? v.z : -big, v.w < big ? v.w : -big));
-  };
-  const float x0 = lo4(lx), y0 = lo4(ly), z0 = lo4(lz);
-  const float x1 = hi4(hx), y1 = hi4(hy), z1 = hi4(hz);
-  constexpr int G = kShadow ? 16 : 4;
-  auto cell = [](float v, float a, float b) {
-    const float f = (v - a) * ((float)G / fmaxf(b - a, 1e-20f));
-    return (uint32_t)min(max((int)f, 0), G - 1);
-  };
-  auto spread = [](uint32_t v) {  // bit k of v to bit 3k
-    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
-  };
-  const uint32_t m = spread(cell(o.x, x0, x1)) | (spread(cell(o.y, y0, y1)) << 1) |
-                     (spread(cell(o.z, z0, z1)) << 2);
-  if (kShadow) return (int)m;
-  // direction: cube face (major axis and sign), then a 3 x 3 cell on the face
-  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-  int face;
-  float u, v, mj;
-  if (ax >= ay && ax >= az) {
-    face = d.x < 0.0f;
-    u = d.y;
-    v = d.z;
-    mj = ax;
-  } else if (ay >= az) {
-    face = 2 + (d.y < 0.0f);
-    u = d.x;
-    v = d.z;
-    mj = ay;
-  } else {
-    face = 4 + (d.z < 0.0f);
-    u = d.x;
-    v = d.y;
-    mj = az;
-  }
-  const float inv = 1.0f / fmaxf(mj, 1e-30f);
-  const int cu = min(max((int)((u * inv + 1.0f) * 1.5f), 0), 2);
-  const int cv = min(max((int)((v * inv + 1.0f) * 1.5f), 0), 2);
-  return (int)((m << 6) | (uint32_t)(face * 9 + cu * 3 + cv));
-}
-
-// warp-aggregated add of 1 per lane to counter[key] (shared or global);
-// returns this lane's rank among the lanes that share its key and the
-// counter's value before the warp's add (in `base`)
 // Count `key` in a shared-memory histogram; returns the counter's value
 // before this lane's add (a rank unique among the lanes and warps that add to
 // the same key).  Plain shared atomics measured 3.3 % faster per frame than
 // aggregating equal keys per warp with __match_any_sync.
 RTX_DEV int count_key(int* counter, int key) { return atomicAdd(counter + key, 1); }
 
-// Keys of the items to sort: kShadow = false, the extension queue (item i is
-// path queue_in[i]); kShadow = true, the shadow records (item i is record i,
-// its ray from the shading point towards the light sample).
-// Each thread takes kHistPer items per step and issues all their loads
-// before computing a key, so the queue -> ray loads of several items are in
-// flight at once.
+// Histogram of the sort keys the shading kernel wrote beside the items
+// (kShadow = false: the extension queue, keys[i] for queue entry i; true:
+// the shadow records, keys[i] for record i).  Each thread takes kHistPer
+// keys per step and issues their loads before counting any.
 constexpr int kHistPer = 4;
 
-// kPre: the shading kernel already wrote the keys (single renders); only
-// their histogram is made here.
-template <bool kJobs, bool kShadow, bool kPre = false>
-__global__ void __launch_bounds__(256) k_raykey_hist(PtArgs a, DeviceScene s0, int* hist, int* keys) {
+template <bool kShadow>
+__global__ void __launch_bounds__(256) k_raykey_hist(PtArgs a, const int* keys, int* hist) {
   __shared__ int sh[kRayKeyBins];
   for (int b = threadIdx.x; b < kRayKeyBins; b += blockDim.x) sh[b] = 0;
   __syncthreads();
   const int n = kShadow ? a.shadow_counts[a.depth] : a.counts[a.depth];
   const int step = gridDim.x * blockDim.x * kHistPer;
-  if (kPre) {
-    for (int base = blockIdx.x * blockDim.x * kHistPer; base < n; base += step) {
-      int k[kHistPer];
-#pragma unroll
-      for (int j = 0; j < kHistPer; ++j) {
-        const int i = base + j * blockDim.x + threadIdx.x;
-        k[j] = i < n ? keys[i] : -1;
-      }
-#pragma unroll
-      for (int j = 0; j < kHistPer; ++j)
-        if (k[j] >= 0) count_key(sh, k[j]);
-    }
-  }
-  for (int base = blockIdx.x * blockDim.x * kHistPer; !kPre && base < n; base += step) {
-    int idx[kHistPer], path[kHistPer];
-    float4 o[kHistPer], d[kHistPer];
+  for (int base = blockIdx.x * blockDim.x * kHistPer; base < n; base += step) {
+    int k[kHistPer];
 #pragma unroll
     for (int j = 0; j < kHistPer; ++j) {
-      idx[j] = base + j * blockDim.x + threadIdx.x;
-      path[j] = 0;
-      if (idx[j] < n) {
-        if (kShadow) {
-          o[j] = a.shadow[4 * (size_t)idx[j]];
-          d[j] = a.shadow[4 * (size_t)idx[j] + 1];
-        } else {
-          path[j] = a.queue_in[idx[j]];
-        }
-      }
-    }
-    if (!kShadow) {
-#pragma unroll
-      for (int j = 0; j < kHistPer; ++j)
-        if (idx[j] < n) {
-          o[j] = a.ray_o[path[j]];
-          d[j] = a.ray_d[path[j]];
-        }
+      const int i = base + j * blockDim.x + threadIdx.x;
+      k[j] = i < n ? keys[i] : -1;
     }
 #pragma unroll
-    for (int j = 0; j < kHistPer; ++j) {
-      if (idx[j] >= n) continue;
-      int k;
-      if (kShadow) {
-        const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + __float_as_int(o[j].w));
-        k = ray_key<true>(s, o[j], make_float4(d[j].x - o[j].x, d[j].y - o[j].y, d[j].z - o[j].z, 0.0f));
-      } else {
-        const DeviceScene s = scene_of<kJobs>(s0, a, a.q0 + path[j]);
-        k = ray_key<false>(s, o[j], d[j]);
-      }
-      keys[idx[j]] = k;
-      count_key(sh, k);
-    }
+    for (int j = 0; j < kHistPer; ++j)
+      if (k[j] >= 0) count_key(sh, k[j]);
   }
   __syncthreads();
   for (int b = threadIdx.x; b < kRayKeyBins; b += blockDim.x)
@@ -1236,10 +1131,7 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
     if (p.sort_rays && depth > 0) {
       static_assert(kRayKeyBins <= kMaxSortBins, "ray keys use the sort histogram");
       if ((e = cudaMemsetAsync(ws->mat_hist, 0, (kMaxSortBins + 1) * sizeof(int), st))) return e;
-      if (a.ekeys)
-        k_raykey_hist<kJobs, false, true><<<grid_sh, 256, 0, st>>>(a, s, ws->mat_hist, ws->keys);
-      else
-        k_raykey_hist<kJobs, false><<<grid_sh, 256, 0, st>>>(a, s, ws->mat_hist, ws->keys);
+      k_raykey_hist<false><<<grid_sh, 256, 0, st>>>(a, ws->keys, ws->mat_hist);
       k_sort_scan<<<1, 1024, 0, st>>>(kRayKeyBins, ws->mat_hist);
       k_raykey_scatter<false><<<grid_sh, 256, 0, st>>>(a, ws->keys, ws->mat_hist, ws->ray_sorted);
       *launches += 3;
@@ -1290,26 +1182,19 @@ static cudaError_t wave_launches(const PtParams& p, PtArgs& a, const DeviceScene
     // the next vertex's sort and closest-hit launch, which touch neither the
     // shadow records nor the radiance.
     cudaStream_t cs = st;
-    // shadow keys: written by the shading kernel into keys2, or made by the
-    // histogram pass (keys2 beside the overlap's next closest-hit sort)
-    int* skeys = a.skeys ? ws->keys2 : ws->keys;
     int* shist = ws->mat_hist;
     if (overlap) {
       if ((e = cudaEventRecord(ws->ev_shaded, st))) return e;
       if ((e = cudaStreamWaitEvent(ws->side, ws->ev_shaded, 0))) return e;
       cs = ws->side;
-      skeys = ws->keys2;
       shist = ws->mat_hist2;
     }
     a.shadow_order = nullptr;
     if (p.sort_rays) {
       if ((e = cudaMemsetAsync(shist, 0, (kMaxSortBins + 1) * sizeof(int), cs))) return e;
-      if (a.skeys)
-        k_raykey_hist<kJobs, true, true><<<grid_sh, 256, 0, cs>>>(a, s, shist, skeys);
-      else
-        k_raykey_hist<kJobs, true><<<grid_sh, 256, 0, cs>>>(a, s, shist, skeys);
+      k_raykey_hist<true><<<grid_sh, 256, 0, cs>>>(a, ws->keys2, shist);
       k_sort_scan<<<1, 1024, 0, cs>>>(kRayKeyBins, shist);
-      k_raykey_scatter<true><<<grid_sh, 256, 0, cs>>>(a, skeys, shist, ws->shadow_order);
+      k_raykey_scatter<true><<<grid_sh, 256, 0, cs>>>(a, ws->keys2, shist, ws->shadow_order);
       *launches += 3;
       a.shadow_order = ws->shadow_order;  // the occlusion kernel visits records in key order
     }
