@@ -540,8 +540,8 @@ __device__ __forceinline__ uint32_t halo_off(int r, int c, int h) { return ((r *
 
 template <int S, bool kRes, bool kTma = false>
 __global__ void __launch_bounds__(kTileThreads, 1)
-    k_conv_fwd_rows(ConvFwd a, const __grid_constant__ CUtensorMap tm_halo) {
-  static_assert(!kTma || kRes, "tensor copies carry the halo only");
+    k_conv_fwd_rows(ConvFwd a, const __grid_constant__ CUtensorMap tm_halo,
+                    const __grid_constant__ CUtensorMap tm_w) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) TileBars bars;
   __shared__ uint32_t tmem_slot;
@@ -552,7 +552,11 @@ __global__ void __launch_bounds__(kTileThreads, 1)
   const int nsl = a.Cin / 16;
   const uint32_t ncols = a.Cout <= 32 ? 32 : (a.Cout <= 64 ? 64 : (a.Cout <= 128 ? 128 : 256));
   const uint32_t tap_bytes = (uint32_t)a.Cout * 32;
-  const uint32_t stage = kTma ? kHaloStage : (kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes);
+  // tensor copies: the halo, then (streamed weights) the slice's nine weight
+  // tiles from the next 1 KB boundary
+  const uint32_t stage = kTma ? kHaloStage + (kRes ? 0u : (9 * tap_bytes + 1023u) & ~1023u)
+                              : (kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes);
+  const uint32_t w_off = kTma ? kHaloStage : kHaloBytes;  // weights within a streamed stage
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
   tile_bars_init<S>(bars, kTma ? 1 : kLoadStride);
   tc::fence_before();
@@ -598,7 +602,7 @@ __global__ void __launch_bounds__(kTileThreads, 1)
   };
   auto mma = [&](int, int st, int buf, int s) {
     const uint32_t sh = s0 + st * stage;
-    const uint32_t sb = kRes ? sw + (uint32_t)s * 9 * tap_bytes : sh + kHaloBytes;
+    const uint32_t sb = kRes ? sw + (uint32_t)s * 9 * tap_bytes : sh + w_off;
     // A: pixel groups 128 B apart (SBO), channel chunks one halo row apart
     // (LBO); tap t starts (dy + 1) halo rows and 1 + dx pixels in (offsets in
     // the descriptors' 16-byte address units)
@@ -639,8 +643,10 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     int n, y, x0;
     tile_of(i, n, y, x0);
     tc::tma_load_5d(s0 + st * stage, &tm_halo, 0, x0 - 1, 2 * s, y - 1, n, bar);
+    // the slice's nine [Cout x 16] weight tiles, tap-major
+    if (!kRes) tc::tma_load_5d(s0 + st * stage + w_off, &tm_w, 0, 0, 2 * s, 0, 0, bar);
   };
-  ws_tiles<S, kTma>(n_tiles, nsl, bars, pre, load, mma, epi, a.err, issue, kHaloBytes);
+  ws_tiles<S, kTma>(n_tiles, nsl, bars, pre, load, mma, epi, a.err, issue, kHaloBytes + (kRes ? 0u : 9 * tap_bytes));
   tc_end(tmem, 2 * ncols);
 }
 
@@ -651,8 +657,8 @@ __global__ void __launch_bounds__(kTileThreads, 1)
 // weights: [channel tile][slice][tap] tiles of NTmax x 16.
 template <int S, bool kRes, bool kTma = false>
 __global__ void __launch_bounds__(kTileThreads, 1)
-    k_conv_dgrad_rows(ConvDgrad a, const __grid_constant__ CUtensorMap tm_halo) {
-  static_assert(!kTma || kRes, "tensor copies carry the halo only");
+    k_conv_dgrad_rows(ConvDgrad a, const __grid_constant__ CUtensorMap tm_halo,
+                      const __grid_constant__ CUtensorMap tm_w) {
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) TileBars bars;
   __shared__ uint32_t tmem_slot;
@@ -664,7 +670,9 @@ __global__ void __launch_bounds__(kTileThreads, 1)
   const int ntm = min(a.ctw, a.Cin);  // widest channel tile
   const uint32_t ncols = ntm <= 32 ? 32 : (ntm <= 64 ? 64 : (ntm <= 128 ? 128 : 256));
   const uint32_t tap_bytes = (uint32_t)ntm * 32;
-  const uint32_t stage = kTma ? kHaloStage : (kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes);
+  const uint32_t stage = kTma ? kHaloStage + (kRes ? 0u : (9 * tap_bytes + 1023u) & ~1023u)
+                              : (kRes ? kHaloBytes : kHaloBytes + 9 * tap_bytes);
+  const uint32_t w_off = kTma ? kHaloStage : kHaloBytes;  // weights within a streamed stage
   if (warp == 0) tc::tmem_alloc(&tmem_slot, 2 * ncols);
   tile_bars_init<S>(bars, kTma ? 1 : kLoadStride);
   tc::fence_before();
@@ -720,7 +728,7 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     const int NT = min(a.ctw, a.Cin - ct * a.ctw);
     const uint32_t idesc = tc::make_idesc_bf16(128, NT);
     const uint32_t sh = s0 + st * stage;
-    const uint32_t sb = kRes ? sw + (uint32_t)(ct * nsl + s) * 9 * tap_bytes : sh + kHaloBytes;
+    const uint32_t sb = kRes ? sw + (uint32_t)(ct * nsl + s) * 9 * tap_bytes : sh + w_off;
     const uint64_t ah = tc::make_desc(sh, kHalo * 16, 128), bw = tc::make_desc(sb, 128, 256);
     const uint32_t d = tmem + buf * ncols;
 #pragma unroll
@@ -758,8 +766,11 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     int n, y, x0, ct;
     tile_of(i, n, y, x0, ct);
     tc::tma_load_5d(s0 + st * stage, &tm_halo, 0, x0 - 1, 2 * s, y - 1, n, bar);
+    // the slice's nine [ntm x 16] tiles of the channel tile (rows past Cin
+    // read zeros), tap-major
+    if (!kRes) tc::tma_load_5d(s0 + st * stage + w_off, &tm_w, 0, 0, 2 * s, (ct * a.ctw) >> 3, 0, bar);
   };
-  ws_tiles<S, kTma>(n_tiles, nsl, bars, pre, load, mma, epi, a.err, issue, kHaloBytes);
+  ws_tiles<S, kTma>(n_tiles, nsl, bars, pre, load, mma, epi, a.err, issue, kHaloBytes + (kRes ? 0u : 9 * tap_bytes));
   tc_end(tmem, 2 * ncols);
 }
 
@@ -1176,7 +1187,7 @@ static bool use_rows(int W, int Ck) { return W >= 64 && Ck % 16 == 0; }
 // deepest ring (6, 4 or 2 stages) that fits 200 KB.
 template <class KR, class K6, class K4, class K2, class Args>
 static cudaError_t launch_tiles(KR kr, K6 k6, K4 k4, K2 k2, bool res, size_t stage, size_t res_bytes, long long T,
-                                const Args& a, const CUtensorMap& tm, cudaStream_t st) {
+                                const Args& a, const CUtensorMap& tm, const CUtensorMap& tw, cudaStream_t st) {
   if (T <= 0) return cudaSuccess;
   int S = 7;
   size_t smem = 7 * stage + res_bytes;
@@ -1189,7 +1200,7 @@ static cudaError_t launch_tiles(KR kr, K6 k6, K4 k4, K2 k2, bool res, size_t sta
   cudaError_t e;
 #define RTX_LAUNCH_TILES(K)                                                                          \
   if ((e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e; \
-  K<<<grid, kTileThreads, smem, st>>>(a, tm);
+  K<<<grid, kTileThreads, smem, st>>>(a, tm, tw);
   if (res) {
     RTX_LAUNCH_TILES(kr)
   } else if (S == 6) {
@@ -1237,6 +1248,24 @@ static bool chunk_major_map(CUtensorMap* m, const void* base, int imgs, int H, i
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Tensor map of a [rows][9][K] BF16 weight array (rows, K multiples of 16)
+// viewed as 5-D (8 of K, row % 8, K chunk, row / 8, tap) with a box of (8, 8,
+// 2, box_rows / 8, 9): a slice's nine K-major [box_rows x 16] tiles land
+// tap-major in the no-swizzle core-matrix layout (tc::tile_offset).  False
+// if it cannot be encoded.
+static bool weight_map(CUtensorMap* m, const void* base, int rows, int K, int box_rows) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(base) & 15) || rows % 8 || K % 16 || box_rows % 8 || box_rows > 2048)
+    return false;
+  const cuuint64_t dims[5] = {8, 8, (cuuint64_t)(K / 8), (cuuint64_t)(rows / 8), 9};
+  const cuuint64_t strides[4] = {(cuuint64_t)9 * K * 2, 16, (cuuint64_t)8 * 9 * K * 2, (cuuint64_t)K * 2};
+  const cuuint32_t box[5] = {8, 8, 2, (cuuint32_t)(box_rows / 8), 9};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // weights kept in shared memory by the persistent kernels up to this size
 constexpr size_t kResidentWeights = 96 * 1024;
 
@@ -1246,16 +1275,22 @@ cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st) {
   if (use_rows(a.W, a.Cin)) {
     const size_t wbytes = (size_t)9 * a.Cin * a.Cout * 2;
     const bool res = wbytes <= kResidentWeights;
-    // resident weights and one full-resolution source: halo slices arrive as
-    // tensor copies, if the map encodes
-    CUtensorMap tm{};
-    const bool tma = kConvTma && res && !a.s2.ptr && !a.s1.up && a.s1.C == a.Cin &&
-                     chunk_major_map(&tm, a.s1.ptr, a.N, a.H, a.W, a.Cin, kHalo, 2, 3);
-    const size_t stage = res ? (tma ? kHaloStage : kHaloBytes) : kHaloBytes + (size_t)9 * a.Cout * 32;
+    // one full-resolution source: halo slices (and streamed weight tiles)
+    // arrive as tensor copies, if the maps encode
+    CUtensorMap tm{}, tw{};
+    const bool tma = kConvTma && !a.s2.ptr && !a.s1.up && a.s1.C == a.Cin &&
+                     chunk_major_map(&tm, a.s1.ptr, a.N, a.H, a.W, a.Cin, kHalo, 2, 3) &&
+                     (res || weight_map(&tw, a.w, a.Cout, a.Cin, a.Cout));
+    const size_t wtiles = (size_t)9 * a.Cout * 32;
+    const size_t stage = tma ? kHaloStage + (res ? 0 : (wtiles + 1023) / 1024 * 1024)
+                             : (res ? kHaloBytes : kHaloBytes + wtiles);
     const long long T = (long long)a.N * a.H * ((a.W + 127) / 128);
-    return launch_tiles(tma ? k_conv_fwd_rows<7, true, true> : k_conv_fwd_rows<7, true>, k_conv_fwd_rows<6, false>,
-                        k_conv_fwd_rows<4, false>, k_conv_fwd_rows<2, false>, res, stage, res ? wbytes : 0, T, a,
-                        tm, st);
+    if (tma)
+      return launch_tiles(k_conv_fwd_rows<7, true, true>, k_conv_fwd_rows<6, false, true>,
+                          k_conv_fwd_rows<4, false, true>, k_conv_fwd_rows<2, false, true>, res, stage,
+                          res ? wbytes : 0, T, a, tm, tw, st);
+    return launch_tiles(k_conv_fwd_rows<7, true>, k_conv_fwd_rows<6, false>, k_conv_fwd_rows<4, false>,
+                        k_conv_fwd_rows<2, false>, res, stage, res ? wbytes : 0, T, a, tm, tw, st);
   }
   size_t stage = 128 * kSlice * 2 + (size_t)a.Cout * kSlice * 2;
   const dim3 grid((unsigned)((P + 127) / 128));
@@ -1283,16 +1318,23 @@ cudaError_t conv_dgrad(const ConvDgrad& a, cudaStream_t st) {
       }
     }
     const int ntb = (a.Cin + b.ctw - 1) / b.ctw;
-    // resident weights: dout's halo slices arrive as tensor copies, if the
-    // map encodes
-    CUtensorMap tm{};
-    const bool tma = kConvTma && res && a.Cout % 16 == 0 &&
-                     chunk_major_map(&tm, a.dout, a.N, a.H, a.W, a.Cout, kHalo, 2, 3);
-    const size_t stage = res ? (tma ? kHaloStage : kHaloBytes) : kHaloBytes + (size_t)9 * b.ctw * 32;
+    // dout's halo slices (and streamed weight tiles) arrive as tensor
+    // copies, if the maps encode
+    CUtensorMap tm{}, tw{};
+    const int ntm = std::min(b.ctw, a.Cin);  // rows of the widest channel tile
+    const bool tma = kConvTma && a.Cout % 16 == 0 &&
+                     chunk_major_map(&tm, a.dout, a.N, a.H, a.W, a.Cout, kHalo, 2, 3) &&
+                     (res || weight_map(&tw, a.wt, a.Cin, a.Cout, ntm));
+    const size_t wtiles = (size_t)9 * ntm * 32;
+    const size_t stage = tma ? kHaloStage + (res ? 0 : (wtiles + 1023) / 1024 * 1024)
+                             : (res ? kHaloBytes : kHaloBytes + (size_t)9 * b.ctw * 32);
     const long long T = (long long)a.N * a.H * ((a.W + 127) / 128) * ntb;
-    return launch_tiles(tma ? k_conv_dgrad_rows<7, true, true> : k_conv_dgrad_rows<7, true>,
-                        k_conv_dgrad_rows<6, false>, k_conv_dgrad_rows<4, false>, k_conv_dgrad_rows<2, false>, res,
-                        stage, res ? wbytes : 0, T, b, tm, st);
+    if (tma)
+      return launch_tiles(k_conv_dgrad_rows<7, true, true>, k_conv_dgrad_rows<6, false, true>,
+                          k_conv_dgrad_rows<4, false, true>, k_conv_dgrad_rows<2, false, true>, res, stage,
+                          res ? wbytes : 0, T, b, tm, tw, st);
+    return launch_tiles(k_conv_dgrad_rows<7, true>, k_conv_dgrad_rows<6, false>, k_conv_dgrad_rows<4, false>,
+                        k_conv_dgrad_rows<2, false>, res, stage, res ? wbytes : 0, T, b, tm, tw, st);
   }
   int nb = std::min(256, a.Cin);
   size_t stage = 128 * kSlice * 2 + (size_t)nb * kSlice * 2;
