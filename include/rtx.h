@@ -82,7 +82,10 @@ enum rtx_option {
   RTX_OPT_BLOCK = 3,          /* threads per block of the persistent wavefront
                                  kernels (extend, shade, connect): 64 or 128
                                  (their register budgets cap blocks at 128) */
-  RTX_OPT_SORT_MATERIAL = 4,  /* 0/1: sort hits by material before shading */
+  RTX_OPT_SORT_MATERIAL = 4,  /* 0 off, 1 on, 2 (default) on for scenes with a
+                                 refracting material (spec_trans != 0) or 8
+                                 materials or more: sort hits by material
+                                 before shading (results unchanged) */
   RTX_OPT_COUNT_VISITS = 5,   /* 0/1: count node visits and triangle tests */
   RTX_OPT_LEAF_SIZE = 6,      /* max triangles per BVH leaf (1..8), next upload */
   RTX_OPT_PRIMARY_CACHE = 7,  /* 0/1: trace each pixel's primary ray once */

@@ -78,7 +78,7 @@ struct rtx_context {
   bool async = false;
   int64_t wave_paths = 0;
   int block = 128;
-  bool sort_material = false;
+  int sort_material = 2;  // 0 off, 1 on, 2 on for scenes with refraction or 8+ materials
   int sort_rays = 2;  // 0 off, 1 on, 2 on for scenes of kSortRaysMinTris triangles or more
   bool count_visits = false;
   int leaf_size = 4;
@@ -161,6 +161,13 @@ bool is_device_ptr(const void* p) {
 // ~1,300 triangles (the 36-triangle Cornell box: 1.12 -> 1.28 ms per
 // frame), 1-2 % faster from ~5,000 and 8-9 % faster at 20,000.
 constexpr int kSortRaysMinTris = 4096;
+// Material-sorted shading pays where a warp's paths would otherwise run
+// different lobes: measured on the 9-material room with glass, metal,
+// clearcoat and subsurface (512^2 x 16 spp) 9.43 -> 6.37 ms per frame, on the
+// 1.3M-triangle icosphere room (5 materials, no refraction) 105.8 -> 116.4 ms.
+static bool sort_material_for(const rtx_context* c, const DeviceScene& s) {
+  return c->sort_material == 2 ? ((s.lobes & kLobeTrans) != 0 || s.n_mats >= 8) : c->sort_material != 0;
+}
 static bool sort_rays_for(const rtx_context* c, int n_tris) {
   return c->sort_rays == 2 ? n_tris >= kSortRaysMinTris : c->sort_rays != 0;
 }
@@ -440,7 +447,7 @@ int rtx_set_option(rtx_context* c, int option, int64_t v) {
       if (v != 64 && v != 128) return fail(c, RTX_ERR_INVALID, "block must be 64 or 128");
       c->block = (int)v;
       return RTX_OK;
-    case RTX_OPT_SORT_MATERIAL: c->sort_material = v != 0; return RTX_OK;
+    case RTX_OPT_SORT_MATERIAL: c->sort_material = v == 2 ? 2 : (v != 0); return RTX_OK;
     case RTX_OPT_SORT_RAYS: c->sort_rays = v == 2 ? 2 : (v != 0); return RTX_OK;
     case RTX_OPT_COUNT_VISITS: c->count_visits = v != 0; return RTX_OK;
     case RTX_OPT_LEAF_SIZE:
@@ -987,7 +994,7 @@ static int render_paths(rtx_context* c, const float* cam, int W, int H, int firs
   p.accumulate = acc;
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
-  p.sort_material = c->sort_material;
+  p.sort_material = sort_material_for(c, c->ds);
   p.sort_rays = sort_rays_for(c, c->ds.n_tris);
   p.overlap = c->overlap;
   p.traversal = c->traversal;
@@ -1110,7 +1117,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   p.block = c->block;
   p.count_visits = c->count_visits;
   p.primary_cache = c->primary_cache;
-  p.sort_material = c->sort_material;
+  p.sort_material = sort_material_for(c, c->bds);
   p.sort_rays = sort_rays_for(c, c->bds.n_tris);
   p.overlap = c->overlap;
   p.traversal = c->traversal;
@@ -1124,7 +1131,7 @@ int rtx_render_batch(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_de
   c->timer.reset();
   // the launch shape: everything the captured kernels bake in
   std::vector<int64_t> key = {n_jobs, max_depth, c->wave_paths, c->block, c->primary_cache, c->count_visits,
-                              c->accumulate, c->sort_material, (int64_t)p.sort_rays, c->traversal, c->overlap,
+                              c->accumulate, (int64_t)p.sort_material, (int64_t)p.sort_rays, c->traversal, c->overlap,
                               c->stack_limit, (int64_t)(intptr_t)o.dev};
   for (int j = 0; j < n_jobs; ++j) key.insert(key.end(), {jobs[j].scene, jobs[j].W, jobs[j].H, jobs[j].spp});
   int launches = 0, ext_launches = 0, vtx_launches = 0;
@@ -1265,15 +1272,15 @@ int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scene
   c->traversal = res.traversal;
   // material-sorted shading helps scenes with many materials and costs a
   // little where there are few: keep whichever is faster
-  res.sort_material = c->sort_material ? 1 : 0;
-  c->sort_material = !c->sort_material;
+  res.sort_material = sort_material_for(c, c->bds) ? 1 : 0;
+  c->sort_material = res.sort_material ? 0 : 1;
   if ((r = time_frame(c, n_jobs, jobs, max_depth, d_out, &ms))) return done(r);
   ++res.trials;
   if (ms < res.ms) {
     res.ms = ms;
-    res.sort_material = c->sort_material ? 1 : 0;
+    res.sort_material = c->sort_material;
   }
-  c->sort_material = res.sort_material != 0;
+  c->sort_material = res.sort_material;
   // ray-sorted traversal: its sorts cost a fixed few launches per vertex
   res.sort_rays = sort_rays_for(c, c->bds.n_tris) ? 1 : 0;
   c->sort_rays = res.sort_rays ? 0 : 1;

@@ -322,21 +322,24 @@ def test_lobe_variants_agree(ctx):
         ctx.upload(scenes.cornell_box())
 
 
-def test_ray_sort_auto_by_scene_size():
+def test_sorts_auto_by_scene():
     """RTX_OPT_SORT_RAYS defaults to 2 (sort when the scene has 4,096
-    triangles or more); a small and a large scene render the same bits with
-    the option at 0, 1 and 2."""
+    triangles or more) and RTX_OPT_SORT_MATERIAL to 2 (sort when a material
+    refracts or there are 8 or more); small, large and many-material scenes
+    render the same bits with either option at 0, 1 and 2."""
     import rendertoy_gb300 as rt
     from helpers import same_bits
     with rt.Context(0) as c:
         assert c.get_option(rt.OPT_SORT_RAYS) == 2
-        for sc in (scenes.cornell_box(), scenes.displaced_icosphere(subdiv=4)):
+        assert c.get_option(rt.OPT_SORT_MATERIAL) == 2
+        for sc in (scenes.cornell_box(), scenes.displaced_icosphere(subdiv=4), scenes.cornell_mixed()):
             c.upload(sc)
-            out = []
-            for v in (2, 0, 1):
-                c.set_option(rt.OPT_SORT_RAYS, v)
-                out.append(c.render_pt(48, 40, 4, 8, seed=3))
-            assert same_bits(out[0], out[1]) and same_bits(out[0], out[2]), sc.name
+            ref = c.render_pt(48, 40, 4, 8, seed=3)
+            for opt in (rt.OPT_SORT_RAYS, rt.OPT_SORT_MATERIAL):
+                for v in (0, 1, 2):
+                    c.set_option(opt, v)
+                    assert same_bits(ref, c.render_pt(48, 40, 4, 8, seed=3)), (sc.name, opt, v)
+                c.set_option(opt, 2)
 
 
 def test_absorbing_media(ctx, oracle):
