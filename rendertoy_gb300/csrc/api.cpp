@@ -175,7 +175,7 @@ static bool sort_rays_for(const rtx_context* c, int n_tris) {
 // The ray sort's origin grids over a scene's bounds: the union of its 4-wide
 // root's children (empty slots hold planes at 1e30 and are skipped), as the
 // device-side key of the sort's histogram pass computes it.
-static SortKeyBounds sort_key_bounds(const std::vector<float4>& nodes4, int root4) {
+static SortKeyBounds sort_key_bounds(const Float4Array& nodes4, int root4) {
   SortKeyBounds kb;
   if (root4 < 0 || nodes4.size() < (size_t)kNode4Vecs * (root4 + 1)) return kb;
   const float4* n = &nodes4[(size_t)kNode4Vecs * root4];

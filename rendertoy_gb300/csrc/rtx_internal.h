@@ -25,7 +25,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/rtx.h"
@@ -105,18 +107,43 @@ struct CamParams {
   int W, H;
 };
 
+// Allocator of the BVH builder's arrays: sizing an array leaves its new
+// elements uninitialised (the builder writes every one), so that sizing
+// ~100 MB of output costs no pass of zero stores.
+template <class T>
+struct UninitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <class U>
+  UninitAlloc(const UninitAlloc<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new ((void*)p) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+};
+using Float4Array = std::vector<float4, UninitAlloc<float4>>;
+
 struct BvhBuildResult {
-  std::vector<float4> nodes;   // 4 per node
-  std::vector<float4> nodes4;  // kNode4Vecs per 4-wide node
-  std::vector<float4> tris;    // 3 per triangle, leaf order
+  Float4Array nodes;   // 4 per node
+  Float4Array nodes4;  // kNode4Vecs per 4-wide node
+  Float4Array tris;    // 3 per triangle, leaf order
   int root = kEmptyRoot;
   int root4 = kEmptyRoot;
   int n_nodes = 0, n_nodes4 = 0, n_leaves = 0, depth = 0, depth4 = 0;
   double ms = 0.0;
 };
 
-// Host binned-SAH build over world-space triangles (verts: n x 9 floats)
-BvhBuildResult build_bvh(const float* verts, int n, int max_leaf);
+// Host binned-SAH build over world-space triangles (verts: n x 9 floats) on
+// `threads` threads (0: one per hardware thread, at most 64); the result is
+// the same bits for every thread count.
+BvhBuildResult build_bvh(const float* verts, int n, int max_leaf, int threads = 0);
 
 // Host-side camera preparation, restating Renderer::PrepareScreenSpace
 CamParams make_cam_params(const float* cam, int W, int H);

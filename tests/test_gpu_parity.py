@@ -342,6 +342,36 @@ def test_sorts_auto_by_scene():
                 c.set_option(opt, 2)
 
 
+def test_nonfinite_triangles_are_never_hit():
+    """Triangles with non-finite vertices (NaN coordinates, infinities,
+    coordinates whose box centre overflows) are accepted and never hit: the
+    Cornell box renders the same bits with six such triangles appended as a
+    mesh of its own with a non-emitting material."""
+    import rendertoy_gb300 as rt
+    from helpers import same_bits
+    sc = scenes.cornell_box()
+    bad = np.array([[np.nan] * 9,
+                    [0, 0, 0, 10, 0, 0, np.nan, 5, 5],
+                    [3e38] * 9,
+                    [-3e38, 2e38, 1, -3e38, 2e38, 2, -3e38, 2e38, 3],
+                    [np.inf, 0, 0, 0, 10, 0, 0, 0, 10],
+                    [0, -np.inf, 0, 10, 0, 0, 0, 0, 10]], np.float32)
+    plain_mat = int(np.nonzero(np.all(sc.mats[:, 3:6] == 0, axis=1))[0][0])
+    sc2 = scenes.Scene(verts=np.concatenate([sc.verts, bad]),
+                       norms=np.concatenate([sc.norms, np.zeros_like(bad)]),
+                       tri_mesh=np.concatenate([sc.tri_mesh, np.full(len(bad), len(sc.mesh_mat), np.int32)]),
+                       mesh_mat=np.append(sc.mesh_mat, plain_mat).astype(np.int32),
+                       mesh_smooth=np.append(sc.mesh_smooth, 0).astype(np.uint8),
+                       mats=sc.mats, sky=sc.sky, ground=sc.ground, camera=sc.camera, name="cornell+nonfinite")
+    with rt.Context(0) as c:
+        c.upload(sc)
+        ref = c.render_pt(48, 40, 4, 8, seed=3)
+        c.upload(sc2)
+        got = c.render_pt(48, 40, 4, 8, seed=3)
+    assert np.isfinite(ref).all()
+    assert same_bits(ref, got)
+
+
 def test_absorbing_media(ctx, oracle):
     """Beer-Lambert absorption inside refracting materials (extinction != 1,
     RenderToy's renderer.cpp:293, 311, 319): per-path radiance against the oracle
