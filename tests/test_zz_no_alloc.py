@@ -5,9 +5,11 @@ device).  It keeps its intermediate image in a fixed device array instead of
 allocating one.
 
 Called through the C ABI several times in a row on device buffers the test
-owns; each result must equal, bit for bit, what rtx_image_gaussian_blur returns
-for the same image (the tolerance of every compositor test here).  Collected
-last so a failing run has already run every other test; it also passes alone.
+owns -- out of place, in place with the largest kernel, and captured into a
+CUDA graph and replayed; each result must equal, bit for bit, what
+rtx_image_gaussian_blur returns for the same image (the tolerance of every
+compositor test here).  Collected last so a failing run has already run every
+other test; it also passes alone.
 """
 import ctypes as C
 
@@ -66,5 +68,29 @@ def test_noalloc_blur_matches_allocating_entry_point():
         r = L.rtx_image_gaussian_blur_noalloc(C.c_void_p(tall.data_ptr()), C.c_void_p(tall.data_ptr()),
                                               16, 70000, 7, 1.5, C.c_void_p(stream), msg, len(msg))
         assert r == 1 and b"65535" in msg.value
+        # captured into a CUDA graph on a stream of its own (after one call on
+        # that stream outside the capture) and replayed: the same bits
+        img = rng.exponential(0.7, (256, 384, 3)).astype(np.float32)
+        d_in = torch.from_numpy(img).cuda()
+        d_out = torch.full_like(d_in, float("nan"))
+        side = torch.cuda.Stream()
+
+        def call():
+            return L.rtx_image_gaussian_blur_noalloc(C.c_void_p(d_in.data_ptr()), C.c_void_p(d_out.data_ptr()),
+                                                     384, 256, 49, 8.0, C.c_void_p(side.cuda_stream), msg,
+                                                     len(msg))
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            assert call() == 0, msg.value
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side):
+            r = call()
+        assert r == 0, msg.value
+        d_out.fill_(float("nan"))
+        graph.replay()
+        torch.cuda.synchronize()
+        want = ctx.gaussian_blur(img, 49, 8.0)
+        assert np.array_equal(d_out.cpu().numpy().view(np.uint32), want.view(np.uint32))
     finally:
         ctx.close()
