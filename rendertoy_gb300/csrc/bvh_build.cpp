@@ -71,9 +71,10 @@ struct Prim {
 
 constexpr int kBins = 16;
 // Ranges of fewer triangles than this are built by one thread from start to
-// end; the tree above them is split on the calling thread.
+// end, into arrays of their own
 constexpr int kTaskPrims = 1 << 14;
-// A half of a split of at least this many triangles gets a thread of its own
+// Above them, a half of a split of at least this many triangles gets a
+// thread of its own; scenes with fewer triangles are built on one thread
 constexpr int kThreadPrims = 1 << 16;
 
 // Bin of a centroid coordinate along one axis.  A centroid that is not a
