@@ -185,7 +185,8 @@ def _f32(a):
 class ObjModel:
     """An OBJ (+ MTL) file imported by rtx_obj_import (no GPU needed): the
     triangle arrays, the meshes (name, smooth flag, Mesh::tris order) and the
-    MTL materials."""
+    MTL materials.  Names are the file's bytes decoded as UTF-8, with bytes
+    that are not UTF-8 kept as surrogate escapes."""
 
     def __init__(self, obj_path, mtl_path=None):
         L = lib()
@@ -210,7 +211,7 @@ class ObjModel:
                 L.rtx_obj_mesh(h, m, C.byref(name), C.byref(sm), None, C.byref(k))
                 t = np.zeros(k.value, np.int32)
                 L.rtx_obj_mesh(h, m, None, None, _ptr(t), C.byref(k))
-                self.mesh_names.append(name.value.decode())
+                self.mesh_names.append(name.value.decode("utf-8", "surrogateescape"))
                 self.mesh_smooth.append(sm.value)
                 self.mesh_tris.append(t)
             self.material_names, recs = [], []
@@ -218,7 +219,7 @@ class ObjModel:
                 name = C.c_char_p()
                 rec = np.zeros(24, np.float32)
                 L.rtx_obj_material(h, m, C.byref(name), _ptr(rec))
-                self.material_names.append(name.value.decode())
+                self.material_names.append(name.value.decode("utf-8", "surrogateescape"))
                 recs.append(rec)
             self.materials = np.stack(recs) if recs else np.zeros((0, 24), np.float32)
         finally:

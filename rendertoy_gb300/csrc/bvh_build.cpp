@@ -417,16 +417,18 @@ struct Builder {
   // Copies each subtree into its block with its indices offset
   static void place(Part& p, float4* nodes, float4* tris) {
     Subtree& s = p.sub;
-    float4* nd = nodes + 4 * (size_t)p.node_base;
-    std::memcpy(nd, s.nodes.data(), s.nodes.size() * sizeof(float4));
-    for (size_t i = 3; i < s.nodes.size(); i += 4) {
-      int c0, c1;
-      std::memcpy(&c0, &nd[i].x, 4);
-      std::memcpy(&c1, &nd[i].y, 4);
-      c0 = reloc(p, c0);
-      c1 = reloc(p, c1);
-      std::memcpy(&nd[i].x, &c0, 4);
-      std::memcpy(&nd[i].y, &c1, 4);
+    if (!s.nodes.empty()) {  // (a subtree that is one leaf has no nodes)
+      float4* nd = nodes + 4 * (size_t)p.node_base;
+      std::memcpy(nd, s.nodes.data(), s.nodes.size() * sizeof(float4));
+      for (size_t i = 3; i < s.nodes.size(); i += 4) {
+        int c0, c1;
+        std::memcpy(&c0, &nd[i].x, 4);
+        std::memcpy(&c1, &nd[i].y, 4);
+        c0 = reloc(p, c0);
+        c1 = reloc(p, c1);
+        std::memcpy(&nd[i].x, &c0, 4);
+        std::memcpy(&nd[i].y, &c1, 4);
+      }
     }
     std::memcpy(tris + 3 * (size_t)p.tri_base, s.tris.data(), s.tris.size() * sizeof(float4));
     Float4Array().swap(s.nodes);

@@ -407,6 +407,7 @@ int rtx_obj_info(const rtx_obj* o, int* n_tris, int* n_meshes, int* n_materials)
 
 int rtx_obj_triangles(const rtx_obj* o, float* verts, float* norms, float* uvs, int32_t* tri_mesh) {
   if (!o) return RTX_ERR_INVALID;
+  if (o->tri_mesh.empty()) return RTX_OK;  // (an empty array's data() may be null)
   if (verts) std::memcpy(verts, o->verts.data(), o->verts.size() * sizeof(float));
   if (norms) std::memcpy(norms, o->norms.data(), o->norms.size() * sizeof(float));
   if (uvs) std::memcpy(uvs, o->uvs.data(), o->uvs.size() * sizeof(float));
@@ -420,7 +421,7 @@ int rtx_obj_mesh(const rtx_obj* o, int mesh, const char** name, uint8_t* smooth,
   if (smooth) *smooth = o->mesh_smooth[mesh];
   const std::vector<int32_t>& t = o->mesh_tris[mesh];
   if (n_tris) *n_tris = (int)t.size();
-  if (tris) std::memcpy(tris, t.data(), t.size() * sizeof(int32_t));
+  if (tris && !t.empty()) std::memcpy(tris, t.data(), t.size() * sizeof(int32_t));
   return RTX_OK;
 }
 
