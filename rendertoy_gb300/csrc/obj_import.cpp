@@ -29,11 +29,13 @@
 // or negative, more than three '/' fields, "s" / "f" before any "o", material
 // keys before any "newmtl"), this parser reports an error instead.
 #include <cerrno>
+#include <charconv>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <limits>
 #include <new>
@@ -81,14 +83,6 @@ struct Cursor {
     while (p < end && *p != '\n') ++p;
     if (p < end) ++p;
   }
-  // std::getline
-  std::string line() {
-    const char* b = p;
-    while (p < end && *p != '\n') ++p;
-    std::string s(b, p);
-    if (p < end) ++p;
-    return s;
-  }
   // operator>>(float&): skips whitespace, then takes the longest prefix of
   // the form [+-]digits[.digits][(e|E)[+-]digits] (num_get's accepted
   // characters), converted with correct rounding; no digits fails the stream
@@ -117,12 +111,18 @@ struct Cursor {
       while (e < end && *e >= '0' && *e <= '9') ++e;
       if (e > e0) q = e;
     }
-    std::string s(b, q);
-    errno = 0;
-    float v = std::strtof(s.c_str(), nullptr);
-    if (errno == ERANGE && std::isinf(v)) {  // num_get: out of range fails the stream
-      failed = true;
-      return false;
+    // std::from_chars rounds as strtof does (correctly) without a copy or
+    // the locale; it takes no '+' and leaves out-of-range values to strtof
+    float v;
+    std::from_chars_result r = std::from_chars(*b == '+' ? b + 1 : b, q, v);
+    if (r.ec != std::errc() || r.ptr != q) {
+      std::string s(b, q);
+      errno = 0;
+      v = std::strtof(s.c_str(), nullptr);
+      if (errno == ERANGE && std::isinf(v)) {  // num_get: out of range fails the stream
+        failed = true;
+        return false;
+      }
     }
     out = v;
     p = q;
@@ -156,60 +156,42 @@ struct Cursor {
   }
 };
 
-// std::stoi: leading whitespace, optional sign, decimal digits; false when no
+// std::stoi on the characters [b, e): leading whitespace, optional sign,
+// decimal digits (anything after them ignored); false when there are no
 // digits or the value does not fit an int
-bool parse_stoi(const std::string& s, int& out) {
-  size_t i = 0;
-  while (i < s.size() && (s[i] == ' ' || s[i] == '\t' || s[i] == '\n' || s[i] == '\r' || s[i] == '\v' ||
-                          s[i] == '\f'))
-    ++i;
-  size_t b = i;
-  if (i < s.size() && (s[i] == '+' || s[i] == '-')) ++i;
-  size_t d0 = i;
-  while (i < s.size() && s[i] >= '0' && s[i] <= '9') ++i;
-  if (i == d0) return false;
-  errno = 0;
-  long v = std::strtol(s.substr(b, i - b).c_str(), nullptr, 10);
-  if (errno == ERANGE || v < std::numeric_limits<int>::min() || v > std::numeric_limits<int>::max()) return false;
+bool parse_stoi(const char* b, const char* e, int& out) {
+  while (b < e && (*b == ' ' || *b == '\t' || *b == '\n' || *b == '\r' || *b == '\v' || *b == '\f')) ++b;
+  const char* q = b;
+  bool neg = false;
+  if (q < e && (*q == '+' || *q == '-')) neg = *q++ == '-';
+  const char* d0 = q;
+  long long v = 0;
+  while (q < e && *q >= '0' && *q <= '9') {
+    if (v <= (1LL << 40)) v = v * 10 + (*q - '0');  // saturates far beyond int
+    ++q;
+  }
+  if (q == d0) return false;
+  if (neg) v = -v;
+  if (v < std::numeric_limits<int>::min() || v > std::numeric_limits<int>::max()) return false;
   out = (int)v;
   return true;
-}
-
-// getline-based split on one delimiter (importer.cpp:15-25): no trailing
-// empty field, a leading one kept
-std::vector<std::string> split(const std::string& s, char delim) {
-  std::vector<std::string> out;
-  size_t i = 0;
-  while (i < s.size()) {
-    size_t j = s.find(delim, i);
-    if (j == std::string::npos) {
-      out.push_back(s.substr(i));
-      break;
-    }
-    out.push_back(s.substr(i, j - i));
-    i = j + 1;
-  }
-  return out;
-}
-
-// std::regex_replace(s, "^ +| +$|( ) +", "$1"): trim spaces at both ends and
-// collapse runs of spaces to one
-std::string collapse_spaces(const std::string& s) {
-  size_t b = 0, e = s.size();
-  while (b < e && s[b] == ' ') ++b;
-  while (e > b && s[e - 1] == ' ') --e;
-  std::string out;
-  out.reserve(e - b);
-  for (size_t i = b; i < e; ++i) {
-    if (s[i] == ' ' && !out.empty() && out.back() == ' ') continue;
-    out.push_back(s[i]);
-  }
-  return out;
 }
 
 bool read_file(const char* path, std::string& data) {
   std::ifstream f(path, std::ios::binary);
   if (!f) return false;
+  // a regular file is read in one piece into a string of its size (a
+  // third of the time of streaming it through a string stream)
+  std::error_code ec;
+  if (std::filesystem::is_regular_file(path, ec)) {
+    uintmax_t n = std::filesystem::file_size(path, ec);
+    if (!ec && n < ((uintmax_t)1 << 40)) {
+      data.resize((size_t)n);
+      f.read(&data[0], (std::streamsize)n);
+      data.resize((size_t)f.gcount());
+      return true;
+    }
+  }
   std::ostringstream ss;
   ss << f.rdbuf();
   data = ss.str();
@@ -235,7 +217,25 @@ int parse_obj(const std::string& text, rtx_obj& o, std::string& err) {
   Cursor c{text.data(), text.data() + text.size()};
   std::vector<V3> vert{{0, 0, 0}}, norm{{0, 0, 0}};
   std::vector<V2> uv{{0, 0}};
+  std::vector<V3> pv, pn;  // one face's vertices
+  std::vector<V2> pt;
   int mesh = -1;
+  // Each mesh's triangles as the faces append them, and where each face's
+  // block starts; Mesh::tris is the blocks in reverse (each face's block is
+  // prepended), each block in its own order.  Built once at the end rather
+  // than by inserting at the front, which costs quadratic time in a large mesh.
+  std::vector<std::vector<int32_t>> appended, blocks;
+  auto finish_mesh_tris = [&] {
+    for (size_t m = 0; m < appended.size(); ++m) {
+      std::vector<int32_t>& mt = o.mesh_tris[m];
+      mt.clear();
+      mt.reserve(appended[m].size());
+      for (size_t b = blocks[m].size(); b-- > 0;) {
+        size_t e = b + 1 < blocks[m].size() ? (size_t)blocks[m][b + 1] : appended[m].size();
+        mt.insert(mt.end(), appended[m].begin() + blocks[m][b], appended[m].begin() + e);
+      }
+    }
+  };
   std::string id;
   while (!c.failed && c.token(id)) {
     if (id == "o") {
@@ -243,6 +243,8 @@ int parse_obj(const std::string& text, rtx_obj& o, std::string& err) {
       o.mesh_names.emplace_back();
       o.mesh_smooth.push_back(0);
       o.mesh_tris.emplace_back();
+      appended.emplace_back();
+      blocks.emplace_back();
       c.token(o.mesh_names.back());
       continue;
     }
@@ -271,18 +273,41 @@ int parse_obj(const std::string& text, rtx_obj& o, std::string& err) {
         err = "'f' before any 'o'";
         return RTX_ERR_INVALID;
       }
-      std::vector<std::string> defs = split(collapse_spaces(c.line()), ' ');
-      std::vector<V3> pv, pn;
-      std::vector<V2> pt;
-      for (const std::string& d : defs) {
-        std::vector<std::string> f = split(d, '/');
-        if (f.size() > 3) {
-          err = "a face vertex with more than three fields";
-          return RTX_ERR_INVALID;
+      // the rest of the line (std::getline), trimmed and split at runs of
+      // spaces (importer.cpp:101 collapses them first); each vertex split at
+      // '/' as getline does (a trailing empty field dropped)
+      const char* lb = c.p;
+      while (c.p < c.end && *c.p != '\n') ++c.p;
+      const char* le = c.p;
+      if (c.p < c.end) ++c.p;
+      pv.clear();
+      pn.clear();
+      pt.clear();
+      for (const char* q = lb; q < le;) {
+        if (*q == ' ') {
+          ++q;
+          continue;
         }
-        int idx[3];
+        const char* fb = q;
+        while (q < le && *q != ' ') ++q;
+        const char* fe = q;
+        const char* sb[4];
+        const char* se[4];
+        int nf = 0;
+        for (const char* i = fb; i < fe;) {
+          const char* j = i;
+          while (j < fe && *j != '/') ++j;
+          if (nf == 3) {
+            err = "a face vertex with more than three fields";
+            return RTX_ERR_INVALID;
+          }
+          sb[nf] = i;
+          se[nf++] = j;
+          i = j < fe ? j + 1 : fe;
+        }
+        int idx[3] = {0, 0, 0};
         bool has[3] = {false, false, false};
-        for (size_t k = 0; k < f.size(); ++k) has[k] = !f[k].empty() && parse_stoi(f[k], idx[k]);
+        for (int k = 0; k < nf; ++k) has[k] = se[k] > sb[k] && parse_stoi(sb[k], se[k], idx[k]);
         auto check = [&](int k, size_t n) {
           if (has[k] && (idx[k] < 0 || (size_t)idx[k] >= n)) {
             err = "face index " + std::to_string(idx[k]) + " out of range";
@@ -295,7 +320,7 @@ int parse_obj(const std::string& text, rtx_obj& o, std::string& err) {
         pt.push_back(has[1] ? uv[idx[1]] : V2{0, 0});
         pn.push_back(has[2] ? norm[idx[2]] : V3{0, 0, 0});
       }
-      std::vector<int32_t> block;
+      blocks[mesh].push_back((int32_t)appended[mesh].size());
       for (size_t b = 1; b + 1 < pv.size(); ++b) {
         size_t ids[3] = {0, b, b + 1};
         int32_t t = (int32_t)o.tri_mesh.size();
@@ -306,14 +331,13 @@ int parse_obj(const std::string& text, rtx_obj& o, std::string& err) {
           o.uvs.insert(o.uvs.end(), {pt[k].x, pt[k].y});
         }
         o.tri_mesh.push_back(mesh);
-        block.push_back(t);
+        appended[mesh].push_back(t);
       }
-      std::vector<int32_t>& mt = o.mesh_tris[mesh];
-      mt.insert(mt.begin(), block.begin(), block.end());
       continue;
     }
     c.ignore_line();
   }
+  finish_mesh_tris();
   return RTX_OK;
 }
 
