@@ -41,6 +41,9 @@ result.  Metric: Msamples/s (pixel samples per second), with Mrays/s beside it.
           tensor-core TFLOP/s against the measured BF16 peak.
   compositor : each filter timed alone on the resident image, achieved GB/s of
           its algorithmic bytes as a fraction of the measured HBM bandwidth.
+  obj_import : the host OBJ importer (one thread) on 262,144 triangles of the
+          bench mesh written as OBJ text; config.scene_upload_s is the whole
+          upload of the bench scene (threaded BVH build, device copies).
 
 ``--impl reference`` times RenderToy's CPU path on the same workload (its
 compiled sources where they run here, otherwise the oracle restatement).
@@ -408,6 +411,37 @@ def cpu_sample_rate(sc, seconds=12.0, threads=0, kind="oracle", depth=DEPTH):
 BATCH_DEPTH = 8
 
 
+def obj_import_block(sc, n_tris=262144):
+    """Host OBJ import (rtx_obj_import through rendertoy_gb300.ObjModel,
+    arrays copied out included): the first `n_tris` triangles of the bench
+    mesh written as OBJ text (`v` / `vn` per corner, `f v//vn`, one object),
+    parsed on one host thread.  Written outside the timing, median of 3."""
+    import tempfile
+
+    import rendertoy_gb300 as rt
+    n = min(n_tris, sc.n_tris)
+    d = tempfile.mkdtemp()
+    path = os.path.join(d, "mesh.obj")
+    with open(path, "w") as f:
+        f.write("o mesh\n")
+        np.savetxt(f, sc.verts[:n].reshape(-1, 3), fmt="v %.6f %.6f %.6f")
+        np.savetxt(f, sc.norms[:n].reshape(-1, 3), fmt="vn %.6f %.6f %.6f")
+        k = np.arange(1, 3 * n + 1).reshape(-1, 3)
+        np.savetxt(f, np.repeat(k, 2, axis=1), fmt="f %d//%d %d//%d %d//%d")
+    size = os.path.getsize(path)
+    ts = []
+    for _ in range(3):
+        t = time.perf_counter()
+        m = rt.ObjModel(path)
+        ts.append(time.perf_counter() - t)
+    assert len(m.tri_mesh) == n
+    os.remove(path)
+    os.rmdir(d)
+    sec = float(np.median(ts))
+    return {"triangles": n, "bytes": size, "ms": sec * 1e3, "mb_per_s": size / sec / 1e6,
+            "mtris_per_s": n / sec / 1e6, "threads": 1}
+
+
 def run_batched(local, rank, n_scenes, steps, warmup, ws=1):
     """The batched config: seeded procedural scenes (1e3-2e6 triangles each,
     textures, 1-4 blackbody quad lights), each frame at its own resolution
@@ -553,7 +587,9 @@ def main():
         k, v = o.split("=")
         ctx.set_option(getattr(rt, "OPT_" + k.upper()), int(v))
         opts[k] = int(v)
+    t0 = time.perf_counter()
     ctx.upload(sc)
+    upload_s = time.perf_counter() - t0
     st0 = ctx.stats()
     if args.profile:
         out = torch.empty((args.res, args.res, 3), dtype=torch.float32, device="cuda")
@@ -727,6 +763,7 @@ def main():
              "config": bconf, "autotune": btune, "clocks": bclk, "graph": True}
 
     cpu = None
+    obj = obj_import_block(sc) if rank == 0 else None
     if rank == 0:
         v, ns, t, cores = cpu_sample_rate(sc, seconds=args.cpu_seconds)
         v5, ns5, t5, _ = cpu_sample_rate(sc, seconds=max(2.0, args.cpu_seconds / 3), depth=5)
@@ -746,7 +783,9 @@ def main():
                        "max_depth": DEPTH, "triangles": sc.n_tris,
                        "l2": "flushed between steps (256 MiB write, outside the timed events)",
                        "bvh_build_ms": st0["bvh_build_ms"], "bvh_nodes": st0["bvh_nodes"],
-                       "scene_gen_s": round(gen_s, 2), "options": opts},
+                       "scene_upload_s": round(upload_s, 3), "scene_gen_s": round(gen_s, 2),
+                       "options": opts},
+            "obj_import": obj,
             "mrays_per_s": mrays,
             "overlap": {"step_ms": total_ms / args.steps,
                         "render_ms_serialised": float(np.median(serial_ms)),
