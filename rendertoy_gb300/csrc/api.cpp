@@ -22,6 +22,7 @@
 #include "nn.h"
 #include "nn_ops.h"
 #include "nn_unet.h"
+#include "host_threads.h"
 #include "rtx_internal.h"
 
 using namespace rtx;
@@ -654,14 +655,28 @@ int rebase_leaf(int ref, int tri_base) {
   return ~(((first + tri_base) << 3) | cnt);
 }
 
+// Runs an entry point's host work and turns an exception (a host allocation
+// that failed, in the scene builders) into an error code: no exception
+// crosses the C ABI.
+template <class F>
+int host_guard(rtx_context* c, F&& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    return c ? fail(c, RTX_ERR_NOMEM, "host allocation failed") : RTX_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    return c ? fail(c, RTX_ERR_INVALID, e.what()) : RTX_ERR_INVALID;
+  }
+}
+
 }  // namespace
 
 extern "C" {
 
-int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* norms,
-                     const int32_t* tri_mesh, int n_meshes, const int32_t* mesh_mat,
-                     const uint8_t* mesh_smooth, int n_mat, const float* mats, const float* sky,
-                     const float* ground) {
+static int scene_upload(rtx_context* c, int n, const float* verts, const float* norms,
+                        const int32_t* tri_mesh, int n_meshes, const int32_t* mesh_mat,
+                        const uint8_t* mesh_smooth, int n_mat, const float* mats, const float* sky,
+                        const float* ground) {
   if (!c) return RTX_ERR_INVALID;
   int r;
   if ((r = check_scene(c, n, verts, norms, tri_mesh, n_meshes, mesh_mat, mesh_smooth, n_mat, mats, sky, ground)))
@@ -715,7 +730,16 @@ int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* nor
   return RTX_OK;
 }
 
-int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
+int rtx_scene_upload(rtx_context* c, int n, const float* verts, const float* norms,
+                     const int32_t* tri_mesh, int n_meshes, const int32_t* mesh_mat,
+                     const uint8_t* mesh_smooth, int n_mat, const float* mats, const float* sky,
+                     const float* ground) {
+  return host_guard(c, [&] {
+    return scene_upload(c, n, verts, norms, tri_mesh, n_meshes, mesh_mat, mesh_smooth, n_mat, mats, sky, ground);
+  });
+}
+
+static int batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   if (!c) return RTX_ERR_INVALID;
   if (n_scenes < 1 || !d) return fail(c, RTX_ERR_INVALID, "at least one scene is needed");
   int r;
@@ -737,19 +761,10 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   // host builds, several scenes at a time
   std::vector<HostScene> hs(n_scenes);
   auto t0 = std::chrono::steady_clock::now();
-  {
-    unsigned nt = std::max(1u, std::min(std::thread::hardware_concurrency(), 16u));
-    std::atomic<int> next{0};
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nt; ++t)
-      th.emplace_back([&] {
-        for (int i; (i = next++) < n_scenes;)
-          build_host_scene(hs[i], d[i].n_tris, d[i].verts, d[i].norms, d[i].tri_mesh, d[i].n_meshes,
-                           d[i].mesh_mat, d[i].mesh_smooth, d[i].n_materials, d[i].materials, d[i].sky,
-                           d[i].ground, c->leaf_size);
-      });
-    for (auto& t : th) t.join();
-  }
+  run_parallel((size_t)n_scenes, std::max(1u, std::min(std::thread::hardware_concurrency(), 16u)), [&](size_t i) {
+    build_host_scene(hs[i], d[i].n_tris, d[i].verts, d[i].norms, d[i].tri_mesh, d[i].n_meshes, d[i].mesh_mat,
+                     d[i].mesh_smooth, d[i].n_materials, d[i].materials, d[i].sky, d[i].ground, c->leaf_size);
+  });
   // merge: node, leaf-record, triangle-id, material and emitter indices rebased
   std::vector<float4> nodes, nodes4, tris, shade, geo;
   std::vector<float> mats;
@@ -861,6 +876,10 @@ int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
   c->stats.node_bytes = 64;
   c->stats.tri_bytes = 48;
   return RTX_OK;
+}
+
+int rtx_batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
+  return host_guard(c, [&] { return batch_upload(c, n_scenes, d); });
 }
 
 int rtx_scene_emitters(rtx_context* c, int32_t* out, int cap, int* n_out) {
@@ -1198,8 +1217,8 @@ static int time_frame(rtx_context* c, int n_jobs, const rtx_job* jobs, int max_d
   return RTX_OK;
 }
 
-int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scenes, int n_jobs,
-                       const rtx_job* jobs, int max_depth, rtx_tune_result* out) {
+static int batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scenes, int n_jobs,
+                          const rtx_job* jobs, int max_depth, rtx_tune_result* out) {
   if (!c) return RTX_ERR_INVALID;
   if (!out || !jobs || n_jobs < 1) return fail(c, RTX_ERR_INVALID, "NULL argument");
   const bool saved_graph = c->use_graph, saved_timer = c->timer.on;
@@ -1303,6 +1322,11 @@ int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scene
   c->overlap = res.overlap != 0;
   *out = res;
   return done(RTX_OK);
+}
+
+int rtx_batch_autotune(rtx_context* c, int n_scenes, const rtx_scene_desc* scenes, int n_jobs,
+                       const rtx_job* jobs, int max_depth, rtx_tune_result* out) {
+  return host_guard(c, [&] { return batch_autotune(c, n_scenes, scenes, n_jobs, jobs, max_depth, out); });
 }
 
 // ---- display resolve and image files --------------------------------------------

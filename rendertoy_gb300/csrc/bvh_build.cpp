@@ -25,10 +25,13 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <memory>
+#include <mutex>
 #include <system_error>
 #include <thread>
 
+#include "host_threads.h"
 #include "rtx_internal.h"
 
 namespace rtx {
@@ -90,26 +93,6 @@ struct Range {
   int begin, end;
   AABB bb, cb;
 };
-
-// Runs fn(k) for k = 0 .. n-1 on up to n_threads threads, the calling thread
-// among them (it takes whatever threads that could not be started leave).
-template <class F>
-void run_parallel(size_t n, unsigned n_threads, F&& fn) {
-  std::atomic<size_t> next{0};
-  auto work = [&] {
-    for (size_t k; (k = next.fetch_add(1)) < n;) fn(k);
-  };
-  std::vector<std::thread> pool;
-  for (unsigned t = 1; t < n_threads && t < n; ++t) {
-    try {
-      pool.emplace_back(work);
-    } catch (const std::system_error&) {
-      break;
-    }
-  }
-  work();
-  for (auto& th : pool) th.join();
-}
 
 // A pass over a range is cut into chunks of at least this many prims, one
 // thread each; the chunks' results are merged in chunk order, which gives
@@ -354,7 +337,10 @@ struct Builder {
     unsigned share = (unsigned)std::max<int64_t>(1, (int64_t)n_threads * (r.end - r.begin) / (int64_t)prims.size());
     Range L, R;
     if (r.end - r.begin < kTaskPrims || split_range(prims.data(), r, depth, max_leaf, L, R, share) < 0) {
-      p.sub = Subtree{verts, prims.data(), max_leaf, pad_abs};
+      p.sub.verts = verts;
+      p.sub.prims = prims.data();
+      p.sub.max_leaf = max_leaf;
+      p.sub.pad_abs = pad_abs;
       p.sub.root = p.sub.build(r, depth);
       return;
     }
@@ -366,17 +352,31 @@ struct Builder {
     // the right half on a thread of its own while this one takes the left,
     // as long as it is large enough to be worth a thread
     std::thread right;
+    std::exception_ptr right_err;
     if (n_threads > 1 && R.end - R.begin >= kThreadPrims) {
       try {
-        right = std::thread([&] { split_part(*p.r, R, depth + 1); });
+        right = std::thread([&] {
+          try {
+            split_part(*p.r, R, depth + 1);
+          } catch (...) {
+            right_err = std::current_exception();
+          }
+        });
       } catch (const std::system_error&) {
       }
     }
-    split_part(*p.l, L, depth + 1);
-    if (right.joinable())
+    try {
+      split_part(*p.l, L, depth + 1);
+    } catch (...) {
+      if (right.joinable()) right.join();
+      throw;
+    }
+    if (right.joinable()) {
       right.join();
-    else
+      if (right_err) std::rethrow_exception(right_err);
+    } else {
       split_part(*p.r, R, depth + 1);
+    }
   }
 
   // Numbers nodes and triangles depth first, as one thread building the
