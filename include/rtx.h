@@ -186,7 +186,10 @@ int rtx_get_stats(rtx_context* ctx, rtx_stats* out);
  * sky / ground: World::sky_emission / ground_reflection.  Emitters are the
  * triangles of meshes whose emission is not zero, in mesh order then triangle
  * order, as the reference collects them.  The arrays are copied; the
- * caller's buffers may be released on return. */
+ * caller's buffers may be released on return.  The BVH is built on host
+ * threads (the same tree for any thread count).  A triangle with a
+ * non-finite vertex is accepted and never hit.  A host allocation that fails
+ * returns RTX_ERR_NOMEM, as rtx_batch_upload and rtx_batch_autotune do. */
 int rtx_scene_upload(rtx_context* ctx, int n_tris, const float* verts,
                      const float* norms, const int32_t* tri_mesh, int n_meshes,
                      const int32_t* mesh_mat, const uint8_t* mesh_smooth,
