@@ -39,9 +39,11 @@ class BVH {
   friend struct RenderContext;
   World* world;
   rtx_context* ctx = nullptr;
-  std::vector<float> snapshot;  // materials, mesh table and emitters as uploaded
+  // materials, mesh table, emitters and environment as uploaded: float bits
+  // and emitter addresses, compared exactly
+  std::vector<uint64_t> snapshot;
   void Upload();
-  std::vector<float> Signature() const;
+  std::vector<uint64_t> Signature() const;
 };
 }  // namespace RenderToy
 #endif

@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <mutex>
 #include <random>
 #include <string>
@@ -258,20 +259,27 @@ BVH::BVH(World* w) : world(w) {
 }
 BVH::~BVH() { rtx_destroy(ctx); }
 
-std::vector<float> BVH::Signature() const {
-  std::vector<float> s;
+std::vector<uint64_t> BVH::Signature() const {
+  // exact: a float by its bits (a NaN field equals itself), an emitter by
+  // its full address (a float of an address would merge nearby ones)
+  std::vector<uint64_t> s;
+  auto put = [&](float f) {
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    s.push_back(b);
+  };
   float rec[RTX_MATERIAL_FLOATS];
   for (auto m : world->meshes) {
     if (m->tex) {
       m->tex->ToRecord(rec);
-      s.insert(s.end(), rec, rec + RTX_MATERIAL_FLOATS);
+      for (float f : rec) put(f);
     }
-    s.push_back(m->smooth ? 1.0f : 0.0f);
+    s.push_back(m->smooth ? 1 : 0);
   }
-  for (auto t : world->Emitters()) s.push_back((float)(uintptr_t)t);
+  for (auto t : world->Emitters()) s.push_back((uint64_t)(uintptr_t)t);
   for (int k = 0; k < 3; ++k) {
-    s.push_back(world->sky_emission[k]);
-    s.push_back(world->ground_reflection[k]);
+    put(world->sky_emission[k]);
+    put(world->ground_reflection[k]);
   }
   return s;
 }
@@ -279,7 +287,7 @@ std::vector<float> BVH::Signature() const {
 void BVH::Upload() {
   const auto& tris = world->triangles;
   int n = (int)tris.size();
-  std::map<const Mesh*, int> mesh_id;
+  std::unordered_map<const Mesh*, int> mesh_id;
   std::vector<const Mesh*> meshes;
   for (auto m : world->meshes)
     if (!mesh_id.count(m)) {
@@ -288,16 +296,28 @@ void BVH::Upload() {
     }
   std::vector<float> verts((size_t)n * 9), norms((size_t)n * 9);
   std::vector<int32_t> tri_mesh(n);
-  std::map<const Triangle*, int> tri_id;
+  // ids are looked up only for the emitters
+  std::unordered_map<const Triangle*, int> tri_id;
+  for (auto t : world->Emitters()) tri_id.emplace(t, -1);
+  const Mesh* last = nullptr;
+  int last_id = -1;
   for (int i = 0; i < n; ++i) {
     const Triangle* t = tris[i];
     if (!t->parent) throw Exception::DeviceException(RTX_ERR_INVALID, "triangle without a parent mesh");
-    if (!mesh_id.count(t->parent)) {
-      mesh_id[t->parent] = (int)meshes.size();
-      meshes.push_back(t->parent);
+    if (t->parent != last) {  // a mesh's triangles usually come together
+      auto it = mesh_id.find(t->parent);
+      if (it == mesh_id.end()) {
+        it = mesh_id.emplace(t->parent, (int)meshes.size()).first;
+        meshes.push_back(t->parent);
+      }
+      last = t->parent;
+      last_id = it->second;
     }
-    tri_mesh[i] = mesh_id[t->parent];
-    tri_id[t] = i;
+    tri_mesh[i] = last_id;
+    if (!tri_id.empty()) {
+      auto it = tri_id.find(t);
+      if (it != tri_id.end() && it->second < 0) it->second = i;
+    }
     for (int k = 0; k < 3; ++k)
       for (int c = 0; c < 3; ++c) {
         verts[9 * (size_t)i + 3 * k + c] = t->WorldVertex(k)[c];
@@ -329,7 +349,7 @@ void BVH::Upload() {
   std::vector<int32_t> em;
   for (auto t : world->Emitters()) {
     auto it = tri_id.find(t);
-    if (it == tri_id.end())
+    if (it == tri_id.end() || it->second < 0)
       throw Exception::DeviceException(RTX_ERR_INVALID, "emitter triangle missing from World::triangles");
     em.push_back(it->second);
   }
