@@ -1,14 +1,17 @@
-// Builds the BVH of a triangle file (n x 9 float32) with 1, 3 and 8 threads
-// and checks each result: both trees (binary and 4-wide) hold every triangle
-// exactly once, every child box contains its subtree's finite vertices, and
-// the bits are the same for every thread count.  Prints one line:
+// Checks the host thread pool, then builds the BVH of a triangle file (n x 9
+// float32) with 1, 3 and 8 threads and checks each result: both trees
+// (binary and 4-wide) hold every triangle exactly once, every child box
+// contains its subtree's finite vertices, and the bits are the same for
+// every thread count.  Prints one line:
 //   "<hash> nodes <n> nodes4 <n> ok" or the first failure.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <stdexcept>
 #include <vector>
 
+#include "host_threads.h"
 #include "rtx_internal.h"
 
 using rtx::BvhBuildResult;
@@ -145,7 +148,28 @@ struct Checker {
   }
 };
 
+// run_parallel (host_threads.h): every index runs once, and an exception on
+// a worker reaches the caller after all threads have joined
+static const char* check_pool() {
+  std::vector<int> hits(1000, 0);
+  rtx::run_parallel(hits.size(), 8, [&](size_t k) { hits[k]++; });
+  for (int h : hits)
+    if (h != 1) return "an index did not run exactly once";
+  try {
+    rtx::run_parallel(1000, 8, [&](size_t k) {
+      if (k == 517) throw std::runtime_error("planted");
+    });
+  } catch (const std::runtime_error&) {
+    return nullptr;
+  }
+  return "a worker's exception did not reach the caller";
+}
+
 int main(int argc, char** argv) {
+  if (const char* e = check_pool()) {
+    std::printf("fail %s\n", e);
+    return 1;
+  }
   if (argc < 3) return 2;
   FILE* f = std::fopen(argv[1], "rb");
   if (!f) return 2;

@@ -8,8 +8,9 @@ extent), many copies of one triangle (all centroids equal) and triangles
 with non-finite vertices.  For each set and leaf size it builds with 1, 3
 and 8 threads and checks that every thread count gives the same bits, that
 both trees (binary and 4-wide) hold every triangle exactly once, and that
-every child box contains its subtree's vertices.  The GPU tests cover what
-the kernels do with the trees.
+every child box contains its subtree's vertices.  It first checks the host
+thread pool the builder uses (every index once; a worker's exception reaches
+the caller).  The GPU tests cover what the kernels do with the trees.
 """
 import os
 import shutil
