@@ -560,7 +560,7 @@ namespace {
 // records, materials and the emitter list.
 struct HostScene {
   BvhBuildResult b;
-  std::vector<float4> shade, geo;
+  Float4Array shade, geo;  // every element written by build_host_scene
   std::vector<float> mats;
   std::vector<int32_t> emitters;
   int n_tris = 0, n_mats = 0;
@@ -597,42 +597,60 @@ int check_scene(rtx_context* c, int n, const float* verts, const float* norms, c
 void build_host_scene(HostScene& h, int n, const float* verts, const float* norms, const int32_t* tri_mesh,
                       int n_meshes, const int32_t* mesh_mat, const uint8_t* mesh_smooth, int n_mat,
                       const float* mats, const float* sky, const float* ground, int leaf_size) {
+  // per-triangle work in chunks on host threads (each triangle's records
+  // are its own, so any split gives the same arrays)
+  unsigned nt = n >= (1 << 16) ? std::max(1u, std::min(std::thread::hardware_concurrency(), 64u)) : 1u;
+  size_t chunks = std::max<size_t>(1, std::min<size_t>(nt, (size_t)n >> 15));
+  auto chunk_range = [&](size_t k, int& b, int& e) {
+    b = (int)((int64_t)n * (int64_t)k / (int64_t)chunks);
+    e = (int)((int64_t)n * (int64_t)(k + 1) / (int64_t)chunks);
+  };
   // Mesh's identity object-to-world turns -0.0 into +0.0 (object.cpp:42-48)
   std::vector<float> v((size_t)n * 9);
-  for (size_t i = 0; i < v.size(); ++i) v[i] = verts[i] + 0.0f;
+  run_parallel(chunks, nt, [&](size_t k) {
+    int b, e;
+    chunk_range(k, b, e);
+    for (size_t i = 9 * (size_t)b; i < 9 * (size_t)e; ++i) v[i] = verts[i] + 0.0f;
+  });
   h.b = build_bvh(v.data(), n, leaf_size);
   h.shade.resize((size_t)n * 4);
   h.geo.resize((size_t)n * 3);
-  for (int i = 0; i < n; ++i) {
-    const float* p = &v[9 * (size_t)i];
-    V3 v0{p[0], p[1], p[2]}, v1{p[3], p[4], p[5]}, v2{p[6], p[7], p[8]};
-    V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
-    V3 cr = cross(e1, e2);
-    float area = std::sqrt(dot(cr, cr)) * 0.5f;                 // Triangle::Area
-    V3 nrm = normalized(cross(normalized(e1), sub(v2, v1)));  // Triangle::Normal
-    int mesh = tri_mesh[i];
-    uint32_t info = (uint32_t)mesh_mat[mesh] | (mesh_smooth[mesh] ? 0x80000000u : 0u);
-    float infof;
-    std::memcpy(&infof, &info, 4);
-    const float* q = norms ? norms + 9 * (size_t)i : nullptr;
-    h.shade[4 * (size_t)i] = make_float4(nrm.x, nrm.y, nrm.z, area);
-    h.shade[4 * (size_t)i + 1] = make_float4(q ? q[0] : 0.f, q ? q[1] : 0.f, q ? q[2] : 0.f, infof);
-    h.shade[4 * (size_t)i + 2] = make_float4(q ? q[3] : 0.f, q ? q[4] : 0.f, q ? q[5] : 0.f, 0.f);
-    h.shade[4 * (size_t)i + 3] = make_float4(q ? q[6] : 0.f, q ? q[7] : 0.f, q ? q[8] : 0.f, 0.f);
-    h.geo[3 * (size_t)i] = make_float4(v0.x, v0.y, v0.z, 0.f);
-    h.geo[3 * (size_t)i + 1] = make_float4(e1.x, e1.y, e1.z, 0.f);
-    h.geo[3 * (size_t)i + 2] = make_float4(e2.x, e2.y, e2.z, 0.f);
-  }
-  // World::PrepareDirectLightSampling (world.cpp:24-37)
-  std::vector<std::vector<int>> per_mesh(n_meshes);
-  for (int i = 0; i < n; ++i) per_mesh[tri_mesh[i]].push_back(i);
-  h.emitters.clear();
+  run_parallel(chunks, nt, [&](size_t k) {
+    int b, e;
+    chunk_range(k, b, e);
+    for (int i = b; i < e; ++i) {
+      const float* p = &v[9 * (size_t)i];
+      V3 v0{p[0], p[1], p[2]}, v1{p[3], p[4], p[5]}, v2{p[6], p[7], p[8]};
+      V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+      V3 cr = cross(e1, e2);
+      float area = std::sqrt(dot(cr, cr)) * 0.5f;                 // Triangle::Area
+      V3 nrm = normalized(cross(normalized(e1), sub(v2, v1)));  // Triangle::Normal
+      int mesh = tri_mesh[i];
+      uint32_t info = (uint32_t)mesh_mat[mesh] | (mesh_smooth[mesh] ? 0x80000000u : 0u);
+      float infof;
+      std::memcpy(&infof, &info, 4);
+      const float* q = norms ? norms + 9 * (size_t)i : nullptr;
+      h.shade[4 * (size_t)i] = make_float4(nrm.x, nrm.y, nrm.z, area);
+      h.shade[4 * (size_t)i + 1] = make_float4(q ? q[0] : 0.f, q ? q[1] : 0.f, q ? q[2] : 0.f, infof);
+      h.shade[4 * (size_t)i + 2] = make_float4(q ? q[3] : 0.f, q ? q[4] : 0.f, q ? q[5] : 0.f, 0.f);
+      h.shade[4 * (size_t)i + 3] = make_float4(q ? q[6] : 0.f, q ? q[7] : 0.f, q ? q[8] : 0.f, 0.f);
+      h.geo[3 * (size_t)i] = make_float4(v0.x, v0.y, v0.z, 0.f);
+      h.geo[3 * (size_t)i + 1] = make_float4(e1.x, e1.y, e1.z, 0.f);
+      h.geo[3 * (size_t)i + 2] = make_float4(e2.x, e2.y, e2.z, 0.f);
+    }
+  });
+  // World::PrepareDirectLightSampling (world.cpp:24-37): the emissive meshes
+  // in order, each one's triangles in id order
+  std::vector<uint8_t> emissive(n_meshes);
   for (int m = 0; m < n_meshes; ++m) {
     const float* em = mats + RTX_MATERIAL_FLOATS * (size_t)mesh_mat[m] + 3;
-    bool emissive = std::fabs(em[0]) > 1e-7f || std::fabs(em[1]) > 1e-7f || std::fabs(em[2]) > 1e-7f;
-    if (emissive)
-      for (int t : per_mesh[m]) h.emitters.push_back(t);
+    emissive[m] = std::fabs(em[0]) > 1e-7f || std::fabs(em[1]) > 1e-7f || std::fabs(em[2]) > 1e-7f;
   }
+  std::vector<std::vector<int>> per_mesh(n_meshes);
+  for (int i = 0; i < n; ++i)
+    if (emissive[tri_mesh[i]]) per_mesh[tri_mesh[i]].push_back(i);
+  h.emitters.clear();
+  for (int m = 0; m < n_meshes; ++m) h.emitters.insert(h.emitters.end(), per_mesh[m].begin(), per_mesh[m].end());
   h.mats.assign(mats, mats + (size_t)n_mat * RTX_MATERIAL_FLOATS);
   h.n_tris = n;
   h.n_mats = n_mat;
