@@ -783,66 +783,94 @@ static int batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
     build_host_scene(hs[i], d[i].n_tris, d[i].verts, d[i].norms, d[i].tri_mesh, d[i].n_meshes, d[i].mesh_mat,
                      d[i].mesh_smooth, d[i].n_materials, d[i].materials, d[i].sky, d[i].ground, c->leaf_size);
   });
-  // merge: node, leaf-record, triangle-id, material and emitter indices rebased
-  std::vector<float4> nodes, nodes4, tris, shade, geo;
-  std::vector<float> mats;
-  std::vector<int32_t> emit;
-  c->bscenes.assign(n_scenes, {});
+  // merge: node, leaf-record, triangle-id, material and emitter indices
+  // rebased.  Each scene's block starts where the sizes of the scenes before
+  // it end, so the scenes are copied into place on host threads.
+  std::vector<size_t> o_nodes(n_scenes + 1, 0), o_nodes4(n_scenes + 1, 0), o_tris(n_scenes + 1, 0),
+      o_mats(n_scenes + 1, 0), o_emit(n_scenes + 1, 0);
+  std::vector<int> tri_bases(n_scenes), mat_bases(n_scenes);
   int tri_base = 0, mat_base = 0;
   for (int i = 0; i < n_scenes; ++i) {
     const HostScene& h = hs[i];
-    int node_base = (int)(nodes.size() / 4);
+    o_nodes[i + 1] = o_nodes[i] + h.b.nodes.size();
+    o_nodes4[i + 1] = o_nodes4[i] + h.b.nodes4.size();
+    o_tris[i + 1] = o_tris[i] + (size_t)h.n_tris;
+    o_mats[i + 1] = o_mats[i] + h.mats.size();
+    o_emit[i + 1] = o_emit[i] + (d[i].n_emitters >= 0 ? (size_t)d[i].n_emitters : h.emitters.size());
+    tri_bases[i] = tri_base;
+    mat_bases[i] = mat_base;
+    tri_base += h.n_tris;
+    mat_base += h.n_mats;
+  }
+  Float4Array nodes(o_nodes[n_scenes]), nodes4(o_nodes4[n_scenes]), tris(3 * o_tris[n_scenes]),
+      shade(4 * o_tris[n_scenes]), geo(3 * o_tris[n_scenes]);
+  std::vector<float> mats(o_mats[n_scenes]);
+  std::vector<int32_t> emit(o_emit[n_scenes]);
+  c->bscenes.assign(n_scenes, {});
+  run_parallel((size_t)n_scenes, std::max(1u, std::min(std::thread::hardware_concurrency(), 16u)), [&](size_t i) {
+    const HostScene& h = hs[i];
+    const int tb = tri_bases[i], mb = mat_bases[i];
+    const int node_base = (int)(o_nodes[i] / 4), node4_base = (int)(o_nodes4[i] / kNode4Vecs);
+    float4* nd = nodes.data() + o_nodes[i];
     for (size_t k = 0; k < h.b.nodes.size(); k += 4) {
-      float4 n0 = h.b.nodes[k], n1 = h.b.nodes[k + 1], n2 = h.b.nodes[k + 2], n3 = h.b.nodes[k + 3];
+      float4 n3 = h.b.nodes[k + 3];
       int ch[2];
       std::memcpy(ch, &n3.x, 8);
-      for (int& x : ch) x = x >= 0 ? x + node_base : rebase_leaf(x, tri_base);
+      for (int& x : ch) x = x >= 0 ? x + node_base : rebase_leaf(x, tb);
       std::memcpy(&n3.x, ch, 8);
-      nodes.insert(nodes.end(), {n0, n1, n2, n3});
+      nd[k] = h.b.nodes[k];
+      nd[k + 1] = h.b.nodes[k + 1];
+      nd[k + 2] = h.b.nodes[k + 2];
+      nd[k + 3] = n3;
     }
     // 4-wide nodes: six float4 of planes, child references in the seventh
     // (empty slots hold 0 behind a box that is never hit)
-    int node4_base = (int)(nodes4.size() / kNode4Vecs);
+    float4* nd4 = nodes4.data() + o_nodes4[i];
     for (size_t k = 0; k < h.b.nodes4.size(); k += kNode4Vecs) {
-      for (int r = 0; r < 6; ++r) nodes4.push_back(h.b.nodes4[k + r]);
+      for (int r6 = 0; r6 < 6; ++r6) nd4[k + r6] = h.b.nodes4[k + r6];
       float4 m = h.b.nodes4[k + 6];
       int ch[4];
       std::memcpy(ch, &m, 16);
-      for (int& x : ch) x = x >= 0 ? x + node4_base : rebase_leaf(x, tri_base);
+      for (int& x : ch) x = x >= 0 ? x + node4_base : rebase_leaf(x, tb);
       std::memcpy(&m, ch, 16);
-      nodes4.push_back(m);
+      nd4[k + 6] = m;
     }
+    float4* tr = tris.data() + 3 * o_tris[i];
     for (size_t k = 0; k < h.b.tris.size(); k += 3) {
-      float4 a = h.b.tris[k];
+      float4 a4 = h.b.tris[k];
       int id;
-      std::memcpy(&id, &a.w, 4);
-      id += tri_base;
-      std::memcpy(&a.w, &id, 4);
-      tris.insert(tris.end(), {a, h.b.tris[k + 1], h.b.tris[k + 2]});
+      std::memcpy(&id, &a4.w, 4);
+      id += tb;
+      std::memcpy(&a4.w, &id, 4);
+      tr[k] = a4;
+      tr[k + 1] = h.b.tris[k + 1];
+      tr[k + 2] = h.b.tris[k + 2];
     }
+    float4* sh = shade.data() + 4 * o_tris[i];
     for (size_t k = 0; k < h.shade.size(); ++k) {
       float4 v = h.shade[k];
       if (k % 4 == 1) {
         uint32_t info;
         std::memcpy(&info, &v.w, 4);
-        info = ((info & 0x7fffffffu) + (uint32_t)mat_base) | (info & 0x80000000u);
+        info = ((info & 0x7fffffffu) + (uint32_t)mb) | (info & 0x80000000u);
         std::memcpy(&v.w, &info, 4);
       }
-      shade.push_back(v);
+      sh[k] = v;
     }
-    geo.insert(geo.end(), h.geo.begin(), h.geo.end());
-    mats.insert(mats.end(), h.mats.begin(), h.mats.end());
+    std::copy(h.geo.begin(), h.geo.end(), geo.begin() + 3 * o_tris[i]);
+    std::copy(h.mats.begin(), h.mats.end(), mats.begin() + o_mats[i]);
     rtx_context::BatchScene& bs = c->bscenes[i];
     int root = h.b.root;
-    bs.root = root == kEmptyRoot ? kEmptyRoot : (root >= 0 ? root + node_base : rebase_leaf(root, tri_base));
+    bs.root = root == kEmptyRoot ? kEmptyRoot : (root >= 0 ? root + node_base : rebase_leaf(root, tb));
     int root4 = h.b.root4;
-    bs.root4 = root4 == kEmptyRoot ? kEmptyRoot : (root4 >= 0 ? root4 + node4_base : rebase_leaf(root4, tri_base));
-    bs.e_begin = (int)emit.size();
+    bs.root4 = root4 == kEmptyRoot ? kEmptyRoot : (root4 >= 0 ? root4 + node4_base : rebase_leaf(root4, tb));
+    bs.e_begin = (int)o_emit[i];
+    int32_t* em = emit.data() + o_emit[i];
     if (d[i].n_emitters >= 0) {
-      for (int k = 0; k < d[i].n_emitters; ++k) emit.push_back(d[i].emitters[k] + tri_base);
+      for (int k = 0; k < d[i].n_emitters; ++k) em[k] = d[i].emitters[k] + tb;
       bs.n_emitters = d[i].n_emitters;
     } else {
-      for (int e : h.emitters) emit.push_back(e + tri_base);
+      for (size_t k = 0; k < h.emitters.size(); ++k) em[k] = h.emitters[k] + tb;
       bs.n_emitters = (int)h.emitters.size();
     }
     bs.n_tris = h.n_tris;
@@ -851,9 +879,7 @@ static int batch_upload(rtx_context* c, int n_scenes, const rtx_scene_desc* d) {
       bs.sky[k] = h.sky[k];
       bs.ground[k] = h.ground[k];
     }
-    tri_base += h.n_tris;
-    mat_base += h.n_mats;
-  }
+  });
   double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if ((r = upload_buf(c, c->b_nodes, nodes.data(), nodes.size() * sizeof(float4), "upload batch nodes"))) return r;
   if ((r = upload_buf(c, c->b_nodes4, nodes4.data(), nodes4.size() * sizeof(float4), "upload batch nodes4")))
