@@ -4,6 +4,7 @@
 #ifndef RTX_COMPAT_BVH_H
 #define RTX_COMPAT_BVH_H
 #include <cstdint>
+#include <unordered_map>
 #include <vector>
 
 #include "ray.h"
@@ -42,6 +43,9 @@ class BVH {
   // materials, mesh table, emitters and environment as uploaded: float bits
   // and emitter addresses, compared exactly
   std::vector<uint64_t> snapshot;
+  // World::triangles index of each triangle, made on the first Intersect
+  // that excludes one (instead of a search of the whole list per call)
+  mutable std::unordered_map<const Triangle*, int32_t> tri_ids;
   void Upload();
   std::vector<uint64_t> Signature() const;
 };

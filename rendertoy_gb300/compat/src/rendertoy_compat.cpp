@@ -285,6 +285,7 @@ std::vector<uint64_t> BVH::Signature() const {
 }
 
 void BVH::Upload() {
+  tri_ids.clear();
   const auto& tris = world->triangles;
   int n = (int)tris.size();
   std::unordered_map<const Mesh*, int> mesh_id;
@@ -365,9 +366,15 @@ const Triangle* BVH::Intersect(const Ray& ray, Vector3f& position, float& t, flo
                                const Triangle* const exclude) const {
   float r[6] = {ray.src[0], ray.src[1], ray.src[2], ray.direction[0], ray.direction[1], ray.direction[2]};
   int32_t ex = -1;
-  if (exclude)
-    for (size_t i = 0; i < world->triangles.size(); ++i)
-      if (world->triangles[i] == exclude) ex = (int32_t)i;
+  if (exclude) {
+    const auto& tris = world->triangles;
+    if (tri_ids.empty()) {  // emptied by each upload
+      tri_ids.reserve(tris.size());
+      for (size_t i = 0; i < tris.size(); ++i) tri_ids[tris[i]] = (int32_t)i;  // the last of repeats, as before
+    }
+    auto it = tri_ids.find(exclude);
+    if (it != tri_ids.end()) ex = it->second;
+  }
   int32_t tri = -1;
   float tuv[3];
   check(rtx_intersect(ctx, 1, r, &ex, &tri, tuv), ctx, "rtx_intersect");

@@ -93,3 +93,25 @@ def test_obj_demo_matches_reference_build(tmp_path, golden):
     for i in (3, 4):  # path traced, tonemapped: RenderToy's mt19937 vs the counter-based stream
         ma, mb = got[i].reshape(-1, 3).mean(0), ref[i].reshape(-1, 3).mean(0)
         assert np.all(np.abs(ma - mb) <= 0.03 * np.abs(mb) + 1e-3), (i, ma, mb)
+
+
+INTERSECT = os.path.join(ROOT, "tests", "compat", "intersect_exclude.cpp")
+
+
+def test_intersect_exclude_compiles_against_compat_headers(tmp_path):
+    from rendertoy_gb300 import build
+    exe = str(tmp_path / "intersect_exclude")
+    build.compile_app(INTERSECT, exe)
+    assert os.path.exists(exe)
+
+
+@pytest.mark.gpu
+def test_intersect_exclude(tmp_path):
+    """BVH::Intersect (RenderToy src/bvh.cpp:266-341) through the compatible
+    API: the closest hit, the hit behind it with that triangle excluded, and
+    no change when an unrelated triangle is excluded."""
+    from rendertoy_gb300 import build
+    exe = str(tmp_path / "intersect_exclude")
+    build.compile_app(INTERSECT, exe)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", (out.stdout, out.stderr)
